@@ -1,0 +1,295 @@
+"""Generate the golden state packs that pin the oracle and the CUDA path to the reference.
+
+Run in this container only (it imports the reference NumPy implementation from its source tree):
+
+    python tests/golden/make_fixtures.py [walk1|strato3|all]
+
+Each fixture is one small state on the reference's reduced grid (4 heights x 10 solar zenith nodes = 40 cells,
+nmu 1, nphi 2, path_n 4, L=16), built by the reference's own assembly (`create_configured` and
+`TransientGeometry.cell`, as `jobs/walkthrough.py:run_example` does). The script stores
+
+* the inputs of the hot path: every cell's rays and segments, the transport constants (`Kernel.setup`), the
+  stored ray-end columns of the ground boundary (`numpy_reference.boundary_end_columns`), the observer rays of
+  `engine_core.Solver.boxes` and the composition vectors of `Solver.apply`;
+* the reference's outputs on those inputs: per-ray radiance of `numpy_reference.transport` (first light, warm
+  with a ground boundary, observer query), `Solver.initialize` moments, `Solver.apply(0)`, `Solver.boxes`, and a
+  complete `Solver.solve` (converged field, evaluation count, residual history).
+
+The solar column table is stored only where the transport can read it (every bilinear corner touched by a
+first-light sample, dilated by two nodes in each direction) so the fixture stays small.
+"""
+
+import copy
+import json
+import os
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REFERENCE_SRC = Path('/root/reference/src')
+
+FIXTURES = dict(
+    # the walkthrough state: clear_34 parameters, exp8 air / triangle ozone, O4 off, no stratospheric layer
+    walk1=dict(strato=False, wavelengths=[550.0]),
+    # the same state with its Gaussian stratospheric sulfate layer (21 km, sigma 3 km) and three wavelengths
+    strato3=dict(strato=True, wavelengths=[450.0, 550.0, 650.0]),
+)
+
+
+def _environment(root):
+    sys.path.insert(0, str(REFERENCE_SRC))
+    from sosfuse2.jobs import walkthrough as wt
+
+    env = wt.example_environment(root)
+    for k in set(os.environ) - set(env):
+        del os.environ[k]
+    os.environ.update(env)
+    cache = root / 'geometry_cache'
+    os.environ.update(
+        SOSFUSE2_COLUMN_CACHE_JOB=str(root), SOSFUSE2_STATE_ID='walkthrough',
+        STRATO_ATTACH_CACHE=str(cache / 'attach_cache'),
+    )
+    return cache
+
+
+def _touched_sun(c, g_cells, strat):
+    """Mask of sun-table entries a first-light sample can read (bilinear corners, dilated by 2)."""
+    from sosfuse2.backends import numpy_reference as nr
+
+    sun_h = c['sun_h']
+    nx = c['sun_col'].shape[1]
+    mask = np.zeros(c['sun_col'].shape[:2], bool)
+    with nr.flush_to_zero():
+        for g in g_cells:
+            st = np.sqrt(np.maximum(0.0, 1 - g['d'][:, 2] ** 2)).astype('f4')
+            for seg in range(g['edges'].shape[1] - 1):
+                for step in range(len(c['u'])):
+                    q = nr.sample(g, seg, step, c, st)
+                    hh = np.clip(q['h'], np.float32(0), np.float32(c['domain'].top_km))
+                    i = np.clip(np.searchsorted(sun_h, hh, side='right') - 1, 0, len(sun_h) - 2)
+                    _, lit, _ = nr.sun_columns(q, c)
+                    # x from the same DS expressions, recomputed loosely: take the full j range the row can touch
+                    height = nr.sub(q['r_DS'], (nr.R, nr.F(0)))
+                    rad = nr.add((nr.R, nr.F(0)), height)
+                    mg = nr.neg(nr.root(nr.divide(nr.mul(height, nr.add((nr.F(2) * nr.R, nr.F(0)), height)),
+                                                  nr.mul(rad, rad))))
+                    delta = nr.sub(nr.divide(q['qz_DS'], q['r_DS']), mg)
+                    x = np.clip(nr.rounded(nr.root(nr.divide(
+                        tuple(np.where(nr.rounded(delta) >= 0, v, nr.F(0)) for v in delta),
+                        nr.sub((nr.F(1), nr.F(0)), mg)))), 0, 1)
+                    j = np.clip((x * np.float32(nx - 1)).astype('i4'), 0, nx - 2)
+                    for di in range(-2, 4):
+                        for dj in range(-2, 4):
+                            mask[np.clip(i + di, 0, len(sun_h) - 1), np.clip(j + dj, 0, nx - 1)] = True
+    return mask
+
+
+def _pack_cells(groups, c, strat):
+    """Concatenate per-cell ray packs into one CSR bundle with per-ray compacted segments."""
+    from sosfuse2.backends import numpy_reference as nr
+
+    cell_off = [0]
+    p, target, d, dloc, weight = [], [], [], [], []
+    seg_off, seg_a, seg_b, seg_lower = [0], [], [], []
+    end_j, end_f, end_col, end_st, hits = [], [], [], [], []
+    for g in groups:
+        n = len(g['d'])
+        cell_off.append(cell_off[-1] + n)
+        if not np.all(g['p'] == g['p'][0]) or not np.all(g['target'] == g['target'][0]):
+            raise ValueError('one start and frame per cell expected')
+        p.append(g['p'][0])
+        target.append(g['target'][0])
+        d.append(g['d'])
+        dloc.append(g['dloc'])
+        weight.append(g['weight'])
+        e = g['edges']
+        for r in range(n):
+            for k in range(e.shape[1] - 1):
+                if e[r, k + 1] - e[r, k] > 1e-8:
+                    seg_a.append(e[r, k])
+                    seg_b.append(e[r, k + 1])
+                    seg_lower.append(bool(g['lower'][r, k]))
+            seg_off.append(len(seg_a))
+        end_j.append(g['end_index'])
+        end_f.append(g['end_fraction'])
+        hits.append(g['hits_ground'])
+        if np.any(g['hits_ground']) and 'gm' in c:
+            col, stcol = nr.boundary_end_columns(g, c, strat)
+        else:
+            col, stcol = g['end_columns'], None
+        end_col.append(np.asarray(col, 'f4'))
+        end_st.append(np.zeros(n, 'f4') if stcol is None else np.asarray(stcol, 'f4'))
+    return dict(
+        cell_off=np.asarray(cell_off, 'i8'),
+        p=np.asarray(p, 'f8'),
+        target=np.asarray(target, 'f8'),
+        d=np.concatenate(d).astype('f8'),
+        dloc=np.concatenate(dloc).astype('f8'),
+        weight=np.concatenate(weight).astype('f8'),
+        seg_off=np.asarray(seg_off, 'i8'),
+        seg_a=np.asarray(seg_a, 'f8'),
+        seg_b=np.asarray(seg_b, 'f8'),
+        seg_lower=np.asarray(seg_lower, 'u1'),
+        end_j=np.concatenate(end_j).astype('i4'),
+        end_f=np.concatenate(end_f).astype('f8'),
+        end_col=np.concatenate(end_col).astype('f4'),
+        end_st=np.concatenate(end_st).astype('f4'),
+        hits=np.concatenate(hits).astype('u1'),
+    )
+
+
+def make(name, spec, out_dir=HERE):
+    root = Path(tempfile.mkdtemp(prefix='sosb_fixture_'))
+    cache = _environment(root)
+    from types import SimpleNamespace
+    from sosfuse2.atmosphere.components import production_only
+    from sosfuse2.jobs import run_state as rs
+    from sosfuse2.jobs import walkthrough as wt
+    from sosfuse2.solve import ray_geometry as gm
+    from sosfuse2.solve.source_solver import Solver
+    from sosfuse2.backends import numpy_reference as nr
+    from sosfuse2.backends.sh_layout import source_size
+
+    production_only()
+    a = SimpleNamespace(reduced=True, settings_json=None, stratosphere=None)
+    st = wt.example_state()
+    if spec['strato']:
+        st['stratosphere'] = dict(status='enabled', profile='gaussian', center_km=21.0, sigma_km=3.0, g=0.63, ssa=1.0)
+    state = rs.effective_state(st, a)
+    cfg = rs.resolve_settings(rs.settings_for(a), state)
+    wl = np.asarray(spec['wavelengths'], float)
+    cfg['wavelengths_nm'] = wl.tolist()
+    cfg['wavelengths'] = len(wl)
+    t0 = time.time()
+    s, scope = rs.create_configured(root / 'tmp' / name / 'prepare_0', cfg, wl, 'numpy', state, 128,
+                                    geometry_cache=cache)
+    geometry = gm.TransientGeometry(s, scope)
+    groups = [geometry.cell(i) for i in range(s.geo.ns)]
+    create_seconds = time.time() - t0
+    nq = cfg['path_n']
+    c = s.kernel.setup(s, nq)
+    strat = 'strato_ext' in c
+    L, K, W = s.kernel.L, s.kernel.K, s.W
+    nh, nc = len(s.geo.h), len(s.geo.chi)
+
+    # observer rays of engine_core.Solver.boxes, captured as the fixed-box path does (record, no transport)
+    raws = []
+
+    def record(raw, solver, _field, first=False):
+        raws.append(raw)
+        return np.zeros((len(raw['d']), solver.W, 2, 4), 'f8')
+
+    s.kernel.transport = record
+    try:
+        s.boxes(np.empty(0, 'f4'), False)
+    finally:
+        del s.kernel.transport
+    nq_query = raws[0]['nq']
+    cq = s.kernel.setup(s, nq_query)
+    u4, w4 = np.polynomial.legendre.leggauss(4)
+    ww = (w4[:, None] * w4[None, :] / 4).ravel()
+
+    bundle = _pack_cells(groups, c, strat)
+    query = _pack_cells(raws, cq, strat)
+    sun_mask = _touched_sun(c, groups, strat)
+    opt = c['density_optics']
+    meta = dict(
+        name=name, L=L, K=K, W=W, nq=nq, nq_query=nq_query, nh=nh, nc=nc, ns=int(s.geo.ns),
+        source_size=int(source_size(s)), strato=bool(strat),
+        g=float(c['g']), mix=float(c['mix']), height=float(c['height']), albedo=float(c['albedo']),
+        top_km=float(c['domain'].top_km), profile_step_km=float(c['domain'].step_km),
+        density_mask=int(opt['mask']), air_surface=float(opt.get('air_surface', 1.0)),
+        tolerance=float(cfg['anderson_tol']), max_eval=64, monitors=len(s.ctx.b.HS) if hasattr(s.ctx.b, 'HS') else 5,
+        n_dirs=7, box_points=16, wavelengths_nm=wl.tolist(), C=float(scope.C),
+        reference='cheek-walnut/sosfuse2 NumPy backend (numpy_reference.transport/project, Solver.solve)',
+        numpy=np.__version__,
+    )
+    arrays = dict(
+        u=np.asarray(c['u'], 'f8'), wu=np.asarray(c['wu'], 'f8'),
+        uq=np.asarray(cq['u'], 'f8'), wuq=np.asarray(cq['wu'], 'f8'),
+        h=c['h'], chi=c['chi'], hr=c['hr'], ha=c['ha'], ext=c['ext'], asca=c['asca'],
+        sun_h=c['sun_h'], sun_col=np.where(sun_mask[..., None], c['sun_col'], np.float32(0)).astype('f4'),
+        sun_mask=sun_mask,
+        gm=c['gm'], gd=c['gd'], gv=c['gv'],
+        density_table=np.asarray(opt['table'], 'f4'),
+        rf=np.asarray(s.rf, 'f4'), af=np.asarray(s.af[:K], 'f4'), ext0=np.asarray(s.ext[0], 'f4'),
+        solar=np.asarray(s.solar, 'f8'), box_ww=ww,
+    )
+    if strat:
+        from sosfuse2.atmosphere.stratosphere import eigen_by_sh
+
+        prof = c['strato_profile']
+        arrays.update(
+            strato_ext=c['strato_ext'], strato_sca=c['strato_sca'], strato_chi=np.asarray(c['strato_chi'], 'f4'),
+            strato_density=c['strato_density'],
+            strato_sun_col=np.where(sun_mask, c['strato_sun_col'], np.float32(0)).astype('f4'),
+            strato_eigen=np.asarray(eigen_by_sh(s.strato, L), 'f4'),
+            strato_sca_source=np.asarray(s.strato['sca'], 'f4'),
+        )
+        meta.update(strato_center=float(prof['center']), strato_sigma=float(prof['sigma']),
+                    strato_norm=float(prof['norm']))
+    for k, v in bundle.items():
+        arrays['cell_' + k] = v
+    for k, v in query.items():
+        arrays['query_' + k] = v
+
+    # ---- reference outputs ----
+    t1 = time.time()
+    solver = Solver(s, geometry, fixed_boxes=False)
+    solver.initialize()
+    arrays['first_moments'] = np.asarray(solver.first_moments, 'f8')
+    arrays['first_flux'] = np.asarray(solver.first_flux, 'f8')
+    zero = np.zeros((s.geo.ns, source_size(s), W), 'f4')
+    g1 = solver.apply(zero)
+    arrays['apply_zero'] = np.asarray(g1, 'f4')
+    arrays['boxes_zero'] = np.asarray(solver.boxes(zero), 'f8')
+    arrays['boxes_g1'] = np.asarray(solver.boxes(g1), 'f8')
+    g2 = solver.apply(g1)
+    arrays['apply_g1'] = np.asarray(g2, 'f4')
+
+    # per-ray transport pins on a few cells (first light; warm with a ground boundary; observer query)
+    pin_cells = [0, 5, 17, ns_last] if (ns_last := s.geo.ns - 1) else [0]
+    boundary = np.asarray(solver.first_flux[:nc], 'f8') * 1.5
+    rad_first, rad_warm = [], []
+    for i in pin_cells:
+        rad_first.append(nr.transport(groups[i], c, zero, True))
+        rad_warm.append(nr.transport(groups[i], c, g1, False, boundary))
+    arrays['pin_cells'] = np.asarray(pin_cells, 'i4')
+    arrays['pin_boundary'] = boundary
+    arrays['pin_first'] = np.concatenate(rad_first).astype('f4')
+    arrays['pin_warm'] = np.concatenate(rad_warm).astype('f4')
+    arrays['pin_query'] = np.concatenate([nr.transport(r, cq, g1, False) for r in raws]).astype('f4')
+    proj_m, proj_f = nr.project(groups[5], rad_warm[1], c)
+    arrays['pin_project_moments'] = proj_m
+    arrays['pin_project_flux'] = proj_f
+
+    t2 = time.time()
+    x, stats = Solver(s, geometry, fixed_boxes=False).solve(64, cfg['anderson_tol'])
+    solve_seconds = time.time() - t2
+    arrays['solve_x'] = np.asarray(x, 'f4')
+    arrays['solve_boxes'] = np.asarray(Solver(s, geometry).boxes(x), 'f8')
+    meta.update(
+        evaluations=int(stats['evaluations']), converged=stats['converged'],
+        history_observer=[h['observer_relative'] for h in stats['history']],
+        history_source=[h['source_relative'] for h in stats['history']],
+        create_seconds=create_seconds, solve_seconds=solve_seconds, outputs_seconds=t2 - t1,
+        rays=int(len(bundle['d'])), segments=int(len(bundle['seg_a'])),
+        query_rays=int(len(query['d'])),
+    )
+    arrays['meta'] = np.asarray(json.dumps(meta))
+    path = out_dir / f'{name}.npz'
+    np.savez_compressed(path, **arrays)
+    print(f'{name}: {path.stat().st_size / 1e6:.2f} MB, evaluations {meta["evaluations"]}, '
+          f'solve {solve_seconds:.1f} s', flush=True)
+    return path
+
+
+if __name__ == '__main__':
+    which = sys.argv[1] if len(sys.argv) > 1 else 'all'
+    for key, spec in FIXTURES.items():
+        if which in ('all', key):
+            make(key, copy.deepcopy(spec))
