@@ -1,0 +1,153 @@
+/* C ABI of libsosb: the GB300 (sm_103a) successive-orders-of-scattering source iteration.
+ *
+ * The library is the drop-in for the transport/iteration boundary of cheek-walnut/sosfuse2: the `Kernel` object that
+ * `create_configured` builds (src/sosfuse2/solve/source_solver.py:1109-1172) and the `Solver` that drives it
+ * (src/sosfuse2/solve/source_iteration.py:100-663). Plain pointers and sizes only; no torch types.
+ *
+ * Conventions
+ *   - Every entry point returns 0 on success, or a nonzero status whose message (prefixed with the reference's error
+ *     code, e.g. "E_NONFINITE_SOURCE", "E_NOT_CONVERGED", "E_SHAPE") is read with sosb_last_error().
+ *   - Host arrays passed to sosb_set_* are copied into device memory owned by the handle; the caller may free them
+ *     after the call returns.
+ *   - Pointers named *_dev are device pointers (e.g. torch tensors' data_ptr()) that the caller keeps alive for the
+ *     duration of the call. All work is issued on the handle's stream (sosb_set_stream) and is complete when a call
+ *     returns, unless stated otherwise.
+ *   - One handle is used by one host thread at a time.
+ *
+ * Field layout (the reference's source layout, src/sosfuse2/backends/sh_layout.py:120-123):
+ *   source[cell][slot][wave], cell = height_index * nc + chi_index, slot 0-3 Rayleigh coherency tensor
+ *   (xx, yy, zz, xz), 4-9 Rayleigh SH coefficients, 10..10+K aerosol SH, then K stratospheric SH when enabled,
+ *   K = (L+1)(L+2)/2, SH index k = l(l+1)/2 + m.
+ */
+#ifndef SOSB_H
+#define SOSB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sosb_state *sosb_handle;
+
+/* Sizes and scalar settings of one state (Kernel.setup constants, source_solver.py:1288-1312). */
+typedef struct {
+    int32_t L;            /* SH order, 2..48 */
+    int32_t W;            /* wavelengths solved together, 1..64 */
+    int32_t nh, nc;       /* height and solar-zenith grid sizes; cells = nh * nc */
+    int32_t nq;           /* Gauss-Legendre nodes per segment, cell transport */
+    int32_t nq_query;     /* nodes per segment, observer rays */
+    int32_t strato;       /* stratospheric layer present: source has 10 + 2K slots */
+    int32_t density_rows; /* rows of the density table (uniform profile grid) */
+    int32_t density_mask; /* bit 0: tabulated air, bit 1: tabulated ozone */
+    int32_t n_sun_h, n_sun_x; /* solar column table shape */
+    int32_t monitors;     /* observer solar elevations used by the stop test (the first rows of the boxes) */
+    int32_t n_monitor_rows; /* all observer solar elevations in the boxes (>= monitors) */
+    int32_t n_dirs;       /* observer directions per elevation (7) */
+    int32_t box_points;   /* Gauss-Legendre points per observer box (16) */
+    double top_km, profile_step_km, mix, g, height, albedo, air_surface;
+    double strato_center, strato_sigma, strato_norm;
+} sosb_dims;
+
+/* Host arrays of the per-state constants. Arrays of an absent layer may be NULL. */
+typedef struct {
+    const double *u, *wu;       /* [nq] nodes and weights on [0, 1] */
+    const double *uq, *wuq;     /* [nq_query] */
+    const float *h, *chi;       /* [nh] km, [nc] rad */
+    const float *hr, *ha;       /* [nh] air and aerosol density shapes at the cell heights */
+    const float *ext;           /* [5][W] extinction per unit profile: air, aerosol, O3, NO2, O4 */
+    const float *asca;          /* [W] aerosol scattering */
+    const float *density_table; /* [density_rows][3] air, ozone, NO2 */
+    const float *sun_h;         /* [n_sun_h] */
+    const float *sun_col;       /* [n_sun_h][n_sun_x][5] */
+    const float *gm;            /* [nh*nc][4][W] first-light Rayleigh moments from the lit ground */
+    const int64_t *goff;        /* [nh*nc + 1] ground directions of each cell */
+    const float *gdir;          /* [goff[last]][3] */
+    const float *gval;          /* [goff[last]][W] */
+    const float *rf;            /* [6] Rayleigh SH factors */
+    const float *af;            /* [K] aerosol phase eigenvalues (g^l) */
+    const float *ext0;          /* [W] air extinction used by the composition */
+    const double *solar;        /* [W] solar spectrum for the observer boxes */
+    const double *box_ww;       /* [box_points] box quadrature weights */
+    const float *strato_ext, *strato_sca; /* [W] */
+    const float *strato_chi;    /* [33][W] Legendre moments of the stratospheric phase */
+    const float *strato_density;/* [nh] stratospheric source density of each height */
+    const float *strato_sun_col;/* [n_sun_h][n_sun_x] */
+    const float *strato_eigen;  /* [K][W] */
+    const float *strato_sca_source; /* [W] */
+} sosb_constants;
+
+/* Host arrays of one ray bundle (ray_geometry.Bundle, src/sosfuse2/solve/ray_geometry.py:290-392): destination
+ * cells, their incoming rays and each ray's segments (only segments with b - a > 1e-8 are integrated). */
+typedef struct {
+    int32_t ncell;
+    int64_t nray, nseg;
+    const int64_t *cell_off;    /* [ncell+1] */
+    const double *p;            /* [ncell][3] start point (km, Earth-centred, sun along +z) */
+    const double *target;       /* [ncell][3][3] local frame */
+    const double *d;            /* [nray][3] direction */
+    const double *dloc;         /* [nray][3] direction in the local frame */
+    const double *weight;       /* [nray] solid-angle weight */
+    const int64_t *seg_off;     /* [nray+1] */
+    const double *seg_a, *seg_b;/* [nseg] path coordinates of the segment ends */
+    const uint8_t *seg_lower;   /* [nseg] 1 when the segment's lower end is at a */
+    const int32_t *end_j;       /* [nray] solar-zenith interval of the ground end */
+    const double *end_f;        /* [nray] fraction within it */
+    const float *end_col;       /* [nray][5] component columns to the ground end */
+    const float *end_st;        /* [nray] stratospheric column to the ground end (may be NULL) */
+    const uint8_t *hits;        /* [nray] ray ends on the ground */
+} sosb_bundle;
+
+typedef struct {
+    int32_t evaluations;
+    int32_t converged;          /* 1 when every wavelength met the tolerance */
+    double seconds;
+    double observer_relative[64]; /* last evaluation, per wavelength */
+    double source_relative[64];
+    int32_t done[64];
+    int64_t kernel_launches;    /* kernels this library launched during the call */
+} sosb_stats;
+
+enum { SOSB_CELLS = 0, SOSB_OBSERVER = 1 };
+
+/* Replaces: source_solver.Kernel.__init__ (source_solver.py:1110-1172) for backend 'b200'. */
+int sosb_create(const sosb_dims *dims, sosb_handle *out);
+int sosb_destroy(sosb_handle h);
+/* Work stream (a cudaStream_t); 0 selects the handle's own stream. */
+int sosb_set_stream(sosb_handle h, void *stream);
+/* Replaces: Kernel.setup (source_solver.py:1243-1339) and constants_device (source_solver.py:2248). */
+int sosb_set_constants(sosb_handle h, const sosb_constants *c);
+/* Replaces: ray_geometry.upload_geometry / device_geometry (ray_geometry.py:205-287) of the cell bundle
+ * (which = SOSB_CELLS) or of the observer rays of engine_core.Solver.boxes (which = SOSB_OBSERVER). */
+int sosb_set_bundle(sosb_handle h, int which, const sosb_bundle *b);
+
+/* Replaces: Kernel.launch (source_solver.py:2428-2456).
+ *   phase 0: transport of every cell's rays (first light when first != 0, else warm with the optional ground
+ *            boundary_dev [nc][W]) projected to moments_dev [cells][4+K][W] and flux_dev [cells][W];
+ *   phase 1: ground pass over the nc surface cells: flux_dev [nc][W] only;
+ *   phase 2: observer rays: radiance_dev [rays][W][4] (SOSB_OBSERVER bundle).
+ * field_dev [cells][slots][W] is ignored for first light. Unused outputs may be NULL. */
+int sosb_evaluate(sosb_handle h, int phase, int first, const float *field_dev, const float *boundary_dev,
+                  float *moments_dev, float *flux_dev, float *radiance_dev);
+/* Replaces: Solver.apply (source_iteration.py:161-216): ground pass, warm pass with the boundary, first-light moments
+ * added, composition into the next source out_dev [cells][slots][W] (first call also runs first light). */
+int sosb_apply(sosb_handle h, const float *field_dev, float *out_dev);
+/* Replaces: Solver.boxes (source_iteration.py:218-222): observer values [n_monitor_rows][n_dirs][W] to host. */
+int sosb_boxes(sosb_handle h, const float *field_dev, double *out_host);
+/* Replaces: Solver.solve (source_iteration.py:309-663): fixed-point iteration from x0 (NULL: zero) with Anderson
+ * depth 4 per wavelength. x_out is a host array [cells][slots][W] (x_out_is_device = 0) or a device pointer.
+ * Returns nonzero with E_NOT_CONVERGED or E_NONFINITE_SOURCE like the reference. */
+int sosb_solve(sosb_handle h, int max_eval, double tolerance, const float *x0_host, float *x_out,
+               int x_out_is_device, sosb_stats *stats);
+/* Message of the last failed call on this handle (empty when none). */
+const char *sosb_last_error(sosb_handle h);
+/* Sizes the handle was created with: cells, slots per cell, K. */
+int sosb_shape(sosb_handle h, int64_t *cells, int32_t *slots, int32_t *K);
+/* Library build identification: "sosb <version> sm_103a". */
+const char *sosb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SOSB_H */

@@ -1,0 +1,621 @@
+// Device math of the SOS transport, compiled both for sm_103a (by nvcc) and for the host (by g++, for CPU tests).
+//
+// One call of `transport_lane` integrates one incoming ray of one destination cell for one wavelength: the ray's
+// segments (shell crossings) are walked node by node with the reference's double-single (two-float) geometry
+// (src/sosfuse2/backends/numpy_reference.py:294-387, arithmetic.py:15-66), the optical depth to each node is the
+// Simpson prefix of the extinction (numpy_reference.py:236-291), and each node adds the scattered source of its
+// four bracketing (height, solar-zenith) cells, rotated into the ray's frame, attenuated and Kahan-summed
+// (numpy_reference.py:467-643). The aerosol source of a corner cell is the SH plane of that cell contracted with
+// the ray's SH basis row (numpy_reference.py:588-600) and kept per corner while the corner cell does not change.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define SOS_HD __host__ __device__ __forceinline__
+#else
+#define SOS_HD inline
+struct float4 {
+    float x, y, z, w;
+};
+#endif
+
+// Error-free transformations need every add and multiply rounded on its own: no contraction into FMA.
+#if defined(__CUDA_ARCH__)
+#define SOS_ADD(a, b) __fadd_rn((a), (b))
+#define SOS_SUB(a, b) __fsub_rn((a), (b))
+#define SOS_MUL(a, b) __fmul_rn((a), (b))
+#define SOS_DIV(a, b) __fdiv_rn((a), (b))
+#define SOS_SQRT(a) __fsqrt_rn(a)
+#define SOS_FMA(a, b, c) __fmaf_rn((a), (b), (c))
+#else
+// the host build uses -ffp-contract=off
+#define SOS_ADD(a, b) ((a) + (b))
+#define SOS_SUB(a, b) ((a) - (b))
+#define SOS_MUL(a, b) ((a) * (b))
+#define SOS_DIV(a, b) ((a) / (b))
+#define SOS_SQRT(a) sqrtf(a)
+#define SOS_FMA(a, b, c) fmaf((a), (b), (c))
+#endif
+
+namespace sos {
+
+constexpr float EARTH_R = 6371.0f;
+constexpr float TRACE_MIN = 1.17549435e-38f;  // FLT_MIN
+constexpr float PI_F = 3.14159265358979f;
+constexpr float C_3_8PI = 0.119366207318921505f;   // 3 / (8 pi), rounded once
+constexpr float C_1_8PI = 0.0397887357729738339f;  // 1 / (8 pi), rounded once
+constexpr float C_4PI = 12.5663706143591725f;      // 4 pi, rounded once
+constexpr int MAX_L = 48;
+
+// ------------------------------------------------------------------ double-single arithmetic
+struct DS {
+    float h, l;
+};
+
+SOS_HD DS ds_make(float h) { return DS{h, 0.0f}; }
+
+SOS_HD DS ds_add(DS a, DS b) {
+    float s = SOS_ADD(a.h, b.h);
+    float v = SOS_SUB(s, a.h);
+    float e = SOS_ADD(SOS_ADD(SOS_SUB(a.h, SOS_SUB(s, v)), SOS_SUB(b.h, v)), SOS_ADD(a.l, b.l));
+    float h = SOS_ADD(s, e);
+    return DS{h, SOS_SUB(e, SOS_SUB(h, s))};
+}
+
+SOS_HD DS ds_neg(DS a) { return DS{-a.h, -a.l}; }
+SOS_HD DS ds_sub(DS a, DS b) { return ds_add(a, ds_neg(b)); }
+
+SOS_HD DS ds_mul(DS a, DS b) {
+    float p = SOS_MUL(a.h, b.h);
+    float e = SOS_FMA(a.h, b.h, -p);  // exact low part of a.h * b.h, one rounding
+    e = SOS_ADD(SOS_ADD(e, SOS_MUL(a.h, b.l)), SOS_MUL(a.l, b.h));
+    float h = SOS_ADD(p, e);
+    return DS{h, SOS_SUB(e, SOS_SUB(h, p))};
+}
+
+SOS_HD DS ds_sqrt(DS a) {
+    float h = SOS_SQRT(fmaxf(a.h, 0.0f));
+    DS e = ds_sub(a, ds_mul(ds_make(h), ds_make(h)));
+    float lo = SOS_DIV(SOS_ADD(e.h, e.l), fmaxf(SOS_MUL(2.0f, h), 1e-30f));
+    return ds_add(ds_make(h), ds_make(lo));
+}
+
+SOS_HD DS ds_div(DS a, DS b) {
+    float h = SOS_DIV(a.h, b.h);
+    DS e = ds_sub(a, ds_mul(ds_make(h), b));
+    float lo = SOS_DIV(SOS_ADD(e.h, e.l), b.h);
+    return ds_add(ds_make(h), ds_make(lo));
+}
+
+SOS_HD float ds_val(DS a) { return SOS_ADD(a.h, a.l); }
+
+SOS_HD float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+// Index i in [0, n-2] with grid[i] <= x < grid[i+1] (searchsorted right, minus one, clipped).
+SOS_HD int bracket(const float* grid, int n, float x) {
+    int lo = 0, hi = n;  // count of grid values <= x by binary search
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (grid[mid] <= x) lo = mid + 1; else hi = mid;
+    }
+    int i = lo - 1;
+    return i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+}
+
+// ------------------------------------------------------------------ inputs
+// Per-state optics and grids (device pointers, or host pointers in the host build).
+struct Optics {
+    int L, K, W, nh, nc, ns, src;   // src = source slots per cell (10 + K or 10 + 2K)
+    int strato;
+    float top_km, mix, g, height, air_surface, inv_step;
+    int density_last, density_mask;
+    float strato_center, strato_sigma, strato_norm;
+    const float* h;        // [nh]
+    const float* chi;      // [nc]
+    const float* hr;       // [nh] air density shape at the cell heights
+    const float* ext;      // [5][W] extinction per unit profile: air, aerosol, O3, NO2, O4
+    const float* asca;     // [W]  aerosol scattering
+    const float* table;    // [rows][3] air, ozone, NO2 on the uniform profile grid
+    int n_sun_h, n_sun_x;
+    const float* sun_h;    // [n_sun_h]
+    const float* sun_col;  // [n_sun_h][n_sun_x][5]
+    const float* strato_sun_col;  // [n_sun_h][n_sun_x]
+    const float* gm;       // [ns][4][W] first-light direct-ground Rayleigh moments
+    const int* goff;       // [ns+1] ground directions per cell
+    const float* gdir;     // [*][3]
+    const float* gval;     // [*][W]
+    const float* strato_ext;  // [W]
+    const float* strato_sca;  // [W]
+    const float* strato_chi;  // [33][W] Legendre moments of the stratospheric phase function
+    const float* sh_a;     // [K] recurrence coefficients (FP32)
+    const float* sh_b;     // [K]
+    const float* sh_d;     // [L+1] diagonal factors
+};
+
+// One bundle of rays: cells (destination points) with their incoming rays and compacted segments.
+struct Rays {
+    int ncell, nray;
+    const int* cell_off;   // [ncell+1]
+    const int* ray_cell;   // [nray]
+    const float* p;        // [ncell][6] start point, double-single (hi xyz, lo xyz)
+    const float* frame;    // [ncell][9] target frame B[k][i]
+    const float4* dir;     // [nray] (dx, dy, dz, sin theta) FP32
+    const float4* dir_lo;  // [nray] (dx_lo, dy_lo, dz_lo, weight)
+    const float4* dloc;    // [nray] (local direction xyz, end fraction)
+    const int* seg_off;    // [nray+1]
+    const float4* seg;     // [nseg] (a_hi, a_lo, b_hi, b_lo) path coordinates of the segment ends
+    const uint8_t* lower;  // [nseg] segment runs upward (its lower end is at a)
+    const int* end_j;      // [nray] solar-zenith interval of the ray's ground end
+    const float* end_col;  // [nray][6] component columns (5) and stratospheric column to the ground end
+    const uint8_t* hits;   // [nray]
+    const float* pcp;      // [nray] cos of the ray's global azimuth, d_x / sin(theta) (projection)
+};
+
+// ------------------------------------------------------------------ optics primitives
+struct Profile {
+    float v[5];
+};
+
+SOS_HD Profile profile_at(const Optics& o, float h) {
+    float hc = clampf(h, 0.0f, o.top_km);
+    float x = hc * o.inv_step;
+    int i = (int)x;
+    if (i > o.density_last) i = o.density_last;
+    float f = x - (float)i;
+    const float* t0 = o.table + 3 * i;
+    const float* t1 = t0 + 3;
+    float tab0 = t0[0] + f * (t1[0] - t0[0]);
+    float tab1 = t0[1] + f * (t1[1] - t0[1]);
+    float tab2 = t0[2] + f * (t1[2] - t0[2]);
+    Profile p;
+    p.v[0] = (o.density_mask & 1) ? tab0 : expf(-h / 8.0f);
+    p.v[1] = expf(-h / o.height);
+    p.v[2] = (o.density_mask & 2) ? tab1 : fmaxf(0.0f, 1.0f - fabsf(h - 25.0f) / 15.0f);
+    p.v[3] = tab2;
+    float q = p.v[0] / o.air_surface;
+    p.v[4] = q * q;
+    return p;
+}
+
+SOS_HD float strato_profile(const Optics& o, float h) {
+    float t = (h - o.strato_center) / o.strato_sigma;
+    return expf(-0.5f * (t * t)) / o.strato_norm;
+}
+
+SOS_HD float extinction(const Optics& o, const Profile& p, float st, int w) {
+    float b = 0.0f;
+    for (int k = 0; k < 5; ++k) b += p.v[k] * o.ext[k * o.W + w];
+    if (o.strato) b += st * o.strato_ext[w];
+    return b;
+}
+
+SOS_HD float hg_phase(float u, float g) {
+    float den = fmaxf(1e-20f, (1.0f + g * g) - (2.0f * g) * u);
+    return (1.0f - g * g) / (C_4PI * (den * sqrtf(den)));
+}
+
+SOS_HD float legendre_phase(const Optics& o, float u, int w) {
+    float p0 = 1.0f, p1 = u;
+    float val = p0 * o.strato_chi[w] + p1 * o.strato_chi[o.W + w];
+    for (int l = 2; l < 33; ++l) {
+        float pn = (((float)(2 * l - 1) * u) * p1 - (float)(l - 1) * p0) / (float)l;
+        val += pn * o.strato_chi[l * o.W + w];
+        p0 = p1;
+        p1 = pn;
+    }
+    return val / C_4PI;
+}
+
+SOS_HD float ftz_value(DS a) {
+    float h = fabsf(a.h) < TRACE_MIN ? 0.0f : a.h;
+    float l = fabsf(a.l) < TRACE_MIN ? 0.0f : a.l;
+    float v = h + l;
+    return fabsf(v) < TRACE_MIN ? 0.0f : v;
+}
+
+// ------------------------------------------------------------------ one quadrature node
+struct Node {
+    DS t;             // path coordinate
+    DS r;             // distance from the Earth's centre
+    DS qz;            // z of the node
+    float h, ds;      // height (clipped), quadrature weight along the path
+    float sw[4];      // bilinear weights of the four corner cells
+    int cell[4];      // corner cells (ir, j), (ir, j+1), (ir+1, j), (ir+1, j+1)
+    int ir;           // height interval
+    float T[4][4];    // Rayleigh coherency rotation
+    float cp;         // cos of the azimuth between the ray and the node's meridian
+    float mu, exd, eyd;  // ray direction in the node's local frame (first light)
+    Profile prof;
+    float st_prof;
+};
+
+struct RayConst {
+    DS p[3], d[3];
+    float B[3][3];    // frame rows B[k][i]
+    float d32[3], dloc[3], pu[4], direct[4], st, weight, end_f;
+};
+
+SOS_HD void path_point(const RayConst& rc, DS t, DS q[3], DS q2[3], DS& r) {
+    for (int k = 0; k < 3; ++k) {
+        q[k] = ds_add(rc.p[k], ds_mul(t, rc.d[k]));
+        q2[k] = ds_mul(q[k], q[k]);
+    }
+    r = ds_sqrt(ds_add(ds_add(q2[0], q2[1]), q2[2]));
+}
+
+SOS_HD float path_height(const Optics& o, DS r) { return clampf(ds_val(ds_sub(r, ds_make(EARTH_R))), 0.0f, o.top_km); }
+
+SOS_HD float beta_at(const Optics& o, const RayConst& rc, DS t, int w) {
+    DS q[3], q2[3], r;
+    path_point(rc, t, q, q2, r);
+    float h = path_height(o, r);
+    Profile p = profile_at(o, h);
+    return extinction(o, p, o.strato ? strato_profile(o, h) : 0.0f, w);
+}
+
+SOS_HD void sample_node(const Optics& o, const RayConst& rc, DS a, DS b, bool lower, DS u, DS wu, Node& n) {
+    DS length = ds_sub(b, a);
+    DS v = lower ? u : ds_sub(ds_make(1.0f), u);
+    DS tt = lower ? ds_add(a, ds_mul(length, ds_mul(u, u))) : ds_sub(b, ds_mul(length, ds_mul(v, v)));
+    n.t = tt;
+    n.ds = ds_val(ds_mul(ds_mul(length, v), wu)) * 2.0f;
+    DS q[3], q2[3], r;
+    path_point(rc, tt, q, q2, r);
+    n.r = r;
+    n.qz = q[2];
+    float h = path_height(o, r);
+    n.h = h;
+    DS xy = ds_sqrt(ds_add(q2[0], q2[1]));
+    float rho = ds_val(xy);
+    float cx = 1.0f, sx = 0.0f;
+    if (rho > 1e-12f) {
+        DS den = DS{fmaxf(xy.h, 1e-30f), xy.l};
+        cx = ds_val(ds_div(q[0], den));
+        sx = ds_val(ds_div(q[1], den));
+    }
+    float angle = atan2f(rho, ds_val(q[2]));
+    int ir = bracket(o.h, o.nh, h);
+    int j = bracket(o.chi, o.nc, angle);
+    float ah = clampf((h - o.h[ir]) / (o.h[ir + 1] - o.h[ir]), 0.0f, 1.0f);
+    float ac = clampf((angle - o.chi[j]) / (o.chi[j + 1] - o.chi[j]), 0.0f, 1.0f);
+    float ang = o.chi[j] + ac * (o.chi[j + 1] - o.chi[j]);
+    float sn = sinf(ang), cc = cosf(ang);
+    // Q rows: local (east, north, up) of the node in global coordinates, columns indexed [k][j]
+    float Q[3][3] = {{-cc * cx, sx, sn * cx}, {-cc * sx, -cx, sn * sx}, {sn, 0.0f, cc}};
+    float A[3][3], dot[3];
+    for (int i = 0; i < 3; ++i)
+        for (int jj = 0; jj < 3; ++jj) {
+            float s = 0.0f;
+            for (int k = 0; k < 3; ++k) s += rc.B[k][i] * Q[k][jj];
+            A[i][jj] = s;
+        }
+    for (int jj = 0; jj < 3; ++jj) {
+        float s = 0.0f;
+        for (int k = 0; k < 3; ++k) s += rc.d32[k] * Q[k][jj];
+        dot[jj] = s;
+    }
+    float Km[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int jj = 0; jj < 3; ++jj) Km[i][jj] = A[i][jj] - rc.dloc[i] * dot[jj];
+    const int PI_[4] = {0, 1, 2, 0}, PK_[4] = {0, 1, 2, 2};
+    for (int pr = 0; pr < 4; ++pr) {
+        int i = PI_[pr], k = PK_[pr];
+        n.T[pr][0] = Km[i][0] * Km[k][0];
+        n.T[pr][1] = Km[i][1] * Km[k][1];
+        n.T[pr][2] = Km[i][2] * Km[k][2];
+        n.T[pr][3] = Km[i][0] * Km[k][2] + Km[i][2] * Km[k][0];
+    }
+    n.mu = dot[2];
+    n.exd = dot[0];
+    n.eyd = dot[1];
+    n.cp = rc.st > 1e-12f ? (rc.d32[0] * cx + rc.d32[1] * sx) / fmaxf(rc.st, 1e-30f) : 1.0f;
+    n.ir = ir;
+    n.cell[0] = ir * o.nc + j;
+    n.cell[1] = ir * o.nc + j + 1;
+    n.cell[2] = (ir + 1) * o.nc + j;
+    n.cell[3] = (ir + 1) * o.nc + j + 1;
+    n.sw[0] = (1.0f - ah) * (1.0f - ac);
+    n.sw[1] = (1.0f - ah) * ac;
+    n.sw[2] = ah * (1.0f - ac);
+    n.sw[3] = ah * ac;
+    n.prof = profile_at(o, h);
+    n.st_prof = o.strato ? strato_profile(o, h) : 0.0f;
+}
+
+// Slant columns towards the sun at the node: bilinear in (height, x), x from the node's solar elevation relative to
+// the geometric horizon (numpy_reference.py:431-458).
+SOS_HD void sun_columns(const Optics& o, const Node& n, float col[5], float& st, float& lit) {
+    float hh = clampf(n.h, 0.0f, o.top_km);
+    DS height = ds_sub(n.r, ds_make(EARTH_R));
+    if (!(ftz_value(height) > 0.0f)) height = DS{0.0f, 0.0f};
+    DS rad = ds_add(ds_make(EARTH_R), height);
+    DS mg = ds_neg(ds_sqrt(ds_div(ds_mul(height, ds_add(ds_make(2.0f * EARTH_R), height)), ds_mul(rad, rad))));
+    DS delta = ds_sub(ds_div(n.qz, n.r), mg);
+    if (ftz_value(delta) == 0.0f) delta = DS{0.0f, 0.0f};
+    bool is_lit = ds_val(delta) >= 0.0f;
+    if (!is_lit) delta = DS{0.0f, 0.0f};
+    float x = clampf(ds_val(ds_sqrt(ds_div(delta, ds_sub(ds_make(1.0f), mg)))), 0.0f, 1.0f);
+    int i = bracket(o.sun_h, o.n_sun_h, hh);
+    float a = (hh - o.sun_h[i]) / (o.sun_h[i + 1] - o.sun_h[i]);
+    float f = x * (float)(o.n_sun_x - 1);
+    int j = (int)f;
+    j = j < 0 ? 0 : (j > o.n_sun_x - 2 ? o.n_sun_x - 2 : j);
+    float bb = f - (float)j;
+    const float* c00 = o.sun_col + ((size_t)i * o.n_sun_x + j) * 5;
+    const float* c10 = c00 + (size_t)o.n_sun_x * 5;
+    const float* c01 = c00 + 5;
+    const float* c11 = c10 + 5;
+    float w00 = (1.0f - a) * (1.0f - bb), w10 = a * (1.0f - bb), w01 = (1.0f - a) * bb, w11 = a * bb;
+    for (int k = 0; k < 5; ++k) {
+        float v = w00 * c00[k];
+        v += w10 * c10[k];
+        v += w01 * c01[k];
+        v += w11 * c11[k];
+        col[k] = v;
+    }
+    st = 0.0f;
+    if (o.strato) {
+        const float* s00 = o.strato_sun_col + (size_t)i * o.n_sun_x + j;
+        st = w00 * s00[0];
+        st += w10 * s00[o.n_sun_x];
+        st += w01 * s00[1];
+        st += w11 * s00[o.n_sun_x + 1];
+    }
+    lit = is_lit ? 1.0f : 0.0f;
+}
+
+SOS_HD void ray_constants(const Rays& b, int ray, RayConst& rc) {
+    int cell = b.ray_cell[ray];
+    const float* p = b.p + 6 * cell;
+    float4 d = b.dir[ray], dl = b.dir_lo[ray], lo = b.dloc[ray];
+    rc.p[0] = DS{p[0], p[3]};
+    rc.p[1] = DS{p[1], p[4]};
+    rc.p[2] = DS{p[2], p[5]};
+    rc.d[0] = DS{d.x, dl.x};
+    rc.d[1] = DS{d.y, dl.y};
+    rc.d[2] = DS{d.z, dl.z};
+    rc.d32[0] = d.x;
+    rc.d32[1] = d.y;
+    rc.d32[2] = d.z;
+    rc.st = d.w;
+    rc.weight = dl.w;
+    const float* f = b.frame + 9 * cell;
+    for (int k = 0; k < 3; ++k)
+        for (int i = 0; i < 3; ++i) rc.B[k][i] = f[3 * k + i];
+    rc.dloc[0] = lo.x;
+    rc.dloc[1] = lo.y;
+    rc.dloc[2] = lo.z;
+    rc.end_f = lo.w;
+    rc.pu[0] = 1.0f - lo.x * lo.x;
+    rc.pu[1] = 1.0f - lo.y * lo.y;
+    rc.pu[2] = 1.0f - lo.z * lo.z;
+    rc.pu[3] = -lo.x * lo.z;
+    const float* u = rc.B[2];
+    float dot = (lo.x * u[0] + lo.y * u[1]) + lo.z * u[2];
+    float e[3] = {u[0] - lo.x * dot, u[1] - lo.y * dot, u[2] - lo.z * dot};
+    const int PI_[4] = {0, 1, 2, 0}, PK_[4] = {0, 1, 2, 2};
+    for (int k = 0; k < 4; ++k) rc.direct[k] = (rc.pu[k] - e[PI_[k]] * e[PK_[k]]) / 2.0f;
+}
+
+// Aerosol SH contraction for one corner cell: cache[m] = sum_l Y_lm(mu) plane[cell][k(l,m)] for m = 0..L, with the
+// normalised associated-Legendre recurrence evaluated on the fly (FP32) from the ray's mu = d_z.
+SOS_HD void sh_contract(const Optics& o, float mu, float st, const float* plane_cell, int wstride, float* cache,
+                        int cstride) {
+    const int L = o.L;
+    float pmm = 0.28209479177387814f;  // 1 / sqrt(4 pi)
+    for (int m = 0; m <= L; ++m) {
+        if (m) pmm = (pmm * o.sh_d[m]) * st;
+        const float scale = m ? 1.41421356237309515f : 1.0f;
+        float p0 = pmm;
+        int k = m * (m + 1) / 2 + m;
+        float acc = (scale * p0) * plane_cell[(size_t)k * wstride];
+        if (m < L) {
+            float p1 = (sqrtf(2.0f * m + 3.0f) * mu) * p0;
+            k = (m + 1) * (m + 2) / 2 + m;
+            acc += (scale * p1) * plane_cell[(size_t)k * wstride];
+            for (int l = m + 2; l <= L; ++l) {
+                k = l * (l + 1) / 2 + m;
+                float p2 = (o.sh_a[k] * mu) * p1 - o.sh_b[k] * p0;
+                acc += (scale * p2) * plane_cell[(size_t)k * wstride];
+                p0 = p1;
+                p1 = p2;
+            }
+        }
+        cache[m * cstride] = acc;
+    }
+}
+
+// Sum over m of cos(m phi) * cache[m], cos(m phi) by the Chebyshev recurrence of cp.
+SOS_HD float azimuth_sum(int L, float cp, const float* cache, int cstride) {
+    cp = clampf(cp, -1.0f, 1.0f);
+    float c0 = 1.0f, c1 = cp;
+    float s = cache[0];
+    if (L >= 1) s += c1 * cache[cstride];
+    for (int m = 2; m <= L; ++m) {
+        float c2 = (2.0f * cp) * c1 - c0;
+        s += c2 * cache[m * cstride];
+        c0 = c1;
+        c1 = c2;
+    }
+    return s;
+}
+
+SOS_HD void kahan(float& total, float& comp, float value) {
+    float y = value - comp;
+    float t = total + y;
+    comp = (t - total) - y;
+    total = t;
+}
+
+// Everything one lane needs that is shared by all rays of a launch.
+struct LaneInputs {
+    const float* field;     // [ns][src][W] current source
+    const float* plane;     // [ns][K][W] aerosol (+ stratospheric) SH plane, already scaled by the cell density
+    const float* boundary;  // [nc][W] ground flux at the surface nodes, or null
+    const float* u_hi;      // quadrature nodes on [0, 1] and weights, double-single
+    const float* u_lo;
+    const float* wu_hi;
+    const float* wu_lo;
+    int nq;
+    int first;
+};
+
+// Integrate one ray for wavelength w. `cache` holds 4 slots x (L+1) floats at stride `cstride`.
+SOS_HD void transport_lane(const Optics& o, const Rays& b, const LaneInputs& in, int ray, int w, float* cache,
+                           int cstride, float out[4]) {
+    RayConst rc;
+    ray_constants(b, ray, rc);
+    const int W = o.W;
+    const float mix = o.mix;
+    const bool first = in.first != 0;
+    float total[4] = {0, 0, 0, 0}, comp[4] = {0, 0, 0, 0};
+    float tau = 0.0f, tauc = 0.0f;
+    const float phase = hg_phase(rc.d32[2], o.g);
+    const float sphase = (o.strato && first) ? legendre_phase(o, rc.d32[2], w) : 0.0f;
+    int tag[4] = {-1, -1, -1, -1};  // cell held by each cache slot
+    const int s0 = b.seg_off[ray], s1 = b.seg_off[ray + 1];
+    for (int s = s0; s < s1; ++s) {
+        float4 sg = b.seg[s];
+        DS a = DS{sg.x, sg.y}, bb = DS{sg.z, sg.w};
+        bool lower = b.lower[s] != 0;
+        DS t0 = a;
+        float beta0 = beta_at(o, rc, t0, w);
+        float acc = 0.0f;
+        for (int step = 0; step < in.nq; ++step) {
+            Node n;
+            sample_node(o, rc, a, bb, lower, DS{in.u_hi[step], in.u_lo[step]}, DS{in.wu_hi[step], in.wu_lo[step]},
+                        n);
+            float beta1 = extinction(o, n.prof, n.st_prof, w);
+            DS tm = ds_add(t0, n.t);
+            tm = DS{tm.h * 0.5f, tm.l * 0.5f};
+            float wpan = ds_val(ds_sub(n.t, t0)) / 6.0f;
+            acc = acc + wpan * ((beta0 + beta1) + 4.0f * beta_at(o, rc, tm, w));
+            t0 = n.t;
+            beta0 = beta1;
+            float mid = (tau - tauc) + acc;
+            float att = n.ds * expf(-mid);
+            float val[4] = {0, 0, 0, 0};
+            if (first) {
+                float col[5], stc, lit;
+                sun_columns(o, n, col, stc, lit);
+                float optical = 0.0f;
+                for (int k = 0; k < 5; ++k) optical += col[k] * o.ext[k * W + w];
+                if (o.strato) optical += stc * o.strato_ext[w];
+                float sun = expf(-optical) * lit;
+                float ground = 0.0f, sground = 0.0f;
+                float aeyd = fabsf(n.eyd);
+                for (int c = 0; c < 4; ++c) {
+                    int cell = n.cell[c];
+                    for (int gi = o.goff[cell]; gi < o.goff[cell + 1]; ++gi) {
+                        const float* gd = o.gdir + 3 * gi;
+                        float m0 = n.mu * gd[2] + n.exd * gd[0];
+                        float m1 = aeyd * gd[1];
+                        float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
+                        float gv = o.gval[(size_t)gi * W + w];
+                        float ph = (hg_phase(up, o.g) + hg_phase(dn, o.g)) / 2.0f;
+                        ground += (n.sw[c] * ph) * gv;
+                        if (o.strato) {
+                            float sph = (legendre_phase(o, up, w) + legendre_phase(o, dn, w)) / 2.0f;
+                            sground += (n.sw[c] * sph) * gv;
+                        }
+                    }
+                }
+                float beam = (n.prof.v[1] * o.asca[w]) * (sun * phase + ground);
+                float ray_ = (sun * n.prof.v[0]) * o.ext[w];
+                float sbeam = o.strato ? (n.st_prof * o.strato_sca[w]) * (sun * sphase + sground) : 0.0f;
+                for (int k = 0; k < 4; ++k) {
+                    val[k] = ray_ * (mix * C_3_8PI * rc.direct[k] + (1.0f - mix) * C_1_8PI * rc.pu[k]) +
+                             beam * rc.pu[k] / 2.0f;
+                    if (o.strato) val[k] += (sbeam * rc.pu[k]) / 2.0f;
+                }
+                for (int c = 0; c < 4; ++c) {
+                    const float* gm = o.gm + (size_t)n.cell[c] * 4 * W + w;
+                    float rm[4] = {gm[0], gm[W], gm[2 * W], gm[3 * W]};
+                    float trace = (rm[0] + rm[1]) + rm[2];
+                    float dens = n.prof.v[0];
+                    for (int k = 0; k < 4; ++k) {
+                        float rot = 0.0f;
+                        for (int u = 0; u < 4; ++u) rot += n.T[k][u] * rm[u];
+                        float tens = dens * (mix * rot + ((1.0f - mix) / 3.0f * trace) * rc.pu[k]);
+                        val[k] += n.sw[c] * tens;
+                    }
+                }
+            } else {
+                // corner slots: reuse a slot whose cell is still a corner, recompute the others
+                int slot_of[4];
+                unsigned used = 0;
+                for (int c = 0; c < 4; ++c) {
+                    slot_of[c] = -1;
+                    for (int q = 0; q < 4; ++q)
+                        if (tag[q] == n.cell[c] && !(used & (1u << q))) {
+                            slot_of[c] = q;
+                            used |= 1u << q;
+                            break;
+                        }
+                }
+                for (int c = 0; c < 4; ++c) {
+                    if (slot_of[c] >= 0) continue;
+                    int q = 0;
+                    while (used & (1u << q)) ++q;
+                    used |= 1u << q;
+                    slot_of[c] = q;
+                    tag[q] = n.cell[c];
+                    sh_contract(o, rc.d32[2], rc.st, in.plane + (size_t)n.cell[c] * o.K * W + w, W,
+                                cache + (size_t)q * (o.L + 1) * cstride, cstride);
+                }
+                float logs = 0.0f, wg = 0.0f, am = 0.0f;
+                for (int c = 0; c < 4; ++c) {
+                    int cell = n.cell[c];
+                    int irc = n.ir + (c >> 1);
+                    float aero = azimuth_sum(o.L, n.cp, cache + (size_t)slot_of[c] * (o.L + 1) * cstride, cstride);
+                    const float* f = in.field + (size_t)cell * o.src * W + w;
+                    float rm[4] = {f[0], f[W], f[2 * W], f[3 * W]};
+                    float trace = (rm[0] + rm[1]) + rm[2];
+                    float dens = o.hr[irc];
+                    float tens[4];
+                    for (int k = 0; k < 4; ++k) {
+                        float rot = 0.0f;
+                        for (int u = 0; u < 4; ++u) rot += n.T[k][u] * rm[u];
+                        tens[k] = dens * (mix * rot + ((1.0f - mix) / 3.0f * trace) * rc.pu[k]);
+                        tens[k] += (aero * rc.pu[k]) / 2.0f;
+                        val[k] += n.sw[c] * tens[k];
+                    }
+                    float tr = (tens[0] + tens[1]) + tens[2];
+                    if (tr >= TRACE_MIN) {  // subnormal or NaN traces do not enter the log-space blend
+                        logs += n.sw[c] * logf(tr);
+                        wg += n.sw[c];
+                        am += n.sw[c] * tr;
+                    }
+                }
+                if (wg > 0.0f && am >= TRACE_MIN) {
+                    float scale = expf(logs - wg * logf(am / wg));
+                    for (int k = 0; k < 4; ++k) val[k] *= scale;
+                }
+            }
+            for (int k = 0; k < 4; ++k) kahan(total[k], comp[k], val[k] * att);
+        }
+        // closing panel to the segment end, then the segment's optical depth into tau (Kahan)
+        DS tm = ds_add(t0, bb);
+        tm = DS{tm.h * 0.5f, tm.l * 0.5f};
+        float wpan = ds_val(ds_sub(bb, t0)) / 6.0f;
+        acc = acc + wpan * ((beta0 + beta_at(o, rc, bb, w)) + 4.0f * beta_at(o, rc, tm, w));
+        kahan(tau, tauc, acc);
+    }
+    if (in.boundary && b.hits[ray]) {
+        int j = b.end_j[ray];
+        float ef = rc.end_f;
+        float E = (1.0f - ef) * in.boundary[j * W + w];
+        E += ef * in.boundary[(j + 1) * W + w];
+        const float* ec = b.end_col + 6 * (size_t)ray;
+        float optical = 0.0f;
+        for (int k = 0; k < 5; ++k) optical += ec[k] * o.ext[k * W + w];
+        if (o.strato) optical += ec[5] * o.strato_ext[w];
+        E *= expf(-optical);
+        for (int k = 0; k < 4; ++k) total[k] += (E * rc.pu[k]) / 2.0f;
+    }
+    for (int k = 0; k < 4; ++k) out[k] = total[k];
+}
+
+}  // namespace sos

@@ -1,0 +1,1078 @@
+// libsosb: GB300 (sm_103a) kernels and C ABI of the successive-orders-of-scattering source iteration.
+//
+// Kernels (one evaluation = ground pass, warm pass, composition; plus two observer passes and Anderson mixing):
+//   transport_kernel  one thread per (ray, wavelength): the ray's line-of-sight integral (sos_math.cuh)
+//   plane_kernel      aerosol (+ stratospheric) SH plane of every cell, scaled by the cell's source density
+//   project_kernel    one block per cell: weighted ray radiance onto 4 Rayleigh + K SH moments and ground flux
+//   compose_kernel    moments -> next source (Solver.apply composition) fused with the convergence metrics
+//   boxes_kernel      observer rays -> Gauss-Legendre box values
+//   norm/feature/dot/mix kernels  Anderson depth-4 residual features, Gram columns (FP64) and the mixing
+// The fixed-point loop (sosb_solve) runs on the host thread over device-resident buffers; per evaluation it reads
+// back only per-wavelength scalars (metrics, box values, Gram columns).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sos_math.cuh"
+#include "sos_pack.h"
+#include "../../include/sosb.h"
+
+using namespace sos;
+
+#define SOSB_VERSION "sosb 0.1 sm_103a"
+
+// ------------------------------------------------------------------------------------------------ device buffers
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct BundleDev {
+    int ncell = 0;
+    int64_t nray = 0, nseg = 0;
+    DevBuf cell_off, ray_cell, p, frame, dir, dir_lo, dloc, pcp, seg_off, seg, lower, end_j, end_col, hits;
+    std::vector<int64_t> host_cell_off;
+};
+
+struct sosb_state {
+    sosb_dims d{};
+    int K = 0, src = 0, ns = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    std::string err;
+    bool have_constants = false;
+    // constants
+    DevBuf h, chi, hr, ha, ext, asca, table, sun_h, sun_col, gm, goff, gdir, gval, rf, af, ext0;
+    DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src;
+    DevBuf sh_a, sh_b, sh_d;
+    DevBuf u_hi, u_lo, wu_hi, wu_lo, uq_hi, uq_lo, wuq_hi, wuq_lo, box_ww, solar;
+    BundleDev cells, obs;
+    // work
+    DevBuf rad, plane, moments, flux, first_moments, first_flux, boundary, metrics, boxes;
+    DevBuf fx, fg, fn, norms, partials, dots, mixw;
+    DevBuf ring_g[4], ring_f[4];
+    bool have_first = false;
+    int64_t launches = 0;
+};
+
+static int fail(sosb_state* s, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (s) s->err = buf;
+    return 1;
+}
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(s, "E_CUDA: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__);          \
+    } while (0)
+
+#define TRY(call)          \
+    do {                   \
+        int r_ = (call);   \
+        if (r_) return r_; \
+    } while (0)
+
+static int dfree(sosb_state* s, DevBuf& b) {
+    if (b.p) CK(cudaFree(b.p));
+    b.p = nullptr;
+    b.bytes = 0;
+    return 0;
+}
+
+static int dalloc(sosb_state* s, DevBuf& b, size_t bytes) {
+    if (b.p && b.bytes >= bytes) return 0;
+    TRY(dfree(s, b));
+    if (bytes == 0) return 0;
+    CK(cudaMalloc(&b.p, bytes));
+    b.bytes = bytes;
+    return 0;
+}
+
+static int dput(sosb_state* s, DevBuf& b, const void* host, size_t bytes) {
+    TRY(dalloc(s, b, bytes));
+    if (bytes) CK(cudaMemcpyAsync(b.p, host, bytes, cudaMemcpyHostToDevice, s->stream));
+    return 0;
+}
+
+template <class T>
+static int dput_vec(sosb_state* s, DevBuf& b, const std::vector<T>& v) {
+    return dput(s, b, v.data(), v.size() * sizeof(T));
+}
+
+template <class T>
+static T* P(const DevBuf& b) {
+    return static_cast<T*>(b.p);
+}
+
+static int grid_for(long long n, int threads) {
+    long long g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > 152LL * 64) g = 152LL * 64;  // grid-stride loops beyond 64 blocks per SM
+    return (int)g;
+}
+
+// ------------------------------------------------------------------------------------------------ kernels
+constexpr int TRANSPORT_THREADS = 128;
+
+__global__ void __launch_bounds__(TRANSPORT_THREADS)
+    transport_kernel(Optics o, Rays b, LaneInputs in, int ray0, int nray, int glog2, int wchunks, float4* rad) {
+    extern __shared__ float cache[];
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long grp = t >> glog2;
+    const int lane = (int)(t & ((1 << glog2) - 1));
+    const long long rr = grp / wchunks;
+    const int w = (int)(grp % wchunks) * 32 + lane;
+    if (rr >= nray || w >= o.W) return;
+    const int ray = ray0 + (int)rr;
+    float out[4];
+    transport_lane(o, b, in, ray, w, cache + threadIdx.x, blockDim.x, out);
+    rad[(size_t)ray * o.W + w] = make_float4(out[0], out[1], out[2], out[3]);
+}
+
+__global__ void plane_kernel(const float* __restrict__ field, const float* __restrict__ ha,
+                             const float* __restrict__ sd, int nc, int K, int src, int W, int strato, long long n,
+                             float* __restrict__ plane) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % W);
+        const long long r = i / W;
+        const int k = (int)(r % K);
+        const int cell = (int)(r / K);
+        const int hi = cell / nc;
+        const float* f = field + (size_t)cell * src * W + w;
+        float v = f[(size_t)(10 + k) * W] * ha[hi];
+        if (strato) v += f[(size_t)(10 + K + k) * W] * sd[hi];
+        plane[i] = v;
+    }
+}
+
+constexpr int PROJ_THREADS = 512;
+constexpr int PROJ_RAYS = 16;
+constexpr int PROJ_OWN = 16;
+
+static size_t project_smem(int K, int W) { return sizeof(float) * (size_t)PROJ_RAYS * (K + 6 * W); }
+
+// One block per cell. Output (slot, w) pairs are owned by threads (registers, Kahan-compensated FP32 over ray
+// chunks); the basis row Y_lm(mu) cos(m phi) of PROJ_RAYS rays is staged in shared memory per chunk
+// (numpy_reference.py:689-711: moments[0:4] = sum wt rad, moments[4+k] = sum (wt trace) (Y_k cos m phi),
+// flux = sum trace wt max(0, dloc_z) * albedo / pi).
+__global__ void __launch_bounds__(PROJ_THREADS)
+    project_kernel(Optics o, Rays b, const float4* __restrict__ rad, int cell0, int ground_only, int out_base,
+                   float* __restrict__ moments, float* __restrict__ flux, float flux_scale) {
+    extern __shared__ float sm[];
+    const int W = o.W, K = o.K, L = o.L;
+    const int cell = cell0 + blockIdx.x;
+    const int r0 = b.cell_off[cell], r1 = b.cell_off[cell + 1];
+    const int nout = (4 + K) * W;
+    float* basis = sm;                    // [PROJ_RAYS][K]
+    float* wtr = basis + PROJ_RAYS * K;   // [PROJ_RAYS][W]  weight * trace
+    float* wr = wtr + PROJ_RAYS * W;      // [PROJ_RAYS][4][W] weight * radiance
+    float* wgr = wr + PROJ_RAYS * 4 * W;  // [PROJ_RAYS][W] trace * weight * max(0, dloc_z)
+    float acc[PROJ_OWN], cmp[PROJ_OWN];
+#pragma unroll
+    for (int i = 0; i < PROJ_OWN; ++i) acc[i] = cmp[i] = 0.0f;
+    float facc = 0.0f, fcmp = 0.0f;
+    const bool do_flux = out_base == 0 && (int)threadIdx.x < W && flux != nullptr;
+    for (int rb = r0; rb < r1; rb += PROJ_RAYS) {
+        const int nr = min(PROJ_RAYS, r1 - rb);
+        __syncthreads();
+        if (!ground_only) {
+            for (int it = threadIdx.x; it < nr * (L + 1); it += blockDim.x) {
+                const int r = it / (L + 1), m = it % (L + 1);
+                const int ray = rb + r;
+                const float4 dv = b.dir[ray];
+                const float mu = dv.z, st = dv.w;
+                const float cp = clampf(b.pcp[ray], -1.0f, 1.0f);
+                float c0 = 1.0f, c1 = cp, cm = 1.0f;
+                if (m == 1) cm = cp;
+                for (int q = 2; q <= m; ++q) {
+                    float c2 = (2.0f * cp) * c1 - c0;
+                    c0 = c1;
+                    c1 = c2;
+                    cm = c2;
+                }
+                float pmm = 0.28209479177387814f;
+                for (int q = 1; q <= m; ++q) pmm = (pmm * o.sh_d[q]) * st;
+                const float scale = m ? 1.41421356237309515f : 1.0f;
+                float* row = basis + r * K;
+                float p0 = pmm;
+                row[m * (m + 1) / 2 + m] = (scale * p0) * cm;
+                if (m < L) {
+                    float p1 = (sqrtf(2.0f * m + 3.0f) * mu) * p0;
+                    row[(m + 1) * (m + 2) / 2 + m] = (scale * p1) * cm;
+                    for (int l = m + 2; l <= L; ++l) {
+                        const int k = l * (l + 1) / 2 + m;
+                        float p2 = (o.sh_a[k] * mu) * p1 - o.sh_b[k] * p0;
+                        row[k] = (scale * p2) * cm;
+                        p0 = p1;
+                        p1 = p2;
+                    }
+                }
+            }
+        }
+        for (int it = threadIdx.x; it < nr * W; it += blockDim.x) {
+            const int r = it / W, w = it % W;
+            const int ray = rb + r;
+            const float4 v = rad[(size_t)ray * W + w];
+            const float wt = b.dir_lo[ray].w;
+            const float tr = (v.x + v.y) + v.z;
+            wtr[r * W + w] = tr * wt;
+            wr[(r * 4 + 0) * W + w] = v.x * wt;
+            wr[(r * 4 + 1) * W + w] = v.y * wt;
+            wr[(r * 4 + 2) * W + w] = v.z * wt;
+            wr[(r * 4 + 3) * W + w] = v.w * wt;
+            wgr[r * W + w] = tr * (wt * fmaxf(0.0f, b.dloc[ray].z));
+        }
+        __syncthreads();
+        if (!ground_only) {
+#pragma unroll
+            for (int i = 0; i < PROJ_OWN; ++i) {
+                const int oi = out_base + threadIdx.x + i * PROJ_THREADS;
+                if (oi < nout) {
+                    const int slot = oi / W, w = oi % W;
+                    float part = 0.0f;
+                    if (slot < 4) {
+                        for (int r = 0; r < nr; ++r) part += wr[(r * 4 + slot) * W + w];
+                    } else {
+                        const int k = slot - 4;
+                        for (int r = 0; r < nr; ++r) part += wtr[r * W + w] * basis[r * K + k];
+                    }
+                    kahan(acc[i], cmp[i], part);
+                }
+            }
+        }
+        if (do_flux) {
+            float part = 0.0f;
+            for (int r = 0; r < nr; ++r) part += wgr[r * W + threadIdx.x];
+            kahan(facc, fcmp, part);
+        }
+    }
+    if (!ground_only && moments) {
+#pragma unroll
+        for (int i = 0; i < PROJ_OWN; ++i) {
+            const int oi = out_base + threadIdx.x + i * PROJ_THREADS;
+            if (oi < nout) moments[(size_t)cell * nout + oi] = acc[i];
+        }
+    }
+    if (do_flux) flux[(size_t)cell * W + threadIdx.x] = facc * flux_scale;
+}
+
+__global__ void add_kernel(const float* a, const float* b, float* out, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] + b[i];
+}
+
+// metrics layout: [0][W] nonfinite count, [1][W] max |g| bits, [2][W] max |g - x| bits (uint32)
+__global__ void compose_kernel(const float* __restrict__ warm, const float* __restrict__ first, const float* __restrict__ x,
+                               const float* __restrict__ rf, const float* __restrict__ af, const float* __restrict__ asca,
+                               const float* __restrict__ ext0, const float* __restrict__ s_eigen,
+                               const float* __restrict__ s_sca, int K, int src, int W, long long n,
+                               unsigned long long done_mask, float* __restrict__ out, unsigned* __restrict__ metrics) {
+    __shared__ unsigned sm_bad[64], sm_mag[64], sm_dif[64];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) sm_bad[i] = sm_mag[i] = sm_dif[i] = 0u;
+    __syncthreads();
+    const int nm = 4 + K;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % W);
+        const long long r = i / W;
+        const int slot = (int)(r % src);
+        const long long cell = r / src;
+        const size_t mb = ((size_t)cell * nm) * W + w;
+        float v;
+        if (slot < 4) {
+            const float m = warm[mb + (size_t)slot * W] + first[mb + (size_t)slot * W];
+            v = m * (C_3_8PI * ext0[w]);
+        } else if (slot < 10) {
+            const float m = warm[mb + (size_t)slot * W] + first[mb + (size_t)slot * W];
+            v = (m * rf[slot - 4]) * ext0[w];
+        } else if (slot < 10 + K) {
+            const int k = slot - 10;
+            const float m = warm[mb + (size_t)(4 + k) * W] + first[mb + (size_t)(4 + k) * W];
+            v = (m * af[k]) * asca[w];
+        } else {
+            const int k = slot - 10 - K;
+            const float m = warm[mb + (size_t)(4 + k) * W] + first[mb + (size_t)(4 + k) * W];
+            v = (m * s_eigen[k * W + w]) * s_sca[w];
+        }
+        if (fabsf(v) < TRACE_MIN) v = 0.0f;
+        const unsigned bad = isfinite(v) ? 0u : 1u;
+        const float xv = x ? x[i] : 0.0f;
+        if ((done_mask >> w) & 1ull) v = xv;
+        out[i] = v;
+        if (bad) atomicAdd(&sm_bad[w], 1u);
+        atomicMax(&sm_mag[w], __float_as_uint(fabsf(v)));
+        atomicMax(&sm_dif[w], __float_as_uint(fabsf(v - xv)));
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < W; w += blockDim.x) {
+        if (sm_bad[w]) atomicAdd(&metrics[w], sm_bad[w]);
+        atomicMax(&metrics[W + w], sm_mag[w]);
+        atomicMax(&metrics[2 * W + w], sm_dif[w]);
+    }
+}
+
+// Observer boxes: out[row][dir][w] = solar[w] sum_n ww[n] (rad_xx + rad_yy + rad_zz)[row, dir, n, w] in FP64.
+__global__ void boxes_kernel(const float4* __restrict__ rad, const double* __restrict__ ww,
+                             const double* __restrict__ solar, int rows, int dirs, int pts, int W, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * dirs * W) return;
+    const int w = i % W;
+    const int rd = i / W;
+    double s = 0.0;
+    for (int n = 0; n < pts; ++n) {
+        const float4 v = rad[((size_t)rd * pts + n) * W + w];
+        s += ww[n] * (((double)v.x + (double)v.y) + (double)v.z);
+    }
+    out[i] = s * solar[w];
+}
+
+// Anderson residual features. norms[cell][w] = |g[cell, :, w]| (FP32), and the per-wavelength max in mx (bits).
+__global__ void norm_kernel(const float* __restrict__ g, int ns, int src, int W, float* __restrict__ norms,
+                            unsigned* __restrict__ mx) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (long long)ns * W;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % W);
+        const long long cell = i / W;
+        const float* p = g + (size_t)cell * src * W + w;
+        float s = 0.0f;
+        for (int k = 0; k < src; ++k) {
+            const float v = p[(size_t)k * W];
+            s += v * v;
+        }
+        const float nv = sqrtf(s);
+        norms[i] = nv;
+        atomicMax(&mx[w], __float_as_uint(nv));
+    }
+}
+
+// feature f = (g - x) / max(norm, 1e-8 max norm) written to ring slot `dst`; FP64 partial dots of f with the ring
+// slots listed in `slots` (nslot <= 4, including dst itself) per block: partials[block][j][w].
+__global__ void feature_kernel(const float* __restrict__ g, const float* __restrict__ x, const float* __restrict__ norms,
+                               const unsigned* __restrict__ mx, int src, int W, long long n, float* __restrict__ dst,
+                               const float* r0, const float* r1, const float* r2, const float* r3, int nslot,
+                               double* __restrict__ partials) {
+    extern __shared__ double sd[];  // [nslot][W]
+    for (int i = threadIdx.x; i < nslot * W; i += blockDim.x) sd[i] = 0.0;
+    __syncthreads();
+    const float* ring[4] = {r0, r1, r2, r3};
+    double loc[4] = {0, 0, 0, 0};
+    int wl = -1;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % W);
+        const long long cell = i / W / src;
+        const float nv = norms[cell * W + w];
+        const float scale = fmaxf(nv, __uint_as_float(mx[w]) * 1e-8f);
+        const float f = (g[i] - x[i]) / scale;
+        dst[i] = f;
+        // the stride is a multiple of W when gridDim*blockDim % W == 0, so w is fixed per thread
+        if (wl != w) {
+            if (wl >= 0)
+                for (int j = 0; j < nslot; ++j) atomicAdd(&sd[j * W + wl], loc[j]);
+            for (int j = 0; j < 4; ++j) loc[j] = 0.0;
+            wl = w;
+        }
+        for (int j = 0; j < nslot; ++j) {
+            const float o = (ring[j] == dst) ? f : ring[j][i];
+            loc[j] += (double)f * (double)o;
+        }
+    }
+    if (wl >= 0)
+        for (int j = 0; j < nslot; ++j) atomicAdd(&sd[j * W + wl], loc[j]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nslot * W; i += blockDim.x) partials[(size_t)blockIdx.x * nslot * W + i] = sd[i];
+}
+
+__global__ void sum_partials_kernel(const double* __restrict__ partials, int blocks, int n, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int b = 0; b < blocks; ++b) s += partials[(size_t)b * n + i];
+    out[i] = s;
+}
+
+// nxt[i] = sum_j c[j][w] ring_g[order j][i] for wavelengths with valid weights, else g[i].
+__global__ void mix_kernel(const float* __restrict__ g, const float* q0, const float* q1, const float* q2,
+                           const float* q3, int m, const float* __restrict__ c, const int* __restrict__ use, int W,
+                           long long n, float* __restrict__ out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % W);
+        if (!use[w]) {
+            out[i] = g[i];
+            continue;
+        }
+        const float* q[4] = {q0, q1, q2, q3};
+        float s = c[w] * q[0][i];
+        for (int j = 1; j < m; ++j) s += c[j * W + w] * q[j][i];
+        out[i] = s;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ host helpers
+static Optics optics_of(const sosb_state* s) {
+    Optics o{};
+    const sosb_dims& d = s->d;
+    o.L = d.L;
+    o.K = s->K;
+    o.W = d.W;
+    o.nh = d.nh;
+    o.nc = d.nc;
+    o.ns = s->ns;
+    o.src = s->src;
+    o.strato = d.strato;
+    o.top_km = (float)d.top_km;
+    o.mix = (float)d.mix;
+    o.g = (float)d.g;
+    o.height = (float)d.height;
+    o.air_surface = (float)d.air_surface;
+    o.inv_step = (float)(1.0 / d.profile_step_km);
+    o.density_last = d.density_rows - 2;
+    o.density_mask = d.density_mask;
+    o.strato_center = (float)d.strato_center;
+    o.strato_sigma = (float)d.strato_sigma;
+    o.strato_norm = (float)d.strato_norm;
+    o.h = P<float>(s->h);
+    o.chi = P<float>(s->chi);
+    o.hr = P<float>(s->hr);
+    o.ext = P<float>(s->ext);
+    o.asca = P<float>(s->asca);
+    o.table = P<float>(s->table);
+    o.n_sun_h = d.n_sun_h;
+    o.n_sun_x = d.n_sun_x;
+    o.sun_h = P<float>(s->sun_h);
+    o.sun_col = P<float>(s->sun_col);
+    o.strato_sun_col = P<float>(s->s_sun_col);
+    o.gm = P<float>(s->gm);
+    o.goff = P<int>(s->goff);
+    o.gdir = P<float>(s->gdir);
+    o.gval = P<float>(s->gval);
+    o.strato_ext = P<float>(s->s_ext);
+    o.strato_sca = P<float>(s->s_sca);
+    o.strato_chi = P<float>(s->s_chi);
+    o.sh_a = P<float>(s->sh_a);
+    o.sh_b = P<float>(s->sh_b);
+    o.sh_d = P<float>(s->sh_d);
+    return o;
+}
+
+static Rays rays_of(const BundleDev& b) {
+    Rays r{};
+    r.ncell = b.ncell;
+    r.nray = (int)b.nray;
+    r.cell_off = P<int>(b.cell_off);
+    r.ray_cell = P<int>(b.ray_cell);
+    r.p = P<float>(b.p);
+    r.frame = P<float>(b.frame);
+    r.dir = P<float4>(b.dir);
+    r.dir_lo = P<float4>(b.dir_lo);
+    r.dloc = P<float4>(b.dloc);
+    r.seg_off = P<int>(b.seg_off);
+    r.seg = P<float4>(b.seg);
+    r.lower = P<uint8_t>(b.lower);
+    r.end_j = P<int>(b.end_j);
+    r.end_col = P<float>(b.end_col);
+    r.hits = P<uint8_t>(b.hits);
+    r.pcp = P<float>(b.pcp);
+    return r;
+}
+
+static int launch_check(sosb_state* s) {
+    s->launches++;
+    CK(cudaGetLastError());
+    return 0;
+}
+
+// transport of rays [ray0, ray0 + nray) of bundle `b` into s->rad
+static int run_transport(sosb_state* s, const BundleDev& b, int64_t ray0, int64_t nray, const float* field,
+                         const float* boundary, int first, bool query) {
+    if (nray <= 0) return 0;
+    const sosb_dims& d = s->d;
+    TRY(dalloc(s, s->rad, (size_t)b.nray * d.W * sizeof(float4)));
+    LaneInputs in{};
+    in.field = field;
+    in.plane = P<float>(s->plane);
+    in.boundary = boundary;
+    in.first = first;
+    if (query) {
+        in.u_hi = P<float>(s->uq_hi);
+        in.u_lo = P<float>(s->uq_lo);
+        in.wu_hi = P<float>(s->wuq_hi);
+        in.wu_lo = P<float>(s->wuq_lo);
+        in.nq = d.nq_query;
+    } else {
+        in.u_hi = P<float>(s->u_hi);
+        in.u_lo = P<float>(s->u_lo);
+        in.wu_hi = P<float>(s->wu_hi);
+        in.wu_lo = P<float>(s->wu_lo);
+        in.nq = d.nq;
+    }
+    const int wchunk = std::min(d.W, 32);
+    int glog2 = 0;
+    while ((1 << glog2) < wchunk) ++glog2;
+    const int wchunks = (d.W + 31) / 32;
+    const long long threads = (long long)nray * wchunks << glog2;
+    const long long blocks = (threads + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
+    const size_t smem = sizeof(float) * 4 * (d.L + 1) * TRANSPORT_THREADS;
+    transport_kernel<<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
+        optics_of(s), rays_of(b), in, (int)ray0, (int)nray, glog2, wchunks, P<float4>(s->rad));
+    return launch_check(s);
+}
+
+static int run_project(sosb_state* s, const BundleDev& b, int ncell, bool ground_only, float* moments, float* flux) {
+    if (ncell <= 0) return 0;
+    const sosb_dims& d = s->d;
+    const int nout = (4 + s->K) * d.W;
+    const size_t smem = project_smem(s->K, d.W);
+    const float flux_scale = (float)(d.albedo / M_PI);
+    const int per_pass = PROJ_THREADS * PROJ_OWN;
+    const int passes = ground_only ? 1 : (nout + per_pass - 1) / per_pass;
+    for (int pass = 0; pass < passes; ++pass) {
+        project_kernel<<<ncell, PROJ_THREADS, smem, s->stream>>>(optics_of(s), rays_of(b), P<float4>(s->rad), 0,
+                                                                 ground_only ? 1 : 0, pass * per_pass, moments,
+                                                                 pass == 0 ? flux : nullptr, flux_scale);
+        TRY(launch_check(s));
+    }
+    return 0;
+}
+
+static int run_plane(sosb_state* s, const float* field) {
+    const sosb_dims& d = s->d;
+    const long long n = (long long)s->ns * s->K * d.W;
+    TRY(dalloc(s, s->plane, n * sizeof(float)));
+    plane_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(field, P<float>(s->ha), P<float>(s->s_density), d.nc, s->K,
+                                                          s->src, d.W, d.strato, n, P<float>(s->plane));
+    return launch_check(s);
+}
+
+static int check_ready(sosb_state* s, bool need_obs) {
+    if (!s->have_constants) return fail(s, "E_STATE: constants not set");
+    if (s->cells.nray == 0) return fail(s, "E_STATE: cell bundle not set");
+    if (need_obs && s->obs.nray == 0) return fail(s, "E_STATE: observer bundle not set");
+    return 0;
+}
+
+static int evaluate_impl(sosb_state* s, int phase, int first, const float* field, const float* boundary,
+                         float* moments, float* flux, float* radiance) {
+    const sosb_dims& d = s->d;
+    TRY(check_ready(s, phase == 2));
+    if (phase == 2) {
+        if (!first) TRY(run_plane(s, field));
+        TRY(run_transport(s, s->obs, 0, s->obs.nray, field, nullptr, first, true));
+        if (radiance)
+            CK(cudaMemcpyAsync(radiance, s->rad.p, (size_t)s->obs.nray * d.W * sizeof(float4), cudaMemcpyDeviceToDevice,
+                               s->stream));
+        return 0;
+    }
+    if (!first) TRY(run_plane(s, field));
+    if (phase == 1) {
+        const int64_t nray = s->cells.host_cell_off[d.nc];
+        TRY(run_transport(s, s->cells, 0, nray, field, nullptr, first, false));
+        TRY(run_project(s, s->cells, d.nc, true, nullptr, flux));
+        return 0;
+    }
+    TRY(run_transport(s, s->cells, 0, s->cells.nray, field, boundary, first, false));
+    TRY(run_project(s, s->cells, s->ns, false, moments, flux));
+    if (radiance)
+        CK(cudaMemcpyAsync(radiance, s->rad.p, (size_t)s->cells.nray * d.W * sizeof(float4), cudaMemcpyDeviceToDevice,
+                           s->stream));
+    return 0;
+}
+
+static int ensure_first(sosb_state* s) {
+    if (s->have_first) return 0;
+    const sosb_dims& d = s->d;
+    TRY(dalloc(s, s->first_moments, (size_t)s->ns * (4 + s->K) * d.W * sizeof(float)));
+    TRY(dalloc(s, s->first_flux, (size_t)s->ns * d.W * sizeof(float)));
+    TRY(evaluate_impl(s, 0, 1, nullptr, nullptr, P<float>(s->first_moments), P<float>(s->first_flux), nullptr));
+    s->have_first = true;
+    return 0;
+}
+
+// Solver.apply: returns metrics on device in s->metrics (reset here)
+static int apply_impl(sosb_state* s, const float* field, float* out, unsigned long long done_mask) {
+    const sosb_dims& d = s->d;
+    TRY(check_ready(s, false));
+    TRY(ensure_first(s));
+    const size_t nmom = (size_t)s->ns * (4 + s->K) * d.W;
+    TRY(dalloc(s, s->moments, nmom * sizeof(float)));
+    TRY(dalloc(s, s->flux, (size_t)s->ns * d.W * sizeof(float)));
+    TRY(dalloc(s, s->boundary, (size_t)d.nc * d.W * sizeof(float)));
+    TRY(dalloc(s, s->metrics, 3 * 64 * sizeof(unsigned)));
+    // ground pass over the surface cells, then the boundary = ground flux + first-light flux
+    TRY(evaluate_impl(s, 1, 0, field, nullptr, nullptr, P<float>(s->flux), nullptr));
+    const int nb = d.nc * d.W;
+    add_kernel<<<(nb + 255) / 256, 256, 0, s->stream>>>(P<float>(s->flux), P<float>(s->first_flux), P<float>(s->boundary),
+                                                        nb);
+    TRY(launch_check(s));
+    // warm pass (the plane of `field` is already current)
+    TRY(run_transport(s, s->cells, 0, s->cells.nray, field, P<float>(s->boundary), 0, false));
+    TRY(run_project(s, s->cells, s->ns, false, P<float>(s->moments), P<float>(s->flux)));
+    CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
+    const long long n = (long long)s->ns * s->src * d.W;
+    compose_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(
+        P<float>(s->moments), P<float>(s->first_moments), field, P<float>(s->rf), P<float>(s->af), P<float>(s->asca),
+        P<float>(s->ext0), P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, done_mask, out,
+        P<unsigned>(s->metrics));
+    return launch_check(s);
+}
+
+static int boxes_impl(sosb_state* s, const float* field, double* out_host) {
+    const sosb_dims& d = s->d;
+    TRY(check_ready(s, true));
+    if (s->obs.nray < (int64_t)d.n_monitor_rows * d.n_dirs * d.box_points)
+        return fail(s, "E_SHAPE: %lld observer rays for %d x %d boxes of %d points", (long long)s->obs.nray,
+                    d.n_monitor_rows, d.n_dirs, d.box_points);
+    TRY(run_plane(s, field));
+    TRY(run_transport(s, s->obs, 0, s->obs.nray, field, nullptr, 0, true));
+    const int n = d.n_monitor_rows * d.n_dirs * d.W;
+    TRY(dalloc(s, s->boxes, n * sizeof(double)));
+    boxes_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(P<float4>(s->rad), P<double>(s->box_ww), P<double>(s->solar),
+                                                        d.n_monitor_rows, d.n_dirs, d.box_points, d.W,
+                                                        P<double>(s->boxes));
+    TRY(launch_check(s));
+    CK(cudaMemcpyAsync(out_host, s->boxes.p, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+// ------------------------------------------------------------------------------------------------ C ABI
+extern "C" {
+
+const char* sosb_version(void) { return SOSB_VERSION; }
+
+const char* sosb_last_error(sosb_handle h) { return h ? h->err.c_str() : "E_HANDLE: null handle"; }
+
+int sosb_create(const sosb_dims* dims, sosb_handle* out) {
+    if (!dims || !out) return 1;
+    *out = nullptr;
+    const sosb_dims& d = *dims;
+    if (d.L < 2 || d.L > MAX_L || d.W < 1 || d.W > 64 || d.nh < 2 || d.nc < 2 || d.nq < 1 || d.nq_query < 1 ||
+        d.density_rows < 2 || d.n_sun_h < 2 || d.n_sun_x < 2 || d.n_dirs < 1 || d.box_points < 1 || d.monitors < 1 ||
+        d.n_monitor_rows < d.monitors)
+        return 2;
+    sosb_state* s = new sosb_state();
+    s->d = d;
+    s->K = (d.L + 1) * (d.L + 2) / 2;
+    s->src = 10 + s->K * (d.strato ? 2 : 1);
+    s->ns = d.nh * d.nc;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return 3;
+    }
+    s->stream = s->own;
+    {
+        const size_t t_smem = sizeof(float) * 4 * (d.L + 1) * TRANSPORT_THREADS;
+        const size_t p_smem = project_smem((d.L + 1) * (d.L + 2) / 2, d.W);
+        if (cudaFuncSetAttribute(transport_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t_smem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_smem) !=
+                cudaSuccess) {
+            cudaStreamDestroy(s->own);
+            delete s;
+            return 5;
+        }
+    }
+    // FP32 SH recurrence constants
+    std::vector<float> a, b, dd;
+    sh_recurrence(d.L, a, b, dd);
+    if (dput_vec(s, s->sh_a, a) || dput_vec(s, s->sh_b, b) || dput_vec(s, s->sh_d, dd)) {
+        sosb_destroy(s);
+        return 4;
+    }
+    *out = s;
+    return 0;
+}
+
+int sosb_destroy(sosb_handle s) {
+    if (!s) return 0;
+    cudaStreamSynchronize(s->stream);
+    DevBuf* bufs[] = {&s->h, &s->chi, &s->hr, &s->ha, &s->ext, &s->asca, &s->table, &s->sun_h, &s->sun_col, &s->gm,
+                      &s->goff, &s->gdir, &s->gval, &s->rf, &s->af, &s->ext0, &s->s_ext, &s->s_sca, &s->s_chi,
+                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->sh_a, &s->sh_b, &s->sh_d,
+                      &s->u_hi, &s->u_lo, &s->wu_hi, &s->wu_lo, &s->uq_hi, &s->uq_lo, &s->wuq_hi, &s->wuq_lo,
+                      &s->box_ww, &s->solar, &s->rad, &s->plane, &s->moments, &s->flux, &s->first_moments,
+                      &s->first_flux, &s->boundary, &s->metrics, &s->boxes, &s->fx, &s->fg, &s->fn, &s->norms,
+                      &s->partials, &s->dots, &s->mixw, &s->ring_g[0], &s->ring_g[1], &s->ring_g[2], &s->ring_g[3],
+                      &s->ring_f[0], &s->ring_f[1], &s->ring_f[2], &s->ring_f[3]};
+    for (DevBuf* b : bufs) dfree(s, *b);
+    for (BundleDev* bd : {&s->cells, &s->obs}) {
+        DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
+                        &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits};
+        for (DevBuf* b : bb) dfree(s, *b);
+    }
+    if (s->own) cudaStreamDestroy(s->own);
+    delete s;
+    return 0;
+}
+
+int sosb_set_stream(sosb_handle s, void* stream) {
+    if (!s) return 1;
+    s->stream = stream ? (cudaStream_t)stream : s->own;
+    return 0;
+}
+
+int sosb_shape(sosb_handle s, int64_t* cells, int32_t* slots, int32_t* K) {
+    if (!s) return 1;
+    if (cells) *cells = s->ns;
+    if (slots) *slots = s->src;
+    if (K) *K = s->K;
+    return 0;
+}
+
+static int put_ds(sosb_state* s, DevBuf& hi, DevBuf& lo, const double* v, int n) {
+    std::vector<float> h, l;
+    split_nodes(v, n, h, l);
+    TRY(dput_vec(s, hi, h));
+    return dput_vec(s, lo, l);
+}
+
+int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
+    if (!s || !c) return 1;
+    const sosb_dims& d = s->d;
+    const int W = d.W, K = s->K, ns = s->ns;
+    if (!c->u || !c->wu || !c->uq || !c->wuq || !c->h || !c->chi || !c->hr || !c->ha || !c->ext || !c->asca ||
+        !c->density_table || !c->sun_h || !c->sun_col || !c->gm || !c->goff || !c->rf || !c->af || !c->ext0 ||
+        !c->solar || !c->box_ww)
+        return fail(s, "E_CONSTANTS: missing array");
+    if (d.strato && (!c->strato_ext || !c->strato_sca || !c->strato_chi || !c->strato_density || !c->strato_sun_col ||
+                     !c->strato_eigen || !c->strato_sca_source))
+        return fail(s, "E_CONSTANTS: missing stratospheric array");
+    TRY(put_ds(s, s->u_hi, s->u_lo, c->u, d.nq));
+    TRY(put_ds(s, s->wu_hi, s->wu_lo, c->wu, d.nq));
+    TRY(put_ds(s, s->uq_hi, s->uq_lo, c->uq, d.nq_query));
+    TRY(put_ds(s, s->wuq_hi, s->wuq_lo, c->wuq, d.nq_query));
+    TRY(dput(s, s->h, c->h, d.nh * 4));
+    TRY(dput(s, s->chi, c->chi, d.nc * 4));
+    TRY(dput(s, s->hr, c->hr, d.nh * 4));
+    TRY(dput(s, s->ha, c->ha, d.nh * 4));
+    TRY(dput(s, s->ext, c->ext, 5 * W * 4));
+    TRY(dput(s, s->asca, c->asca, W * 4));
+    TRY(dput(s, s->table, c->density_table, (size_t)d.density_rows * 3 * 4));
+    TRY(dput(s, s->sun_h, c->sun_h, d.n_sun_h * 4));
+    TRY(dput(s, s->sun_col, c->sun_col, (size_t)d.n_sun_h * d.n_sun_x * 5 * 4));
+    TRY(dput(s, s->gm, c->gm, (size_t)ns * 4 * W * 4));
+    std::vector<int> goff(ns + 1);
+    for (int i = 0; i <= ns; ++i) goff[i] = (int)c->goff[i];
+    const int ng = goff[ns];
+    TRY(dput_vec(s, s->goff, goff));
+    if (ng > 0) {
+        if (!c->gdir || !c->gval) return fail(s, "E_CONSTANTS: missing ground directions");
+        TRY(dput(s, s->gdir, c->gdir, (size_t)ng * 3 * 4));
+        TRY(dput(s, s->gval, c->gval, (size_t)ng * W * 4));
+    } else {
+        TRY(dalloc(s, s->gdir, 16));
+        TRY(dalloc(s, s->gval, 16));
+    }
+    TRY(dput(s, s->rf, c->rf, 6 * 4));
+    TRY(dput(s, s->af, c->af, K * 4));
+    TRY(dput(s, s->ext0, c->ext0, W * 4));
+    TRY(dput(s, s->solar, c->solar, W * 8));
+    TRY(dput(s, s->box_ww, c->box_ww, d.box_points * 8));
+    if (d.strato) {
+        TRY(dput(s, s->s_ext, c->strato_ext, W * 4));
+        TRY(dput(s, s->s_sca, c->strato_sca, W * 4));
+        TRY(dput(s, s->s_chi, c->strato_chi, 33 * W * 4));
+        TRY(dput(s, s->s_density, c->strato_density, d.nh * 4));
+        TRY(dput(s, s->s_sun_col, c->strato_sun_col, (size_t)d.n_sun_h * d.n_sun_x * 4));
+        TRY(dput(s, s->s_eigen, c->strato_eigen, (size_t)K * W * 4));
+        TRY(dput(s, s->s_sca_src, c->strato_sca_source, W * 4));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->have_constants = true;
+    s->have_first = false;
+    return 0;
+}
+
+int sosb_set_bundle(sosb_handle s, int which, const sosb_bundle* b) {
+    if (!s || !b) return 1;
+    if (which != SOSB_CELLS && which != SOSB_OBSERVER) return fail(s, "E_BUNDLE: unknown bundle %d", which);
+    if (which == SOSB_CELLS && b->ncell != s->ns)
+        return fail(s, "E_SHAPE: cell bundle has %d cells, state %d", b->ncell, s->ns);
+    PackedBundle pk;
+    const std::string msg = pack_bundle(b, s->d.nc, pk);
+    if (!msg.empty()) return fail(s, "%s", msg.c_str());
+    BundleDev& bd = which == SOSB_CELLS ? s->cells : s->obs;
+    bd.ncell = pk.ncell;
+    bd.nray = pk.nray;
+    bd.nseg = pk.nseg;
+    bd.host_cell_off.assign(b->cell_off, b->cell_off + b->ncell + 1);
+    TRY(dput_vec(s, bd.cell_off, pk.cell_off));
+    TRY(dput_vec(s, bd.ray_cell, pk.ray_cell));
+    TRY(dput_vec(s, bd.p, pk.p));
+    TRY(dput_vec(s, bd.frame, pk.frame));
+    TRY(dput_vec(s, bd.dir, pk.dir));
+    TRY(dput_vec(s, bd.dir_lo, pk.dir_lo));
+    TRY(dput_vec(s, bd.dloc, pk.dloc));
+    TRY(dput_vec(s, bd.pcp, pk.pcp));
+    TRY(dput_vec(s, bd.seg_off, pk.seg_off));
+    TRY(dput_vec(s, bd.seg, pk.seg));
+    TRY(dput_vec(s, bd.lower, pk.lower));
+    TRY(dput_vec(s, bd.end_j, pk.end_j));
+    TRY(dput_vec(s, bd.end_col, pk.end_col));
+    TRY(dput_vec(s, bd.hits, pk.hits));
+    CK(cudaStreamSynchronize(s->stream));
+    if (which == SOSB_CELLS) s->have_first = false;
+    return 0;
+}
+
+int sosb_evaluate(sosb_handle s, int phase, int first, const float* field_dev, const float* boundary_dev,
+                  float* moments_dev, float* flux_dev, float* radiance_dev) {
+    if (!s) return 1;
+    if (phase < 0 || phase > 2) return fail(s, "E_PHASE: %d", phase);
+    if (!first && !field_dev) return fail(s, "E_FIELD: warm transport needs a field");
+    if (first && phase == 1) return fail(s, "E_PHASE: first light has no ground pass");
+    s->err.clear();
+    TRY(evaluate_impl(s, phase, first, field_dev, boundary_dev, moments_dev, flux_dev, radiance_dev));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int sosb_apply(sosb_handle s, const float* field_dev, float* out_dev) {
+    if (!s) return 1;
+    if (!field_dev || !out_dev) return fail(s, "E_FIELD: null field");
+    s->err.clear();
+    TRY(apply_impl(s, field_dev, out_dev, 0ull));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int sosb_boxes(sosb_handle s, const float* field_dev, double* out_host) {
+    if (!s) return 1;
+    if (!field_dev || !out_host) return fail(s, "E_FIELD: null pointer");
+    s->err.clear();
+    return boxes_impl(s, field_dev, out_host);
+}
+
+// Solve the regularised Gram system (FP64, partial pivoting); weights normalised to sum 1 and rejected unless finite
+// with max |w| < 8 (source_iteration.py:25-33). Returns false when singular or rejected.
+static bool anderson_weights(int n, const double* G, float* out) {
+    double A[4][5];
+    double tr = 0.0;
+    for (int i = 0; i < n; ++i) tr += G[i * n + i];
+    const double reg = std::max(tr * 1e-10, 1e-30);
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) A[i][j] = G[i * n + j] + (i == j ? reg : 0.0);
+        A[i][n] = 1.0;
+    }
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(A[r][c]) > std::fabs(A[piv][c])) piv = r;
+        if (A[piv][c] == 0.0) return false;
+        if (piv != c)
+            for (int j = 0; j <= n; ++j) std::swap(A[c][j], A[piv][j]);
+        for (int r = c + 1; r < n; ++r) {
+            const double f = A[r][c] / A[c][c];
+            for (int j = c; j <= n; ++j) A[r][j] -= f * A[c][j];
+        }
+    }
+    double x[4];
+    for (int i = n - 1; i >= 0; --i) {
+        double v = A[i][n];
+        for (int j = i + 1; j < n; ++j) v -= A[i][j] * x[j];
+        x[i] = v / A[i][i];
+    }
+    double sum = 0.0;
+    for (int i = 0; i < n; ++i) sum += x[i];
+    double mx = 0.0;
+    for (int i = 0; i < n; ++i) {
+        x[i] /= sum;
+        if (!std::isfinite(x[i])) return false;
+        mx = std::max(mx, std::fabs(x[i]));
+    }
+    if (!(mx < 8.0)) return false;
+    for (int i = 0; i < n; ++i) out[i] = (float)x[i];
+    return true;
+}
+
+int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, float* x_out, int x_out_is_device,
+               sosb_stats* stats) {
+    if (!s) return 1;
+    if (!x_out) return fail(s, "E_FIELD: null output");
+    s->err.clear();
+    const auto t_start = std::chrono::steady_clock::now();
+    const int64_t launches0 = s->launches;
+    TRY(check_ready(s, true));
+    const sosb_dims& d = s->d;
+    const int W = d.W;
+    const size_t n = (size_t)s->ns * s->src * W;
+    const size_t bytes = n * sizeof(float);
+    TRY(dalloc(s, s->fx, bytes));
+    TRY(dalloc(s, s->fg, bytes));
+    TRY(dalloc(s, s->fn, bytes));
+    for (int j = 0; j < 4; ++j) {
+        TRY(dalloc(s, s->ring_g[j], bytes));
+        TRY(dalloc(s, s->ring_f[j], bytes));
+    }
+    TRY(dalloc(s, s->norms, (size_t)s->ns * W * sizeof(float)));
+    TRY(dalloc(s, s->mixw, (size_t)(4 * W) * sizeof(float) + 64 * sizeof(int)));
+    const int fthreads = 256;
+    // the feature kernel's grid stride must be a multiple of W (one wavelength per thread)
+    int q_w = W;
+    for (int a = 256, b = W; b;) {
+        const int t = a % b;
+        a = b;
+        b = t;
+        if (!b) q_w = W / a;
+    }
+    int fblocks = std::max(1, std::min(152 * 8, (int)((n + 255) / 256)));
+    fblocks = std::max(q_w, (fblocks / q_w) * q_w);
+    TRY(dalloc(s, s->partials, (size_t)fblocks * 4 * W * sizeof(double)));
+    TRY(dalloc(s, s->dots, (size_t)4 * W * sizeof(double)));
+    if (x0_host)
+        CK(cudaMemcpyAsync(s->fx.p, x0_host, bytes, cudaMemcpyHostToDevice, s->stream));
+    else
+        CK(cudaMemsetAsync(s->fx.p, 0, bytes, s->stream));
+    float* x = P<float>(s->fx);
+    float* g = P<float>(s->fg);
+    float* nxt = P<float>(s->fn);
+    const int rows = d.n_monitor_rows, stop = d.monitors, dirs = d.n_dirs;
+    const int nbox = rows * dirs * W;
+    std::vector<double> old_b(nbox), new_b(nbox);
+    std::vector<unsigned> met(3 * W);
+    std::vector<int> done(W, 0);
+    // ring bookkeeping shared by all active wavelengths: slots in age order (oldest first)
+    std::vector<int> order;
+    std::vector<double> gram(W * 16, 0.0);                 // [w][slot][slot]
+    std::vector<float> obs(4 * W * 64, 0.0f);               // [slot][w][stop*dirs]
+    std::vector<double> dots(4 * W);
+    std::vector<float> weights(4 * W);
+    std::vector<int> use(64);
+    const int nfeat_obs = stop * dirs;
+    const double obs_scale = std::sqrt((double)((size_t)s->ns * s->src) / (double)nfeat_obs);
+    int it = 0;
+    bool all_done = false;
+    std::vector<double> rr(W), ss(W);
+    for (it = 1; it <= max_eval; ++it) {
+        TRY(boxes_impl(s, x, old_b.data()));
+        unsigned long long mask = 0;
+        for (int w = 0; w < W; ++w)
+            if (done[w]) mask |= 1ull << w;
+        TRY(apply_impl(s, x, g, mask));
+        CK(cudaMemcpyAsync(met.data(), s->metrics.p, 3 * W * sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        long long bad = 0;
+        for (int w = 0; w < W; ++w) bad += met[w];
+        if (bad) return fail(s, "E_NONFINITE_SOURCE: %lld values after evaluation %d", bad, it);
+        TRY(boxes_impl(s, g, new_b.data()));
+        for (int w = 0; w < W; ++w) {
+            double r = 0.0;
+            for (int i = 0; i < stop * dirs; ++i) {
+                const double nv = new_b[i * W + w], ov = old_b[i * W + w];
+                r = std::max(r, std::fabs(nv - ov) / std::max(std::fabs(nv), 1e-30));
+            }
+            float mg, df;
+            std::memcpy(&mg, &met[W + w], 4);
+            std::memcpy(&df, &met[2 * W + w], 4);
+            rr[w] = r;
+            ss[w] = (double)(df / std::max(mg, 1e-30f));
+            if (it >= 2 && std::max(r, ss[w]) <= tol) done[w] = 1;
+        }
+        all_done = std::all_of(done.begin(), done.end(), [](int v) { return v != 0; });
+        if (all_done) {
+            std::swap(x, g);
+            break;
+        }
+        // Anderson: new ring slot for g and its residual feature
+        int slot;
+        if ((int)order.size() < 4) {
+            slot = (int)order.size();
+        } else {
+            slot = order.front();
+            order.erase(order.begin());
+        }
+        order.push_back(slot);
+        CK(cudaMemcpyAsync(s->ring_g[slot].p, g, bytes, cudaMemcpyDeviceToDevice, s->stream));
+        CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
+        norm_kernel<<<grid_for((long long)s->ns * W, 256), 256, 0, s->stream>>>(g, s->ns, s->src, W, P<float>(s->norms),
+                                                                              P<unsigned>(s->metrics));
+        TRY(launch_check(s));
+        const int m = (int)order.size();
+        const float* rp[4] = {nullptr, nullptr, nullptr, nullptr};
+        for (int j = 0; j < m; ++j) rp[j] = P<float>(s->ring_f[order[j]]);
+        const int fb = fblocks;
+        const int per = fthreads;
+        feature_kernel<<<fb, per, (size_t)m * W * sizeof(double), s->stream>>>(
+            g, x, P<float>(s->norms), P<unsigned>(s->metrics), s->src, W, (long long)n, P<float>(s->ring_f[slot]), rp[0],
+            rp[1], rp[2], rp[3], m, P<double>(s->partials));
+        TRY(launch_check(s));
+        sum_partials_kernel<<<(m * W + 127) / 128, 128, 0, s->stream>>>(P<double>(s->partials), fb, m * W,
+                                                                         P<double>(s->dots));
+        TRY(launch_check(s));
+        CK(cudaMemcpyAsync(dots.data(), s->dots.p, (size_t)m * W * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (int w = 0; w < W; ++w) {
+            use[w] = 0;
+            if (done[w]) continue;
+            float* ob = &obs[((size_t)slot * W + w) * 64];
+            for (int i = 0; i < nfeat_obs; ++i) {
+                const double nv = new_b[i * W + w], ov = old_b[i * W + w];
+                ob[i] = (float)((nv - ov) / std::max(std::fabs(nv), 1e-20) * obs_scale);
+            }
+            for (int j = 0; j < m; ++j) {
+                const float* oj = &obs[((size_t)order[j] * W + w) * 64];
+                double v = dots[j * W + w];
+                for (int i = 0; i < nfeat_obs; ++i) v += (double)ob[i] * (double)oj[i];
+                gram[w * 16 + slot * 4 + order[j]] = v;
+                gram[w * 16 + order[j] * 4 + slot] = v;
+            }
+            if (m > 1) {
+                double G[16];
+                for (int i = 0; i < m; ++i)
+                    for (int j = 0; j < m; ++j) G[i * m + j] = gram[w * 16 + order[i] * 4 + order[j]];
+                float wt[4];
+                if (anderson_weights(m, G, wt)) {
+                    use[w] = 1;
+                    for (int j = 0; j < m; ++j) weights[j * W + w] = wt[j];
+                }
+            }
+        }
+        CK(cudaMemcpyAsync(s->mixw.p, weights.data(), 4 * W * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(P<char>(s->mixw) + 4 * W * sizeof(float), use.data(), W * sizeof(int), cudaMemcpyHostToDevice,
+                           s->stream));
+        const float* q[4] = {nullptr, nullptr, nullptr, nullptr};
+        for (int j = 0; j < m; ++j) q[j] = P<float>(s->ring_g[order[j]]);
+        mix_kernel<<<grid_for((long long)n, 256), 256, 0, s->stream>>>(
+            g, q[0], q[1], q[2], q[3], m, P<float>(s->mixw),
+            reinterpret_cast<const int*>(P<char>(s->mixw) + 4 * W * sizeof(float)), W, (long long)n, nxt);
+        TRY(launch_check(s));
+        std::swap(x, nxt);
+    }
+    if (it > max_eval) it = max_eval;
+    if (x_out_is_device)
+        CK(cudaMemcpyAsync(x_out, x, bytes, cudaMemcpyDeviceToDevice, s->stream));
+    else
+        CK(cudaMemcpyAsync(x_out, x, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (stats) {
+        std::memset(stats, 0, sizeof *stats);
+        stats->evaluations = it;
+        stats->converged = all_done ? 1 : 0;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        for (int w = 0; w < W; ++w) {
+            stats->observer_relative[w] = rr[w];
+            stats->source_relative[w] = ss[w];
+            stats->done[w] = done[w];
+        }
+        stats->kernel_launches = s->launches - launches0;
+    }
+    if (!all_done) {
+        int nd = 0;
+        for (int w = 0; w < W; ++w) nd += done[w];
+        return fail(s, "E_NOT_CONVERGED: %d/%d within %g", nd, W, tol);
+    }
+    return 0;
+}
+
+}  // extern "C"

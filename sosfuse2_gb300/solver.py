@@ -1,0 +1,191 @@
+"""The `b200` backend: a Kernel and a Solver with the reference's interface, over libsosb (C ABI, sm_103a).
+
+`Kernel` stands where the reference's `source_solver.Kernel` stands (src/sosfuse2/solve/source_solver.py:1109-2484):
+it owns the device copy of one state's constants and ray bundles and runs `launch` (phases 0, 1, 2 and first light)
+and the observer `transport`. `Solver` stands where `source_iteration.Solver` stands
+(src/sosfuse2/solve/source_iteration.py:100-663): `initialize`, `apply`, `boxes` and `solve(max_eval, tolerance)`
+with the same return values and the same error codes (E_NONFINITE_SOURCE, E_NOT_CONVERGED).
+
+Device buffers are torch CUDA tensors; every call runs on torch's current stream. There is no CPU path: without a
+GPU or without the built library the constructor raises.
+"""
+
+import ctypes
+import time
+
+import numpy as np
+
+from . import _abi
+from .state import PackedState
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError('E_CUDA_DEVICE: no CUDA device (the b200 backend has no CPU path)')
+    return torch
+
+
+class Kernel:
+    """Device-resident state of one packed state (constants, cell bundle, observer bundle)."""
+
+    backend = 'b200'
+
+    def __init__(self, state, device=None, library=None):
+        torch = _torch()
+        self.torch = torch
+        self.state = state if isinstance(state, PackedState) else PackedState(state)
+        self.device = torch.device(device or 'cuda')
+        self.lib = _abi.library(library)
+        st = self.state
+        self.L, self.K, self.W = st.L, st.K, st.W
+        self.deterministic = True
+        self._dims = st.dims()
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            rc = self.lib.sosb_create(ctypes.byref(self._dims), ctypes.byref(handle))
+            if rc:
+                raise RuntimeError(f'E_CREATE: sosb_create returned {rc}')
+            self.h = handle
+            self._check(self.lib.sosb_set_stream(self.h, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+            self._check(self.lib.sosb_set_constants(self.h, ctypes.byref(st.constants())))
+            self._check(self.lib.sosb_set_bundle(self.h, _abi.CELLS, ctypes.byref(st.abi_bundle('cell'))))
+            self._check(self.lib.sosb_set_bundle(self.h, _abi.OBSERVER, ctypes.byref(st.abi_bundle('query'))))
+        st._keep.clear()
+        self.n_query = len(st['query_d'])
+        self.n_rays = len(st['cell_d'])
+
+    def _check(self, rc):
+        if rc:
+            msg = self.lib.sosb_last_error(self.h).decode()
+            if msg.startswith('E_NONFINITE_SOURCE') or msg.startswith('E_NOT_CONVERGED'):
+                raise RuntimeError(msg)
+            raise RuntimeError(msg or f'E_NATIVE: status {rc}')
+
+    def close(self):
+        if getattr(self, 'h', None):
+            self.lib.sosb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ reference Kernel surface
+    def _stream(self):
+        self.lib.sosb_set_stream(self.h, ctypes.c_void_p(self.torch.cuda.current_stream(self.device).cuda_stream))
+
+    def field(self, value=None):
+        """A device field [cells, slots, W] (zeros, or a copy of `value`)."""
+        if value is None:
+            return self.torch.zeros(self.state.shape, dtype=self.torch.float32, device=self.device)
+        return self.torch.as_tensor(np.ascontiguousarray(value, np.float32), device=self.device).contiguous()
+
+    def _dev(self, t):
+        if t is None:
+            return None
+        if not (t.is_cuda and t.dtype == self.torch.float32 and t.is_contiguous()):
+            raise ValueError('E_LAYOUT: expected a contiguous float32 CUDA tensor')
+        return ctypes.c_void_p(t.data_ptr())
+
+    def launch(self, phase, first=False, field=None, boundary=None, radiance=False):
+        """Kernel.launch: (moments [cells, 4+K, W], flux [cells, W], radiance [rays, W, 4]) for the phase; phase 0
+        also returns the per-ray radiance of the cell rays when `radiance`."""
+        torch = self.torch
+        st = self.state
+        self._stream()
+        f32 = dict(dtype=torch.float32, device=self.device)
+        moments = flux = rad = None
+        if phase == 0:
+            moments = torch.empty((st.ns, 4 + self.K, self.W), **f32)
+            flux = torch.empty((st.ns, self.W), **f32)
+            if radiance:
+                rad = torch.empty((self.n_rays, self.W, 4), **f32)
+        elif phase == 1:
+            flux = torch.empty((st.nc, self.W), **f32)
+        else:
+            rad = torch.empty((self.n_query, self.W, 4), **f32)
+        self._check(self.lib.sosb_evaluate(self.h, phase, int(bool(first)), self._dev(field), self._dev(boundary),
+                                           self._dev(moments), self._dev(flux), self._dev(rad)))
+        return moments, flux, rad
+
+    def transport(self, field, first=False):
+        """Observer-ray radiance [rays, W, 4] (Kernel.transport of the observer rays)."""
+        return self.launch(2, first, field)[2]
+
+    def host(self, t):
+        return t.detach().cpu().numpy()
+
+    def sync(self):
+        self.torch.cuda.synchronize(self.device)
+
+    def memory(self):
+        return self.torch.cuda.max_memory_allocated(self.device)
+
+
+class Solver:
+    """source_iteration.Solver over the b200 Kernel."""
+
+    def __init__(self, state, kernel=None, device=None):
+        self.kernel = kernel or Kernel(state, device)
+        self.state = self.kernel.state
+        self.first_moments = None
+        self.first_flux = None
+        self.timings = dict(apply_seconds=[], setup_seconds=0.0)
+
+    def initialize(self):
+        if self.first_moments is None:
+            t = time.perf_counter()
+            self.first_moments, self.first_flux, _ = self.kernel.launch(0, True)
+            self.timings['setup_seconds'] = time.perf_counter() - t
+
+    def apply(self, field):
+        k = self.kernel
+        k._stream()
+        out = k.torch.empty_like(field)
+        t = time.perf_counter()
+        k._check(k.lib.sosb_apply(k.h, k._dev(field), k._dev(out)))
+        self.timings['apply_seconds'].append(time.perf_counter() - t)
+        return out
+
+    def boxes(self, field):
+        k = self.kernel
+        k._stream()
+        rows = k._dims.n_monitor_rows
+        out = np.empty((rows, k._dims.n_dirs, k.W), np.float64)
+        k._check(k.lib.sosb_boxes(k.h, k._dev(field), out.ctypes.data_as(_abi.P_f64)))
+        return out
+
+    def solve(self, max_eval=16, tolerance=0.005, initial=None, device_out=False):
+        """Solver.solve: (field, stats). The field is a host array unless device_out (then a CUDA tensor)."""
+        k = self.kernel
+        k._stream()
+        st = self.state
+        stats = _abi.Stats()
+        x0 = None if initial is None else np.ascontiguousarray(initial, np.float32)
+        if device_out:
+            out = k.field()
+            out_ptr = ctypes.c_void_p(out.data_ptr())
+        else:
+            out = np.empty(st.shape, np.float32)
+            out_ptr = out.ctypes.data_as(ctypes.c_void_p)
+        t = time.perf_counter()
+        rc = k.lib.sosb_solve(k.h, int(max_eval), float(tolerance),
+                              None if x0 is None else x0.ctypes.data_as(ctypes.c_void_p), out_ptr, int(device_out),
+                              ctypes.byref(stats))
+        seconds = time.perf_counter() - t
+        self.last_stats = stats
+        k._check(rc)
+        W = k.W
+        return out, dict(
+            seconds=seconds,
+            evaluations=int(stats.evaluations),
+            tolerance=tolerance,
+            converged=[bool(stats.done[w]) for w in range(W)],
+            observer_relative=[float(stats.observer_relative[w]) for w in range(W)],
+            source_relative=[float(stats.source_relative[w]) for w in range(W)],
+            kernel_launches=int(stats.kernel_launches),
+        )

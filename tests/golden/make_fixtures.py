@@ -2,7 +2,7 @@
 
 Run in this container only (it imports the reference NumPy implementation from its source tree):
 
-    python tests/golden/make_fixtures.py [walk1|strato3|all]
+    python tests/golden/make_fixtures.py [walk1|strato1|strato15|all]
 
 Each fixture is one small state on the reference's reduced grid (4 heights x 10 solar zenith nodes = 40 cells,
 nmu 1, nphi 2, path_n 4, L=16), built by the reference's own assembly (`create_configured` and
@@ -35,8 +35,10 @@ REFERENCE_SRC = Path('/root/reference/src')
 FIXTURES = dict(
     # the walkthrough state: clear_34 parameters, exp8 air / triangle ozone, O4 off, no stratospheric layer
     walk1=dict(strato=False, wavelengths=[550.0]),
-    # the same state with its Gaussian stratospheric sulfate layer (21 km, sigma 3 km) and three wavelengths
-    strato3=dict(strato=True, wavelengths=[450.0, 550.0, 650.0]),
+    # the same state with its Gaussian stratospheric sulfate layer (21 km, sigma 3 km)
+    strato1=dict(strato=True, wavelengths=[550.0]),
+    # the stratospheric state over one 15-wavelength chunk (the reference kernel takes 1 or 15 wavelengths)
+    strato15=dict(strato=True, wavelengths=(360 + (np.arange(15) + 0.5) * 470 / 15).tolist()),
 )
 
 

@@ -1,0 +1,65 @@
+"""The C ABI without a GPU: libsosb builds for sm_103a, loads, exports every entry point include/sosb.h declares,
+and the ctypes mirror (sosfuse2_gb300._abi) lays its structs out field for field like the header."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from conftest import ROOT
+from sosfuse2_gb300 import _abi, build
+
+HEADER = (ROOT / 'include' / 'sosb.h').read_text()
+
+
+def declared_functions():
+    return sorted(set(re.findall(r'^\s*(?:int|const char \*)\s*(sosb_\w+)\s*\(', HEADER, re.M)))
+
+
+def header_struct_fields(name):
+    body = re.search(r'typedef struct \{([^}]*)\}\s*' + name + ';', HEADER).group(1)
+    body = re.sub(r'/\*.*?\*/', '', body, flags=re.S)
+    fields = []
+    for decl in body.split(';'):
+        decl = decl.strip()
+        if not decl:
+            continue
+        decl = re.sub(r'^(const\s+)?\w+\s*', '', decl)
+        for part in decl.split(','):
+            nm = re.sub(r'[\s*]|\[.*\]', '', part)
+            if nm:
+                fields.append(nm)
+    return fields
+
+
+@pytest.fixture(scope='module')
+def lib():
+    path = build.build()
+    return ctypes.CDLL(str(path))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 12
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(_abi.SIGNATURES)
+
+
+def test_version_string(lib):
+    lib.sosb_version.restype = ctypes.c_char_p
+    assert lib.sosb_version().decode().endswith('sm_103a')
+
+
+@pytest.mark.parametrize('cname,pytype', [('sosb_dims', _abi.Dims), ('sosb_constants', _abi.Constants),
+                                           ('sosb_bundle', _abi.Bundle), ('sosb_stats', _abi.Stats)])
+def test_struct_layout_matches_header(cname, pytype):
+    assert header_struct_fields(cname) == [f[0] for f in pytype._fields_]
+
+
+def test_null_handle_is_an_error(lib):
+    lib.sosb_last_error.restype = ctypes.c_char_p
+    lib.sosb_last_error.argtypes = [ctypes.c_void_p]
+    assert lib.sosb_last_error(None).startswith(b'E_HANDLE')
+    assert lib.sosb_destroy(None) == 0

@@ -1,0 +1,85 @@
+"""CUDA path (libsosb through the C ABI) against the reference's golden outputs on the same packed states.
+
+Tolerances, the reference's numeric gate (src/sosfuse2/checks/gate.py:659-686): radiance and moments rtol 1e-3 on
+every element above 1e-6 of the array maximum (and 1e-5 of the maximum overall); converged source relative L2
+<= 1e-3 per wavelength; observer radiance of the converged source rtol 1e-3.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, fixture_names, ray_index, rel_l2_per_wave, rel_max
+
+pytestmark = pytest.mark.gpu
+
+
+def close(a, ref, rtol=1e-3, floor=1e-6, overall=1e-5):
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    scale = max(float(np.max(np.abs(ref))), 1e-300)
+    big = np.abs(ref) > floor * scale
+    worst = float(np.max(np.abs(a - ref))) / scale
+    assert worst <= overall, f'max error {worst:.3g} of the maximum'
+    bad = np.abs(a[big] - ref[big]) > rtol * np.abs(ref[big])
+    assert not bad.any(), f'{bad.sum()} elements beyond rtol {rtol}'
+
+
+@pytest.fixture(scope='module', params=fixture_names())
+def solver(request):
+    import torch
+
+    from sosfuse2_gb300.solver import Solver
+    from sosfuse2_gb300.state import PackedState
+
+    s = Solver(PackedState(GOLDEN / f'{request.param}.npz'), device='cuda:0')
+    yield s
+    s.kernel.close()
+    torch.cuda.synchronize()
+
+
+def test_first_light(solver):
+    st = solver.state
+    m, f, _ = solver.kernel.launch(0, True)
+    close(m.cpu().numpy(), st['first_moments'])
+    close(f.cpu().numpy(), st['first_flux'])
+
+
+def test_warm_and_query_radiance(solver):
+    k, st = solver.kernel, solver.state
+    g1 = k.field(st['apply_zero'])
+    boundary = k.torch.as_tensor(np.ascontiguousarray(st['pin_boundary'], np.float32), device=k.device)
+    _, _, rad = k.launch(0, False, g1, boundary, radiance=True)
+    idx = ray_index(st, st['pin_cells'])
+    close(rad.cpu().numpy()[idx], st['pin_warm'])
+    close(k.transport(g1).cpu().numpy(), st['pin_query'])
+
+
+def test_apply_and_boxes(solver):
+    k, st = solver.kernel, solver.state
+    zero = k.field()
+    g1 = solver.apply(zero)
+    close(g1.cpu().numpy(), st['apply_zero'])
+    close(solver.apply(k.field(st['apply_zero'])).cpu().numpy(), st['apply_g1'])
+    close(solver.boxes(zero), st['boxes_zero'])
+    close(solver.boxes(k.field(st['apply_zero'])), st['boxes_g1'])
+
+
+def test_solve_matches_reference(solver):
+    st = solver.state
+    x, stats = solver.solve(int(st.meta['max_eval']), float(st.meta['tolerance']))
+    assert stats['converged'] == [True] * st.W
+    assert abs(stats['evaluations'] - st.meta['evaluations']) <= 2
+    assert np.all(rel_l2_per_wave(x, st['solve_x']) <= 1e-3)
+    b = solver.boxes(solver.kernel.field(x))
+    assert rel_max(b, st['solve_boxes']) <= 1e-3
+    assert stats['kernel_launches'] > 0
+
+
+def test_solve_errors(solver):
+    st = solver.state
+    with pytest.raises(RuntimeError, match='E_NOT_CONVERGED'):
+        solver.solve(2, 1e-9)
+    bad = np.zeros(st.shape, np.float32)
+    bad[0, 10, 0] = np.nan
+    with pytest.raises(RuntimeError, match='E_NONFINITE_SOURCE'):
+        solver.solve(3, 1e-3, initial=bad)

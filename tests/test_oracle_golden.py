@@ -1,0 +1,72 @@
+"""The oracle against the reference's golden outputs (tests/golden/*.npz, made by tests/golden/make_fixtures.py).
+
+Tolerances: the oracle restates the reference's FP32 arithmetic operation for operation, so the per-ray transport
+and projection agree to a few FP32 ulps; the solve may take a different FP32 Gram rounding, so the converged field
+is held to the reference's numeric gate (source relative L2 <= 1e-3 per wavelength, radiance rtol 1e-3).
+"""
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, fixture_names, ray_index, rel_l2_per_wave, rel_max
+from oracle import sos_oracle as so
+
+
+@pytest.fixture(scope='module', params=fixture_names())
+def pack(request):
+    return so.StatePack(GOLDEN / f'{request.param}.npz')
+
+
+def _cells(pk, cells):
+    b = pk.bundle('cell')
+    idx = ray_index(pk, cells)
+    out = dict(b)
+    off = b['cell_off']
+    new_off = np.r_[0, np.cumsum([off[i + 1] - off[i] for i in cells])]
+    segs = [np.arange(b['seg_off'][r], b['seg_off'][r + 1]) for r in idx]
+    seg_idx = np.concatenate(segs)
+    out.update(cell_off=new_off, p=b['p'][cells], target=b['target'][cells],
+               seg_off=np.r_[0, np.cumsum([len(s) for s in segs])], seg_a=b['seg_a'][seg_idx],
+               seg_b=b['seg_b'][seg_idx], seg_lower=b['seg_lower'][seg_idx],
+               **{k: b[k][idx] for k in ('d', 'dloc', 'weight', 'end_j', 'end_f', 'end_col', 'end_st', 'hits')})
+    return out
+
+
+def test_transport_pins(pack):
+    cells = list(pack['pin_cells'])
+    b = _cells(pack, cells)
+    zero = np.zeros((pack.ns, pack.source_size, pack.W), np.float32)
+    assert rel_max(so.transport(pack, b, zero, True), pack['pin_first']) < 1e-6
+    warm = so.transport(pack, b, pack['apply_zero'], False, pack['pin_boundary'])
+    assert rel_max(warm, pack['pin_warm']) < 1e-6
+    q = so.transport(pack, pack.bundle('query'), pack['apply_zero'], False, query=True)
+    assert rel_max(q, pack['pin_query']) < 1e-6
+
+
+def test_projection_pin(pack):
+    b = _cells(pack, [5])
+    rad = so.transport(pack, b, pack['apply_zero'], False, pack['pin_boundary'])
+    m, f = so.project(pack, b, rad)
+    assert rel_max(m[0], pack['pin_project_moments']) < 1e-6
+    assert rel_max(f[0], pack['pin_project_flux']) < 1e-6
+
+
+def test_apply_and_boxes(pack):
+    o = so.Oracle(pack)
+    o.initialize()
+    assert rel_max(o.first_moments, pack['first_moments']) < 1e-6
+    assert rel_max(o.first_flux, pack['first_flux']) < 1e-6
+    zero = np.zeros((pack.ns, pack.source_size, pack.W), np.float32)
+    assert rel_max(o.apply(zero), pack['apply_zero']) < 1e-6
+    assert rel_max(o.apply(pack['apply_zero']), pack['apply_g1']) < 1e-6
+    assert rel_max(o.boxes(zero), pack['boxes_zero']) < 1e-6
+    assert rel_max(o.boxes(pack['apply_zero']), pack['boxes_g1']) < 1e-6
+
+
+def test_solve_matches_reference():
+    pk = so.StatePack(GOLDEN / 'walk1.npz')
+    x, stats = so.Oracle(pk).solve()
+    assert stats['converged'] == [True] * pk.W
+    assert abs(stats['evaluations'] - pk.meta['evaluations']) <= 1
+    assert np.all(rel_l2_per_wave(x, pk['solve_x']) <= 1e-3)
+    assert rel_max(so.boxes(pk, x), pk['solve_boxes']) <= 1e-3
