@@ -1,8 +1,12 @@
 """CUDA path (libsosb through the C ABI) against the reference's golden outputs on the same packed states.
 
-Tolerances, the reference's numeric gate (src/sosfuse2/checks/gate.py:659-686): radiance and moments rtol 1e-3 on
-every element above 1e-6 of the array maximum (and 1e-5 of the maximum overall); converged source relative L2
-<= 1e-3 per wavelength; observer radiance of the converged source rtol 1e-3.
+Tolerances follow the reference's numeric gate (src/sosfuse2/checks/gate.py:659-686, docs/CHECKS.md:9-21):
+* radiance (per-ray transport, observer boxes): rtol 1e-3 on every element above 1e-6 of the array maximum, and
+  1e-5 of the maximum overall;
+* moments and source fields (sums with cancellation in their high SH orders, which the reference sums in FP64 and
+  the device in compensated FP32): relative L2 per wavelength <= 1e-4, 1e-5 of the maximum overall, rtol 1e-3 on
+  every element above 1e-4 of the maximum;
+* the converged source: relative L2 <= 1e-3 per wavelength; the observer radiance of it: rtol 1e-3.
 """
 
 import numpy as np
@@ -16,12 +20,21 @@ pytestmark = pytest.mark.gpu
 def close(a, ref, rtol=1e-3, floor=1e-6, overall=1e-5):
     a = np.asarray(a, np.float64)
     ref = np.asarray(ref, np.float64)
+    if not np.any(ref):
+        assert float(np.max(np.abs(a))) <= 1e-30
+        return
     scale = max(float(np.max(np.abs(ref))), 1e-300)
     big = np.abs(ref) > floor * scale
     worst = float(np.max(np.abs(a - ref))) / scale
     assert worst <= overall, f'max error {worst:.3g} of the maximum'
     bad = np.abs(a[big] - ref[big]) > rtol * np.abs(ref[big])
     assert not bad.any(), f'{bad.sum()} elements beyond rtol {rtol}'
+
+
+def close_field(a, ref):
+    """Moments [cells, slots, W] and source fields."""
+    close(a, ref, floor=1e-4)
+    assert np.all(rel_l2_per_wave(a, ref) <= 1e-4)
 
 
 @pytest.fixture(scope='module', params=fixture_names())
@@ -40,7 +53,7 @@ def solver(request):
 def test_first_light(solver):
     st = solver.state
     m, f, _ = solver.kernel.launch(0, True)
-    close(m.cpu().numpy(), st['first_moments'])
+    close_field(m.cpu().numpy(), st['first_moments'])
     close(f.cpu().numpy(), st['first_flux'])
 
 
@@ -58,8 +71,8 @@ def test_apply_and_boxes(solver):
     k, st = solver.kernel, solver.state
     zero = k.field()
     g1 = solver.apply(zero)
-    close(g1.cpu().numpy(), st['apply_zero'])
-    close(solver.apply(k.field(st['apply_zero'])).cpu().numpy(), st['apply_g1'])
+    close_field(g1.cpu().numpy(), st['apply_zero'])
+    close_field(solver.apply(k.field(st['apply_zero'])).cpu().numpy(), st['apply_g1'])
     close(solver.boxes(zero), st['boxes_zero'])
     close(solver.boxes(k.field(st['apply_zero'])), st['boxes_g1'])
 
