@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""Benchmark: converged SOS solves per second on one GB300 (one step = one complete Solver.solve).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config 0|1]
+
+Workload: a seeded synthetic state (sosfuse2_gb300.synth) built before the timed region and made device-resident;
+each step is one complete solve (first light, evaluations until every wavelength meets the tolerance, Anderson
+mixing). `value` = solves/s with inputs resident; `e2e` = the same through the public API with host buffers (state
+upload, solve, download of the converged field). The dominant kernel is timed live with CUDA events recorded by the
+library on its own work stream; `roofline.achieved` is its algorithmic bytes per launch over its mean launch time.
+`cpu_baseline` and the `--impl reference` arm time the CPU port of the reference algorithm (oracle/) on the host
+cores, one process per core, on a bounded sample of the same workload (first light plus one evaluation per process,
+extrapolated by the GPU run's evaluation count).
+
+Multi-GPU: solves are independent, so N ranks run N replicas (weak scaling, no collective on the data path); the
+barrier and the max over ranks only bracket the timing.
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = 'converged solves/s on 1 GB300 at ≤1e-3 rel err: learned-start+batched vs plain'
+L2_BYTES = 129 << 20
+
+
+# ------------------------------------------------------------------------------------------------ helpers
+def args_():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=5)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='gb300', choices=('gb300', 'reference'))
+    p.add_argument('--config', type=int, default=0, choices=(0, 1))
+    p.add_argument('--seed', type=int, default=0)
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    return p.parse_args()
+
+
+def workload(config, seed):
+    from sosfuse2_gb300 import synth
+
+    if config == 0:
+        return synth.config0(seed=seed), ('config0: plain SOS, 550 nm, 101 heights 0-100 km x 10 solar-zenith nodes, '
+                                          'nmu 1, nphi 2, path_n 4, L=16, stratospheric layer, tolerance 1e-3')
+    return synth.config1(seed=seed), ('config1: plain SOS, 30 wavelengths 400-700 nm, 241 heights 0-120 km x 75 '
+                                      'solar-zenith nodes, nmu 12, nphi 16, path_n 12, L=32, tolerance 1e-3')
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device_index=0):
+        self.file = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(device_index), '--query-gpu=' + self.FIELDS,
+                                          '--format=csv,noheader,nounits', '-lms', '200'], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=['nvidia-smi unavailable'])
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.file.seek(0)
+        rows = [r.split(', ') for r in self.file.read().strip().splitlines() if r.count(',') >= 8]
+        os.unlink(self.file.name)
+        if not rows:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=['no samples'])
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace('.', '').isdigit()]
+        names = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap')
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.strip() == 'Active'})
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                    reasons=reasons, samples=len(rows))
+
+
+def peaks():
+    try:
+        m = json.loads((ROOT / 'MEASURED_PEAKS.json').read_text())
+        return float(m['hbm_gbs']), 'measured'
+    except (OSError, ValueError, KeyError):
+        return 6800.0, 'fallback'
+
+
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (profiles/*.txt, 'traffic_bytes_per_launch')."""
+    for f in sorted((ROOT / 'profiles').glob('*.txt')):
+        for line in f.read_text().splitlines():
+            if line.startswith(f'traffic_bytes_per_launch {kernel} '):
+                try:
+                    return float(line.split()[2])
+                except ValueError:
+                    pass
+    return None
+
+
+def transport_bytes(state):
+    """Algorithmic (compulsory) DRAM bytes of the transport launches of one solve with E evaluations:
+    per launch, each ray's geometry (48 B direction words, 16 B local direction, 4+4+4+4 B azimuth, cell, offsets,
+    end interval, 24 B end columns, 1 B hit flag), each segment (16 B ends, 1 B flag), each cell (24 B start,
+    36 B frame), the field's Rayleigh slots and SH plane read once (warm passes), the output radiance (16 B per ray
+    and wavelength). Returns bytes per launch kind: first, ground, warm, observer."""
+    a = state.arrays
+    W, K, ns, nc = state.W, state.K, state.ns, state.nc
+    def geom(prefix, cells=None):
+        off = a[prefix + '_cell_off']
+        seg = a[prefix + '_seg_off']
+        n = len(off) - 1 if cells is None else cells
+        rays = int(off[n])
+        segs = int(seg[rays])
+        return rays, rays * (48 + 16 + 16 + 24 + 1) + segs * 17 + n * 60
+    r_all, g_all = geom('cell')
+    r_gnd, g_gnd = geom('cell', nc)
+    r_obs, g_obs = geom('query')
+    field = ns * (4 + K) * W * 4
+    return dict(first=g_all + r_all * W * 16,
+                ground=g_gnd + field + r_gnd * W * 16,
+                warm=g_all + field + r_all * W * 16,
+                observer=g_obs + field + r_obs * W * 16)
+
+
+# ------------------------------------------------------------------------------------------------ CPU baseline
+def _oracle_sample(job):
+    """One process: first light and one warm pass of the oracle on a strided 1/parts share of the cells, plus the full
+    observer boxes; returns (first-light seconds, warm-pass seconds) scaled to all cells, and the boxes seconds."""
+    path, part, parts = job
+    os.environ.setdefault('OMP_NUM_THREADS', '1')
+    from oracle import sos_oracle as so
+
+    pk = so.StatePack(path)
+    cells = list(range(part, pk.ns, parts))
+    b = pk.subset(cells)
+    frac = len(b['d']) / len(pk['cell_d'])
+    x = np.zeros(pk.shape, np.float32)
+    t0 = time.perf_counter()
+    rad = so.transport(pk, b, x, first=True)
+    so.project(pk, b, rad)
+    t1 = time.perf_counter()
+    boundary = np.ones((pk.nc, pk.W))
+    rad = so.transport(pk, b, x, first=False, boundary=boundary)
+    so.project(pk, b, rad)
+    t2 = time.perf_counter()
+    so.boxes(pk, x)
+    t3 = time.perf_counter()
+    return (t1 - t0) / frac, (t2 - t1) / frac, t3 - t2
+
+
+def cpu_baseline(arrays, evaluations, procs=None):
+    """Solves/s of the CPU port over `procs` host cores, one independent solve per core: each core's solve time is
+    first light + E x (ground pass + warm pass + 2 observer passes), measured on a bounded sample (strided cell
+    shares, one per process) and extrapolated linearly by ray count."""
+    import multiprocessing as mp
+
+    procs = procs or min(os.cpu_count() or 1, 16)
+    with tempfile.NamedTemporaryFile(suffix='.npz', delete=False) as f:
+        np.savez(f, **arrays)
+        path = f.name
+    from sosfuse2_gb300.state import PackedState
+
+    st = PackedState(arrays)
+    ground_frac = float(st['cell_cell_off'][st.nc]) / float(st['cell_cell_off'][-1])
+    ctx = mp.get_context('spawn')
+    env = dict(OMP_NUM_THREADS='1', OPENBLAS_NUM_THREADS='1', MKL_NUM_THREADS='1')
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        t = time.perf_counter()
+        with ctx.Pool(procs) as pool:
+            res = pool.map(_oracle_sample, [(path, i, procs) for i in range(procs)])
+        wall = time.perf_counter() - t
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        os.unlink(path)
+    first = statistics.mean(r[0] for r in res)
+    warm = statistics.mean(r[1] for r in res)
+    boxes = statistics.mean(r[2] for r in res)
+    per_eval = warm * (1 + ground_frac) + 2 * boxes
+    solve_s = first + evaluations * per_eval
+    return dict(value=procs / solve_s, unit='solves/s', cores=procs, kind='port',
+                sample=f'{procs} processes, each: first light and one warm pass on a strided 1/{procs} share of the '
+                       f'cells plus the observer boxes ({wall:.1f} s wall); per core {first:.1f} s first light + '
+                       f'{per_eval:.2f} s per evaluation, extrapolated by ray count to {evaluations} evaluations per '
+                       f'solve'), wall
+
+
+# ------------------------------------------------------------------------------------------------ arms
+def run_reference(a, rank):
+    if rank != 0:
+        return
+    arrays, desc = workload(a.config, a.seed)
+    from sosfuse2_gb300.state import PackedState
+
+    evaluations = int(PackedState(arrays).meta.get('evaluations_hint', 12))
+    values = []
+    for _ in range(a.warmup):
+        pass  # CPU arm: nothing to warm up beyond imports
+    wall_total = 0.0
+    for _ in range(a.steps):
+        cb, wall = cpu_baseline(arrays, evaluations)
+        values.append(cb['value'])
+        wall_total += wall
+    v = statistics.mean(values)
+    cb['value'] = v
+    print(json.dumps(dict(
+        impl='reference', metric=METRIC, value=v, unit='solves/s', n_gpus=a.gpus, steps=a.steps, warmup=a.warmup,
+        ms_per_step=1e3 / v if v else None, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f32',
+        data='synthetic', config=dict(workload=desc, note='CPU port of the reference algorithm (oracle/), the '
+                                                           'reference itself being Python on the same path'),
+        cpu_baseline=cb, e2e=dict(value=v, unit='solves/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0))), flush=True)
+
+
+def run_gb300(a, rank, world):
+    import torch
+
+    from sosfuse2_gb300 import _abi, build
+    from sosfuse2_gb300.solver import Solver
+    from sosfuse2_gb300.state import PackedState
+
+    build.build()
+    local = int(os.environ.get('LOCAL_RANK', 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group('nccl')
+    arrays, desc = workload(a.config, a.seed + rank)
+    state = PackedState(arrays)
+    solver = Solver(state, device=f'cuda:{local}')
+    k = solver.kernel
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=k.device)
+    tol = float(state.meta['tolerance'])
+    max_eval = int(state.meta['max_eval'])
+    for _ in range(max(a.warmup, 0)):
+        solver.solve(max_eval, tol, device_out=True)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    k.lib.sosb_set_timing(k.h, 1)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    step_ms = []
+    evaluations = []
+    launches = 0
+    for _ in range(a.steps):
+        flush.fill_(1.0)  # L2 flush between timed solves, outside the events
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, st = solver.solve(max_eval, tol, device_out=True)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        evaluations.append(st['evaluations'])
+        launches += st['kernel_launches']
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = (_abi.c_dbl * 7)()
+    cnt = (_abi.c_i64 * 7)()
+    k.lib.sosb_get_timing(k.h, ms, cnt, 7)
+    k.lib.sosb_set_timing(k.h, 0)
+    total_ms = sum(step_ms)
+    t = torch.tensor([total_ms], device=k.device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    total_ms = float(t.item())
+    value = world * a.steps / (total_ms / 1e3)
+    # end to end through the public API: host state in, host converged field out
+    e2e_ms = []
+    h2d = sum(v.nbytes for key, v in arrays.items() if key != 'meta')
+    d2h = int(np.prod(state.shape)) * 4
+    for _ in range(max(1, min(a.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = Solver(PackedState(arrays), device=f'cuda:{local}')
+        x, _ = s2.solve(max_eval, tol)
+        torch.cuda.synchronize()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        s2.kernel.close()
+    e2e = dict(value=world / (statistics.mean(e2e_ms) / 1e3), unit='solves/s', h2d_bytes_per_step=int(h2d),
+               d2h_bytes_per_step=int(d2h))
+    if rank != 0:
+        return
+    classes = _abi.KERNEL_CLASSES
+    times = {classes[i]: dict(ms=ms[i], launches=int(cnt[i]), share=ms[i] / max(sum(ms), 1e-30)) for i in range(7)}
+    top = max(range(7), key=lambda i: ms[i])
+    E = statistics.mean(evaluations)
+    peak, peak_kind = peaks()
+    roof = None
+    if classes[top] == 'transport':
+        b = transport_bytes(state)
+        per_solve = b['first'] + E * (b['ground'] + b['warm'] + 2 * b['observer'])
+        per_solve_launches = 1 + 4 * E
+        per_launch = per_solve / per_solve_launches
+        mean_ms = ms[top] / max(cnt[top], 1)
+        achieved = per_launch / (mean_ms / 1e3) / 1e9
+        roof = dict(kernel='transport_kernel', bound='hbm', achieved=achieved, peak=peak, unit='GB/s',
+                    frac=achieved / peak, peak_source=peak_kind, traffic=profiled_traffic('transport_kernel'),
+                    bytes_per_launch=per_launch, mean_launch_ms=mean_ms)
+    cb = None
+    if world == 1 and not a.no_cpu_baseline:
+        cb, _ = cpu_baseline(arrays, int(round(E)))
+    out = dict(
+        metric=METRIC, value=value, unit='solves/s', n_gpus=world, steps=a.steps, warmup=a.warmup,
+        ms_per_step=total_ms / a.steps, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f32',
+        data='synthetic (seeded atmosphere on the reference geometry, sosfuse2_gb300.synth)',
+        config=dict(workload=desc, rays=state.meta['rays'], segments=state.meta['segments'], cells=state.ns,
+                    evaluations_per_solve=E, l2='flushed between timed solves (512 MiB write outside the events)',
+                    form='plain (no learned start, one state per launch)', parallelism=f'replicas x{world}'),
+        roofline=roof, kernel_times=times, cpu_baseline=cb, e2e=e2e, gpu_launches=int(launches), clocks=clk)
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    a = args_()
+    rank = int(os.environ.get('RANK', 0))
+    world = int(os.environ.get('WORLD_SIZE', 1))
+    if a.impl == 'reference':
+        run_reference(a, rank)
+    else:
+        run_gb300(a, rank, world)
+
+
+if __name__ == '__main__':
+    main()

@@ -134,11 +134,17 @@ int sosb_evaluate(sosb_handle h, int phase, int first, const float *field_dev, c
 int sosb_apply(sosb_handle h, const float *field_dev, float *out_dev);
 /* Replaces: Solver.boxes (source_iteration.py:218-222): observer values [n_monitor_rows][n_dirs][W] to host. */
 int sosb_boxes(sosb_handle h, const float *field_dev, double *out_host);
-/* Replaces: Solver.solve (source_iteration.py:309-663): fixed-point iteration from x0 (NULL: zero) with Anderson
- * depth 4 per wavelength. x_out is a host array [cells][slots][W] (x_out_is_device = 0) or a device pointer.
+/* Replaces: Solver.solve (source_iteration.py:309-663): first light, then the fixed-point iteration from x0 (NULL:
+ * zero) with Anderson depth 4 per wavelength. x_out is a host array [cells][slots][W] (x_out_is_device = 0) or a device pointer.
  * Returns nonzero with E_NOT_CONVERGED or E_NONFINITE_SOURCE like the reference. */
 int sosb_solve(sosb_handle h, int max_eval, double tolerance, const float *x0_host, float *x_out,
                int x_out_is_device, sosb_stats *stats);
+/* Kernel timing with CUDA events on the work stream (no counterpart in the reference's ABI; its Kernel.timed_launch,
+ * source_solver.py:1478-1523, keeps a per-kind launch log). Classes: 0 transport, 1 projection, 2 SH plane,
+ * 3 composition, 4 observer boxes, 5 Anderson, 6 other. sosb_set_timing(h, 1) starts and clears the totals;
+ * sosb_get_timing fills ms[k] and launches[k] for k < n. */
+int sosb_set_timing(sosb_handle h, int on);
+int sosb_get_timing(sosb_handle h, double *ms, int64_t *launches, int n);
 /* Message of the last failed call on this handle (empty when none). */
 const char *sosb_last_error(sosb_handle h);
 /* Sizes the handle was created with: cells, slots per cell, K. */

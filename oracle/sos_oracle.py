@@ -185,12 +185,38 @@ class StatePack:
         for k in ('L', 'K', 'W', 'nq', 'nq_query', 'nh', 'nc', 'ns', 'source_size'):
             setattr(self, k, int(self.meta[k]))
         self.strato = bool(self.meta['strato'])
+        self.shape = (self.ns, self.source_size, self.W)
+        if 'gd' not in self.arrays:
+            # ground directions given as CSR (goff, gdir, gval): pad per cell; zero values add nothing
+            goff = self.arrays['goff']
+            ng = int(np.diff(goff).max(initial=0))
+            gd = np.zeros((self.ns, max(ng, 1), 3), F)
+            gv = np.zeros((self.ns, max(ng, 1), self.W), F)
+            for c in range(self.ns):
+                a, b = goff[c], goff[c + 1]
+                gd[c, : b - a] = self.arrays['gdir'][a:b]
+                gv[c, : b - a] = self.arrays['gval'][a:b]
+            self.arrays['gd'], self.arrays['gv'] = gd, gv
 
     def __getitem__(self, key):
         return self.arrays[key]
 
     def __contains__(self, key):
         return key in self.arrays
+
+    def subset(self, cells):
+        """Cell bundle restricted to the listed cells (rays and segments of those cells, in order)."""
+        b = self.bundle('cell')
+        off = b['cell_off']
+        rays = np.concatenate([np.arange(off[i], off[i + 1]) for i in cells])
+        segs = [np.arange(b['seg_off'][r], b['seg_off'][r + 1]) for r in rays]
+        seg_idx = np.concatenate(segs) if segs else np.zeros(0, int)
+        out = dict(cell_off=np.r_[0, np.cumsum([off[i + 1] - off[i] for i in cells])], p=b['p'][cells],
+                   target=b['target'][cells], seg_off=np.r_[0, np.cumsum([len(x) for x in segs])],
+                   seg_a=b['seg_a'][seg_idx], seg_b=b['seg_b'][seg_idx], seg_lower=b['seg_lower'][seg_idx])
+        for k in ('d', 'dloc', 'weight', 'end_j', 'end_f', 'end_col', 'end_st', 'hits'):
+            out[k] = b[k][rays]
+        return out
 
     def bundle(self, prefix, cells=None):
         """Bundle dict ('cell' or 'query'); `cells` selects the first n cells (the ground pass uses nc)."""
@@ -511,10 +537,11 @@ def _sample_value(pk, r, q, field, first, phase, sphase, g, mix, hr, ha):
                 sph = (legendre_phase(np.clip(m0 + m1, F(-1), F(1)), pk['strato_chi'])
                        + legendre_phase(np.clip(m0 - m1, F(-1), F(1)), pk['strato_chi'])) / F(2)
                 swph = q['sw'][:, corner, None, None] * sph
-            for gi in range(gd.shape[1]):
-                ground += wph[:, gi, None] * gv[cells, gi]
-                if strat:
-                    sground += swph[:, gi] * gv[cells, gi]
+            # sum over the cell's ground directions (the reference adds them one by one, in the same order)
+            gvc = gv[cells]
+            ground += np.einsum('ng,ngw->nw', wph, gvc, dtype=F)
+            if strat:
+                sground += np.einsum('ngw,ngw->nw', swph, gvc, dtype=F)
         beam = (q['prof'][:, 1, None] * pk['asca']) * (sun * phase[:, None] + ground)
         if strat:
             sbeam = (q['st_prof'][:, None] * pk['strato_sca']) * (sun * sphase + sground)

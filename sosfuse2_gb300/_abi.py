@@ -23,6 +23,7 @@ P_u8 = ctypes.POINTER(ctypes.c_uint8)
 
 CELLS = 0
 OBSERVER = 1
+KERNEL_CLASSES = ('transport', 'projection', 'plane', 'composition', 'boxes', 'anderson', 'other')
 
 
 class Dims(ctypes.Structure):
@@ -75,6 +76,8 @@ SIGNATURES = {
     'sosb_boxes': ([ctypes.c_void_p, ctypes.c_void_p, P_f64], c_int),
     'sosb_solve': ([ctypes.c_void_p, c_int, c_dbl, ctypes.c_void_p, ctypes.c_void_p, c_int, ctypes.POINTER(Stats)],
                    c_int),
+    'sosb_set_timing': ([ctypes.c_void_p, c_int], c_int),
+    'sosb_get_timing': ([ctypes.c_void_p, P_f64, P_i64, c_int], c_int),
     'sosb_last_error': ([ctypes.c_void_p], ctypes.c_char_p),
     'sosb_shape': ([ctypes.c_void_p, P_i64, P_i32, P_i32], c_int),
     'sosb_version': ([], ctypes.c_char_p),

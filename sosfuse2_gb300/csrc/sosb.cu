@@ -41,8 +41,21 @@ struct BundleDev {
     std::vector<int64_t> host_cell_off;
 };
 
+// kernel classes timed by sosb_set_timing / sosb_get_timing
+enum { K_TRANSPORT = 0, K_PROJECT, K_PLANE, K_COMPOSE, K_BOXES, K_ANDERSON, K_OTHER, K_CLASSES };
+
+struct TimedLaunch {
+    int cls;
+    cudaEvent_t a, b;
+};
+
 struct sosb_state {
     sosb_dims d{};
+    bool timing = false;
+    std::vector<TimedLaunch> timed;
+    std::vector<cudaEvent_t> event_pool;
+    double timed_ms[K_CLASSES] = {0};
+    int64_t timed_count[K_CLASSES] = {0};
     int K = 0, src = 0, ns = 0;
     cudaStream_t own = nullptr, stream = nullptr;
     std::string err;
@@ -492,6 +505,48 @@ static int launch_check(sosb_state* s) {
     return 0;
 }
 
+static int take_event(sosb_state* s, cudaEvent_t& e) {
+    if (!s->event_pool.empty()) {
+        e = s->event_pool.back();
+        s->event_pool.pop_back();
+        return 0;
+    }
+    CK(cudaEventCreate(&e));
+    return 0;
+}
+
+// Brackets one kernel launch with events on the work stream when timing is on.
+struct Timer {
+    sosb_state* s;
+    int cls;
+    cudaEvent_t a = nullptr, b = nullptr;
+    Timer(sosb_state* st, int c) : s(st), cls(c) {
+        if (s->timing && take_event(s, a) == 0 && take_event(s, b) == 0) cudaEventRecord(a, s->stream);
+    }
+    ~Timer() {
+        if (s->timing && a && b) {
+            cudaEventRecord(b, s->stream);
+            s->timed.push_back(TimedLaunch{cls, a, b});
+        }
+    }
+};
+
+// Folds finished event pairs into the per-class totals.
+static int collect_timing(sosb_state* s) {
+    if (s->timed.empty()) return 0;
+    CK(cudaStreamSynchronize(s->stream));
+    for (const TimedLaunch& t : s->timed) {
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, t.a, t.b));
+        s->timed_ms[t.cls] += ms;
+        s->timed_count[t.cls] += 1;
+        s->event_pool.push_back(t.a);
+        s->event_pool.push_back(t.b);
+    }
+    s->timed.clear();
+    return 0;
+}
+
 // transport of rays [ray0, ray0 + nray) of bundle `b` into s->rad
 static int run_transport(sosb_state* s, const BundleDev& b, int64_t ray0, int64_t nray, const float* field,
                          const float* boundary, int first, bool query) {
@@ -523,6 +578,7 @@ static int run_transport(sosb_state* s, const BundleDev& b, int64_t ray0, int64_
     const long long threads = (long long)nray * wchunks << glog2;
     const long long blocks = (threads + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
     const size_t smem = sizeof(float) * 4 * (d.L + 1) * TRANSPORT_THREADS;
+    Timer timer(s, K_TRANSPORT);
     transport_kernel<<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
         optics_of(s), rays_of(b), in, (int)ray0, (int)nray, glog2, wchunks, P<float4>(s->rad));
     return launch_check(s);
@@ -537,6 +593,7 @@ static int run_project(sosb_state* s, const BundleDev& b, int ncell, bool ground
     const int per_pass = PROJ_THREADS * PROJ_OWN;
     const int passes = ground_only ? 1 : (nout + per_pass - 1) / per_pass;
     for (int pass = 0; pass < passes; ++pass) {
+        Timer timer(s, K_PROJECT);
         project_kernel<<<ncell, PROJ_THREADS, smem, s->stream>>>(optics_of(s), rays_of(b), P<float4>(s->rad), 0,
                                                                  ground_only ? 1 : 0, pass * per_pass, moments,
                                                                  pass == 0 ? flux : nullptr, flux_scale);
@@ -549,6 +606,7 @@ static int run_plane(sosb_state* s, const float* field) {
     const sosb_dims& d = s->d;
     const long long n = (long long)s->ns * s->K * d.W;
     TRY(dalloc(s, s->plane, n * sizeof(float)));
+    Timer timer(s, K_PLANE);
     plane_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(field, P<float>(s->ha), P<float>(s->s_density), d.nc, s->K,
                                                           s->src, d.W, d.strato, n, P<float>(s->plane));
     return launch_check(s);
@@ -611,14 +669,18 @@ static int apply_impl(sosb_state* s, const float* field, float* out, unsigned lo
     // ground pass over the surface cells, then the boundary = ground flux + first-light flux
     TRY(evaluate_impl(s, 1, 0, field, nullptr, nullptr, P<float>(s->flux), nullptr));
     const int nb = d.nc * d.W;
+    {
+    Timer timer(s, K_OTHER);
     add_kernel<<<(nb + 255) / 256, 256, 0, s->stream>>>(P<float>(s->flux), P<float>(s->first_flux), P<float>(s->boundary),
                                                         nb);
+    }
     TRY(launch_check(s));
     // warm pass (the plane of `field` is already current)
     TRY(run_transport(s, s->cells, 0, s->cells.nray, field, P<float>(s->boundary), 0, false));
     TRY(run_project(s, s->cells, s->ns, false, P<float>(s->moments), P<float>(s->flux)));
     CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
     const long long n = (long long)s->ns * s->src * d.W;
+    Timer timer(s, K_COMPOSE);
     compose_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(
         P<float>(s->moments), P<float>(s->first_moments), field, P<float>(s->rf), P<float>(s->af), P<float>(s->asca),
         P<float>(s->ext0), P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, done_mask, out,
@@ -636,13 +698,16 @@ static int boxes_impl(sosb_state* s, const float* field, double* out_host) {
     TRY(run_transport(s, s->obs, 0, s->obs.nray, field, nullptr, 0, true));
     const int n = d.n_monitor_rows * d.n_dirs * d.W;
     TRY(dalloc(s, s->boxes, n * sizeof(double)));
+    {
+    Timer timer(s, K_BOXES);
     boxes_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(P<float4>(s->rad), P<double>(s->box_ww), P<double>(s->solar),
                                                         d.n_monitor_rows, d.n_dirs, d.box_points, d.W,
                                                         P<double>(s->boxes));
+    }
     TRY(launch_check(s));
     CK(cudaMemcpyAsync(out_host, s->boxes.p, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    return 0;
+    return collect_timing(s);
 }
 
 // ------------------------------------------------------------------------------------------------ C ABI
@@ -711,8 +776,31 @@ int sosb_destroy(sosb_handle s) {
                         &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits};
         for (DevBuf* b : bb) dfree(s, *b);
     }
+    collect_timing(s);
+    for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
     if (s->own) cudaStreamDestroy(s->own);
     delete s;
+    return 0;
+}
+
+int sosb_set_timing(sosb_handle s, int on) {
+    if (!s) return 1;
+    TRY(collect_timing(s));
+    s->timing = on != 0;
+    for (int k = 0; k < K_CLASSES; ++k) {
+        s->timed_ms[k] = 0.0;
+        s->timed_count[k] = 0;
+    }
+    return 0;
+}
+
+int sosb_get_timing(sosb_handle s, double* ms, int64_t* launches, int n) {
+    if (!s || !ms || !launches) return 1;
+    TRY(collect_timing(s));
+    for (int k = 0; k < n && k < K_CLASSES; ++k) {
+        ms[k] = s->timed_ms[k];
+        launches[k] = s->timed_count[k];
+    }
     return 0;
 }
 
@@ -904,6 +992,7 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
     const auto t_start = std::chrono::steady_clock::now();
     const int64_t launches0 = s->launches;
     TRY(check_ready(s, true));
+    s->have_first = false;  // a solve always includes its first-light pass
     const sosb_dims& d = s->d;
     const int W = d.W;
     const size_t n = (size_t)s->ns * s->src * W;
@@ -995,20 +1084,30 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
         order.push_back(slot);
         CK(cudaMemcpyAsync(s->ring_g[slot].p, g, bytes, cudaMemcpyDeviceToDevice, s->stream));
         CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
-        norm_kernel<<<grid_for((long long)s->ns * W, 256), 256, 0, s->stream>>>(g, s->ns, s->src, W, P<float>(s->norms),
-                                                                              P<unsigned>(s->metrics));
+        {
+            Timer t(s, K_ANDERSON);
+            norm_kernel<<<grid_for((long long)s->ns * W, 256), 256, 0, s->stream>>>(g, s->ns, s->src, W,
+                                                                                  P<float>(s->norms),
+                                                                                  P<unsigned>(s->metrics));
+        }
         TRY(launch_check(s));
         const int m = (int)order.size();
         const float* rp[4] = {nullptr, nullptr, nullptr, nullptr};
         for (int j = 0; j < m; ++j) rp[j] = P<float>(s->ring_f[order[j]]);
         const int fb = fblocks;
         const int per = fthreads;
-        feature_kernel<<<fb, per, (size_t)m * W * sizeof(double), s->stream>>>(
-            g, x, P<float>(s->norms), P<unsigned>(s->metrics), s->src, W, (long long)n, P<float>(s->ring_f[slot]), rp[0],
-            rp[1], rp[2], rp[3], m, P<double>(s->partials));
+        {
+            Timer t(s, K_ANDERSON);
+            feature_kernel<<<fb, per, (size_t)m * W * sizeof(double), s->stream>>>(
+                g, x, P<float>(s->norms), P<unsigned>(s->metrics), s->src, W, (long long)n, P<float>(s->ring_f[slot]),
+                rp[0], rp[1], rp[2], rp[3], m, P<double>(s->partials));
+        }
         TRY(launch_check(s));
-        sum_partials_kernel<<<(m * W + 127) / 128, 128, 0, s->stream>>>(P<double>(s->partials), fb, m * W,
-                                                                         P<double>(s->dots));
+        {
+            Timer t(s, K_ANDERSON);
+            sum_partials_kernel<<<(m * W + 127) / 128, 128, 0, s->stream>>>(P<double>(s->partials), fb, m * W,
+                                                                             P<double>(s->dots));
+        }
         TRY(launch_check(s));
         CK(cudaMemcpyAsync(dots.data(), s->dots.p, (size_t)m * W * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
@@ -1043,9 +1142,12 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
                            s->stream));
         const float* q[4] = {nullptr, nullptr, nullptr, nullptr};
         for (int j = 0; j < m; ++j) q[j] = P<float>(s->ring_g[order[j]]);
-        mix_kernel<<<grid_for((long long)n, 256), 256, 0, s->stream>>>(
-            g, q[0], q[1], q[2], q[3], m, P<float>(s->mixw),
-            reinterpret_cast<const int*>(P<char>(s->mixw) + 4 * W * sizeof(float)), W, (long long)n, nxt);
+        {
+            Timer t(s, K_ANDERSON);
+            mix_kernel<<<grid_for((long long)n, 256), 256, 0, s->stream>>>(
+                g, q[0], q[1], q[2], q[3], m, P<float>(s->mixw),
+                reinterpret_cast<const int*>(P<char>(s->mixw) + 4 * W * sizeof(float)), W, (long long)n, nxt);
+        }
         TRY(launch_check(s));
         std::swap(x, nxt);
     }

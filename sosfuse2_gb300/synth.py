@@ -1,0 +1,529 @@
+"""Seeded synthetic states (packed states of sosfuse2_gb300.state) for the benchmark configurations.
+
+The GPU machine has no reference installation, so the workloads are built here from a synthetic atmosphere on the
+reference's geometry. The geometry restates the reference's ray construction:
+
+* local frame of a cell point, src/sosfuse2/rays/shell_segments.py:37-40, and the target basis, solve/engine_core.py:8-20;
+* ring-edge incoming-direction quadrature (sinh-mapped Gauss-Legendre in mu between the horizon, tangent, shadow
+  and ring edges, trapezoid in azimuth), src/sosfuse2/rays/incoming_rings.py:11-126;
+* segment ends: shell exit, opaque-ground hit, tangent point and shadow-cylinder crossings
+  (rays/shell_segments.py:43-66), plus the extra shells at 10, 25, 40 (and 80) km (solve/ray_geometry.py:28-82);
+* the observer boxes: 5 solar elevations x 7 directions x 4x4 Gauss-Legendre points at 0.1 km, 24 nodes per segment
+  (solve/engine_core.py:208-238, solve/engine.py:435-446).
+
+Slant columns (towards the sun from any point, and to the ground along any downward ray) depend only on the height
+and the zenith cosine of a ray, because every profile here is a function of height alone; they are tabulated once per
+state on a (height, x) grid like the reference's solar table (rays/shell_segments.py:109-112,230-325) and
+interpolated bilinearly. The first-light ground term (solve/engine_core.py:103-147) is built from those tables.
+
+The atmosphere: air exp(-h/8); ozone as a Chapman layer; tropospheric aerosol exp(-h/H) with Henyey-Greenstein
+phase; optional stratospheric Gaussian layer with Henyey-Greenstein Legendre moments; optional NO2 Gaussian layer
+and O4 proportional to the squared air density; Lambertian ground. Spectral shapes are seeded smooth curves.
+"""
+
+import json
+import math
+
+import numpy as np
+
+R = 6371.0
+OBSERVER_KM = 0.1
+SUN_HEIGHT_INTERVALS = 80
+MONITOR_ELEVATIONS = (2.0, -3.0, -6.0, -9.0, -12.0)
+DIRS = ((2, 0), (10, 0), (30, 0), (10, 180), (30, 180), (10, 90), (89, 0))
+DU = 2.687e16  # molecules cm^-2 per Dobson unit
+
+
+def production_chi_deg():
+    """The 75 solar-zenith nodes of the reference's full grid (rays/shell_segments.py:88-102)."""
+    return np.unique(np.r_[np.arange(0, 81, 10), np.arange(80, 85, 1), np.arange(85, 110, 0.5),
+                           np.arange(110, 120, 2), np.arange(120, 181, 10)]).astype(float)
+
+
+REDUCED_CHI_DEG = np.array([0.0, 60.0, 85.0, 90.0, 93.0, 96.0, 105.0, 110.0, 140.0, 180.0])
+
+
+def gauss01(n):
+    x, w = np.polynomial.legendre.leggauss(n)
+    return (x + 1) / 2, w / 2
+
+
+def frame(r, chi):
+    up = np.array([np.sin(chi), 0.0, np.cos(chi)])
+    ex = np.array([-np.cos(chi), 0.0, np.sin(chi)])
+    return r * up, up, ex
+
+
+def target_basis(p):
+    """Orthonormal local frame (east-like, north-like, up) of a point, as columns of a 3x3 matrix."""
+    r = np.linalg.norm(p)
+    up = p / r
+    ex = np.array([0.0, 0.0, 1.0]) - up[2] * up
+    n = np.linalg.norm(ex)
+    ex = ex / n if n > 1e-12 else np.array([-(1.0 if up[2] >= 0 else -1.0), 0.0, 0.0])
+    return np.stack([ex, np.cross(up, ex), up], -1)
+
+
+# ------------------------------------------------------------------------------------------------ quadrature
+def _ring_mus(r, chi, phi, heights, p, up, ex, ey):
+    """Zenith cosines where the view plane at azimuth phi meets the shadow ring of each shell."""
+    horizontal = np.cos(phi) * ex + np.sin(phi) * ey
+    normal = np.cross(up, horizontal)
+    amp = R * math.hypot(normal[0], normal[1])
+    if amp < 1e-10:
+        return []
+    angle = math.atan2(normal[1], normal[0])
+    out = []
+    for h in heights:
+        z = -math.sqrt(max(0.0, (R + h) ** 2 - R * R))
+        target = -normal[2] * z / amp
+        if abs(target) > 1:
+            continue
+        delta = math.acos(target)
+        for az in (angle - delta, angle + delta):
+            q = np.array([R * math.cos(az), R * math.sin(az), z])
+            d = q - p
+            length = math.sqrt(d @ d)
+            if length < 1e-8:
+                continue
+            d /= length
+            if d @ horizontal <= 1e-10:
+                continue
+            b = p @ d
+            disc = b * b - r * r + R * R
+            hit = -b - math.sqrt(max(0.0, disc))
+            if disc >= 0 and b < 0 and hit >= -1e-7 and hit < length - 1e-5:
+                continue
+            out.append(float(d @ up))
+    return out
+
+
+def ring_quadrature(r, chi, nmu, nphi, heights, rings=True, a=4.0):
+    """Incoming directions in the local frame (ex, ey, up) and solid-angle weights (sum 4 pi)."""
+    mg = -math.sqrt(max(0.0, 1 - (R / r) ** 2))
+    sa = math.sinh(a)
+    u, wu = gauss01(nmu)
+    sinchi, coschi = math.sin(chi), math.cos(chi)
+    rp = r * sinchi
+    p, up, ex = frame(r, chi)
+    ey = np.cross(up, ex)
+    mus, phis, ws = [], [], []
+    for j, phi in enumerate(np.linspace(0, np.pi, nphi + 1)):
+        edges = [-1.0, 1.0, mg, 0.0, mg - 0.05234, mg + 0.05234, mg - 0.0061, mg + 0.0061]
+        if rp > R + 1e-8 and abs(sinchi) > 1e-8:
+            kk = R / math.sqrt(rp * rp - R * R)
+            for sign in (-1, 1):
+                t = math.cos(phi) * coschi / sinchi + sign * math.sin(phi) / (kk * sinchi)
+                mu = t / math.sqrt(1 + t * t)
+                st = math.sqrt(1 - mu * mu)
+                dx = mu * sinchi - st * math.cos(phi) * coschi
+                dy = -st * math.sin(phi)
+                dz = mu * coschi + st * math.cos(phi) * sinchi
+                tmin = -rp * dx / max(dx * dx + dy * dy, 1e-25)
+                if abs(dx) + abs(dy) < 1e-10 or (tmin > 0 and r * coschi + tmin * dz < 0):
+                    edges.append(mu)
+        if phi < np.pi / 6:
+            mu = coschi / math.sqrt(coschi ** 2 + math.cos(phi) ** 2 * sinchi ** 2 + 1e-300)
+            edges.extend([mu, mu - 0.012, mu + 0.012])
+        if rings:
+            edges += _ring_mus(r, chi, phi, heights, p, up, ex, ey)
+        edges = np.unique(np.clip(edges, -1, 1))
+        delta = edges - mg
+        tt = np.sign(delta) * np.arcsinh(np.abs(delta) / np.where(delta < 0, 1 + mg, 1 - mg) * sa) / a
+        keep = tt[1:] - tt[:-1] >= 1e-10
+        left = tt[:-1][keep, None]
+        right = tt[1:][keep, None]
+        t = left + (right - left) * u
+        den = np.where(t < 0, 1 + mg, 1 - mg)
+        mus.append((mg + np.sign(t) * den * np.sinh(a * np.abs(t)) / sa).ravel())
+        ws.append(((right - left) * wu * den * a * np.cosh(a * np.abs(t)) / sa * (2 * np.pi / nphi)
+                   * (0.5 if j in (0, nphi) else 1.0)).ravel())
+        phis.append(np.full(t.size, phi))
+    mu = np.concatenate(mus)
+    phi = np.concatenate(phis)
+    st = np.sqrt(np.maximum(0, 1 - mu * mu))
+    return np.column_stack([st * np.cos(phi), st * np.sin(phi), mu]), np.concatenate(ws)
+
+
+# ------------------------------------------------------------------------------------------------ segments
+def ray_edges(p, d, top, shells):
+    """Sorted path coordinates of every crossing: start, tangent, shadow-cylinder roots, extra shells, end."""
+    b = np.sum(p * d, -1)
+    pp = np.sum(p * p, -1)
+    end = -b + np.sqrt(np.maximum(b * b - pp + (R + top) ** 2, 0))
+    disc = b * b - pp + R * R
+    hit = -b - np.sqrt(np.maximum(disc, 0))
+    ground = (disc >= 0) & (b < 0) & (hit >= -1e-7)
+    end = np.maximum(np.where(ground, np.maximum(hit, 0), end), 0)
+    tangent = np.where((-b > 0) & (-b < end), -b, end)
+    aa = d[:, 0] ** 2 + d[:, 1] ** 2
+    bb = p[:, 0] * d[:, 0] + p[:, 1] * d[:, 1]
+    cc = p[:, 0] ** 2 + p[:, 1] ** 2 - R * R
+    ds = bb * bb - aa * cc
+    cols = [np.zeros_like(end), tangent, end]
+    for sign in (-1, 1):
+        root = (-bb + sign * np.sqrt(np.maximum(ds, 0))) / np.maximum(aa, 1e-30)
+        ok = (aa > 1e-20) & (ds >= 0) & (root > 0) & (root < end) & (p[:, 2] + root * d[:, 2] < 0)
+        cols.append(np.where(ok, root, end))
+    for height in shells:
+        disc2 = b * b - pp + (R + height) ** 2
+        for sign in (-1, 1):
+            root = -b + sign * np.sqrt(np.maximum(disc2, 0))
+            cols.append(np.where((disc2 > 0) & (root > 0) & (root < end), root, end))
+    return np.sort(np.column_stack(cols), axis=-1), ground
+
+
+def compact_segments(p, d, edges):
+    """Valid segments (b - a > 1e-8) of each ray: CSR offsets, ends and the lower-end flag."""
+    a, b = edges[:, :-1], edges[:, 1:]
+    valid = (b - a) > 1e-8
+    qa = p[:, None, :] + a[..., None] * d[:, None, :]
+    qb = p[:, None, :] + b[..., None] * d[:, None, :]
+    lower = np.sum(qa * qa, -1) <= np.sum(qb * qb, -1)
+    counts = valid.sum(1)
+    return (np.r_[0, np.cumsum(counts)].astype(np.int64), a[valid], b[valid], lower[valid].astype(np.uint8))
+
+
+# ------------------------------------------------------------------------------------------------ atmosphere
+class Atmosphere:
+    """Synthetic seeded atmosphere on 0..top km for wavelengths `wl` (nm)."""
+
+    def __init__(self, wl, seed=0, top=80.0, aod=0.1, ssa=0.95, g=0.7, scale_height=1.2, angstrom=1.3,
+                 ozone_du=300.0, ozone_peak=22.0, ozone_sigma_cm2=3e-21, albedo=0.3,
+                 strato_tau=0.01, strato_center=20.0, strato_sigma=3.0, strato_g=0.6,
+                 no2_column=0.0, no2_center=25.0, o4=False):
+        rng = np.random.default_rng(seed)
+        self.wl = np.asarray(wl, float)
+        self.W = len(self.wl)
+        self.top = float(top)
+        self.g, self.ssa, self.H, self.albedo = g, ssa, scale_height, albedo
+        w = self.wl
+        # Rayleigh with the lambda^-4 law; ozone Chappuis-like smooth band scaled so 550 nm has ozone_sigma_cm2
+        self.ray = 0.013558 * (550.0 / w) ** 4
+        bump = lambda x, c, s: np.exp(-0.5 * ((x - c) / s) ** 2)  # noqa: E731
+        jitter = 1 + 0.05 * rng.standard_normal(3)
+        o3_shape = (bump(w, 600.0 * jitter[0] ** 0.02, 55.0) + 0.08) / (bump(550.0, 600.0 * jitter[0] ** 0.02, 55.0)
+                                                                        + 0.08)
+        self.o3_sigma = ozone_sigma_cm2 * o3_shape
+        self.ozone_du = ozone_du
+        self.ozone_peak = ozone_peak
+        self.aer = aod / (scale_height * -math.expm1(-80.0 / scale_height)) * (550.0 / w) ** angstrom
+        self.no2_column = no2_column
+        self.no2_center = no2_center
+        self.no2_sigma = (1.0 + 0.4 * rng.random()) * 1e-19 * (450.0 / w) ** 2.0 * (1 + 0.1 * np.sin(w / 7.0))
+        self.o4 = bool(o4)
+        self.o4_coeff = (1e-3 * (bump(w, 477.0, 4.0) + 0.6 * bump(w, 577.0, 5.0) + 0.9 * bump(w, 630.0, 4.0))
+                         if o4 else np.zeros(self.W))
+        self.strato = strato_tau > 0
+        self.strato_tau, self.strato_center, self.strato_sigma, self.strato_g = (strato_tau, strato_center,
+                                                                                 strato_sigma, strato_g)
+        if self.strato:
+            z = np.linspace(0, 80.0, 8001)
+            self.strato_norm = float(np.trapezoid(np.exp(-0.5 * ((z - strato_center) / strato_sigma) ** 2), z))
+            self.strato_ext = strato_tau * (550.0 / w) ** 0.8
+        self.solar = 1.85 * (1 + 0.1 * np.sin(w / 13.0 + rng.random())) * np.exp(-((w - 480.0) / 400.0) ** 2)
+
+    # ozone Chapman shape normalised to a 15 km column (the reference's triangle normalisation)
+    def ozone_shape(self, h):
+        if not hasattr(self, '_o3_norm'):
+            zz = np.linspace(0, 120, 12001)
+            z = (zz - self.ozone_peak) / 5.0
+            self._o3_norm = 15.0 / np.trapezoid(np.exp(1 - z - np.exp(-z)), zz)
+        z = (np.asarray(h, float) - self.ozone_peak) / 5.0
+        return np.exp(1 - z - np.exp(-z)) * self._o3_norm
+
+    def no2_shape(self, h):
+        return np.exp(-0.5 * ((np.asarray(h, float) - self.no2_center) / 4.0) ** 2)
+
+    def profiles(self, h):
+        """[n, 5] air, aerosol, ozone, NO2, O4 shapes (the kernel's profile_at with the density table)."""
+        h = np.clip(np.asarray(h, float), 0, self.top)
+        air = np.exp(-h / 8.0)
+        return np.stack([air, np.exp(-h / self.H), self.ozone_shape(h), self.no2_shape(h), air * air], -1)
+
+    def strato_profile(self, h):
+        if not self.strato:
+            return np.zeros_like(np.asarray(h, float))
+        return np.exp(-0.5 * ((np.asarray(h, float) - self.strato_center) / self.strato_sigma) ** 2) / self.strato_norm
+
+    def ext(self):
+        """[5, W] extinction per unit profile (km^-1)."""
+        # beta [km^-1] = sigma [cm^2] * column [cm^-2] * shape / (column integral of the shape [km])
+        o3 = self.o3_sigma * self.ozone_du * DU / 15.0
+        no2_norm = 4.0 * math.sqrt(2 * math.pi)
+        no2 = self.no2_sigma * self.no2_column / no2_norm
+        return np.stack([self.ray, self.aer, o3, no2, self.o4_coeff])
+
+
+# ------------------------------------------------------------------------------------------------ column tables
+def _columns_along(r0, mu, atm, shells, n):
+    """Columns (5 components + stratosphere) from radius r0 along zenith cosine mu to the top or the ground."""
+    p = np.column_stack([np.zeros_like(mu), np.zeros_like(mu), np.full_like(mu, r0)])
+    d = np.column_stack([np.sqrt(np.maximum(1 - mu * mu, 0)), np.zeros_like(mu), mu])
+    edges, ground = ray_edges(p, d, atm.top, shells)
+    u, wu = gauss01(n)
+    out = np.zeros((len(mu), 6))
+    for k in range(edges.shape[1] - 1):
+        a, b = edges[:, k, None], edges[:, k + 1, None]
+        t = a + (b - a) * u
+        q = p[:, None, :] + t[..., None] * d[:, None, :]
+        h = np.linalg.norm(q, axis=-1) - R
+        w = (b - a) * wu
+        prof = atm.profiles(h.ravel()).reshape(*h.shape, 5)
+        out[:, :5] += np.einsum('rn,rnk->rk', w, prof)
+        out[:, 5] += np.sum(w * atm.strato_profile(h), -1)
+    return out, ground
+
+
+class ColumnTable:
+    """Slant columns on a (height, x) grid for upward (sun) and downward (ground) rays."""
+
+    def __init__(self, atm, shells, scale=2, n=32):
+        self.top = atm.top
+        self.h = np.linspace(0, math.sqrt(atm.top), SUN_HEIGHT_INTERVALS * scale + 1) ** 2
+        self.x = np.linspace(0, 1, 400 * scale + 1)
+        self.up = np.empty((len(self.h), len(self.x), 6))
+        self.down = np.empty_like(self.up)
+        for i, h in enumerate(self.h):
+            r = R + h
+            mg = -math.sqrt(max(0.0, 1 - (R / r) ** 2))
+            mu = mg + (1 - mg) * self.x ** 2
+            mu[0] = mg + 1e-9
+            self.up[i] = _columns_along(r, mu, atm, shells, n)[0]
+            mud = mg - (1 + mg) * self.x ** 2
+            mud[0] = mg - 1e-9
+            self.down[i] = _columns_along(r, np.maximum(mud, -1.0), atm, shells, n)[0]
+
+    def lookup(self, h, mu):
+        """Columns [n, 6] and whether the ray escapes (mu >= horizon cosine)."""
+        h = np.clip(np.asarray(h, float), 0, self.top)
+        mu = np.asarray(mu, float)
+        r = R + h
+        mg = -np.sqrt(np.maximum(0, 1 - (R / np.maximum(r, R)) ** 2))
+        escape = mu >= mg
+        x_up = np.sqrt(np.clip((mu - mg) / (1 - mg), 0, 1))
+        x_dn = np.sqrt(np.clip((mg - mu) / (1 + mg), 0, 1))
+        i = np.clip(np.searchsorted(self.h, h, side='right') - 1, 0, len(self.h) - 2)
+        a = (h - self.h[i]) / (self.h[i + 1] - self.h[i])
+        out = np.empty((len(h), 6))
+        for sel, x, tab in ((escape, x_up, self.up), (~escape, x_dn, self.down)):
+            f = x[sel] * (len(self.x) - 1)
+            j = np.clip(f.astype(int), 0, len(self.x) - 2)
+            bb = (f - j)[:, None]
+            aa = a[sel][:, None]
+            ii = i[sel]
+            out[sel] = ((1 - aa) * (1 - bb) * tab[ii, j] + aa * (1 - bb) * tab[ii + 1, j] + (1 - aa) * bb * tab[ii, j + 1]
+                        + aa * bb * tab[ii + 1, j + 1])
+        return out, escape
+
+
+# ------------------------------------------------------------------------------------------------ state
+def _shells(top):
+    return (10.0, 25.0, 40.0) + ((80.0,) if top > 80.0 else ())
+
+
+def _ring_heights(top):
+    return (0.0, 1.2, 8.0, 25.0, 40.0) + ((80.0, top) if top > 80.0 else (top,))
+
+
+def _ray_block(p, d, chi_grid, top, table, with_ground_columns):
+    shells = _shells(top)
+    edges, ground = ray_edges(p, d, top, shells)
+    seg_off, seg_a, seg_b, seg_lower = compact_segments(p, d, edges)
+    end = edges[:, -1]
+    qe = p + end[:, None] * d
+    re = np.linalg.norm(qe, axis=-1)
+    ch = np.arccos(np.clip(qe[:, 2] / re, -1, 1))
+    j = np.clip(np.searchsorted(chi_grid, ch, side='right') - 1, 0, len(chi_grid) - 2)
+    f = np.clip((ch - chi_grid[j]) / (chi_grid[j + 1] - chi_grid[j]), 0, 1)
+    hits = re < R + 1e-5
+    end_col = np.zeros((len(d), 5), np.float32)
+    end_st = np.zeros(len(d), np.float32)
+    if with_ground_columns and hits.any():
+        r0 = np.linalg.norm(p[hits], axis=-1)
+        mu = np.sum(p[hits] * d[hits], -1) / r0
+        cols, _ = table.lookup(r0 - R, mu)
+        end_col[hits] = cols[:, :5]
+        end_st[hits] = cols[:, 5]
+    return dict(seg_off=seg_off, seg_a=seg_a, seg_b=seg_b, seg_lower=seg_lower, end_j=j.astype(np.int32), end_f=f,
+                end_col=end_col, end_st=end_st, hits=hits.astype(np.uint8))
+
+
+def build_bundle(points, dirs_local, weights, chi_grid, top, table, atm, with_ground_columns=True, block=1 << 20):
+    """points: (p, up, ex) per cell; dirs_local, weights: that cell's incoming directions in its local frame and
+    their solid-angle weights. Rays are processed in blocks of about `block` to bound host memory."""
+    cell_off = [0]
+    P, T, D, DL, WT = [], [], [], [], []
+    for (p, up, ex), loc, w in zip(points, dirs_local, weights):
+        ey = np.cross(up, ex)
+        d = loc[:, 0, None] * ex + loc[:, 1, None] * ey + loc[:, 2, None] * up
+        B = target_basis(p)
+        P.append(p)
+        T.append(B)
+        D.append(d)
+        DL.append(d @ B)
+        WT.append(w)
+        cell_off.append(cell_off[-1] + len(d))
+    cell_off = np.asarray(cell_off, np.int64)
+    d = np.concatenate(D)
+    P = np.asarray(P)
+    ray_cell = np.repeat(np.arange(len(P)), np.diff(cell_off))
+    parts = []
+    for r0 in range(0, len(d), block):
+        r1 = min(r0 + block, len(d))
+        parts.append(_ray_block(P[ray_cell[r0:r1]], d[r0:r1], chi_grid, top, table, with_ground_columns))
+    seg_off = [np.zeros(1, np.int64)]
+    base = 0
+    for part in parts:
+        seg_off.append(part['seg_off'][1:] + base)
+        base += int(part['seg_off'][-1])
+    out = dict(cell_off=cell_off, p=P, target=np.asarray(T), d=d, dloc=np.concatenate(DL), weight=np.concatenate(WT),
+               seg_off=np.concatenate(seg_off))
+    for k in ('seg_a', 'seg_b', 'seg_lower', 'end_j', 'end_f', 'end_col', 'end_st', 'hits'):
+        out[k] = np.concatenate([part[k] for part in parts])
+    return out
+
+
+def ground_terms(h, chi, atm, table, ext, nmu=3, nphi=32):
+    """First-light direct-ground sources of each cell: Rayleigh moments gm [ns, 4, W] and the lit ground directions
+    with their values (solve/engine_core.py:103-147 restated on the column tables)."""
+    C = 3 / (16 * math.pi)
+    ns = len(h) * len(chi)
+    gm = np.zeros((ns, 4, atm.W))
+    goff, gdir, gval = [0], [], []
+    for cell in range(ns):
+        ih, ic = divmod(cell, len(chi))
+        r = R + h[ih]
+        loc, w = ring_quadrature(r, chi[ic], nmu, nphi, (), rings=False)
+        p, up, ex = frame(r, chi[ic])
+        ey = np.cross(up, ex)
+        d = loc[:, 0, None] * ex + loc[:, 1, None] * ey + loc[:, 2, None] * up
+        col, escape = table.lookup(np.full(len(d), h[ih]), loc[:, 2])
+        hit = ~escape
+        # ground point of each downward ray
+        b = d @ p
+        disc = b * b - r * r + R * R
+        t = -b - np.sqrt(np.maximum(disc, 0))
+        q = p + t[:, None] * d
+        rq = np.linalg.norm(q, axis=-1)
+        cos_sun = q[:, 2] / rq
+        sun, lit = table.lookup(np.zeros(len(d)), cos_sun)
+        od = (sun[:, :5] + col[:, :5]) @ ext
+        if atm.strato:
+            od += (sun[:, 5] + col[:, 5])[:, None] * atm.strato_ext[None, :]
+        value = (atm.albedo / math.pi * np.maximum(0, cos_sun)[:, None] * np.exp(-od) * lit[:, None] * hit[:, None]
+                 * w[:, None])
+        take = np.any(value > 0, axis=1)
+        gdir.append(loc[take])
+        gval.append(value[take])
+        goff.append(goff[-1] + int(take.sum()))
+        factor = np.stack([(1 - loc[:, 0] ** 2) / 2, (1 - loc[:, 1] ** 2) / 2, (1 - loc[:, 2] ** 2) / 2,
+                           -loc[:, 0] * loc[:, 2] / 2], -1)
+        gm[cell] = (factor.T @ value) * (2 * C * ext[0])[None, :]
+    return (gm.astype(np.float32), np.asarray(goff, np.int64), np.concatenate(gdir).astype(np.float32),
+            np.concatenate(gval).astype(np.float32))
+
+
+def make_state(h, chi_deg, wl, L, nmu, nphi, path_n, atm, seed=0, query_n=24, sun_scale=2, tolerance=1e-3,
+               max_eval=64, name='synthetic'):
+    """A packed state (dict for sosfuse2_gb300.state.PackedState) of the synthetic atmosphere."""
+    h = np.asarray(h, float)
+    chi = np.deg2rad(np.asarray(chi_deg, float))
+    top = float(h[-1])
+    if abs(top - atm.top) > 1e-9:
+        raise ValueError('E_SYNTH: grid top and atmosphere top differ')
+    W = atm.W
+    K = (L + 1) * (L + 2) // 2
+    shells = _shells(top)
+    table = ColumnTable(atm, shells, scale=sun_scale)
+    ext = atm.ext()
+    # cell rays
+    points, dirs, weights = [], [], []
+    for ih in range(len(h)):
+        for ic in range(len(chi)):
+            r = R + h[ih]
+            loc, w = ring_quadrature(r, chi[ic], nmu, nphi, _ring_heights(top))
+            points.append(frame(r, chi[ic]))
+            dirs.append(loc)
+            weights.append(w)
+    cells = build_bundle(points, dirs, weights, chi, top, table, atm)
+    # observer rays: 5 solar elevations x 7 directions x 4x4 Gauss-Legendre points
+    u4, w4 = np.polynomial.legendre.leggauss(4)
+    qpts, qdirs, qw = [], [], []
+    for hs in MONITOR_ELEVATIONS:
+        el = np.array([e + de for e, z in DIRS for de in u4 for dz in u4])
+        az = np.array([z + dz for e, z in DIRS for de in u4 for dz in u4])
+        e, zz = np.deg2rad(el), np.deg2rad(az)
+        loc = np.column_stack([np.cos(e) * np.cos(zz), np.cos(e) * np.sin(zz), np.sin(e)])
+        qpts.append(frame(R + OBSERVER_KM, np.deg2rad(90 - hs)))
+        qdirs.append(loc)
+        qw.append(np.ones(len(loc)))
+    query = build_bundle(qpts, qdirs, qw, chi, top, table, atm, with_ground_columns=False)
+    gm, goff, gdir, gval = ground_terms(h, chi, atm, table, ext)
+    u, wu = gauss01(path_n)
+    uq, wuq = gauss01(query_n)
+    step = 0.5
+    zt = np.arange(int(round(top / step)) + 1) * step
+    prof = atm.profiles(zt)
+    density_table = np.column_stack([prof[:, 0], prof[:, 2], prof[:, 3]]).astype(np.float32)
+    levels = np.array([l for l in range(L + 1) for m in range(l + 1)])
+    hr = np.exp(-h / 8.0)
+    ha = np.exp(-h / atm.H)
+    meta = dict(
+        name=name, L=L, K=K, W=W, nq=path_n, nq_query=query_n, nh=len(h), nc=len(chi), ns=len(h) * len(chi),
+        source_size=10 + K * (2 if atm.strato else 1), strato=atm.strato, g=atm.g, mix=(1 - 0.03) / (1 + 0.015),
+        height=atm.H, albedo=atm.albedo, top_km=top, profile_step_km=step, density_mask=2, air_surface=1.0,
+        tolerance=tolerance, max_eval=max_eval, monitors=len(MONITOR_ELEVATIONS), n_dirs=len(DIRS), box_points=16,
+        wavelengths_nm=atm.wl.tolist(), seed=seed, C=3 / (16 * math.pi),
+        rays=int(len(cells['d'])), segments=int(len(cells['seg_a'])), query_rays=int(len(query['d'])),
+    )
+    arrays = dict(
+        meta=json.dumps(meta), u=u, wu=wu, uq=uq, wuq=wuq,
+        h=h.astype(np.float32), chi=chi.astype(np.float32), hr=hr.astype(np.float32), ha=ha.astype(np.float32),
+        ext=ext.astype(np.float32), asca=(ext[1] * atm.ssa).astype(np.float32),
+        sun_h=table.h.astype(np.float32), sun_col=np.ascontiguousarray(table.up[:, :, :5], np.float32),
+        gm=gm, goff=goff, gdir=gdir, gval=gval, density_table=density_table,
+        rf=((levels[:6] == 0) + 0.1 * (levels[:6] == 2)).astype(np.float32),
+        af=(atm.g ** levels).astype(np.float32), ext0=ext[0].astype(np.float32), solar=atm.solar.astype(np.float64),
+        box_ww=(w4[:, None] * w4[None, :] / 4).ravel(),
+    )
+    if atm.strato:
+        lm = np.arange(33)
+        chi_l = ((2 * lm + 1) * atm.strato_g ** lm)[:, None] * np.ones((1, W))
+        cell_edges = np.r_[h[0], (h[:-1] + h[1:]) / 2, h[-1]]
+        cdf = np.array([math.erf((z - atm.strato_center) / (math.sqrt(2) * atm.strato_sigma)) for z in cell_edges])
+        avg = np.diff(cdf) * atm.strato_sigma * math.sqrt(math.pi / 2) / atm.strato_norm / np.diff(cell_edges)
+        arrays.update(
+            strato_ext=atm.strato_ext.astype(np.float32), strato_sca=atm.strato_ext.astype(np.float32),
+            strato_chi=chi_l.astype(np.float32), strato_density=avg.astype(np.float32),
+            strato_sun_col=np.ascontiguousarray(table.up[:, :, 5], np.float32),
+            strato_eigen=(atm.strato_g ** levels[:, None] * np.ones((1, W))).astype(np.float32),
+            strato_sca_source=atm.strato_ext.astype(np.float32),
+        )
+        meta.update(strato_center=atm.strato_center, strato_sigma=atm.strato_sigma, strato_norm=atm.strato_norm)
+        arrays['meta'] = json.dumps(meta)
+    for k, v in cells.items():
+        arrays['cell_' + k] = v
+    for k, v in query.items():
+        arrays['query_' + k] = v
+    return arrays
+
+
+# ------------------------------------------------------------------------------------------------ configurations
+def config0(seed=0, **kw):
+    """Plain SOS reduced grid: 550 nm, 101 heights on 0-100 km, the reduced 10-node solar-zenith grid, nmu 1, nphi 2,
+    path_n 4, L=16, Chapman ozone 300 DU, tropospheric aerosol AOD 0.1 / ssa 0.95 / g 0.7 / H 1.2 km, stratospheric
+    Gaussian 20 km (sigma 3 km, AOD 0.01, g 0.6), NO2/O4 off, albedo 0.3."""
+    atm = Atmosphere([550.0], seed=seed, top=100.0)
+    return make_state(np.arange(101.0), REDUCED_CHI_DEG, atm.wl, 16, 1, 2, 4, atm, seed=seed, name='config0', **kw)
+
+
+def config1(seed=0, nh=241, W=30, nmu=12, nphi=16, path_n=12, L=32, chi_deg=None, **kw):
+    """Plain SOS full table: 30 wavelengths 400-700 nm, 241 heights on 0-120 km, the 75 production solar-zenith
+    nodes, nmu 12, nphi 16, path_n 12, L=32; config-0 atmosphere plus an NO2 Gaussian layer at 25 km (5e15 cm^-2)
+    and O4. Smaller grids of the same construction are available through the keyword arguments."""
+    wl = np.linspace(400.0, 700.0, W)
+    atm = Atmosphere(wl, seed=seed, top=120.0, no2_column=5e15, o4=True)
+    chi = production_chi_deg() if chi_deg is None else np.asarray(chi_deg, float)
+    return make_state(np.linspace(0.0, 120.0, nh), chi, wl, L, nmu, nphi, path_n, atm, seed=seed, name='config1',
+                      **kw)

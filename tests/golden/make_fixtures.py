@@ -37,8 +37,9 @@ FIXTURES = dict(
     walk1=dict(strato=False, wavelengths=[550.0]),
     # the same state with its Gaussian stratospheric sulfate layer (21 km, sigma 3 km)
     strato1=dict(strato=True, wavelengths=[550.0]),
-    # the stratospheric state over one 15-wavelength chunk (the reference kernel takes 1 or 15 wavelengths)
-    strato15=dict(strato=True, wavelengths=(360 + (np.arange(15) + 0.5) * 470 / 15).tolist()),
+    # the stratospheric state over one 15-wavelength chunk, 450-730 nm (the reference kernel takes 1 or 15
+    # wavelengths; its solve of this state does not converge within 64 evaluations below 400 nm)
+    strato15=dict(strato=True, wavelengths=(450.0 + 20.0 * np.arange(15)).tolist()),
 )
 
 
