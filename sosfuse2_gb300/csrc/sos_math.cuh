@@ -462,13 +462,158 @@ struct LaneInputs {
     int first;
 };
 
-// Integrate one ray for wavelength w. `cache` holds 4 slots x (L+1) floats at stride `cstride`.
+// First-light value of one node for wavelength w: single scattering of the attenuated sun (Rayleigh tensor,
+// aerosol and stratospheric phase), light from the lit ground through the cell ground directions, and the direct
+// ground Rayleigh moments of the four corners (numpy_reference.py:515-568,573-622 with first=True).
+SOS_HD void first_light_value(const Optics& o, const RayConst& rc, const Node& n, int w, float phase, float sphase,
+                              float val[4]) {
+    const int W = o.W;
+    const float mix = o.mix;
+    float col[5], stc, lit;
+    sun_columns(o, n, col, stc, lit);
+    float optical = 0.0f;
+    for (int k = 0; k < 5; ++k) optical += col[k] * o.ext[k * W + w];
+    if (o.strato) optical += stc * o.strato_ext[w];
+    const float sun = expf(-optical) * lit;
+    float ground = 0.0f, sground = 0.0f;
+    const float aeyd = fabsf(n.eyd);
+    for (int c = 0; c < 4; ++c) {
+        const int cell = n.cell[c];
+        for (int gi = o.goff[cell]; gi < o.goff[cell + 1]; ++gi) {
+            const float* gd = o.gdir + 3 * gi;
+            const float m0 = n.mu * gd[2] + n.exd * gd[0];
+            const float m1 = aeyd * gd[1];
+            const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
+            const float gv = o.gval[(size_t)gi * W + w];
+            const float ph = (hg_phase(up, o.g) + hg_phase(dn, o.g)) / 2.0f;
+            ground += (n.sw[c] * ph) * gv;
+            if (o.strato) {
+                const float sph = (legendre_phase(o, up, w) + legendre_phase(o, dn, w)) / 2.0f;
+                sground += (n.sw[c] * sph) * gv;
+            }
+        }
+    }
+    const float beam = (n.prof.v[1] * o.asca[w]) * (sun * phase + ground);
+    const float ray_ = (sun * n.prof.v[0]) * o.ext[w];
+    const float sbeam = o.strato ? (n.st_prof * o.strato_sca[w]) * (sun * sphase + sground) : 0.0f;
+    for (int k = 0; k < 4; ++k) {
+        val[k] = ray_ * (mix * C_3_8PI * rc.direct[k] + (1.0f - mix) * C_1_8PI * rc.pu[k]) + beam * rc.pu[k] / 2.0f;
+        if (o.strato) val[k] += (sbeam * rc.pu[k]) / 2.0f;
+    }
+    for (int c = 0; c < 4; ++c) {
+        const float* gm = o.gm + (size_t)n.cell[c] * 4 * W + w;
+        const float rm[4] = {gm[0], gm[W], gm[2 * W], gm[3 * W]};
+        const float trace = (rm[0] + rm[1]) + rm[2];
+        const float dens = n.prof.v[0];
+        for (int k = 0; k < 4; ++k) {
+            float rot = 0.0f;
+            for (int u = 0; u < 4; ++u) rot += n.T[k][u] * rm[u];
+            val[k] += n.sw[c] * (dens * (mix * rot + ((1.0f - mix) / 3.0f * trace) * rc.pu[k]));
+        }
+    }
+}
+
+// Warm (multiple-scattering) value of one node for wavelength w from the current source: Rayleigh tensor of each
+// corner rotated into the ray frame plus its aerosol SH source aero[c], bilinear in the corners, rescaled so that the
+// trace follows the log-space (geometric) blend of the corner traces (numpy_reference.py:89-103,573-628).
+SOS_HD void warm_value(const Optics& o, const RayConst& rc, const Node& n, const float* field, int w,
+                       const float aero[4], float val[4]) {
+    const int W = o.W;
+    const float mix = o.mix;
+    float logs = 0.0f, wg = 0.0f, am = 0.0f;
+    for (int k = 0; k < 4; ++k) val[k] = 0.0f;
+    for (int c = 0; c < 4; ++c) {
+        const int cell = n.cell[c];
+        const float* f = field + (size_t)cell * o.src * W + w;
+        const float rm[4] = {f[0], f[W], f[2 * W], f[3 * W]};
+        const float trace = (rm[0] + rm[1]) + rm[2];
+        const float dens = o.hr[n.ir + (c >> 1)];
+        float tens[4];
+        for (int k = 0; k < 4; ++k) {
+            float rot = 0.0f;
+            for (int u = 0; u < 4; ++u) rot += n.T[k][u] * rm[u];
+            tens[k] = dens * (mix * rot + ((1.0f - mix) / 3.0f * trace) * rc.pu[k]);
+            tens[k] += (aero[c] * rc.pu[k]) / 2.0f;
+            val[k] += n.sw[c] * tens[k];
+        }
+        const float tr = (tens[0] + tens[1]) + tens[2];
+        if (tr >= TRACE_MIN) {  // subnormal or NaN traces do not enter the log-space blend
+            logs += n.sw[c] * logf(tr);
+            wg += n.sw[c];
+            am += n.sw[c] * tr;
+        }
+    }
+    if (wg > 0.0f && am >= TRACE_MIN) {
+        const float scale = expf(logs - wg * logf(am / wg));
+        for (int k = 0; k < 4; ++k) val[k] *= scale;
+    }
+}
+
+// SH synthesis of one cell's plane at the ray direction: sum_m cos(m phi) sum_l Y_lm(mu) plane[k(l,m)], with the
+// same FP32 recurrences as sh_contract and azimuth_sum, without keeping the per-m sums.
+SOS_HD float sh_synth(const Optics& o, float mu, float st, float cp, const float* plane_cell, int wstride) {
+    const int L = o.L;
+    cp = clampf(cp, -1.0f, 1.0f);
+    float pmm = 0.28209479177387814f;
+    float c0 = 1.0f, c1 = cp;
+    float total = 0.0f;
+    for (int m = 0; m <= L; ++m) {
+        float cm;
+        if (m == 0) {
+            cm = 1.0f;
+        } else if (m == 1) {
+            cm = cp;
+        } else {
+            const float c2 = (2.0f * cp) * c1 - c0;
+            c0 = c1;
+            c1 = c2;
+            cm = c2;
+        }
+        if (m) pmm = (pmm * o.sh_d[m]) * st;
+        const float scale = m ? 1.41421356237309515f : 1.0f;
+        float p0 = pmm;
+        int k = m * (m + 1) / 2 + m;
+        float acc = (scale * p0) * plane_cell[(size_t)k * wstride];
+        if (m < L) {
+            float p1 = (sqrtf(2.0f * m + 3.0f) * mu) * p0;
+            k = (m + 1) * (m + 2) / 2 + m;
+            acc += (scale * p1) * plane_cell[(size_t)k * wstride];
+            for (int l = m + 2; l <= L; ++l) {
+                k = l * (l + 1) / 2 + m;
+                const float p2 = (o.sh_a[k] * mu) * p1 - o.sh_b[k] * p0;
+                acc += (scale * p2) * plane_cell[(size_t)k * wstride];
+                p0 = p1;
+                p1 = p2;
+            }
+        }
+        total += cm * acc;
+    }
+    return total;
+}
+
+SOS_HD void boundary_term(const Optics& o, const Rays& b, const RayConst& rc, const float* boundary, int ray, int w,
+                          float total[4]) {
+    if (!boundary || !b.hits[ray]) return;
+    const int W = o.W;
+    const int j = b.end_j[ray];
+    const float ef = rc.end_f;
+    float E = (1.0f - ef) * boundary[j * W + w];
+    E += ef * boundary[(j + 1) * W + w];
+    const float* ec = b.end_col + 6 * (size_t)ray;
+    float optical = 0.0f;
+    for (int k = 0; k < 5; ++k) optical += ec[k] * o.ext[k * W + w];
+    if (o.strato) optical += ec[5] * o.strato_ext[w];
+    E *= expf(-optical);
+    for (int k = 0; k < 4; ++k) total[k] += (E * rc.pu[k]) / 2.0f;
+}
+
+// Integrate one ray for wavelength w, node by node. `cache` holds 4 slots x (L+1) floats at stride `cstride`: the
+// per-m SH sums of the cells at the current corners, recomputed only when a corner moves to another cell.
 SOS_HD void transport_lane(const Optics& o, const Rays& b, const LaneInputs& in, int ray, int w, float* cache,
                            int cstride, float out[4]) {
     RayConst rc;
     ray_constants(b, ray, rc);
     const int W = o.W;
-    const float mix = o.mix;
     const bool first = in.first != 0;
     float total[4] = {0, 0, 0, 0}, comp[4] = {0, 0, 0, 0};
     float tau = 0.0f, tauc = 0.0f;
@@ -477,9 +622,9 @@ SOS_HD void transport_lane(const Optics& o, const Rays& b, const LaneInputs& in,
     int tag[4] = {-1, -1, -1, -1};  // cell held by each cache slot
     const int s0 = b.seg_off[ray], s1 = b.seg_off[ray + 1];
     for (int s = s0; s < s1; ++s) {
-        float4 sg = b.seg[s];
-        DS a = DS{sg.x, sg.y}, bb = DS{sg.z, sg.w};
-        bool lower = b.lower[s] != 0;
+        const float4 sg = b.seg[s];
+        const DS a = DS{sg.x, sg.y}, bb = DS{sg.z, sg.w};
+        const bool lower = b.lower[s] != 0;
         DS t0 = a;
         float beta0 = beta_at(o, rc, t0, w);
         float acc = 0.0f;
@@ -487,61 +632,17 @@ SOS_HD void transport_lane(const Optics& o, const Rays& b, const LaneInputs& in,
             Node n;
             sample_node(o, rc, a, bb, lower, DS{in.u_hi[step], in.u_lo[step]}, DS{in.wu_hi[step], in.wu_lo[step]},
                         n);
-            float beta1 = extinction(o, n.prof, n.st_prof, w);
+            const float beta1 = extinction(o, n.prof, n.st_prof, w);
             DS tm = ds_add(t0, n.t);
             tm = DS{tm.h * 0.5f, tm.l * 0.5f};
-            float wpan = ds_val(ds_sub(n.t, t0)) / 6.0f;
+            const float wpan = ds_val(ds_sub(n.t, t0)) / 6.0f;
             acc = acc + wpan * ((beta0 + beta1) + 4.0f * beta_at(o, rc, tm, w));
             t0 = n.t;
             beta0 = beta1;
-            float mid = (tau - tauc) + acc;
-            float att = n.ds * expf(-mid);
-            float val[4] = {0, 0, 0, 0};
+            const float att = n.ds * expf(-((tau - tauc) + acc));
+            float val[4];
             if (first) {
-                float col[5], stc, lit;
-                sun_columns(o, n, col, stc, lit);
-                float optical = 0.0f;
-                for (int k = 0; k < 5; ++k) optical += col[k] * o.ext[k * W + w];
-                if (o.strato) optical += stc * o.strato_ext[w];
-                float sun = expf(-optical) * lit;
-                float ground = 0.0f, sground = 0.0f;
-                float aeyd = fabsf(n.eyd);
-                for (int c = 0; c < 4; ++c) {
-                    int cell = n.cell[c];
-                    for (int gi = o.goff[cell]; gi < o.goff[cell + 1]; ++gi) {
-                        const float* gd = o.gdir + 3 * gi;
-                        float m0 = n.mu * gd[2] + n.exd * gd[0];
-                        float m1 = aeyd * gd[1];
-                        float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
-                        float gv = o.gval[(size_t)gi * W + w];
-                        float ph = (hg_phase(up, o.g) + hg_phase(dn, o.g)) / 2.0f;
-                        ground += (n.sw[c] * ph) * gv;
-                        if (o.strato) {
-                            float sph = (legendre_phase(o, up, w) + legendre_phase(o, dn, w)) / 2.0f;
-                            sground += (n.sw[c] * sph) * gv;
-                        }
-                    }
-                }
-                float beam = (n.prof.v[1] * o.asca[w]) * (sun * phase + ground);
-                float ray_ = (sun * n.prof.v[0]) * o.ext[w];
-                float sbeam = o.strato ? (n.st_prof * o.strato_sca[w]) * (sun * sphase + sground) : 0.0f;
-                for (int k = 0; k < 4; ++k) {
-                    val[k] = ray_ * (mix * C_3_8PI * rc.direct[k] + (1.0f - mix) * C_1_8PI * rc.pu[k]) +
-                             beam * rc.pu[k] / 2.0f;
-                    if (o.strato) val[k] += (sbeam * rc.pu[k]) / 2.0f;
-                }
-                for (int c = 0; c < 4; ++c) {
-                    const float* gm = o.gm + (size_t)n.cell[c] * 4 * W + w;
-                    float rm[4] = {gm[0], gm[W], gm[2 * W], gm[3 * W]};
-                    float trace = (rm[0] + rm[1]) + rm[2];
-                    float dens = n.prof.v[0];
-                    for (int k = 0; k < 4; ++k) {
-                        float rot = 0.0f;
-                        for (int u = 0; u < 4; ++u) rot += n.T[k][u] * rm[u];
-                        float tens = dens * (mix * rot + ((1.0f - mix) / 3.0f * trace) * rc.pu[k]);
-                        val[k] += n.sw[c] * tens;
-                    }
-                }
+                first_light_value(o, rc, n, w, phase, sphase, val);
             } else {
                 // corner slots: reuse a slot whose cell is still a corner, recompute the others
                 int slot_of[4];
@@ -565,56 +666,21 @@ SOS_HD void transport_lane(const Optics& o, const Rays& b, const LaneInputs& in,
                     sh_contract(o, rc.d32[2], rc.st, in.plane + (size_t)n.cell[c] * o.K * W + w, W,
                                 cache + (size_t)q * (o.L + 1) * cstride, cstride);
                 }
-                float logs = 0.0f, wg = 0.0f, am = 0.0f;
-                for (int c = 0; c < 4; ++c) {
-                    int cell = n.cell[c];
-                    int irc = n.ir + (c >> 1);
-                    float aero = azimuth_sum(o.L, n.cp, cache + (size_t)slot_of[c] * (o.L + 1) * cstride, cstride);
-                    const float* f = in.field + (size_t)cell * o.src * W + w;
-                    float rm[4] = {f[0], f[W], f[2 * W], f[3 * W]};
-                    float trace = (rm[0] + rm[1]) + rm[2];
-                    float dens = o.hr[irc];
-                    float tens[4];
-                    for (int k = 0; k < 4; ++k) {
-                        float rot = 0.0f;
-                        for (int u = 0; u < 4; ++u) rot += n.T[k][u] * rm[u];
-                        tens[k] = dens * (mix * rot + ((1.0f - mix) / 3.0f * trace) * rc.pu[k]);
-                        tens[k] += (aero * rc.pu[k]) / 2.0f;
-                        val[k] += n.sw[c] * tens[k];
-                    }
-                    float tr = (tens[0] + tens[1]) + tens[2];
-                    if (tr >= TRACE_MIN) {  // subnormal or NaN traces do not enter the log-space blend
-                        logs += n.sw[c] * logf(tr);
-                        wg += n.sw[c];
-                        am += n.sw[c] * tr;
-                    }
-                }
-                if (wg > 0.0f && am >= TRACE_MIN) {
-                    float scale = expf(logs - wg * logf(am / wg));
-                    for (int k = 0; k < 4; ++k) val[k] *= scale;
-                }
+                float aero[4];
+                for (int c = 0; c < 4; ++c)
+                    aero[c] = azimuth_sum(o.L, n.cp, cache + (size_t)slot_of[c] * (o.L + 1) * cstride, cstride);
+                warm_value(o, rc, n, in.field, w, aero, val);
             }
             for (int k = 0; k < 4; ++k) kahan(total[k], comp[k], val[k] * att);
         }
         // closing panel to the segment end, then the segment's optical depth into tau (Kahan)
         DS tm = ds_add(t0, bb);
         tm = DS{tm.h * 0.5f, tm.l * 0.5f};
-        float wpan = ds_val(ds_sub(bb, t0)) / 6.0f;
+        const float wpan = ds_val(ds_sub(bb, t0)) / 6.0f;
         acc = acc + wpan * ((beta0 + beta_at(o, rc, bb, w)) + 4.0f * beta_at(o, rc, tm, w));
         kahan(tau, tauc, acc);
     }
-    if (in.boundary && b.hits[ray]) {
-        int j = b.end_j[ray];
-        float ef = rc.end_f;
-        float E = (1.0f - ef) * in.boundary[j * W + w];
-        E += ef * in.boundary[(j + 1) * W + w];
-        const float* ec = b.end_col + 6 * (size_t)ray;
-        float optical = 0.0f;
-        for (int k = 0; k < 5; ++k) optical += ec[k] * o.ext[k * W + w];
-        if (o.strato) optical += ec[5] * o.strato_ext[w];
-        E *= expf(-optical);
-        for (int k = 0; k < 4; ++k) total[k] += (E * rc.pu[k]) / 2.0f;
-    }
+    boundary_term(o, b, rc, in.boundary, ray, w, total);
     for (int k = 0; k < 4; ++k) out[k] = total[k];
 }
 

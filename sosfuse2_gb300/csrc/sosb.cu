@@ -154,6 +154,167 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
     rad[(size_t)ray * o.W + w] = make_float4(out[0], out[1], out[2], out[3]);
 }
 
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }
+
+// Sample-parallel transport for few wavelengths (W <= WM): one warp per ray, lane i takes the ray's node i (batches
+// of 32 nodes, segment-major). Each lane evaluates its node's geometry and its Simpson panel [previous node, node]
+// (plus the segment's closing panel on its last node); a warp prefix sum of the panel integrals gives every node's
+// optical depth; each lane forms its node's value with the corner SH synthesised directly; a warp reduction sums the
+// ray. Numerically this is transport_lane with the sums regrouped (panel and ray sums in tree order).
+template <int WM>
+__global__ void __launch_bounds__(TRANSPORT_THREADS)
+    transport_warp_kernel(Optics o, Rays b, LaneInputs in, int ray0, int nray, float4* rad) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= nray) return;  // the whole warp leaves together
+    const int ray = ray0 + (int)warp;
+    const int W = o.W;
+    RayConst rc;
+    ray_constants(b, ray, rc);
+    const bool first = in.first != 0;
+    const int nq = in.nq;
+    const int s0 = b.seg_off[ray], s1 = b.seg_off[ray + 1];
+    const int nsamp = (s1 - s0) * nq;
+    const float phase = hg_phase(rc.d32[2], o.g);
+    float sphase[WM], tot[WM][4], cmp[WM][4], carry[WM], carry_beta[WM];
+#pragma unroll
+    for (int w = 0; w < WM; ++w) {
+        sphase[w] = (o.strato && first && w < W) ? legendre_phase(o, rc.d32[2], w) : 0.0f;
+        carry[w] = carry_beta[w] = 0.0f;
+        for (int k = 0; k < 4; ++k) tot[w][k] = cmp[w][k] = 0.0f;
+    }
+    DS carry_t = DS{0.0f, 0.0f};
+    for (int base = 0; base < nsamp; base += 32) {
+        const int i = base + lane;
+        const bool act = i < nsamp;
+        Node n;
+        n.t = DS{0.0f, 0.0f};
+        float bnode[WM], e[WM], close[WM];
+#pragma unroll
+        for (int w = 0; w < WM; ++w) bnode[w] = e[w] = close[w] = 0.0f;
+        int step = 0;
+        DS a{0.0f, 0.0f}, bb{0.0f, 0.0f};
+        if (act) {
+            const int sl = i / nq;
+            step = i - sl * nq;
+            const float4 sg = b.seg[s0 + sl];
+            a = DS{sg.x, sg.y};
+            bb = DS{sg.z, sg.w};
+            sample_node(o, rc, a, bb, b.lower[s0 + sl] != 0, DS{in.u_hi[step], in.u_lo[step]},
+                        DS{in.wu_hi[step], in.wu_lo[step]}, n);
+#pragma unroll
+            for (int w = 0; w < WM; ++w)
+                if (w < W) bnode[w] = extinction(o, n.prof, n.st_prof, w);
+        }
+        const float pth = __shfl_up_sync(FULL_MASK, n.t.h, 1), ptl = __shfl_up_sync(FULL_MASK, n.t.l, 1);
+        float pbeta[WM];
+#pragma unroll
+        for (int w = 0; w < WM; ++w) pbeta[w] = __shfl_up_sync(FULL_MASK, bnode[w], 1);
+        if (act) {
+            DS t0;
+            float beta0[WM];
+            if (step == 0) {
+                t0 = a;
+                DS q[3], q2[3], r;
+                path_point(rc, a, q, q2, r);
+                const float h = path_height(o, r);
+                const Profile pa = profile_at(o, h);
+                const float sa = o.strato ? strato_profile(o, h) : 0.0f;
+#pragma unroll
+                for (int w = 0; w < WM; ++w) beta0[w] = w < W ? extinction(o, pa, sa, w) : 0.0f;
+            } else if (lane == 0) {
+                t0 = carry_t;
+#pragma unroll
+                for (int w = 0; w < WM; ++w) beta0[w] = carry_beta[w];
+            } else {
+                t0 = DS{pth, ptl};
+#pragma unroll
+                for (int w = 0; w < WM; ++w) beta0[w] = pbeta[w];
+            }
+            {
+                const DS tm = ds_half(ds_add(t0, n.t));
+                DS q[3], q2[3], r;
+                path_point(rc, tm, q, q2, r);
+                const float h = path_height(o, r);
+                const Profile pm = profile_at(o, h);
+                const float sm = o.strato ? strato_profile(o, h) : 0.0f;
+                const float wpan = ds_val(ds_sub(n.t, t0)) / 6.0f;
+#pragma unroll
+                for (int w = 0; w < WM; ++w)
+                    if (w < W) e[w] = wpan * ((beta0[w] + bnode[w]) + 4.0f * extinction(o, pm, sm, w));
+            }
+            if (step == nq - 1) {
+                DS q[3], q2[3], r;
+                path_point(rc, bb, q, q2, r);
+                float h = path_height(o, r);
+                const Profile pb = profile_at(o, h);
+                const float sb = o.strato ? strato_profile(o, h) : 0.0f;
+                const DS tm = ds_half(ds_add(n.t, bb));
+                path_point(rc, tm, q, q2, r);
+                h = path_height(o, r);
+                const Profile pm = profile_at(o, h);
+                const float sm = o.strato ? strato_profile(o, h) : 0.0f;
+                const float wpan = ds_val(ds_sub(bb, n.t)) / 6.0f;
+#pragma unroll
+                for (int w = 0; w < WM; ++w)
+                    if (w < W) {
+                        close[w] = wpan * ((bnode[w] + extinction(o, pb, sb, w)) + 4.0f * extinction(o, pm, sm, w));
+                        e[w] += close[w];
+                    }
+            }
+        }
+        float S[WM];
+#pragma unroll
+        for (int w = 0; w < WM; ++w) {
+            float v = e[w];
+#pragma unroll
+            for (int dd = 1; dd < 32; dd <<= 1) {
+                const float u = __shfl_up_sync(FULL_MASK, v, dd);
+                if (lane >= dd) v += u;
+            }
+            S[w] = v;
+        }
+        if (act) {
+#pragma unroll
+            for (int w = 0; w < WM; ++w) {
+                if (w >= W) continue;
+                const float att = n.ds * expf(-((carry[w] + S[w]) - close[w]));
+                float val[4];
+                if (first) {
+                    first_light_value(o, rc, n, w, phase, sphase[w], val);
+                } else {
+                    float aero[4];
+                    for (int c = 0; c < 4; ++c)
+                        aero[c] = sh_synth(o, rc.d32[2], rc.st, n.cp, in.plane + (size_t)n.cell[c] * o.K * W + w, W);
+                    warm_value(o, rc, n, in.field, w, aero, val);
+                }
+                for (int k = 0; k < 4; ++k) kahan(tot[w][k], cmp[w][k], val[k] * att);
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < WM; ++w) {
+            carry[w] += __shfl_sync(FULL_MASK, S[w], 31);
+            carry_beta[w] = __shfl_sync(FULL_MASK, bnode[w], 31);
+        }
+        carry_t = DS{__shfl_sync(FULL_MASK, n.t.h, 31), __shfl_sync(FULL_MASK, n.t.l, 31)};
+    }
+#pragma unroll
+    for (int w = 0; w < WM; ++w) {
+        float v[4];
+        for (int k = 0; k < 4; ++k) {
+            v[k] = tot[w][k] - cmp[w][k];
+#pragma unroll
+            for (int dd = 16; dd >= 1; dd >>= 1) v[k] += __shfl_xor_sync(FULL_MASK, v[k], dd);
+        }
+        if (lane == 0 && w < W) {
+            boundary_term(o, b, rc, in.boundary, ray, w, v);
+            rad[(size_t)ray * W + w] = make_float4(v[0], v[1], v[2], v[3]);
+        }
+    }
+}
+
 __global__ void plane_kernel(const float* __restrict__ field, const float* __restrict__ ha,
                              const float* __restrict__ sd, int nc, int K, int src, int W, int strato, long long n,
                              float* __restrict__ plane) {
@@ -570,6 +731,18 @@ static int run_transport(sosb_state* s, const BundleDev& b, int64_t ray0, int64_
         in.wu_hi = P<float>(s->wu_hi);
         in.wu_lo = P<float>(s->wu_lo);
         in.nq = d.nq;
+    }
+    if (d.W <= 4) {
+        // sample-parallel: one warp per ray
+        const long long blocks = (nray * 32 + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
+        Timer timer(s, K_TRANSPORT);
+        if (d.W == 1)
+            transport_warp_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, 0, s->stream>>>(
+                optics_of(s), rays_of(b), in, (int)ray0, (int)nray, P<float4>(s->rad));
+        else
+            transport_warp_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, 0, s->stream>>>(
+                optics_of(s), rays_of(b), in, (int)ray0, (int)nray, P<float4>(s->rad));
+        return launch_check(s);
     }
     const int wchunk = std::min(d.W, 32);
     int glog2 = 0;

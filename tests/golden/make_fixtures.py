@@ -271,12 +271,16 @@ def make(name, spec, out_dir=HERE):
     arrays['pin_project_flux'] = proj_f
 
     t2 = time.time()
-    x, stats = Solver(s, geometry, fixed_boxes=False).solve(64, cfg['anderson_tol'])
+    try:
+        x, stats = Solver(s, geometry, fixed_boxes=False).solve(64, cfg['anderson_tol'])
+    except RuntimeError as exc:  # the reference's own outcome (E_NOT_CONVERGED) is recorded, not hidden
+        x, stats = None, dict(evaluations=64, converged=[], history=[], error=str(exc))
     solve_seconds = time.time() - t2
-    arrays['solve_x'] = np.asarray(x, 'f4')
-    arrays['solve_boxes'] = np.asarray(Solver(s, geometry).boxes(x), 'f8')
+    if x is not None:
+        arrays['solve_x'] = np.asarray(x, 'f4')
+        arrays['solve_boxes'] = np.asarray(Solver(s, geometry).boxes(x), 'f8')
     meta.update(
-        evaluations=int(stats['evaluations']), converged=stats['converged'],
+        evaluations=int(stats['evaluations']), converged=stats['converged'], solve_error=stats.get('error'),
         history_observer=[h['observer_relative'] for h in stats['history']],
         history_source=[h['source_relative'] for h in stats['history']],
         create_seconds=create_seconds, solve_seconds=solve_seconds, outputs_seconds=t2 - t1,

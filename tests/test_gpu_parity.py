@@ -79,6 +79,8 @@ def test_apply_and_boxes(solver):
 
 def test_solve_matches_reference(solver):
     st = solver.state
+    if 'solve_x' not in st:
+        pytest.skip('the reference solve of this state did not converge: ' + str(st.meta.get('solve_error')))
     x, stats = solver.solve(int(st.meta['max_eval']), float(st.meta['tolerance']))
     assert stats['converged'] == [True] * st.W
     assert abs(stats['evaluations'] - st.meta['evaluations']) <= 2
