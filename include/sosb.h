@@ -132,6 +132,18 @@ int sosb_evaluate(sosb_handle h, int phase, int first, const float *field_dev, c
 /* Replaces: Solver.apply (source_iteration.py:161-216): ground pass, warm pass with the boundary, first-light moments
  * added, composition into the next source out_dev [cells][slots][W] (first call also runs first light). */
 int sosb_apply(sosb_handle h, const float *field_dev, float *out_dev);
+/* Allocation-free composition (no counterpart in the reference): the composition step of Solver.apply with the
+ * reference's source metrics, for callers that must not allocate device memory once a state is set up - for example
+ * a host loop that runs inside a service whose device memory is fully reserved by another allocator, or a pipeline
+ * that cannot afford the device-wide synchronisation a cudaMalloc may cause. moments_dev [cells][4+K][W] (warm pass)
+ * plus first_moments_dev (first light) are composed into out_dev [cells][slots][W]; wavelengths whose bit is set in
+ * done_mask keep x_dev's values. Per wavelength it returns the count of non-finite composed values and
+ * max|g - x| / max|g|. It calls no cudaMalloc, cudaFree or allocating library routine: its reduction scratch is a
+ * file-scope device array of 3 x 64 words (W <= 64; larger W is rejected with E_SHAPE). The first call on each device
+ * looks that array's address up (cudaGetSymbolAddress) with the device current, so make the first call before any
+ * stream capture. Every call shares the array and clears it first: calls that overlap on the GPU race. */
+int sosb_compose_static(sosb_handle h, const float *moments_dev, const float *first_moments_dev, const float *x_dev,
+                        uint64_t done_mask, float *out_dev, int64_t *nonfinite_host, double *source_relative_host);
 /* Replaces: Solver.boxes (source_iteration.py:218-222): observer values [n_monitor_rows][n_dirs][W] to host. */
 int sosb_boxes(sosb_handle h, const float *field_dev, double *out_host);
 /* Replaces: Solver.solve (source_iteration.py:309-663): first light, then the fixed-point iteration from x0 (NULL:

@@ -76,6 +76,8 @@ SIGNATURES = {
     'sosb_boxes': ([ctypes.c_void_p, ctypes.c_void_p, P_f64], c_int),
     'sosb_solve': ([ctypes.c_void_p, c_int, c_dbl, ctypes.c_void_p, ctypes.c_void_p, c_int, ctypes.POINTER(Stats)],
                    c_int),
+    'sosb_compose_static': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                             ctypes.c_void_p, P_i64, P_f64], c_int),
     'sosb_set_timing': ([ctypes.c_void_p, c_int], c_int),
     'sosb_get_timing': ([ctypes.c_void_p, P_f64, P_i64, c_int], c_int),
     'sosb_last_error': ([ctypes.c_void_p], ctypes.c_char_p),

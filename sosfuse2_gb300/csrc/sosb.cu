@@ -17,6 +17,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1105,6 +1106,65 @@ int sosb_apply(sosb_handle s, const float* field_dev, float* out_dev) {
     s->err.clear();
     TRY(apply_impl(s, field_dev, out_dev, 0ull));
     CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+// ------------------------------------------------------------------------ allocation-free composition
+// Scratch of sosb_compose_static: the composition kernel's per-wavelength reduction words (nonfinite count, max |g|,
+// max |g - x|), 3 x SOSB_STATIC_WAVES words. It lives in a file-scope device array, so this entry point never
+// allocates; every GPU that loads the library holds these 768 bytes until the process exits.
+#define SOSB_STATIC_WAVES 64
+static __device__ __align__(256) unsigned g_compose_scratch[3 * SOSB_STATIC_WAVES];
+
+// The array's name is only a host-side stand-in for it; the device address is looked up once per device, with that
+// device current, and kept here.
+static std::mutex g_compose_scratch_lock;
+static unsigned* g_compose_scratch_dev[256] = {nullptr};
+
+static int compose_scratch_address(sosb_state* s, unsigned** out) {
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(s, "E_DEVICE: device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> guard(g_compose_scratch_lock);
+    if (!g_compose_scratch_dev[dev]) {
+        void* ptr = nullptr;
+        CK(cudaGetSymbolAddress(&ptr, g_compose_scratch));
+        g_compose_scratch_dev[dev] = static_cast<unsigned*>(ptr);
+    }
+    *out = g_compose_scratch_dev[dev];
+    return 0;
+}
+
+int sosb_compose_static(sosb_handle s, const float* moments_dev, const float* first_moments_dev, const float* x_dev,
+                        uint64_t done_mask, float* out_dev, int64_t* nonfinite_host, double* source_relative_host) {
+    if (!s) return 1;
+    s->err.clear();
+    const sosb_dims& d = s->d;
+    if (!s->have_constants) return fail(s, "E_STATE: constants not set");
+    if (!moments_dev || !first_moments_dev || !x_dev || !out_dev || !nonfinite_host || !source_relative_host)
+        return fail(s, "E_FIELD: null pointer");
+    if (d.W > SOSB_STATIC_WAVES)
+        return fail(s, "E_SHAPE: %d wavelengths exceed the static composition scratch (%d)", d.W, SOSB_STATIC_WAVES);
+    unsigned* scratch = nullptr;
+    TRY(compose_scratch_address(s, &scratch));
+    // the scratch keeps the previous call's words: clear the part this call accumulates into
+    CK(cudaMemsetAsync(scratch, 0, 3 * SOSB_STATIC_WAVES * sizeof(unsigned), s->stream));
+    const long long n = (long long)s->ns * s->src * d.W;
+    compose_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(
+        moments_dev, first_moments_dev, x_dev, P<float>(s->rf), P<float>(s->af), P<float>(s->asca), P<float>(s->ext0),
+        P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, (unsigned long long)done_mask, out_dev,
+        scratch);
+    TRY(launch_check(s));
+    unsigned words[3 * SOSB_STATIC_WAVES];
+    CK(cudaMemcpyAsync(words, scratch, 3 * d.W * sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    for (int w = 0; w < d.W; ++w) {
+        float mg, df;
+        std::memcpy(&mg, &words[d.W + w], 4);
+        std::memcpy(&df, &words[2 * d.W + w], 4);
+        nonfinite_host[w] = words[w];
+        source_relative_host[w] = (double)(df / std::max(mg, 1e-30f));
+    }
     return 0;
 }
 
