@@ -91,60 +91,6 @@ def _touched_sun(c, g_cells, strat):
     return mask
 
 
-def _pack_cells(groups, c, strat):
-    """Concatenate per-cell ray packs into one CSR bundle with per-ray compacted segments."""
-    from sosfuse2.backends import numpy_reference as nr
-
-    cell_off = [0]
-    p, target, d, dloc, weight = [], [], [], [], []
-    seg_off, seg_a, seg_b, seg_lower = [0], [], [], []
-    end_j, end_f, end_col, end_st, hits = [], [], [], [], []
-    for g in groups:
-        n = len(g['d'])
-        cell_off.append(cell_off[-1] + n)
-        if not np.all(g['p'] == g['p'][0]) or not np.all(g['target'] == g['target'][0]):
-            raise ValueError('one start and frame per cell expected')
-        p.append(g['p'][0])
-        target.append(g['target'][0])
-        d.append(g['d'])
-        dloc.append(g['dloc'])
-        weight.append(g['weight'])
-        e = g['edges']
-        for r in range(n):
-            for k in range(e.shape[1] - 1):
-                if e[r, k + 1] - e[r, k] > 1e-8:
-                    seg_a.append(e[r, k])
-                    seg_b.append(e[r, k + 1])
-                    seg_lower.append(bool(g['lower'][r, k]))
-            seg_off.append(len(seg_a))
-        end_j.append(g['end_index'])
-        end_f.append(g['end_fraction'])
-        hits.append(g['hits_ground'])
-        if np.any(g['hits_ground']) and 'gm' in c:
-            col, stcol = nr.boundary_end_columns(g, c, strat)
-        else:
-            col, stcol = g['end_columns'], None
-        end_col.append(np.asarray(col, 'f4'))
-        end_st.append(np.zeros(n, 'f4') if stcol is None else np.asarray(stcol, 'f4'))
-    return dict(
-        cell_off=np.asarray(cell_off, 'i8'),
-        p=np.asarray(p, 'f8'),
-        target=np.asarray(target, 'f8'),
-        d=np.concatenate(d).astype('f8'),
-        dloc=np.concatenate(dloc).astype('f8'),
-        weight=np.concatenate(weight).astype('f8'),
-        seg_off=np.asarray(seg_off, 'i8'),
-        seg_a=np.asarray(seg_a, 'f8'),
-        seg_b=np.asarray(seg_b, 'f8'),
-        seg_lower=np.asarray(seg_lower, 'u1'),
-        end_j=np.concatenate(end_j).astype('i4'),
-        end_f=np.concatenate(end_f).astype('f8'),
-        end_col=np.concatenate(end_col).astype('f4'),
-        end_st=np.concatenate(end_st).astype('f4'),
-        hits=np.concatenate(hits).astype('u1'),
-    )
-
-
 def make(name, spec, out_dir=HERE):
     root = Path(tempfile.mkdtemp(prefix='sosb_fixture_'))
     cache = _environment(root)
@@ -176,69 +122,23 @@ def make(name, spec, out_dir=HERE):
     nq = cfg['path_n']
     c = s.kernel.setup(s, nq)
     strat = 'strato_ext' in c
-    L, K, W = s.kernel.L, s.kernel.K, s.W
-    nh, nc = len(s.geo.h), len(s.geo.chi)
+    W, nc = s.W, len(s.geo.chi)
+    # inputs of the hot path, packed by the product's own adapter
+    sys.path.insert(0, str(HERE.parents[1]))
+    from sosfuse2_gb300.reference_adapter import observer_rays, pack_state
 
-    # observer rays of engine_core.Solver.boxes, captured as the fixed-box path does (record, no transport)
-    raws = []
-
-    def record(raw, solver, _field, first=False):
-        raws.append(raw)
-        return np.zeros((len(raw['d']), solver.W, 2, 4), 'f8')
-
-    s.kernel.transport = record
-    try:
-        s.boxes(np.empty(0, 'f4'), False)
-    finally:
-        del s.kernel.transport
-    nq_query = raws[0]['nq']
-    cq = s.kernel.setup(s, nq_query)
-    u4, w4 = np.polynomial.legendre.leggauss(4)
-    ww = (w4[:, None] * w4[None, :] / 4).ravel()
-
-    bundle = _pack_cells(groups, c, strat)
-    query = _pack_cells(raws, cq, strat)
+    arrays = pack_state(s, geometry, scope, float(cfg['anderson_tol']), 64)
+    meta = json.loads(arrays['meta'])
+    meta.update(name=name, reference='cheek-walnut/sosfuse2 NumPy backend (numpy_reference.transport/project, '
+                                     'Solver.solve)', numpy=np.__version__, create_seconds=create_seconds)
+    raws = observer_rays(s)
+    cq = s.kernel.setup(s, raws[0]['nq'])
+    # the solar tables only where a first-light sample can read them
     sun_mask = _touched_sun(c, groups, strat)
-    opt = c['density_optics']
-    meta = dict(
-        name=name, L=L, K=K, W=W, nq=nq, nq_query=nq_query, nh=nh, nc=nc, ns=int(s.geo.ns),
-        source_size=int(source_size(s)), strato=bool(strat),
-        g=float(c['g']), mix=float(c['mix']), height=float(c['height']), albedo=float(c['albedo']),
-        top_km=float(c['domain'].top_km), profile_step_km=float(c['domain'].step_km),
-        density_mask=int(opt['mask']), air_surface=float(opt.get('air_surface', 1.0)),
-        tolerance=float(cfg['anderson_tol']), max_eval=64, monitors=len(s.ctx.b.HS) if hasattr(s.ctx.b, 'HS') else 5,
-        n_dirs=7, box_points=16, wavelengths_nm=wl.tolist(), C=float(scope.C),
-        reference='cheek-walnut/sosfuse2 NumPy backend (numpy_reference.transport/project, Solver.solve)',
-        numpy=np.__version__,
-    )
-    arrays = dict(
-        u=np.asarray(c['u'], 'f8'), wu=np.asarray(c['wu'], 'f8'),
-        uq=np.asarray(cq['u'], 'f8'), wuq=np.asarray(cq['wu'], 'f8'),
-        h=c['h'], chi=c['chi'], hr=c['hr'], ha=c['ha'], ext=c['ext'], asca=c['asca'],
-        sun_h=c['sun_h'], sun_col=np.where(sun_mask[..., None], c['sun_col'], np.float32(0)).astype('f4'),
-        sun_mask=sun_mask,
-        gm=c['gm'], gd=c['gd'], gv=c['gv'],
-        density_table=np.asarray(opt['table'], 'f4'),
-        rf=np.asarray(s.rf, 'f4'), af=np.asarray(s.af[:K], 'f4'), ext0=np.asarray(s.ext[0], 'f4'),
-        solar=np.asarray(s.solar, 'f8'), box_ww=ww,
-    )
+    arrays['sun_col'] = np.where(sun_mask[..., None], c['sun_col'], np.float32(0)).astype('f4')
+    arrays['sun_mask'] = sun_mask
     if strat:
-        from sosfuse2.atmosphere.stratosphere import eigen_by_sh
-
-        prof = c['strato_profile']
-        arrays.update(
-            strato_ext=c['strato_ext'], strato_sca=c['strato_sca'], strato_chi=np.asarray(c['strato_chi'], 'f4'),
-            strato_density=c['strato_density'],
-            strato_sun_col=np.where(sun_mask, c['strato_sun_col'], np.float32(0)).astype('f4'),
-            strato_eigen=np.asarray(eigen_by_sh(s.strato, L), 'f4'),
-            strato_sca_source=np.asarray(s.strato['sca'], 'f4'),
-        )
-        meta.update(strato_center=float(prof['center']), strato_sigma=float(prof['sigma']),
-                    strato_norm=float(prof['norm']))
-    for k, v in bundle.items():
-        arrays['cell_' + k] = v
-    for k, v in query.items():
-        arrays['query_' + k] = v
+        arrays['strato_sun_col'] = np.where(sun_mask, c['strato_sun_col'], np.float32(0)).astype('f4')
 
     # ---- reference outputs ----
     t1 = time.time()
@@ -284,8 +184,6 @@ def make(name, spec, out_dir=HERE):
         history_observer=[h['observer_relative'] for h in stats['history']],
         history_source=[h['source_relative'] for h in stats['history']],
         create_seconds=create_seconds, solve_seconds=solve_seconds, outputs_seconds=t2 - t1,
-        rays=int(len(bundle['d'])), segments=int(len(bundle['seg_a'])),
-        query_rays=int(len(query['d'])),
     )
     arrays['meta'] = np.asarray(json.dumps(meta))
     path = out_dir / f'{name}.npz'
