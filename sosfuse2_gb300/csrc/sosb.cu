@@ -316,6 +316,192 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
     }
 }
 
+// Node record shared by the lanes of one warp: everything the per-wavelength part of a node needs.
+constexpr int REC_WORDS = 73;  // odd stride: the 32 lanes write their records without bank conflicts
+struct NodeRec {
+    float r_h, r_l, qz_h, qz_l, h, ds, cp, mu, exd, eyd, st_prof;
+    float sw[4];
+    int cell[4];
+    int ir, flags;  // bit 0: first node of its segment, bit 1: last node of its segment
+    float T[16];
+    float prof[5];
+    float pa[6];   // profiles (+ stratospheric) at the segment start (first node only)
+    float pm[6];   // at the panel midpoint
+    float pb[6];   // at the segment end (last node only)
+    float pmc[6];  // at the closing panel's midpoint (last node only)
+    float wpan, wpc;
+};
+static_assert(sizeof(NodeRec) <= REC_WORDS * 4, "node record exceeds its stride");
+
+SOS_HD float ext6(const Optics& o, const float* p6, int w) {
+    float b = 0.0f;
+    for (int k = 0; k < 5; ++k) b += p6[k] * o.ext[k * o.W + w];
+    if (o.strato) b += p6[5] * o.strato_ext[w];
+    return b;
+}
+
+SOS_HD void profile6(const Optics& o, const RayConst& rc, DS t, float* p6) {
+    DS q[3], q2[3], r;
+    path_point(rc, t, q, q2, r);
+    const float h = path_height(o, r);
+    const Profile p = profile_at(o, h);
+    for (int k = 0; k < 5; ++k) p6[k] = p.v[k];
+    p6[5] = o.strato ? strato_profile(o, h) : 0.0f;
+}
+
+// Transport for many wavelengths: one warp per (ray, chunk of 32 wavelengths). Phase A: lane j evaluates node
+// base+j's geometry and the profiles its Simpson panels need, into a shared-memory record. Phase B: lane = wavelength
+// walks the 32 records in order, exactly as transport_lane does (same per-wavelength operation order), with its own
+// 4-slot corner SH cache in shared memory.
+constexpr int WAVE_WARPS = 2;
+
+__global__ void __launch_bounds__(WAVE_WARPS * 32)
+    transport_wave_kernel(Optics o, Rays b, LaneInputs in, int ray0, int nray, int wchunks, float4* rad) {
+    extern __shared__ float wave_sm[];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const long long warp = (long long)blockIdx.x * WAVE_WARPS + wid;
+    if (warp >= (long long)nray * wchunks) return;  // the whole warp leaves together
+    const int ray = ray0 + (int)(warp / wchunks);
+    const int w = (int)(warp % wchunks) * 32 + lane;
+    const bool wok = w < o.W;
+    const int wl = wok ? w : o.W - 1;  // idle lanes compute a valid wavelength and store nothing
+    const int L1 = o.L + 1;
+    float* recs = wave_sm + (size_t)wid * (32 * REC_WORDS + 4 * L1 * 32);
+    float* cache = recs + 32 * REC_WORDS + lane;  // [slot*(L+1) + m] * 32 + lane
+    RayConst rc;
+    ray_constants(b, ray, rc);
+    const bool first = in.first != 0;
+    const int nq = in.nq;
+    const int s0 = b.seg_off[ray], s1 = b.seg_off[ray + 1];
+    const int nsamp = (s1 - s0) * nq;
+    const float phase = hg_phase(rc.d32[2], o.g);
+    const float sphase = (o.strato && first) ? legendre_phase(o, rc.d32[2], wl) : 0.0f;
+    float total[4] = {0, 0, 0, 0}, comp[4] = {0, 0, 0, 0};
+    float tau = 0.0f, tauc = 0.0f, acc = 0.0f, beta0 = 0.0f;
+    int tag[4] = {-1, -1, -1, -1};
+    DS carry_t = DS{0.0f, 0.0f};
+    for (int base = 0; base < nsamp; base += 32) {
+        const int i = base + lane;
+        const int cnt = min(32, nsamp - base);
+        DS tnode = DS{0.0f, 0.0f};
+        __syncwarp();
+        if (i < nsamp) {
+            NodeRec* R = reinterpret_cast<NodeRec*>(recs + lane * REC_WORDS);
+            const int sl = i / nq;
+            const int step = i - sl * nq;
+            const float4 sg = b.seg[s0 + sl];
+            const DS a = DS{sg.x, sg.y}, bb = DS{sg.z, sg.w};
+            Node n;
+            sample_node(o, rc, a, bb, b.lower[s0 + sl] != 0, DS{in.u_hi[step], in.u_lo[step]},
+                        DS{in.wu_hi[step], in.wu_lo[step]}, n);
+            tnode = n.t;
+            R->r_h = n.r.h; R->r_l = n.r.l; R->qz_h = n.qz.h; R->qz_l = n.qz.l; R->h = n.h; R->ds = n.ds;
+            R->cp = n.cp; R->mu = n.mu; R->exd = n.exd; R->eyd = n.eyd; R->st_prof = n.st_prof;
+            for (int c = 0; c < 4; ++c) { R->sw[c] = n.sw[c]; R->cell[c] = n.cell[c]; }
+            R->ir = n.ir;
+            R->flags = (step == 0 ? 1 : 0) | (step == nq - 1 ? 2 : 0);
+            for (int k = 0; k < 4; ++k)
+                for (int u = 0; u < 4; ++u) R->T[4 * k + u] = n.T[k][u];
+            for (int k = 0; k < 5; ++k) R->prof[k] = n.prof.v[k];
+            R->wpan = 0.0f;  // set below, once the previous node's coordinate is known
+            if (step == 0) profile6(o, rc, a, R->pa);
+            if (step == nq - 1) {
+                profile6(o, rc, bb, R->pb);
+                profile6(o, rc, ds_half(ds_add(n.t, bb)), R->pmc);
+                R->wpc = ds_val(ds_sub(bb, n.t)) / 6.0f;
+            }
+        }
+        const float pth = __shfl_up_sync(FULL_MASK, tnode.h, 1), ptl = __shfl_up_sync(FULL_MASK, tnode.l, 1);
+        if (i < nsamp) {
+            NodeRec* R = reinterpret_cast<NodeRec*>(recs + lane * REC_WORDS);
+            const int sl = i / nq;
+            const int step = i - sl * nq;
+            DS t0;
+            if (step == 0) {
+                const float4 sg = b.seg[s0 + sl];
+                t0 = DS{sg.x, sg.y};
+            } else {
+                t0 = lane == 0 ? carry_t : DS{pth, ptl};
+            }
+            profile6(o, rc, ds_half(ds_add(t0, tnode)), R->pm);
+            R->wpan = ds_val(ds_sub(tnode, t0)) / 6.0f;
+        }
+        carry_t = DS{__shfl_sync(FULL_MASK, tnode.h, 31), __shfl_sync(FULL_MASK, tnode.l, 31)};
+        __syncwarp();
+        // phase B: this lane's wavelength over the records in order
+        for (int j = 0; j < cnt; ++j) {
+            const NodeRec* R = reinterpret_cast<const NodeRec*>(recs + j * REC_WORDS);
+            const int flags = R->flags;
+            if (flags & 1) {
+                acc = 0.0f;
+                beta0 = ext6(o, R->pa, wl);
+            }
+            float beta1 = 0.0f;
+            for (int k = 0; k < 5; ++k) beta1 += R->prof[k] * o.ext[k * o.W + wl];
+            if (o.strato) beta1 += R->st_prof * o.strato_ext[wl];
+            acc = acc + R->wpan * ((beta0 + beta1) + 4.0f * ext6(o, R->pm, wl));
+            beta0 = beta1;
+            const float att = R->ds * expf(-((tau - tauc) + acc));
+            Node n;
+            n.r = DS{R->r_h, R->r_l};
+            n.qz = DS{R->qz_h, R->qz_l};
+            n.h = R->h;
+            n.ds = R->ds;
+            n.cp = R->cp;
+            n.mu = R->mu;
+            n.exd = R->exd;
+            n.eyd = R->eyd;
+            n.st_prof = R->st_prof;
+            for (int c = 0; c < 4; ++c) { n.sw[c] = R->sw[c]; n.cell[c] = R->cell[c]; }
+            n.ir = R->ir;
+            for (int k = 0; k < 4; ++k)
+                for (int u = 0; u < 4; ++u) n.T[k][u] = R->T[4 * k + u];
+            for (int k = 0; k < 5; ++k) n.prof.v[k] = R->prof[k];
+            float val[4];
+            if (first) {
+                first_light_value(o, rc, n, wl, phase, sphase, val);
+            } else {
+                int slot_of[4];
+                unsigned used = 0;
+                for (int c = 0; c < 4; ++c) {
+                    slot_of[c] = -1;
+                    for (int q = 0; q < 4; ++q)
+                        if (tag[q] == n.cell[c] && !(used & (1u << q))) {
+                            slot_of[c] = q;
+                            used |= 1u << q;
+                            break;
+                        }
+                }
+                for (int c = 0; c < 4; ++c) {
+                    if (slot_of[c] >= 0) continue;
+                    int q = 0;
+                    while (used & (1u << q)) ++q;
+                    used |= 1u << q;
+                    slot_of[c] = q;
+                    tag[q] = n.cell[c];
+                    sh_contract(o, rc.d32[2], rc.st, in.plane + (size_t)n.cell[c] * o.K * o.W + wl, o.W,
+                                cache + (size_t)q * L1 * 32, 32);
+                }
+                float aero[4];
+                for (int c = 0; c < 4; ++c) aero[c] = azimuth_sum(o.L, n.cp, cache + (size_t)slot_of[c] * L1 * 32, 32);
+                warm_value(o, rc, n, in.field, wl, aero, val);
+            }
+            for (int k = 0; k < 4; ++k) kahan(total[k], comp[k], val[k] * att);
+            if (flags & 2) {
+                acc = acc + R->wpc * ((beta0 + ext6(o, R->pb, wl)) + 4.0f * ext6(o, R->pmc, wl));
+                kahan(tau, tauc, acc);
+            }
+        }
+    }
+    if (wok) {
+        boundary_term(o, b, rc, in.boundary, ray, w, total);
+        rad[(size_t)ray * o.W + w] = make_float4(total[0], total[1], total[2], total[3]);
+    }
+}
+
+static size_t wave_smem(int L) { return sizeof(float) * (size_t)WAVE_WARPS * (32 * REC_WORDS + 4 * (L + 1) * 32); }
+
 __global__ void plane_kernel(const float* __restrict__ field, const float* __restrict__ ha,
                              const float* __restrict__ sd, int nc, int K, int src, int W, int strato, long long n,
                              float* __restrict__ plane) {
@@ -745,6 +931,16 @@ static int run_transport(sosb_state* s, const BundleDev& b, int64_t ray0, int64_
                 optics_of(s), rays_of(b), in, (int)ray0, (int)nray, P<float4>(s->rad));
         return launch_check(s);
     }
+    {
+        // many wavelengths: one warp per (ray, chunk of 32 wavelengths), geometry shared through shared memory
+        const int wchunks = (d.W + 31) / 32;
+        const long long warps = (long long)nray * wchunks;
+        const long long blocks = (warps + WAVE_WARPS - 1) / WAVE_WARPS;
+        Timer timer(s, K_TRANSPORT);
+        transport_wave_kernel<<<(unsigned)blocks, WAVE_WARPS * 32, wave_smem(d.L), s->stream>>>(
+            optics_of(s), rays_of(b), in, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
+        return launch_check(s);
+    }
     const int wchunk = std::min(d.W, 32);
     int glog2 = 0;
     while ((1 << glog2) < wchunk) ++glog2;
@@ -916,7 +1112,9 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
         if (cudaFuncSetAttribute(transport_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t_smem) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_smem) !=
-                cudaSuccess) {
+                cudaSuccess ||
+            cudaFuncSetAttribute(transport_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)wave_smem(d.L)) != cudaSuccess) {
             cudaStreamDestroy(s->own);
             delete s;
             return 5;
