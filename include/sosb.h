@@ -157,6 +157,12 @@ int sosb_solve(sosb_handle h, int max_eval, double tolerance, const float *x0_ho
  * sosb_get_timing fills ms[k] and launches[k] for k < n. */
 int sosb_set_timing(sosb_handle h, int on);
 int sosb_get_timing(sosb_handle h, double *ms, int64_t *launches, int n);
+/* Batched form of Solver.solve (no single counterpart in the reference, whose pipeline runs one state per process,
+ * src/sosfuse2/jobs/pipeline_execution.py): n independent states, each its own handle and stream, solved concurrently
+ * by `threads` host threads (0: one per state) so that their small launches overlap on the GPU. status[i] is state
+ * i's sosb_solve result (its message in sosb_last_error(hs[i])); returns nonzero when any state failed. */
+int sosb_solve_batch(sosb_handle *hs, int n, int max_eval, double tolerance, const float *const *x0_host,
+                     float *const *x_out, int x_out_is_device, sosb_stats *stats, int *status, int threads);
 /* Message of the last failed call on this handle (empty when none). */
 const char *sosb_last_error(sosb_handle h);
 /* Sizes the handle was created with: cells, slots per cell, K. */

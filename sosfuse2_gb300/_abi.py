@@ -78,6 +78,8 @@ SIGNATURES = {
                    c_int),
     'sosb_compose_static': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                              ctypes.c_void_p, P_i64, P_f64], c_int),
+    'sosb_solve_batch': ([ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_dbl, ctypes.POINTER(ctypes.c_void_p),
+                          ctypes.POINTER(ctypes.c_void_p), c_int, ctypes.POINTER(Stats), P_i32, c_int], c_int),
     'sosb_set_timing': ([ctypes.c_void_p, c_int], c_int),
     'sosb_get_timing': ([ctypes.c_void_p, P_f64, P_i64, c_int], c_int),
     'sosb_last_error': ([ctypes.c_void_p], ctypes.c_char_p),

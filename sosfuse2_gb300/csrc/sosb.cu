@@ -18,6 +18,8 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <thread>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -1606,6 +1608,28 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
         return fail(s, "E_NOT_CONVERGED: %d/%d within %g", nd, W, tol);
     }
     return 0;
+}
+
+
+int sosb_solve_batch(sosb_handle* hs, int n, int max_eval, double tol, const float* const* x0_host,
+                     float* const* x_out, int x_out_is_device, sosb_stats* stats, int* status, int threads) {
+    if (!hs || !x_out || !status || n < 0) return 1;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 2;
+    const int nt = std::max(1, std::min(threads > 0 ? threads : n, n));
+    std::atomic<int> next(0);
+    auto work = [&]() {
+        cudaSetDevice(dev);
+        for (int i = next++; i < n; i = next++)
+            status[i] = sosb_solve(hs[i], max_eval, tol, x0_host ? x0_host[i] : nullptr, x_out[i], x_out_is_device,
+                                   stats ? &stats[i] : nullptr);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(work);
+    for (auto& t : pool) t.join();
+    int failed = 0;
+    for (int i = 0; i < n; ++i) failed += status[i] != 0;
+    return failed ? 3 : 0;
 }
 
 }  // extern "C"

@@ -189,3 +189,43 @@ class Solver:
             source_relative=[float(stats.source_relative[w]) for w in range(W)],
             kernel_launches=int(stats.kernel_launches),
         )
+
+
+class BatchSolver:
+    """Many independent states solved together (sosb_solve_batch): each state has its own handle and stream, and the
+    library's host threads run their fixed-point loops concurrently so the GPU overlaps their launches."""
+
+    def __init__(self, states, device=None):
+        self.kernels = [Kernel(st, device) for st in states]
+        for k in self.kernels:
+            k._check(k.lib.sosb_set_stream(k.h, None))  # each handle on its own stream
+        self.lib = self.kernels[0].lib if self.kernels else _abi.library()
+
+    def close(self):
+        for k in self.kernels:
+            k.close()
+
+    def solve(self, max_eval=64, tolerance=1e-3, initial=None, threads=0):
+        """[(field, stats) or RuntimeError per state]; fields are host arrays."""
+        n = len(self.kernels)
+        outs = [np.empty(k.state.shape, np.float32) for k in self.kernels]
+        x0 = None if initial is None else [np.ascontiguousarray(a, np.float32) for a in initial]
+        handles = (ctypes.c_void_p * n)(*[k.h.value for k in self.kernels])
+        out_ptrs = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
+        x0_ptrs = None if x0 is None else (ctypes.c_void_p * n)(*[a.ctypes.data for a in x0])
+        stats = (_abi.Stats * n)()
+        status = (ctypes.c_int32 * n)()
+        t = time.perf_counter()
+        self.lib.sosb_solve_batch(handles, n, int(max_eval), float(tolerance), x0_ptrs, out_ptrs, 0, stats, status,
+                                  int(threads))
+        seconds = time.perf_counter() - t
+        results = []
+        for i, k in enumerate(self.kernels):
+            if status[i]:
+                results.append(RuntimeError(k.lib.sosb_last_error(k.h).decode()))
+                continue
+            st = stats[i]
+            results.append((outs[i], dict(evaluations=int(st.evaluations), converged=[bool(st.done[w]) for w in range(k.W)],
+                                          seconds=float(st.seconds), kernel_launches=int(st.kernel_launches))))
+        self.seconds = seconds
+        return results
