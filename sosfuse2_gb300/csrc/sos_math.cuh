@@ -132,7 +132,10 @@ struct Optics {
     const float* sh_a;     // [K] recurrence coefficients (FP32)
     const float* sh_b;     // [K]
     const float* sh_d;     // [L+1] diagonal factors
+    const float* strato_lut;  // [STRATO_LUT_BINS + 1][W] stratospheric phase per sr on a uniform grid of u in [-1, 1]
 };
+
+constexpr int STRATO_LUT_BINS = 4096;
 
 // One bundle of rays: cells (destination points) with their incoming rays and compacted segments.
 struct Rays {
@@ -206,6 +209,17 @@ SOS_HD float legendre_phase(const Optics& o, float u, int w) {
         p1 = pn;
     }
     return val / C_4PI;
+}
+
+// Stratospheric phase by linear interpolation in its table (built from the same 33 Legendre moments in FP64), the
+// form the reference's CUDA path evaluates it in (kernel.cu strato_lut_build); used in the first-light ground sums.
+SOS_HD float legendre_phase_lut(const Optics& o, float u, int w) {
+    const float x = (clampf(u, -1.0f, 1.0f) + 1.0f) * (0.5f * STRATO_LUT_BINS);
+    int i = (int)x;
+    i = i > STRATO_LUT_BINS - 1 ? STRATO_LUT_BINS - 1 : i;
+    const float f = x - (float)i;
+    const float a = o.strato_lut[(size_t)i * o.W + w], b = o.strato_lut[(size_t)(i + 1) * o.W + w];
+    return a + f * (b - a);
 }
 
 SOS_HD float ftz_value(DS a) {
@@ -488,7 +502,7 @@ SOS_HD void first_light_value(const Optics& o, const RayConst& rc, const Node& n
             const float ph = (hg_phase(up, o.g) + hg_phase(dn, o.g)) / 2.0f;
             ground += (n.sw[c] * ph) * gv;
             if (o.strato) {
-                const float sph = (legendre_phase(o, up, w) + legendre_phase(o, dn, w)) / 2.0f;
+                const float sph = (legendre_phase_lut(o, up, w) + legendre_phase_lut(o, dn, w)) / 2.0f;
                 sground += (n.sw[c] * sph) * gv;
             }
         }
@@ -589,6 +603,76 @@ SOS_HD float sh_synth(const Optics& o, float mu, float st, float cp, const float
         total += cm * acc;
     }
     return total;
+}
+
+// The ray's SH basis at azimuth 0, Y[k] = scale_m P_lm(mu) (k = l(l+1)/2 + m), written by the lanes of a warp
+// (lane m computes column m by the upward recurrence, the same FP32 steps as sh_synth).
+SOS_HD void sh_basis_column(const Optics& o, float mu, float st, int m, float* Y) {
+    const int L = o.L;
+    float pmm = 0.28209479177387814f;
+    for (int q = 1; q <= m; ++q) pmm = (pmm * o.sh_d[q]) * st;
+    const float scale = m ? 1.41421356237309515f : 1.0f;
+    float p0 = pmm;
+    Y[m * (m + 1) / 2 + m] = scale * p0;
+    if (m < L) {
+        float p1 = (sqrtf(2.0f * m + 3.0f) * mu) * p0;
+        Y[(m + 1) * (m + 2) / 2 + m] = scale * p1;
+        for (int l = m + 2; l <= L; ++l) {
+            const int k = l * (l + 1) / 2 + m;
+            const float p2 = (o.sh_a[k] * mu) * p1 - o.sh_b[k] * p0;
+            Y[k] = scale * p2;
+            p0 = p1;
+            p1 = p2;
+        }
+    }
+}
+
+// sum_m cos(m phi) sum_l Y[k(l,m)] plane_c[k] for the four corner planes at once.
+SOS_HD void sh_synth4(int L, const float* Y, float cp, const float* const pc[4], int wstride, float out[4]) {
+    cp = clampf(cp, -1.0f, 1.0f);
+    float c0 = 1.0f, c1 = cp;
+    for (int c = 0; c < 4; ++c) out[c] = 0.0f;
+    for (int m = 0; m <= L; ++m) {
+        float cm;
+        if (m == 0) {
+            cm = 1.0f;
+        } else if (m == 1) {
+            cm = cp;
+        } else {
+            const float c2 = (2.0f * cp) * c1 - c0;
+            c0 = c1;
+            c1 = c2;
+            cm = c2;
+        }
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+        int k = m * (m + 1) / 2 + m;
+        for (int l = m; l <= L; ++l) {
+            const float y = Y[k];
+            const size_t off = (size_t)k * wstride;
+            s0 += y * pc[0][off];
+            s1 += y * pc[1][off];
+            s2 += y * pc[2][off];
+            s3 += y * pc[3][off];
+            k += l + 1;
+        }
+        out[0] += cm * s0;
+        out[1] += cm * s1;
+        out[2] += cm * s2;
+        out[3] += cm * s3;
+    }
+}
+
+// Per-m sums of one cell from a shared basis (the cached form of sh_synth4).
+SOS_HD void sh_contract_basis(int L, const float* Y, const float* plane_cell, int wstride, float* cache, int cstride) {
+    for (int m = 0; m <= L; ++m) {
+        float s = 0.0f;
+        int k = m * (m + 1) / 2 + m;
+        for (int l = m; l <= L; ++l) {
+            s += Y[k] * plane_cell[(size_t)k * wstride];
+            k += l + 1;
+        }
+        cache[m * cstride] = s;
+    }
 }
 
 SOS_HD void boundary_term(const Optics& o, const Rays& b, const RayConst& rc, const float* boundary, int ray, int w,

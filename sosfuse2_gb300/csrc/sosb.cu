@@ -65,7 +65,7 @@ struct sosb_state {
     bool have_constants = false;
     // constants
     DevBuf h, chi, hr, ha, ext, asca, table, sun_h, sun_col, gm, goff, gdir, gval, rf, af, ext0;
-    DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src;
+    DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src, s_lut;
     DevBuf sh_a, sh_b, sh_d;
     DevBuf u_hi, u_lo, wu_hi, wu_lo, uq_hi, uq_lo, wuq_hi, wuq_lo, box_ww, solar;
     BundleDev cells, obs;
@@ -159,6 +159,8 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
+static size_t warp_smem(int K) { return sizeof(float) * (size_t)K * (TRANSPORT_THREADS / 32); }
+
 SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }
 
 // Sample-parallel transport for few wavelengths (W <= WM): one warp per ray, lane i takes the ray's node i (batches
@@ -181,6 +183,12 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
     const int s0 = b.seg_off[ray], s1 = b.seg_off[ray + 1];
     const int nsamp = (s1 - s0) * nq;
     const float phase = hg_phase(rc.d32[2], o.g);
+    extern __shared__ float warp_sm[];
+    float* Y = warp_sm + (threadIdx.x >> 5) * o.K;  // this ray's SH basis, shared by the warp
+    if (!first) {
+        for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
+        __syncwarp();
+    }
     float sphase[WM], tot[WM][4], cmp[WM][4], carry[WM], carry_beta[WM];
 #pragma unroll
     for (int w = 0; w < WM; ++w) {
@@ -289,8 +297,9 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
                     first_light_value(o, rc, n, w, phase, sphase[w], val);
                 } else {
                     float aero[4];
-                    for (int c = 0; c < 4; ++c)
-                        aero[c] = sh_synth(o, rc.d32[2], rc.st, n.cp, in.plane + (size_t)n.cell[c] * o.K * W + w, W);
+                    const float* pc[4];
+                    for (int c = 0; c < 4; ++c) pc[c] = in.plane + (size_t)n.cell[c] * o.K * W + w;
+                    sh_synth4(o.L, Y, n.cp, pc, W, aero);
                     warm_value(o, rc, n, in.field, w, aero, val);
                 }
                 for (int k = 0; k < 4; ++k) kahan(tot[w][k], cmp[w][k], val[k] * att);
@@ -369,10 +378,15 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
     const bool wok = w < o.W;
     const int wl = wok ? w : o.W - 1;  // idle lanes compute a valid wavelength and store nothing
     const int L1 = o.L + 1;
-    float* recs = wave_sm + (size_t)wid * (32 * REC_WORDS + 4 * L1 * 32);
+    float* recs = wave_sm + (size_t)wid * (32 * REC_WORDS + 4 * L1 * 32 + o.K);
     float* cache = recs + 32 * REC_WORDS + lane;  // [slot*(L+1) + m] * 32 + lane
+    float* Y = recs + 32 * REC_WORDS + 4 * L1 * 32;  // this ray's SH basis, shared by the warp
     RayConst rc;
     ray_constants(b, ray, rc);
+    if (in.first == 0) {
+        for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
+        __syncwarp();
+    }
     const bool first = in.first != 0;
     const int nq = in.nq;
     const int s0 = b.seg_off[ray], s1 = b.seg_off[ray + 1];
@@ -482,8 +496,8 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
                     used |= 1u << q;
                     slot_of[c] = q;
                     tag[q] = n.cell[c];
-                    sh_contract(o, rc.d32[2], rc.st, in.plane + (size_t)n.cell[c] * o.K * o.W + wl, o.W,
-                                cache + (size_t)q * L1 * 32, 32);
+                    sh_contract_basis(o.L, Y, in.plane + (size_t)n.cell[c] * o.K * o.W + wl, o.W,
+                                      cache + (size_t)q * L1 * 32, 32);
                 }
                 float aero[4];
                 for (int c = 0; c < 4; ++c) aero[c] = azimuth_sum(o.L, n.cp, cache + (size_t)slot_of[c] * L1 * 32, 32);
@@ -502,7 +516,9 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
     }
 }
 
-static size_t wave_smem(int L) { return sizeof(float) * (size_t)WAVE_WARPS * (32 * REC_WORDS + 4 * (L + 1) * 32); }
+static size_t wave_smem(int L) {
+    return sizeof(float) * (size_t)WAVE_WARPS * (32 * REC_WORDS + 4 * (L + 1) * 32 + (L + 1) * (L + 2) / 2);
+}
 
 __global__ void plane_kernel(const float* __restrict__ field, const float* __restrict__ ha,
                              const float* __restrict__ sd, int nc, int K, int src, int W, int strato, long long n,
@@ -825,6 +841,7 @@ static Optics optics_of(const sosb_state* s) {
     o.sh_a = P<float>(s->sh_a);
     o.sh_b = P<float>(s->sh_b);
     o.sh_d = P<float>(s->sh_d);
+    o.strato_lut = P<float>(s->s_lut);
     return o;
 }
 
@@ -926,10 +943,10 @@ static int run_transport(sosb_state* s, const BundleDev& b, int64_t ray0, int64_
         const long long blocks = (nray * 32 + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
         Timer timer(s, K_TRANSPORT);
         if (d.W == 1)
-            transport_warp_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, 0, s->stream>>>(
+            transport_warp_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, warp_smem(s->K), s->stream>>>(
                 optics_of(s), rays_of(b), in, (int)ray0, (int)nray, P<float4>(s->rad));
         else
-            transport_warp_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, 0, s->stream>>>(
+            transport_warp_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, warp_smem(s->K), s->stream>>>(
                 optics_of(s), rays_of(b), in, (int)ray0, (int)nray, P<float4>(s->rad));
         return launch_check(s);
     }
@@ -1116,7 +1133,11 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
             cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_smem) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(transport_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)wave_smem(d.L)) != cudaSuccess) {
+                                 (int)wave_smem(d.L)) != cudaSuccess ||
+            cudaFuncSetAttribute(transport_warp_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
+            cudaFuncSetAttribute(transport_warp_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess) {
             cudaStreamDestroy(s->own);
             delete s;
             return 5;
@@ -1138,7 +1159,7 @@ int sosb_destroy(sosb_handle s) {
     cudaStreamSynchronize(s->stream);
     DevBuf* bufs[] = {&s->h, &s->chi, &s->hr, &s->ha, &s->ext, &s->asca, &s->table, &s->sun_h, &s->sun_col, &s->gm,
                       &s->goff, &s->gdir, &s->gval, &s->rf, &s->af, &s->ext0, &s->s_ext, &s->s_sca, &s->s_chi,
-                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->sh_a, &s->sh_b, &s->sh_d,
+                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->s_lut, &s->sh_a, &s->sh_b, &s->sh_d,
                       &s->u_hi, &s->u_lo, &s->wu_hi, &s->wu_lo, &s->uq_hi, &s->uq_lo, &s->wuq_hi, &s->wuq_lo,
                       &s->box_ww, &s->solar, &s->rad, &s->plane, &s->moments, &s->flux, &s->first_moments,
                       &s->first_flux, &s->boundary, &s->metrics, &s->boxes, &s->fx, &s->fg, &s->fn, &s->norms,
@@ -1249,6 +1270,23 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
         TRY(dput(s, s->s_sun_col, c->strato_sun_col, (size_t)d.n_sun_h * d.n_sun_x * 4));
         TRY(dput(s, s->s_eigen, c->strato_eigen, (size_t)K * W * 4));
         TRY(dput(s, s->s_sca_src, c->strato_sca_source, W * 4));
+        // phase table on u in [-1, 1] from the 33 Legendre moments (FP64 recurrence, per sr)
+        std::vector<float> lut((size_t)(STRATO_LUT_BINS + 1) * W);
+        for (int i = 0; i <= STRATO_LUT_BINS; ++i) {
+            const double u = -1.0 + 2.0 * i / STRATO_LUT_BINS;
+            for (int w = 0; w < W; ++w) {
+                double p0 = 1.0, p1 = u;
+                double v = c->strato_chi[w] + u * c->strato_chi[W + w];
+                for (int l = 2; l < 33; ++l) {
+                    const double pn = ((2.0 * l - 1) * u * p1 - (l - 1.0) * p0) / l;
+                    v += pn * c->strato_chi[l * W + w];
+                    p0 = p1;
+                    p1 = pn;
+                }
+                lut[(size_t)i * W + w] = (float)(v / (4.0 * M_PI));
+            }
+        }
+        TRY(dput_vec(s, s->s_lut, lut));
     }
     CK(cudaStreamSynchronize(s->stream));
     s->have_constants = true;

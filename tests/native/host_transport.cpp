@@ -38,6 +38,24 @@ extern "C" int host_transport(const sosb_dims* d, const sosb_constants* c, const
     o.strato_sun_col = c->strato_sun_col; o.gm = c->gm; o.goff = goff.data(); o.gdir = c->gdir; o.gval = c->gval;
     o.strato_ext = c->strato_ext; o.strato_sca = c->strato_sca; o.strato_chi = c->strato_chi;
     o.sh_a = sa.data(); o.sh_b = sb.data(); o.sh_d = sdg.data();
+    std::vector<float> lut;
+    if (d->strato) {
+        lut.resize((size_t)(STRATO_LUT_BINS + 1) * W);
+        for (int i = 0; i <= STRATO_LUT_BINS; ++i) {
+            const double u = -1.0 + 2.0 * i / STRATO_LUT_BINS;
+            for (int w = 0; w < W; ++w) {
+                double p0 = 1.0, p1 = u, v = c->strato_chi[w] + u * c->strato_chi[W + w];
+                for (int l = 2; l < 33; ++l) {
+                    const double pn = ((2.0 * l - 1) * u * p1 - (l - 1.0) * p0) / l;
+                    v += pn * c->strato_chi[l * W + w];
+                    p0 = p1;
+                    p1 = pn;
+                }
+                lut[(size_t)i * W + w] = (float)(v / (4.0 * 3.14159265358979323846));
+            }
+        }
+    }
+    o.strato_lut = lut.data();
     Rays r{};
     r.ncell = pk.ncell; r.nray = (int)pk.nray; r.cell_off = pk.cell_off.data(); r.ray_cell = pk.ray_cell.data();
     r.p = pk.p.data(); r.frame = pk.frame.data(); r.dir = reinterpret_cast<const float4*>(pk.dir.data());
