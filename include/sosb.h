@@ -163,6 +163,27 @@ int sosb_get_timing(sosb_handle h, double *ms, int64_t *launches, int n);
  * i's sosb_solve result (its message in sosb_last_error(hs[i])); returns nonzero when any state failed. */
 int sosb_solve_batch(sosb_handle *hs, int n, int max_eval, double tolerance, const float *const *x0_host,
                      float *const *x_out, int x_out_is_device, sosb_stats *stats, int *status, int threads);
+/* Tensor-core BF16 GEMM (tcgen05, TMA, TMEM; no counterpart in the reference, used by the learned warm start):
+ * C[M x N] = A[M x K] * B[N x K]^T with A, B row-major BF16 device matrices (16-byte aligned), FP32 accumulation.
+ * M and N multiples of 128, K of 64. epilogue 0: c_f32 = C; 1: c_f32 = C + bias[n] and c_bf16 = gelu(C + bias[n]);
+ * 2: c_f32 = C + bias[n]. Asynchronous on `stream`; sosb_tc_check(stream) synchronises and reports a GEMM whose
+ * pipeline wait ran out (E_TC_TIMEOUT). Messages of these calls: sosb_tc_last_error(). */
+int sosb_gemm_bf16(const void *A, const void *B, int M, int N, int K, const float *bias, int epilogue, float *c_f32,
+                   void *c_bf16, void *stream);
+int sosb_tc_check(void *stream);
+const char *sosb_tc_last_error(void);
+/* Elementwise kernels of the warm-start MLP's training step (asynchronous on `stream`): GELU backward
+ * (dz = dh * gelu'(z), BF16 and FP32 copies), transpose to BF16 (rows x cols -> cols x rows), column sums (bias
+ * gradients), Adam on FP32 master weights with a BF16 copy, the mean squared error gradient with per-block partial
+ * sums of squares, and FP32 -> BF16 conversion. */
+int sosb_mlp_gelu_backward(const float *dh, const float *z, long long n, void *dz_bf16, float *dz_f32, void *stream);
+int sosb_mlp_transpose(const void *in, int in_is_f32, int rows, int cols, void *out_bf16, void *stream);
+int sosb_mlp_column_sum(const float *g, int rows, int cols, float *out, void *stream);
+int sosb_mlp_adam(float *w, const float *g, float *m, float *v, long long n, float lr, float b1, float b2, float eps,
+                  int step, float decay, void *w_bf16, void *stream);
+int sosb_mlp_mse(const float *p, const float *y, long long n, float scale, float *d, float *partial, int blocks,
+                 void *stream);
+int sosb_mlp_to_bf16(const float *in, long long n, void *out, void *stream);
 /* Message of the last failed call on this handle (empty when none). */
 const char *sosb_last_error(sosb_handle h);
 /* Sizes the handle was created with: cells, slots per cell, K. */

@@ -80,6 +80,20 @@ SIGNATURES = {
                              ctypes.c_void_p, P_i64, P_f64], c_int),
     'sosb_solve_batch': ([ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_dbl, ctypes.POINTER(ctypes.c_void_p),
                           ctypes.POINTER(ctypes.c_void_p), c_int, ctypes.POINTER(Stats), P_i32, c_int], c_int),
+    'sosb_gemm_bf16': ([ctypes.c_void_p, ctypes.c_void_p, c_int, c_int, c_int, ctypes.c_void_p, c_int,
+                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], c_int),
+    'sosb_tc_check': ([ctypes.c_void_p], c_int),
+    'sosb_tc_last_error': ([], ctypes.c_char_p),
+    'sosb_mlp_gelu_backward': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
+                                ctypes.c_void_p, ctypes.c_void_p], c_int),
+    'sosb_mlp_transpose': ([ctypes.c_void_p, c_int, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p], c_int),
+    'sosb_mlp_column_sum': ([ctypes.c_void_p, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p], c_int),
+    'sosb_mlp_adam': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
+                       ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int, ctypes.c_float,
+                       ctypes.c_void_p, ctypes.c_void_p], c_int),
+    'sosb_mlp_mse': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_float, ctypes.c_void_p,
+                      ctypes.c_void_p, c_int, ctypes.c_void_p], c_int),
+    'sosb_mlp_to_bf16': ([ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p], c_int),
     'sosb_set_timing': ([ctypes.c_void_p, c_int], c_int),
     'sosb_get_timing': ([ctypes.c_void_p, P_f64, P_i64, c_int], c_int),
     'sosb_last_error': ([ctypes.c_void_p], ctypes.c_char_p),

@@ -8,14 +8,14 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / 'csrc'
 OUT = PKG / '_lib' / 'libsosb.so'
-SOURCES = [CSRC / 'sosb.cu']
+SOURCES = [CSRC / 'sosb.cu', CSRC / 'tc_gemm.cu']
 HEADERS = [CSRC / 'sos_math.cuh', CSRC / 'sos_pack.h', PKG.parent / 'include' / 'sosb.h']
 
 NVCC_FLAGS = [
     '-gencode', 'arch=compute_103a,code=sm_103a',
     '-O3', '-lineinfo', '-std=c++17',
     '-ftz=true',           # the reference's device arithmetic: FP32 subnormals flushed
-    '-Xcompiler', '-fPIC', '-shared',
+    '-Xcompiler', '-fPIC', '-shared', '--threads', '2',
 ]
 
 

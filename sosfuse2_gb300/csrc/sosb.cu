@@ -1486,7 +1486,8 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
         b = t;
         if (!b) q_w = W / a;
     }
-    int fblocks = std::max(1, std::min(152 * 8, (int)((n + 255) / 256)));
+    // about 16 elements per thread; at most 8 blocks per SM
+    int fblocks = std::max(1, std::min(152 * 8, (int)((n + 256 * 16 - 1) / (256 * 16))));
     fblocks = std::max(q_w, (fblocks / q_w) * q_w);
     TRY(dalloc(s, s->partials, (size_t)fblocks * 4 * W * sizeof(double)));
     TRY(dalloc(s, s->dots, (size_t)4 * W * sizeof(double)));
