@@ -106,6 +106,7 @@ typedef struct {
     double source_relative[64];
     int32_t done[64];
     int64_t kernel_launches;    /* kernels this library launched during the call */
+    int32_t start_fallback;     /* sosb_solve_warm: 1 when the supplied start was replaced by the fallback start */
 } sosb_stats;
 
 enum { SOSB_CELLS = 0, SOSB_OBSERVER = 1 };
@@ -157,6 +158,12 @@ int sosb_solve(sosb_handle h, int max_eval, double tolerance, const float *x0_ho
  * sosb_get_timing fills ms[k] and launches[k] for k < n. */
 int sosb_set_timing(sosb_handle h, int on);
 int sosb_get_timing(sosb_handle h, double *ms, int64_t *launches, int n);
+/* Warm-started Solver.solve (no counterpart in the reference; the learned start): iterate from the device field
+ * x0_dev, reusing the first-light moments of the preceding sosb_apply on this handle. If the first evaluation's
+ * largest source relative change max|g - x|/max|g| exceeds fallback_ss, the iteration restarts from fallback_dev
+ * (e.g. the single-scattering source apply(0)); stats->start_fallback records it. */
+int sosb_solve_warm(sosb_handle h, int max_eval, double tolerance, const float *x0_dev, double fallback_ss,
+                    const float *fallback_dev, float *x_out, int x_out_is_device, sosb_stats *stats);
 /* Batched form of Solver.solve (no single counterpart in the reference, whose pipeline runs one state per process,
  * src/sosfuse2/jobs/pipeline_execution.py): n independent states, each its own handle and stream, solved concurrently
  * by `threads` host threads (0: one per state) so that their small launches overlap on the GPU. status[i] is state
@@ -184,6 +191,13 @@ int sosb_mlp_adam(float *w, const float *g, float *m, float *v, long long n, flo
 int sosb_mlp_mse(const float *p, const float *y, long long n, float scale, float *d, float *partial, int blocks,
                  void *stream);
 int sosb_mlp_to_bf16(const float *in, long long n, void *out, void *stream);
+/* Batched forms of sosb_apply and sosb_solve_warm (no counterpart in the reference): n handles, each on its own
+ * stream, run by `threads` host threads (0: one per handle); status[i] is handle i's result. */
+int sosb_apply_batch(sosb_handle *hs, int n, const float *const *fields_dev, float *const *outs_dev, int *status,
+                     int threads);
+int sosb_solve_warm_batch(sosb_handle *hs, int n, int max_eval, double tolerance, const float *const *x0_dev,
+                          double fallback_ss, const float *const *fallback_dev, float *const *x_out,
+                          int x_out_is_device, sosb_stats *stats, int *status, int threads);
 /* Message of the last failed call on this handle (empty when none). */
 const char *sosb_last_error(sosb_handle h);
 /* Sizes the handle was created with: cells, slots per cell, K. */

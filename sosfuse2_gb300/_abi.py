@@ -59,7 +59,7 @@ class Stats(ctypes.Structure):
     _fields_ = [
         ('evaluations', c_int), ('converged', c_int), ('seconds', c_dbl),
         ('observer_relative', c_dbl * 64), ('source_relative', c_dbl * 64), ('done', c_int * 64),
-        ('kernel_launches', c_i64),
+        ('kernel_launches', c_i64), ('start_fallback', c_int),
     ]
 
 
@@ -78,6 +78,13 @@ SIGNATURES = {
                    c_int),
     'sosb_compose_static': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                              ctypes.c_void_p, P_i64, P_f64], c_int),
+    'sosb_solve_warm': ([ctypes.c_void_p, c_int, c_dbl, ctypes.c_void_p, c_dbl, ctypes.c_void_p, ctypes.c_void_p, c_int,
+                         ctypes.POINTER(Stats)], c_int),
+    'sosb_apply_batch': ([ctypes.POINTER(ctypes.c_void_p), c_int, ctypes.POINTER(ctypes.c_void_p),
+                          ctypes.POINTER(ctypes.c_void_p), P_i32, c_int], c_int),
+    'sosb_solve_warm_batch': ([ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_dbl, ctypes.POINTER(ctypes.c_void_p),
+                               c_dbl, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p), c_int,
+                               ctypes.POINTER(Stats), P_i32, c_int], c_int),
     'sosb_solve_batch': ([ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_dbl, ctypes.POINTER(ctypes.c_void_p),
                           ctypes.POINTER(ctypes.c_void_p), c_int, ctypes.POINTER(Stats), P_i32, c_int], c_int),
     'sosb_gemm_bf16': ([ctypes.c_void_p, ctypes.c_void_p, c_int, c_int, c_int, ctypes.c_void_p, c_int,

@@ -1099,6 +1099,22 @@ static int boxes_impl(sosb_state* s, const float* field, double* out_host) {
     return collect_timing(s);
 }
 
+// Runs fn(i) for i < n on `threads` host threads with the caller's device current.
+template <class F>
+static void run_parallel(int n, int threads, F fn) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int nt = std::max(1, std::min(threads > 0 ? threads : n, n));
+    std::atomic<int> next(0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&]() {
+            cudaSetDevice(dev);
+            for (int i = next++; i < n; i = next++) fn(i);
+        });
+    for (auto& t : pool) t.join();
+}
+
 // ------------------------------------------------------------------------------------------------ C ABI
 extern "C" {
 
@@ -1455,15 +1471,19 @@ static bool anderson_weights(int n, const double* G, float* out) {
     return true;
 }
 
-int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, float* x_out, int x_out_is_device,
-               sosb_stats* stats) {
-    if (!s) return 1;
+// The fixed-point loop. x0: NULL (zero start), a host (x0_device = 0) or device field. keep_first: reuse the
+// first-light moments already computed on this handle. fallback_dev: when the first evaluation's largest source
+// relative change exceeds fallback_ss, the iteration restarts from this device field.
+static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, int x0_device, bool keep_first,
+                      double fallback_ss, const float* fallback_dev, float* x_out, int x_out_is_device,
+                      sosb_stats* stats) {
     if (!x_out) return fail(s, "E_FIELD: null output");
     s->err.clear();
     const auto t_start = std::chrono::steady_clock::now();
     const int64_t launches0 = s->launches;
     TRY(check_ready(s, true));
-    s->have_first = false;  // a solve always includes its first-light pass
+    if (!keep_first) s->have_first = false;  // a solve includes its first-light pass unless told otherwise
+    int fell_back = 0;
     const sosb_dims& d = s->d;
     const int W = d.W;
     const size_t n = (size_t)s->ns * s->src * W;
@@ -1491,8 +1511,9 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
     fblocks = std::max(q_w, (fblocks / q_w) * q_w);
     TRY(dalloc(s, s->partials, (size_t)fblocks * 4 * W * sizeof(double)));
     TRY(dalloc(s, s->dots, (size_t)4 * W * sizeof(double)));
-    if (x0_host)
-        CK(cudaMemcpyAsync(s->fx.p, x0_host, bytes, cudaMemcpyHostToDevice, s->stream));
+    if (x0)
+        CK(cudaMemcpyAsync(s->fx.p, x0, bytes, x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                           s->stream));
     else
         CK(cudaMemsetAsync(s->fx.p, 0, bytes, s->stream));
     float* x = P<float>(s->fx);
@@ -1539,6 +1560,12 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
             rr[w] = r;
             ss[w] = (double)(df / std::max(mg, 1e-30f));
             if (it >= 2 && std::max(r, ss[w]) <= tol) done[w] = 1;
+        }
+        if (it == 1 && fallback_dev && !fell_back && *std::max_element(ss.begin(), ss.end()) > fallback_ss) {
+            // the supplied start is further from the fixed point than the fallback start: restart from it
+            CK(cudaMemcpyAsync(x, fallback_dev, bytes, cudaMemcpyDeviceToDevice, s->stream));
+            fell_back = 1;
+            continue;
         }
         all_done = std::all_of(done.begin(), done.end(), [](int v) { return v != 0; });
         if (all_done) {
@@ -1640,6 +1667,7 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
             stats->done[w] = done[w];
         }
         stats->kernel_launches = s->launches - launches0;
+        stats->start_fallback = fell_back;
     }
     if (!all_done) {
         int nd = 0;
@@ -1649,6 +1677,20 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
     return 0;
 }
 
+
+int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, float* x_out, int x_out_is_device,
+               sosb_stats* stats) {
+    if (!s) return 1;
+    return solve_impl(s, max_eval, tol, x0_host, 0, false, 0.0, nullptr, x_out, x_out_is_device, stats);
+}
+
+int sosb_solve_warm(sosb_handle s, int max_eval, double tol, const float* x0_dev, double fallback_ss,
+                    const float* fallback_dev, float* x_out, int x_out_is_device, sosb_stats* stats) {
+    if (!s) return 1;
+    if (!x0_dev) return fail(s, "E_FIELD: null start");
+    if (!s->have_first) return fail(s, "E_STATE: no first light on this handle (run an apply first)");
+    return solve_impl(s, max_eval, tol, x0_dev, 1, true, fallback_ss, fallback_dev, x_out, x_out_is_device, stats);
+}
 
 int sosb_solve_batch(sosb_handle* hs, int n, int max_eval, double tol, const float* const* x0_host,
                      float* const* x_out, int x_out_is_device, sosb_stats* stats, int* status, int threads) {
@@ -1669,6 +1711,30 @@ int sosb_solve_batch(sosb_handle* hs, int n, int max_eval, double tol, const flo
     int failed = 0;
     for (int i = 0; i < n; ++i) failed += status[i] != 0;
     return failed ? 3 : 0;
+}
+
+
+int sosb_apply_batch(sosb_handle* hs, int n, const float* const* fields, float* const* outs, int* status,
+                     int threads) {
+    if (!hs || !fields || !outs || !status || n < 0) return 1;
+    run_parallel(n, threads, [&](int i) { status[i] = sosb_apply(hs[i], fields[i], outs[i]); });
+    for (int i = 0; i < n; ++i)
+        if (status[i]) return 3;
+    return 0;
+}
+
+int sosb_solve_warm_batch(sosb_handle* hs, int n, int max_eval, double tol, const float* const* x0_dev,
+                          double fallback_ss, const float* const* fallback_dev, float* const* x_out,
+                          int x_out_is_device, sosb_stats* stats, int* status, int threads) {
+    if (!hs || !x0_dev || !x_out || !status || n < 0) return 1;
+    run_parallel(n, threads, [&](int i) {
+        status[i] = sosb_solve_warm(hs[i], max_eval, tol, x0_dev[i], fallback_ss,
+                                    fallback_dev ? fallback_dev[i] : nullptr, x_out[i], x_out_is_device,
+                                    stats ? &stats[i] : nullptr);
+    });
+    for (int i = 0; i < n; ++i)
+        if (status[i]) return 3;
+    return 0;
 }
 
 }  // extern "C"

@@ -56,6 +56,15 @@ class Kernel:
         self.n_query = len(st['query_d'])
         self.n_rays = len(st['cell_d'])
 
+    def update(self, state):
+        """Replace the constants by those of another state with the same geometry (bundles stay on the device)."""
+        st = state if isinstance(state, PackedState) else PackedState(state)
+        if st.shape != self.state.shape or len(st['cell_d']) != self.n_rays:
+            raise ValueError('E_SHAPE: update needs a state of the same geometry')
+        self._check(self.lib.sosb_set_constants(self.h, ctypes.byref(st.constants())))
+        st._keep.clear()
+        self.state = st
+
     def _check(self, rc):
         if rc:
             msg = self.lib.sosb_last_error(self.h).decode()

@@ -193,6 +193,7 @@ class Atmosphere:
                  strato_tau=0.01, strato_center=20.0, strato_sigma=3.0, strato_g=0.6,
                  no2_column=0.0, no2_center=25.0, o4=False):
         rng = np.random.default_rng(seed)
+        self.aod = aod
         self.wl = np.asarray(wl, float)
         self.W = len(self.wl)
         self.top = float(top)
@@ -384,129 +385,158 @@ def build_bundle(points, dirs_local, weights, chi_grid, top, table, atm, with_gr
     return out
 
 
-def ground_terms(h, chi, atm, table, ext, nmu=3, nphi=32):
-    """First-light direct-ground sources of each cell: Rayleigh moments gm [ns, 4, W] and the lit ground directions
-    with their values (solve/engine_core.py:103-147 restated on the column tables)."""
-    C = 3 / (16 * math.pi)
-    ns = len(h) * len(chi)
-    gm = np.zeros((ns, 4, atm.W))
-    goff, gdir, gval = [0], [], []
-    for cell in range(ns):
-        ih, ic = divmod(cell, len(chi))
-        r = R + h[ih]
-        loc, w = ring_quadrature(r, chi[ic], nmu, nphi, (), rings=False)
-        p, up, ex = frame(r, chi[ic])
-        ey = np.cross(up, ex)
-        d = loc[:, 0, None] * ex + loc[:, 1, None] * ey + loc[:, 2, None] * up
-        col, escape = table.lookup(np.full(len(d), h[ih]), loc[:, 2])
-        hit = ~escape
-        # ground point of each downward ray
-        b = d @ p
-        disc = b * b - r * r + R * R
-        t = -b - np.sqrt(np.maximum(disc, 0))
-        q = p + t[:, None] * d
-        rq = np.linalg.norm(q, axis=-1)
-        cos_sun = q[:, 2] / rq
-        sun, lit = table.lookup(np.zeros(len(d)), cos_sun)
-        od = (sun[:, :5] + col[:, :5]) @ ext
+class Family:
+    """Everything of a state that depends only on the grid and the profile shapes: the column tables, the cell and
+    observer ray bundles, and the ground-illumination rays of every cell. States of one family differ only in the
+    amounts (aerosol optical depth, single-scattering albedo, asymmetry, ozone column, albedo, stratospheric optical
+    depth), so `state()` costs a fraction of a second."""
+
+    def __init__(self, h, chi_deg, L, nmu, nphi, path_n, shape, query_n=24, sun_scale=2, tolerance=1e-3, max_eval=64,
+                 name='synthetic', ground_nmu=3, ground_nphi=32):
+        self.h = np.asarray(h, float)
+        self.chi = np.deg2rad(np.asarray(chi_deg, float))
+        self.top = float(self.h[-1])
+        if abs(self.top - shape.top) > 1e-9:
+            raise ValueError('E_SYNTH: grid top and atmosphere top differ')
+        self.L, self.path_n, self.query_n, self.name = L, path_n, query_n, name
+        self.tolerance, self.max_eval = tolerance, max_eval
+        self.shape = shape
+        shells = _shells(self.top)
+        self.table = ColumnTable(shape, shells, scale=sun_scale)
+        points, dirs, weights = [], [], []
+        for ih in range(len(self.h)):
+            for ic in range(len(self.chi)):
+                r = R + self.h[ih]
+                loc, w = ring_quadrature(r, self.chi[ic], nmu, nphi, _ring_heights(self.top))
+                points.append(frame(r, self.chi[ic]))
+                dirs.append(loc)
+                weights.append(w)
+        self.cells = build_bundle(points, dirs, weights, self.chi, self.top, self.table, shape)
+        u4, w4 = np.polynomial.legendre.leggauss(4)
+        self.box_ww = (w4[:, None] * w4[None, :] / 4).ravel()
+        qpts, qdirs, qw = [], [], []
+        for hs in MONITOR_ELEVATIONS:
+            el = np.array([e + de for e, z in DIRS for de in u4 for dz in u4])
+            az = np.array([z + dz for e, z in DIRS for de in u4 for dz in u4])
+            e, zz = np.deg2rad(el), np.deg2rad(az)
+            loc = np.column_stack([np.cos(e) * np.cos(zz), np.cos(e) * np.sin(zz), np.sin(e)])
+            qpts.append(frame(R + OBSERVER_KM, np.deg2rad(90 - hs)))
+            qdirs.append(loc)
+            qw.append(np.ones(len(loc)))
+        self.query = build_bundle(qpts, qdirs, qw, self.chi, self.top, self.table, shape, with_ground_columns=False)
+        self._ground_rays(ground_nmu, ground_nphi)
+
+    def _ground_rays(self, nmu, nphi):
+        """Per cell: the directions of a ring quadrature without shadow rings, their weights, and for the downward
+        ones the columns to the ground and from the ground point to the sun (solve/engine_core.py:103-147)."""
+        table, h, chi = self.table, self.h, self.chi
+        loc_all, w_all, col_all, sun_all, cos_all, ok_all, counts = [], [], [], [], [], [], []
+        for cell in range(len(h) * len(chi)):
+            ih, ic = divmod(cell, len(chi))
+            r = R + h[ih]
+            loc, w = ring_quadrature(r, chi[ic], nmu, nphi, (), rings=False)
+            p, up, ex = frame(r, chi[ic])
+            ey = np.cross(up, ex)
+            d = loc[:, 0, None] * ex + loc[:, 1, None] * ey + loc[:, 2, None] * up
+            col, escape = table.lookup(np.full(len(d), h[ih]), loc[:, 2])
+            b = d @ p
+            disc = b * b - r * r + R * R
+            t = -b - np.sqrt(np.maximum(disc, 0))
+            q = p + t[:, None] * d
+            cos_sun = q[:, 2] / np.linalg.norm(q, axis=-1)
+            sun, lit = table.lookup(np.zeros(len(d)), cos_sun)
+            loc_all.append(loc)
+            w_all.append(w)
+            col_all.append(col)
+            sun_all.append(sun)
+            cos_all.append(cos_sun)
+            ok_all.append(lit & ~escape)
+            counts.append(len(w))
+        self.g_loc = np.concatenate(loc_all)
+        self.g_w = np.concatenate(w_all)
+        self.g_cols = np.concatenate(col_all) + np.concatenate(sun_all)
+        self.g_cos = np.maximum(0, np.concatenate(cos_all))
+        self.g_ok = np.concatenate(ok_all)
+        self.g_cell = np.repeat(np.arange(len(counts)), counts)
+        lo = self.g_loc
+        self.g_factor = np.stack([(1 - lo[:, 0] ** 2) / 2, (1 - lo[:, 1] ** 2) / 2, (1 - lo[:, 2] ** 2) / 2,
+                                  -lo[:, 0] * lo[:, 2] / 2], -1)
+
+    def ground(self, atm, ext):
+        """gm [ns, 4, W], goff, gdir, gval of one atmosphere (vectorised over all ground rays)."""
+        od = self.g_cols[:, :5] @ ext
         if atm.strato:
-            od += (sun[:, 5] + col[:, 5])[:, None] * atm.strato_ext[None, :]
-        value = (atm.albedo / math.pi * np.maximum(0, cos_sun)[:, None] * np.exp(-od) * lit[:, None] * hit[:, None]
-                 * w[:, None])
+            od += self.g_cols[:, 5, None] * atm.strato_ext[None, :]
+        value = (atm.albedo / math.pi * self.g_cos[:, None] * np.exp(-od) * self.g_ok[:, None] * self.g_w[:, None])
+        ns = len(self.h) * len(self.chi)
+        gm = np.zeros((ns, 4, atm.W))
+        for k in range(4):
+            for w in range(atm.W):
+                gm[:, k, w] = np.bincount(self.g_cell, weights=self.g_factor[:, k] * value[:, w], minlength=ns)
+        gm *= (2 * (3 / (16 * math.pi)) * ext[0])[None, None, :]
         take = np.any(value > 0, axis=1)
-        gdir.append(loc[take])
-        gval.append(value[take])
-        goff.append(goff[-1] + int(take.sum()))
-        factor = np.stack([(1 - loc[:, 0] ** 2) / 2, (1 - loc[:, 1] ** 2) / 2, (1 - loc[:, 2] ** 2) / 2,
-                           -loc[:, 0] * loc[:, 2] / 2], -1)
-        gm[cell] = (factor.T @ value) * (2 * C * ext[0])[None, :]
-    return (gm.astype(np.float32), np.asarray(goff, np.int64), np.concatenate(gdir).astype(np.float32),
-            np.concatenate(gval).astype(np.float32))
+        goff = np.r_[0, np.cumsum(np.bincount(self.g_cell[take], minlength=ns))].astype(np.int64)
+        return (gm.astype(np.float32), goff, self.g_loc[take].astype(np.float32), value[take].astype(np.float32))
+
+    def state(self, atm, seed=0):
+        """Packed-state arrays of atmosphere `atm` (same profile shapes as the family's)."""
+        h, chi, L, W = self.h, self.chi, self.L, atm.W
+        K = (L + 1) * (L + 2) // 2
+        ext = atm.ext()
+        gm, goff, gdir, gval = self.ground(atm, ext)
+        u, wu = gauss01(self.path_n)
+        uq, wuq = gauss01(self.query_n)
+        step = 0.5
+        zt = np.arange(int(round(self.top / step)) + 1) * step
+        prof = atm.profiles(zt)
+        density_table = np.column_stack([prof[:, 0], prof[:, 2], prof[:, 3]]).astype(np.float32)
+        levels = np.array([l for l in range(L + 1) for m in range(l + 1)])
+        meta = dict(
+            name=self.name, L=L, K=K, W=W, nq=self.path_n, nq_query=self.query_n, nh=len(h), nc=len(chi),
+            ns=len(h) * len(chi), source_size=10 + K * (2 if atm.strato else 1), strato=atm.strato, g=atm.g,
+            mix=(1 - 0.03) / (1 + 0.015), height=atm.H, albedo=atm.albedo, top_km=self.top, profile_step_km=step,
+            density_mask=2, air_surface=1.0, tolerance=self.tolerance, max_eval=self.max_eval,
+            monitors=len(MONITOR_ELEVATIONS), n_dirs=len(DIRS), box_points=16, wavelengths_nm=atm.wl.tolist(),
+            seed=seed, C=3 / (16 * math.pi), rays=int(len(self.cells['d'])), segments=int(len(self.cells['seg_a'])),
+            query_rays=int(len(self.query['d'])),
+            amounts=dict(aod=atm.aod, ssa=atm.ssa, g=atm.g, ozone_du=atm.ozone_du, albedo=atm.albedo,
+                         strato_tau=atm.strato_tau))
+        arrays = dict(
+            u=u, wu=wu, uq=uq, wuq=wuq, h=h.astype(np.float32), chi=chi.astype(np.float32),
+            hr=np.exp(-h / 8.0).astype(np.float32), ha=np.exp(-h / atm.H).astype(np.float32),
+            ext=ext.astype(np.float32), asca=(ext[1] * atm.ssa).astype(np.float32),
+            sun_h=self.table.h.astype(np.float32), sun_col=np.ascontiguousarray(self.table.up[:, :, :5], np.float32),
+            gm=gm, goff=goff, gdir=gdir, gval=gval, density_table=density_table,
+            rf=((levels[:6] == 0) + 0.1 * (levels[:6] == 2)).astype(np.float32),
+            af=(atm.g ** levels).astype(np.float32), ext0=ext[0].astype(np.float32),
+            solar=atm.solar.astype(np.float64), box_ww=self.box_ww)
+        if atm.strato:
+            lm = np.arange(33)
+            chi_l = ((2 * lm + 1) * atm.strato_g ** lm)[:, None] * np.ones((1, W))
+            cell_edges = np.r_[h[0], (h[:-1] + h[1:]) / 2, h[-1]]
+            cdf = np.array([math.erf((z - atm.strato_center) / (math.sqrt(2) * atm.strato_sigma)) for z in cell_edges])
+            avg = np.diff(cdf) * atm.strato_sigma * math.sqrt(math.pi / 2) / atm.strato_norm / np.diff(cell_edges)
+            arrays.update(
+                strato_ext=atm.strato_ext.astype(np.float32), strato_sca=atm.strato_ext.astype(np.float32),
+                strato_chi=chi_l.astype(np.float32), strato_density=avg.astype(np.float32),
+                strato_sun_col=np.ascontiguousarray(self.table.up[:, :, 5], np.float32),
+                strato_eigen=(atm.strato_g ** levels[:, None] * np.ones((1, W))).astype(np.float32),
+                strato_sca_source=atm.strato_ext.astype(np.float32))
+            meta.update(strato_center=atm.strato_center, strato_sigma=atm.strato_sigma, strato_norm=atm.strato_norm)
+        arrays['meta'] = json.dumps(meta)
+        for k, v in self.cells.items():
+            arrays['cell_' + k] = v
+        for k, v in self.query.items():
+            arrays['query_' + k] = v
+        return arrays
 
 
 def make_state(h, chi_deg, wl, L, nmu, nphi, path_n, atm, seed=0, query_n=24, sun_scale=2, tolerance=1e-3,
                max_eval=64, name='synthetic'):
     """A packed state (dict for sosfuse2_gb300.state.PackedState) of the synthetic atmosphere."""
-    h = np.asarray(h, float)
-    chi = np.deg2rad(np.asarray(chi_deg, float))
-    top = float(h[-1])
-    if abs(top - atm.top) > 1e-9:
-        raise ValueError('E_SYNTH: grid top and atmosphere top differ')
-    W = atm.W
-    K = (L + 1) * (L + 2) // 2
-    shells = _shells(top)
-    table = ColumnTable(atm, shells, scale=sun_scale)
-    ext = atm.ext()
-    # cell rays
-    points, dirs, weights = [], [], []
-    for ih in range(len(h)):
-        for ic in range(len(chi)):
-            r = R + h[ih]
-            loc, w = ring_quadrature(r, chi[ic], nmu, nphi, _ring_heights(top))
-            points.append(frame(r, chi[ic]))
-            dirs.append(loc)
-            weights.append(w)
-    cells = build_bundle(points, dirs, weights, chi, top, table, atm)
-    # observer rays: 5 solar elevations x 7 directions x 4x4 Gauss-Legendre points
-    u4, w4 = np.polynomial.legendre.leggauss(4)
-    qpts, qdirs, qw = [], [], []
-    for hs in MONITOR_ELEVATIONS:
-        el = np.array([e + de for e, z in DIRS for de in u4 for dz in u4])
-        az = np.array([z + dz for e, z in DIRS for de in u4 for dz in u4])
-        e, zz = np.deg2rad(el), np.deg2rad(az)
-        loc = np.column_stack([np.cos(e) * np.cos(zz), np.cos(e) * np.sin(zz), np.sin(e)])
-        qpts.append(frame(R + OBSERVER_KM, np.deg2rad(90 - hs)))
-        qdirs.append(loc)
-        qw.append(np.ones(len(loc)))
-    query = build_bundle(qpts, qdirs, qw, chi, top, table, atm, with_ground_columns=False)
-    gm, goff, gdir, gval = ground_terms(h, chi, atm, table, ext)
-    u, wu = gauss01(path_n)
-    uq, wuq = gauss01(query_n)
-    step = 0.5
-    zt = np.arange(int(round(top / step)) + 1) * step
-    prof = atm.profiles(zt)
-    density_table = np.column_stack([prof[:, 0], prof[:, 2], prof[:, 3]]).astype(np.float32)
-    levels = np.array([l for l in range(L + 1) for m in range(l + 1)])
-    hr = np.exp(-h / 8.0)
-    ha = np.exp(-h / atm.H)
-    meta = dict(
-        name=name, L=L, K=K, W=W, nq=path_n, nq_query=query_n, nh=len(h), nc=len(chi), ns=len(h) * len(chi),
-        source_size=10 + K * (2 if atm.strato else 1), strato=atm.strato, g=atm.g, mix=(1 - 0.03) / (1 + 0.015),
-        height=atm.H, albedo=atm.albedo, top_km=top, profile_step_km=step, density_mask=2, air_surface=1.0,
-        tolerance=tolerance, max_eval=max_eval, monitors=len(MONITOR_ELEVATIONS), n_dirs=len(DIRS), box_points=16,
-        wavelengths_nm=atm.wl.tolist(), seed=seed, C=3 / (16 * math.pi),
-        rays=int(len(cells['d'])), segments=int(len(cells['seg_a'])), query_rays=int(len(query['d'])),
-    )
-    arrays = dict(
-        meta=json.dumps(meta), u=u, wu=wu, uq=uq, wuq=wuq,
-        h=h.astype(np.float32), chi=chi.astype(np.float32), hr=hr.astype(np.float32), ha=ha.astype(np.float32),
-        ext=ext.astype(np.float32), asca=(ext[1] * atm.ssa).astype(np.float32),
-        sun_h=table.h.astype(np.float32), sun_col=np.ascontiguousarray(table.up[:, :, :5], np.float32),
-        gm=gm, goff=goff, gdir=gdir, gval=gval, density_table=density_table,
-        rf=((levels[:6] == 0) + 0.1 * (levels[:6] == 2)).astype(np.float32),
-        af=(atm.g ** levels).astype(np.float32), ext0=ext[0].astype(np.float32), solar=atm.solar.astype(np.float64),
-        box_ww=(w4[:, None] * w4[None, :] / 4).ravel(),
-    )
-    if atm.strato:
-        lm = np.arange(33)
-        chi_l = ((2 * lm + 1) * atm.strato_g ** lm)[:, None] * np.ones((1, W))
-        cell_edges = np.r_[h[0], (h[:-1] + h[1:]) / 2, h[-1]]
-        cdf = np.array([math.erf((z - atm.strato_center) / (math.sqrt(2) * atm.strato_sigma)) for z in cell_edges])
-        avg = np.diff(cdf) * atm.strato_sigma * math.sqrt(math.pi / 2) / atm.strato_norm / np.diff(cell_edges)
-        arrays.update(
-            strato_ext=atm.strato_ext.astype(np.float32), strato_sca=atm.strato_ext.astype(np.float32),
-            strato_chi=chi_l.astype(np.float32), strato_density=avg.astype(np.float32),
-            strato_sun_col=np.ascontiguousarray(table.up[:, :, 5], np.float32),
-            strato_eigen=(atm.strato_g ** levels[:, None] * np.ones((1, W))).astype(np.float32),
-            strato_sca_source=atm.strato_ext.astype(np.float32),
-        )
-        meta.update(strato_center=atm.strato_center, strato_sigma=atm.strato_sigma, strato_norm=atm.strato_norm)
-        arrays['meta'] = json.dumps(meta)
-    for k, v in cells.items():
-        arrays['cell_' + k] = v
-    for k, v in query.items():
-        arrays['query_' + k] = v
-    return arrays
+    fam = Family(h, chi_deg, L, nmu, nphi, path_n, atm, query_n=query_n, sun_scale=sun_scale, tolerance=tolerance,
+                 max_eval=max_eval, name=name)
+    return fam.state(atm, seed)
 
 
 # ------------------------------------------------------------------------------------------------ configurations
@@ -516,6 +546,27 @@ def config0(seed=0, **kw):
     Gaussian 20 km (sigma 3 km, AOD 0.01, g 0.6), NO2/O4 off, albedo 0.3."""
     atm = Atmosphere([550.0], seed=seed, top=100.0)
     return make_state(np.arange(101.0), REDUCED_CHI_DEG, atm.wl, 16, 1, 2, 4, atm, seed=seed, name='config0', **kw)
+
+
+def config0_family(**kw):
+    """The state family of config 0's grid (amounts vary, profile shapes fixed)."""
+    atm = Atmosphere([550.0], seed=0, top=100.0)
+    return Family(np.arange(101.0), REDUCED_CHI_DEG, 16, 1, 2, 4, atm, name='config0-family', **kw)
+
+
+def random_amounts(seed):
+    """Amounts drawn from the batched configuration's ranges: AOD U(0.02, 0.5), g U(0.5, 0.8), ozone U(250, 400) DU,
+    albedo U(0.05, 0.8)."""
+    rng = np.random.default_rng(seed)
+    return dict(aod=float(rng.uniform(0.02, 0.5)), g=float(rng.uniform(0.5, 0.8)),
+                ozone_du=float(rng.uniform(250, 400)), albedo=float(rng.uniform(0.05, 0.8)))
+
+
+def family_state(family, seed):
+    """A state of `family` with amounts random_amounts(seed)."""
+    a = random_amounts(seed)
+    atm = Atmosphere(family.shape.wl, seed=seed, top=family.top, scale_height=family.shape.H, **a)
+    return family.state(atm, seed)
 
 
 def config1(seed=0, nh=241, W=30, nmu=12, nphi=16, path_n=12, L=32, chi_deg=None, **kw):
