@@ -313,7 +313,7 @@ def generate(family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3, log=No
     from .synth import family_state
 
     kernel = None
-    ws_rows, ws_targets, evals, ss_single = [], [], [], []
+    ws_rows, ws_targets, evals, ss_single, skipped = [], [], [], [], []
     helper = None
     for i, seed in enumerate(seeds):
         st = PackedState(family_state(family, seed))
@@ -324,7 +324,13 @@ def generate(family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3, log=No
             kernel.update(st)
         solver = Solver(st, kernel=kernel)
         g1 = solver.apply(kernel.field())
-        x, stats = solver.solve(max_eval, tolerance, device_out=True)
+        try:
+            x, stats = solver.solve(max_eval, tolerance, device_out=True)
+        except RuntimeError as exc:  # states the plain iteration does not converge on teach nothing: skip them
+            if not str(exc).startswith('E_NOT_CONVERGED'):
+                raise
+            skipped.append(seed)
+            continue
         g2 = solver.apply(g1)
         ss_single.append(float(((g2 - g1).abs().amax() / g2.abs().amax().clamp_min(1e-30)).item()))
         X, norm = helper.rows(st, g1)
@@ -334,6 +340,7 @@ def generate(family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3, log=No
         if log and i % 64 == 0:
             log(i, stats['evaluations'])
     kernel.close()
+    generate.skipped = skipped
     return torch.cat(ws_rows), torch.cat(ws_targets), np.asarray(evals), np.asarray(ss_single)
 
 
@@ -350,7 +357,7 @@ def train_warm_start(family, n_train=512, epochs=30, seed=10000, device='cuda:0'
     losses = ws.train(X, Y, epochs=epochs, lr=1e-3, log=log)
     t2 = time.perf_counter()
     ws.fallback_ss = float(np.quantile(ss1, 0.9))
-    return ws, dict(train_solves=n_train, rows=int(X.shape[0]), generate_seconds=t1 - t0, train_seconds=t2 - t1,
+    return ws, dict(train_solves=n_train, not_converged=len(generate.skipped), rows=int(X.shape[0]), generate_seconds=t1 - t0, train_seconds=t2 - t1,
                     plain_evaluations_mean=float(evals.mean()), loss_first=losses[0], loss_last=losses[-1],
                     fallback_ss=ws.fallback_ss, gemm_launches=ws.mlp.gemm_launches)
 
@@ -374,13 +381,25 @@ def evaluate(ws, family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3):
         solver = Solver(st, kernel=kernel)
         torch.cuda.synchronize()
         t = time.perf_counter()
-        xp, sp = solver.solve(max_eval, tolerance, device_out=True)
+        try:
+            xp, sp = solver.solve(max_eval, tolerance, device_out=True)
+        except RuntimeError as exc:
+            if not str(exc).startswith('E_NOT_CONVERGED'):
+                raise
+            out.append(dict(seed=seed, plain_evaluations=None, error=str(exc)))
+            continue
         torch.cuda.synchronize()
         tp = time.perf_counter() - t
         t = time.perf_counter()
         g1 = solver.apply(kernel.field())
         x0 = ws.predict_start(st, g1)
-        xl, sl = solve_warm(solver, x0, g1, ws.fallback_ss, max_eval, tolerance)
+        try:
+            xl, sl = solve_warm(solver, x0, g1, ws.fallback_ss, max_eval, tolerance)
+        except RuntimeError as exc:
+            if not str(exc).startswith('E_NOT_CONVERGED'):
+                raise
+            out.append(dict(seed=seed, plain_evaluations=sp['evaluations'], learned_evaluations=None, error=str(exc)))
+            continue
         torch.cuda.synchronize()
         tl = time.perf_counter() - t
         bp, bl = solver.boxes(xp), solver.boxes(xl)

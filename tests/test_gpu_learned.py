@@ -16,7 +16,8 @@ def test_learned_start_reduces_evaluations():
     fam = synth.config0_family()
     ws, report = learned.train_warm_start(fam, n_train=96, epochs=25, seed=10000)
     assert report['loss_last'] < report['loss_first']
-    res = learned.evaluate(ws, fam, range(90000, 90008))
+    res = [r for r in learned.evaluate(ws, fam, range(90000, 90008)) if r['plain_evaluations'] is not None]
+    assert len(res) >= 6 and all(r.get('learned_evaluations') for r in res), res
     plain = np.mean([r['plain_evaluations'] for r in res])
     learn = np.mean([r['learned_evaluations'] for r in res])
     assert learn < plain, (learn, plain, res)
