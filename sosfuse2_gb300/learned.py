@@ -9,7 +9,8 @@ gathers and the random batch order.
 Rows are (cell, wavelength) pairs. Input: the cell's height and solar zenith, the log extinctions of air, aerosol,
 ozone and stratospheric aerosol at the cell and the optical depth above it, single-scattering albedo, albedo, the
 mixture's first 8 phase moments, the cell's single-scattering source g1 = apply(0) divided by its norm, and that norm.
-Target: (x* - g1) / |g1| over all source slots, x* the converged source. The start is g1 + |g1| * prediction; if the
+Target: (x* - g1) / s over all source slots, x* the converged source and s = |g1| floored at 1e-4 of the state's
+largest cell norm (cells in the Earth's shadow have no single scattering). The start is g1 + s * prediction; if the
 first evaluation from it changes the source more than the single-scattering start typically does, the solve restarts
 from g1 (sosb_solve_warm's fallback).
 """
@@ -247,8 +248,11 @@ class WarmStart:
         torch = self.torch
         opt = torch.as_tensor(cell_features(state), dtype=torch.float32, device=self.device)
         g = g1.permute(0, 2, 1).reshape(-1, self.n_slots)  # (cell, w) rows
-        norm = g.norm(dim=1, keepdim=True).clamp_min(1e-30)
-        x = torch.cat([opt, g / norm, torch.log10(norm)], 1)
+        raw = g.norm(dim=1, keepdim=True)
+        # cells in the Earth's shadow have no single scattering but a multiple-scattering source: scale each cell by
+        # its norm floored at 1e-4 of the state's largest
+        norm = raw.clamp_min(max(float(raw.max()) * 1e-4, 1e-30))
+        x = torch.cat([opt, g / norm, torch.log10(raw.clamp_min(1e-30))], 1)
         return x, norm
 
     @staticmethod

@@ -49,4 +49,4 @@ def test_training_reduces_loss():
     T = torch.zeros(8192, net.n_out_p, device='cuda:0')
     T[:, :64] = torch.tanh(X[:, :64] @ torch.randn(64, 64, device='cuda:0', generator=g) / 8)
     losses = net.train(X.to(torch.bfloat16), T, epochs=8, batch=1024, lr=2e-3)
-    assert losses[-1] < 0.2 * losses[0]
+    assert losses[-1] < 0.5 * losses[0]
