@@ -9,8 +9,8 @@ gathers and the random batch order.
 Rows are (cell, wavelength) pairs. Input: the cell's height and solar zenith, the log extinctions of air, aerosol,
 ozone and stratospheric aerosol at the cell and the optical depth above it, single-scattering albedo, albedo, the
 mixture's first 8 phase moments, the cell's single-scattering source g1 = apply(0) divided by its norm, and that norm.
-Target: (x* - g1) / s over all source slots, x* the converged source and s = |g1| floored at 1e-4 of the state's
-largest cell norm (cells in the Earth's shadow have no single scattering). The start is g1 + s * prediction; if the
+Target: (x* - g1) / |g1| over all source slots, x* the converged source, for cells with single scattering; cells in
+the Earth's shadow (|g1| below 1e-8 of the largest) keep g1. The start is g1 + |g1| * prediction; if the
 first evaluation from it changes the source more than the single-scattering start typically does, the solve restarts
 from g1 (sosb_solve_warm's fallback).
 """
@@ -248,12 +248,15 @@ class WarmStart:
         torch = self.torch
         opt = torch.as_tensor(cell_features(state), dtype=torch.float32, device=self.device)
         g = g1.permute(0, 2, 1).reshape(-1, self.n_slots)  # (cell, w) rows
-        raw = g.norm(dim=1, keepdim=True)
-        # cells in the Earth's shadow have no single scattering but a multiple-scattering source: scale each cell by
-        # its norm floored at 1e-4 of the state's largest
-        norm = raw.clamp_min(max(float(raw.max()) * 1e-4, 1e-30))
-        x = torch.cat([opt, g / norm, torch.log10(raw.clamp_min(1e-30))], 1)
+        norm = g.norm(dim=1, keepdim=True).clamp_min(1e-30)
+        x = torch.cat([opt, g / norm, torch.log10(norm)], 1)
         return x, norm
+
+    @staticmethod
+    def lit(norm):
+        """Rows with single scattering (|g1| above 1e-8 of the state's largest); cells in the Earth's shadow have
+        none, so a relative correction is undefined there and their start stays g1."""
+        return (norm > norm.max() * 1e-8).squeeze(1)
 
     @staticmethod
     def targets(g1, x_star, norm, n_slots):
@@ -286,6 +289,7 @@ class WarmStart:
         """The warm start [ns, slots, W] (device) of a state whose single-scattering source is g1."""
         X, norm = self.rows(state, g1)
         pred = self.mlp.predict(self._pad_in(X))[:X.shape[0], :self.n_slots] * self.y_std + self.y_mean
+        pred = pred * self.lit(norm)[:, None]
         ns, slots, W = g1.shape
         x0 = g1.permute(0, 2, 1).reshape(-1, slots) + norm * pred
         return x0.reshape(ns, W, slots).permute(0, 2, 1).contiguous()
@@ -338,8 +342,9 @@ def generate(family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3, log=No
         g2 = solver.apply(g1)
         ss_single.append(float(((g2 - g1).abs().amax() / g2.abs().amax().clamp_min(1e-30)).item()))
         X, norm = helper.rows(st, g1)
-        ws_rows.append(X)
-        ws_targets.append(WarmStart.targets(g1, x, norm, st.source_size))
+        lit = WarmStart.lit(norm)
+        ws_rows.append(X[lit])
+        ws_targets.append(WarmStart.targets(g1, x, norm, st.source_size)[lit])
         evals.append(stats['evaluations'])
         if log and i % 64 == 0:
             log(i, stats['evaluations'])
