@@ -17,6 +17,7 @@ barrier and the max over ranks only bracket the timing.
 """
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -46,6 +47,10 @@ def args_():
     p.add_argument('--config', type=int, default=0, choices=(0, 1))
     p.add_argument('--seed', type=int, default=0)
     p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--no-forms', action='store_true', help='plain single-state solve only')
+    p.add_argument('--batch', type=int, default=64, help='states per batched step')
+    p.add_argument('--train-solves', type=int, default=512)
+    p.add_argument('--epochs', type=int, default=30)
     return p.parse_args()
 
 
@@ -232,24 +237,87 @@ def run_reference(a, rank):
         cpu_baseline=cb, e2e=dict(value=v, unit='solves/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0))), flush=True)
 
 
+def _batch_kernels(fam, seeds, device):
+    from sosfuse2_gb300.solver import Kernel
+    from sosfuse2_gb300.state import PackedState
+    from sosfuse2_gb300.synth import family_state
+
+    states = [PackedState(family_state(fam, sd)) for sd in seeds]
+    kernels = [Kernel(st, device) for st in states]
+    for k in kernels:
+        k._check(k.lib.sosb_set_stream(k.h, None))
+    return states, kernels
+
+
+def _time_batched(a, fam, ws, device, seeds):
+    """Plain and learned-start batched solves of the held-out family states: converged solves/s of each form."""
+    import torch
+
+    from sosfuse2_gb300 import _abi, learned
+
+    states, kernels = _batch_kernels(fam, seeds, device)
+    n = len(kernels)
+    lib = kernels[0].lib
+    handles = (ctypes.c_void_p * n)(*[k.h.value for k in kernels])
+    outs = [k.field() for k in kernels]
+    out_ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])
+    res = {}
+    for form in ('plain', 'learned'):
+        times, conv, evals, launches = [], [], [], 0
+        for step in range(a.warmup + a.steps):
+            for k, st in zip(kernels, states):
+                k.update(st)  # no first light carried between steps
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if form == 'plain':
+                stats = (_abi.Stats * n)()
+                status = (ctypes.c_int32 * n)()
+                lib.sosb_solve_batch(handles, n, 64, 1e-3, None, out_ptrs, 1, stats, status, 0)
+                ok = [not status[i] for i in range(n)]
+                ev = [stats[i].evaluations for i in range(n) if not status[i]]
+                nl = sum(stats[i].kernel_launches for i in range(n))
+            else:
+                g0 = ws.mlp.gemm_launches
+                r = learned.solve_batch(ws, kernels, states)
+                ok = [not isinstance(x, Exception) for x in r]
+                ev = [x[1]['evaluations'] for x in r if not isinstance(x, Exception)]
+                # warm solves + the apply(0) of every state (about a tenth of a solve's launches) + network GEMMs
+                nl = sum(x[1]['kernel_launches'] for x in r if not isinstance(x, Exception)) + ws.mlp.gemm_launches - g0
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            if step >= a.warmup:
+                times.append(dt)
+                conv.append(sum(ok))
+                evals.extend(ev)
+                launches += nl
+        res[form] = dict(value=sum(conv) / sum(times), seconds_per_batch=statistics.mean(times), states=n,
+                         converged_per_batch=statistics.mean(conv), evaluations_mean=statistics.mean(evals),
+                         kernel_launches=launches)
+    for k in kernels:
+        k.close()
+    return res
+
+
 def run_gb300(a, rank, world):
     import torch
 
-    from sosfuse2_gb300 import _abi, build
+    from sosfuse2_gb300 import _abi, build, learned, synth
     from sosfuse2_gb300.solver import Solver
     from sosfuse2_gb300.state import PackedState
 
     build.build()
     local = int(os.environ.get('LOCAL_RANK', 0))
     torch.cuda.set_device(local)
+    device = f'cuda:{local}'
     dist = None
     if world > 1:
         import torch.distributed as dist  # noqa: F811
 
         dist.init_process_group('nccl')
+    # ---------------------------------------------------------------- plain single-state solve (kernel roofline)
     arrays, desc = workload(a.config, a.seed + rank)
     state = PackedState(arrays)
-    solver = Solver(state, device=f'cuda:{local}')
+    solver = Solver(state, device=device)
     k = solver.kernel
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=k.device)
     tol = float(state.meta['tolerance'])
@@ -259,13 +327,9 @@ def run_gb300(a, rank, world):
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     k.lib.sosb_set_timing(k.h, 1)
-    if dist:
-        dist.barrier()
     torch.cuda.synchronize()
     clocks = Clocks(local)
-    step_ms = []
-    evaluations = []
-    launches = 0
+    step_ms, evaluations, launches = [], [], 0
     for _ in range(a.steps):
         flush.fill_(1.0)  # L2 flush between timed solves, outside the events
         e0 = torch.cuda.Event(enable_timing=True)
@@ -277,33 +341,71 @@ def run_gb300(a, rank, world):
         step_ms.append(e0.elapsed_time(e1))
         evaluations.append(st['evaluations'])
         launches += st['kernel_launches']
-    torch.cuda.synchronize()
-    clk = clocks.stop()
     ms = (_abi.c_dbl * 7)()
     cnt = (_abi.c_i64 * 7)()
     k.lib.sosb_get_timing(k.h, ms, cnt, 7)
     k.lib.sosb_set_timing(k.h, 0)
-    total_ms = sum(step_ms)
-    t = torch.tensor([total_ms], device=k.device)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-    total_ms = float(t.item())
-    value = world * a.steps / (total_ms / 1e3)
-    # end to end through the public API: host state in, host converged field out
-    e2e_ms = []
-    h2d = sum(v.nbytes for key, v in arrays.items() if key != 'meta')
-    d2h = int(np.prod(state.shape)) * 4
-    for _ in range(max(1, min(a.steps, 3))):
-        torch.cuda.synchronize()
+    plain_ms = statistics.mean(step_ms)
+    # ---------------------------------------------------------------- batched forms on the config-0 family
+    forms = None
+    if a.config == 0 and not a.no_forms:
+        fam = synth.config0_family()
         t0 = time.perf_counter()
-        s2 = Solver(PackedState(arrays), device=f'cuda:{local}')
-        x, _ = s2.solve(max_eval, tol)
-        torch.cuda.synchronize()
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-        s2.kernel.close()
-    e2e = dict(value=world / (statistics.mean(e2e_ms) / 1e3), unit='solves/s', h2d_bytes_per_step=int(h2d),
-               d2h_bytes_per_step=int(d2h))
+        ws, report = learned.train_warm_start(fam, n_train=a.train_solves, epochs=a.epochs, seed=10000, device=device)
+        report['seconds'] = time.perf_counter() - t0
+        seeds = list(range(90000, 90000 + a.batch))
+        forms = _time_batched(a, fam, ws, device, seeds)
+        forms['training'] = report
+        forms['learned_vs_plain'] = forms['learned']['value'] / max(forms['plain']['value'], 1e-30)
+        launches += forms['plain']['kernel_launches'] + forms['learned']['kernel_launches']
+    clk = clocks.stop()
+    value_plain = 1e3 / plain_ms
+    value = forms['learned']['value'] if forms else value_plain
+    t = torch.tensor([value], device=k.device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MIN)
+        dist.barrier()
+    value = float(t.item()) * world
+    # ---------------------------------------------------------------- end to end through the public API
+    e2e_ms = []
+    if forms:
+        from sosfuse2_gb300.synth import family_state
+
+        seeds = list(range(90000, 90000 + a.batch))
+        host = [family_state(fam, sd) for sd in seeds]
+        h2d = sum(v.nbytes for arr in host for key, v in arr.items() if key != 'meta')
+        d2h = sum(int(np.prod(PackedState(arr).shape)) * 4 for arr in host)
+        for _ in range(max(1, min(a.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sts = [PackedState(arr) for arr in host]
+            from sosfuse2_gb300.solver import Kernel
+
+            kernels = [Kernel(st, device) for st in sts]
+            for kk in kernels:
+                kk._check(kk.lib.sosb_set_stream(kk.h, None))
+            r = learned.solve_batch(ws, kernels, sts)
+            fields = [x[0].cpu().numpy() for x in r if not isinstance(x, Exception)]
+            torch.cuda.synchronize()
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            conv = len(fields)
+            for kk in kernels:
+                kk.close()
+        e2e = dict(value=world * conv / (statistics.mean(e2e_ms) / 1e3), unit='solves/s', h2d_bytes_per_step=int(h2d),
+                   d2h_bytes_per_step=int(d2h))
+    else:
+        h2d = sum(v.nbytes for key, v in arrays.items() if key != 'meta')
+        d2h = int(np.prod(state.shape)) * 4
+        for _ in range(max(1, min(a.steps, 3))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s2 = Solver(PackedState(arrays), device=device)
+            s2.solve(max_eval, tol)
+            torch.cuda.synchronize()
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            s2.kernel.close()
+        e2e = dict(value=world / (statistics.mean(e2e_ms) / 1e3), unit='solves/s', h2d_bytes_per_step=int(h2d),
+                   d2h_bytes_per_step=int(d2h))
     if rank != 0:
         return
     classes = _abi.KERNEL_CLASSES
@@ -319,20 +421,33 @@ def run_gb300(a, rank, world):
         per_launch = per_solve / per_solve_launches
         mean_ms = ms[top] / max(cnt[top], 1)
         achieved = per_launch / (mean_ms / 1e3) / 1e9
-        roof = dict(kernel='transport_kernel', bound='hbm', achieved=achieved, peak=peak, unit='GB/s',
-                    frac=achieved / peak, peak_source=peak_kind, traffic=profiled_traffic('transport_kernel'),
-                    bytes_per_launch=per_launch, mean_launch_ms=mean_ms)
+        roof = dict(kernel='transport_warp_kernel' if state.W <= 4 else 'transport_wave_kernel', bound='hbm',
+                    achieved=achieved, peak=peak, unit='GB/s', frac=achieved / peak, peak_source=peak_kind,
+                    traffic=profiled_traffic('transport_warp_kernel' if state.W <= 4 else 'transport_wave_kernel'),
+                    bytes_per_launch=per_launch, mean_launch_ms=mean_ms,
+                    measured_on='plain single-state solve of the workload below')
     cb = None
     if world == 1 and not a.no_cpu_baseline:
         cb, _ = cpu_baseline(arrays, int(round(E)))
+    if forms:
+        wl = (f'config-0 family batch: {a.batch} held-out seeded states (seeds 90000+) on the config-0 grid (101 '
+              f'heights x 10 solar-zenith nodes, nmu 1, nphi 2, path_n 4, L=16, 550 nm, stratospheric layer), amounts '
+              f'from the batched configuration ranges (AOD 0.02-0.5, g 0.5-0.8, ozone 250-400 DU, albedo 0.05-0.8); '
+              f'learned start + concurrent batched solves; value counts converged solves only')
+        step_ms_out = forms['learned']['seconds_per_batch'] * 1e3
+    else:
+        wl = desc
+        step_ms_out = plain_ms
     out = dict(
         metric=METRIC, value=value, unit='solves/s', n_gpus=world, steps=a.steps, warmup=a.warmup,
-        ms_per_step=total_ms / a.steps, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f32',
+        ms_per_step=step_ms_out, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f32',
         data='synthetic (seeded atmosphere on the reference geometry, sosfuse2_gb300.synth)',
-        config=dict(workload=desc, rays=state.meta['rays'], segments=state.meta['segments'], cells=state.ns,
-                    evaluations_per_solve=E, l2='flushed between timed solves (512 MiB write outside the events)',
-                    form='plain (no learned start, one state per launch)', parallelism=f'replicas x{world}'),
-        roofline=roof, kernel_times=times, cpu_baseline=cb, e2e=e2e, gpu_launches=int(launches), clocks=clk)
+        config=dict(workload=wl, plain_single_state=desc, rays=state.meta['rays'], segments=state.meta['segments'],
+                    cells=state.ns, evaluations_per_plain_solve=E, plain_single_solves_per_s=value_plain,
+                    l2='flushed between timed plain solves (512 MiB write outside the events); batch steps exceed L2',
+                    parallelism=f'replicas x{world}'),
+        forms=forms, roofline=roof, kernel_times=times, cpu_baseline=cb, e2e=e2e, gpu_launches=int(launches),
+        clocks=clk)
     print(json.dumps(out), flush=True)
 
 

@@ -399,6 +399,8 @@ def evaluate(ws, family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3):
             continue
         torch.cuda.synchronize()
         tp = time.perf_counter() - t
+        kernel.update(st)  # drop the plain solve's first light: the learned path computes its own
+        torch.cuda.synchronize()
         t = time.perf_counter()
         g1 = solver.apply(kernel.field())
         x0 = ws.predict_start(st, g1)
@@ -419,3 +421,52 @@ def evaluate(ws, family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3):
                         source_rel_l2=float(((xl - xp).norm() / xp.norm()).item())))
     kernel.close()
     return out
+
+
+def solve_batch(ws, kernels, states, max_eval=64, tolerance=1e-3, threads=0):
+    """Learned-start batched solves: apply(0) on every handle concurrently, one network pass over all states' rows,
+    then the warm-started solves concurrently. Returns [(field, stats) or RuntimeError] per state."""
+    import torch
+
+    n = len(kernels)
+    lib = kernels[0].lib
+    handles = (ctypes.c_void_p * n)(*[k.h.value for k in kernels])
+    zeros = [k.field() for k in kernels]
+    g1 = [torch.empty_like(z) for z in zeros]
+    status = (ctypes.c_int32 * n)()
+    torch.cuda.synchronize()
+    lib.sosb_apply_batch(handles, n, (ctypes.c_void_p * n)(*[z.data_ptr() for z in zeros]),
+                         (ctypes.c_void_p * n)(*[g.data_ptr() for g in g1]), status, int(threads))
+    for i in range(n):
+        if status[i]:
+            raise RuntimeError(lib.sosb_last_error(kernels[i].h).decode())
+    rows, norms, counts = [], [], []
+    for st, g in zip(states, g1):
+        X, norm = ws.rows(st, g)
+        rows.append(X)
+        norms.append(norm)
+        counts.append(X.shape[0])
+    X = torch.cat(rows)
+    pred = ws.mlp.predict(ws._pad_in(X))[:X.shape[0], :ws.n_slots] * ws.y_std + ws.y_mean
+    starts, r0 = [], 0
+    for st, g, norm, c in zip(states, g1, norms, counts):
+        p = pred[r0:r0 + c] * ws.lit(norm)[:, None]
+        r0 += c
+        ns, slots, W = g.shape
+        x0 = g.permute(0, 2, 1).reshape(-1, slots) + norm * p
+        starts.append(x0.reshape(ns, W, slots).permute(0, 2, 1).contiguous())
+    outs = [torch.empty_like(g) for g in g1]
+    stats = (_abi.Stats * n)()
+    torch.cuda.synchronize()
+    lib.sosb_solve_warm_batch(handles, n, int(max_eval), float(tolerance),
+                              (ctypes.c_void_p * n)(*[x.data_ptr() for x in starts]), float(ws.fallback_ss),
+                              (ctypes.c_void_p * n)(*[g.data_ptr() for g in g1]),
+                              (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs]), 1, stats, status, int(threads))
+    res = []
+    for i in range(n):
+        if status[i]:
+            res.append(RuntimeError(lib.sosb_last_error(kernels[i].h).decode()))
+        else:
+            res.append((outs[i], dict(evaluations=int(stats[i].evaluations) + 1, fallback=bool(stats[i].start_fallback),
+                                      kernel_launches=int(stats[i].kernel_launches))))
+    return res
