@@ -8,7 +8,8 @@ gathers and the random batch order.
 
 Rows are (cell, wavelength) pairs. Input: the cell's height and solar zenith, the log extinctions of air, aerosol,
 ozone and stratospheric aerosol at the cell and the optical depth above it, single-scattering albedo, albedo, the
-mixture's first 8 phase moments, the cell's single-scattering source g1 = apply(0) divided by its norm, and that norm.
+mixture's first 8 phase moments, the column optical depths of the four components, the cell's single-scattering source
+g1 = apply(0) divided by its norm, and that norm.
 Target: (x* - g1) / |g1| over all source slots, x* the converged source, for cells with single scattering; cells in
 the Earth's shadow (|g1| below 1e-8 of the largest) keep g1. The start is g1 + |g1| * prediction; if the
 first evaluation from it changes the source more than the single-scattering start typically does, the solve restarts
@@ -195,7 +196,7 @@ class MLP:
 
 # ---------------------------------------------------------------------------------------------------- features
 def cell_features(state):
-    """Optics features of every (cell, wavelength) row of a packed state [ns * W, 20] (FP64 on the host)."""
+    """Optics features of every (cell, wavelength) row of a packed state [ns * W, 24] (FP64 on the host)."""
     a, m = state.arrays, state.meta
     h, chi = a['h'].astype(float), a['chi'].astype(float)
     nh, nc, W = len(h), len(chi), state.W
@@ -227,6 +228,12 @@ def cell_features(state):
         feats.append(col(np.log10(np.maximum(v, 1e-12))[:, None, :]))
     feats += [col(ssa[:, None, :]), np.full(nh * nc * W, float(m['albedo'])), np.full(nh * nc * W, g)]
     feats += [col(moments[:, None, :, l]) for l in range(8)]
+    # whole-atmosphere quantities (multiple scattering at a cell depends on the whole column, not only the cell):
+    # total optical depths of air, aerosol, ozone and stratospheric aerosol
+    tau_air, tau_aer, tau_o3 = (np.trapezoid(beta[k], h, axis=0) for k in range(3))
+    tau_st = np.trapezoid(st, h, axis=0)
+    for v in (tau_air, tau_aer, tau_o3, tau_st):
+        feats.append(col(np.log10(np.maximum(v, 1e-12))[None, None, :]))
     return np.stack(feats, -1)
 
 
@@ -235,7 +242,7 @@ class WarmStart:
 
     def __init__(self, n_slots, W=1, width=512, depth=4, device='cuda', seed=0):
         self.n_slots = n_slots
-        self.n_opt = 20
+        self.n_opt = 24
         self.n_in = self.n_opt + n_slots + 1
         self.mlp = MLP(self.n_in, n_slots, width, depth, device, seed)
         self.torch = self.mlp.torch
