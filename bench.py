@@ -119,28 +119,40 @@ def profiled_traffic(kernel):
 
 
 def transport_bytes(state):
-    """Algorithmic (compulsory) DRAM bytes of the transport launches of one solve with E evaluations:
-    per launch, each ray's geometry (48 B direction words, 16 B local direction, 4+4+4+4 B azimuth, cell, offsets,
-    end interval, 24 B end columns, 1 B hit flag), each segment (16 B ends, 1 B flag), each cell (24 B start,
-    36 B frame), the field's Rayleigh slots and SH plane read once (warm passes), the output radiance (16 B per ray
-    and wavelength). Returns bytes per launch kind: first, ground, warm, observer."""
+    """Algorithmic (compulsory) DRAM bytes of one transport launch of each kind.
+
+    first (full geometry, one launch per solve; it also writes the node table): per ray its geometry (48 B direction
+    words, 16 B local direction, 4+4+4+4 B azimuth, cell, offsets, end interval, 24 B end columns, 1 B hit flag), per
+    segment 16 B ends and 1 B flag, per cell 24 B start and 36 B frame, the node table written (32 + 4 W B per node)
+    and the output radiance (16 B per ray and wavelength).
+    ground, warm, observer (node-table launches, 4 per evaluation): per node the table (32 + 4 W B), per ray 48 B
+    direction words, 16 B local direction, 4 B cell, 4 B segment offset and the 16 W B output, per cell 60 B, the
+    field's 4 Rayleigh slots and the SH plane (4 + K floats per cell and wavelength) read once, and for rays that
+    end on the ground 29 B of boundary data."""
     a = state.arrays
     W, K, ns, nc = state.W, state.K, state.ns, state.nc
-    def geom(prefix, cells=None):
+    node_b = 32 + 4 * W
+
+    def bundle(prefix, nq, cells=None):
         off = a[prefix + '_cell_off']
         seg = a[prefix + '_seg_off']
         n = len(off) - 1 if cells is None else cells
         rays = int(off[n])
         segs = int(seg[rays])
-        return rays, rays * (48 + 16 + 16 + 24 + 1) + segs * 17 + n * 60
-    r_all, g_all = geom('cell')
-    r_gnd, g_gnd = geom('cell', nc)
-    r_obs, g_obs = geom('query')
+        hits = int(np.count_nonzero(a[prefix + '_hits'][:rays]))
+        return rays, segs, segs * nq, n, hits
+
+    nq, nqq = int(state.meta['nq']), int(state.meta['nq_query'])
     field = ns * (4 + K) * W * 4
-    return dict(first=g_all + r_all * W * 16,
-                ground=g_gnd + field + r_gnd * W * 16,
-                warm=g_all + field + r_all * W * 16,
-                observer=g_obs + field + r_obs * W * 16)
+    r, sg, nodes, n, _ = bundle('cell', nq)
+    first = r * (48 + 16 + 16 + 24 + 1) + sg * 17 + n * 60 + nodes * node_b + r * W * 16
+
+    def table(prefix, q, cells=None, boundary=False):
+        rays, _, nodes, n, hits = bundle(prefix, q, cells)
+        return nodes * node_b + rays * (48 + 16 + 8 + 16 * W) + n * 60 + field + (hits * 29 if boundary else 0)
+
+    return dict(first=first, ground=table('cell', nq, nc), warm=table('cell', nq, boundary=True),
+                observer=table('query', nqq))
 
 
 # ------------------------------------------------------------------------------------------------ CPU baseline
@@ -341,9 +353,10 @@ def run_gb300(a, rank, world):
         step_ms.append(e0.elapsed_time(e1))
         evaluations.append(st['evaluations'])
         launches += st['kernel_launches']
-    ms = (_abi.c_dbl * 7)()
-    cnt = (_abi.c_i64 * 7)()
-    k.lib.sosb_get_timing(k.h, ms, cnt, 7)
+    ncls = len(_abi.KERNEL_CLASSES)
+    ms = (_abi.c_dbl * ncls)()
+    cnt = (_abi.c_i64 * ncls)()
+    k.lib.sosb_get_timing(k.h, ms, cnt, ncls)
     k.lib.sosb_set_timing(k.h, 0)
     plain_ms = statistics.mean(step_ms)
     # ---------------------------------------------------------------- batched forms on the config-0 family
@@ -409,23 +422,27 @@ def run_gb300(a, rank, world):
     if rank != 0:
         return
     classes = _abi.KERNEL_CLASSES
-    times = {classes[i]: dict(ms=ms[i], launches=int(cnt[i]), share=ms[i] / max(sum(ms), 1e-30)) for i in range(7)}
-    top = max(range(7), key=lambda i: ms[i])
+    ncls = len(classes)
+    times = {classes[i]: dict(ms=ms[i], launches=int(cnt[i]), share=ms[i] / max(sum(ms), 1e-30))
+             for i in range(ncls)}
+    top = max(range(ncls), key=lambda i: ms[i])
     E = statistics.mean(evaluations)
     peak, peak_kind = peaks()
     roof = None
-    if classes[top] == 'transport':
+    if classes[top] in ('transport', 'transport_table'):
         b = transport_bytes(state)
-        per_solve = b['first'] + E * (b['ground'] + b['warm'] + 2 * b['observer'])
-        per_solve_launches = 1 + 4 * E
-        per_launch = per_solve / per_solve_launches
+        if classes[top] == 'transport_table':
+            # ground + warm + 2 observer launches per evaluation, all from node tables
+            per_launch = (b['ground'] + b['warm'] + 2 * b['observer']) / 4
+            name = 'transport_table_kernel' if state.W <= 4 else 'transport_table_wave_kernel'
+        else:
+            per_launch = b['first']
+            name = 'transport_warp_kernel' if state.W <= 4 else 'transport_wave_kernel'
         mean_ms = ms[top] / max(cnt[top], 1)
         achieved = per_launch / (mean_ms / 1e3) / 1e9
-        roof = dict(kernel='transport_warp_kernel' if state.W <= 4 else 'transport_wave_kernel', bound='hbm',
-                    achieved=achieved, peak=peak, unit='GB/s', frac=achieved / peak, peak_source=peak_kind,
-                    traffic=profiled_traffic('transport_warp_kernel' if state.W <= 4 else 'transport_wave_kernel'),
-                    bytes_per_launch=per_launch, mean_launch_ms=mean_ms,
-                    measured_on='plain single-state solve of the workload below')
+        roof = dict(kernel=name, bound='hbm', achieved=achieved, peak=peak, unit='GB/s', frac=achieved / peak,
+                    peak_source=peak_kind, traffic=profiled_traffic(name), bytes_per_launch=per_launch,
+                    mean_launch_ms=mean_ms, measured_on='plain single-state solve of the workload below')
     cb = None
     if world == 1 and not a.no_cpu_baseline:
         cb, _ = cpu_baseline(arrays, int(round(E)))

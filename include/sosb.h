@@ -116,6 +116,11 @@ int sosb_create(const sosb_dims *dims, sosb_handle *out);
 int sosb_destroy(sosb_handle h);
 /* Work stream (a cudaStream_t); 0 selects the handle's own stream. */
 int sosb_set_stream(sosb_handle h, void *stream);
+/* No reference counterpart. Node tables (default on): the first transport launch over a whole bundle after its rays
+ * or the optics change stores each node's frame angles, corner fractions and attenuation (32 + 4 W bytes a node,
+ * only within half the free device memory), and later warm launches read them instead of recomputing the
+ * double-single geometry and the optical-depth prefix. 0 turns them off (every launch recomputes). */
+int sosb_set_node_tables(sosb_handle h, int enable);
 /* Replaces: Kernel.setup (source_solver.py:1243-1339) and constants_device (source_solver.py:2248). */
 int sosb_set_constants(sosb_handle h, const sosb_constants *c);
 /* Replaces: ray_geometry.upload_geometry / device_geometry (ray_geometry.py:205-287) of the cell bundle
@@ -153,8 +158,9 @@ int sosb_boxes(sosb_handle h, const float *field_dev, double *out_host);
 int sosb_solve(sosb_handle h, int max_eval, double tolerance, const float *x0_host, float *x_out,
                int x_out_is_device, sosb_stats *stats);
 /* Kernel timing with CUDA events on the work stream (no counterpart in the reference's ABI; its Kernel.timed_launch,
- * source_solver.py:1478-1523, keeps a per-kind launch log). Classes: 0 transport, 1 projection, 2 SH plane,
- * 3 composition, 4 observer boxes, 5 Anderson, 6 other. sosb_set_timing(h, 1) starts and clears the totals;
+ * source_solver.py:1478-1523, keeps a per-kind launch log). Classes: 0 transport with its geometry (first light,
+ * node-table builds), 1 projection, 2 SH plane, 3 composition, 4 observer boxes, 5 Anderson, 6 other, 7 transport
+ * from node tables. sosb_set_timing(h, 1) starts and clears the totals;
  * sosb_get_timing fills ms[k] and launches[k] for k < n. */
 int sosb_set_timing(sosb_handle h, int on);
 int sosb_get_timing(sosb_handle h, double *ms, int64_t *launches, int n);

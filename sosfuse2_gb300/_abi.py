@@ -23,7 +23,7 @@ P_u8 = ctypes.POINTER(ctypes.c_uint8)
 
 CELLS = 0
 OBSERVER = 1
-KERNEL_CLASSES = ('transport', 'projection', 'plane', 'composition', 'boxes', 'anderson', 'other')
+KERNEL_CLASSES = ('transport', 'projection', 'plane', 'composition', 'boxes', 'anderson', 'other', 'transport_table')
 
 
 class Dims(ctypes.Structure):
@@ -68,6 +68,7 @@ SIGNATURES = {
     'sosb_create': ([ctypes.POINTER(Dims), ctypes.POINTER(ctypes.c_void_p)], c_int),
     'sosb_destroy': ([ctypes.c_void_p], c_int),
     'sosb_set_stream': ([ctypes.c_void_p, ctypes.c_void_p], c_int),
+    'sosb_set_node_tables': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_constants': ([ctypes.c_void_p, ctypes.POINTER(Constants)], c_int),
     'sosb_set_bundle': ([ctypes.c_void_p, c_int, ctypes.POINTER(Bundle)], c_int),
     'sosb_evaluate': ([ctypes.c_void_p, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -133,6 +133,7 @@ struct Optics {
     const float* sh_b;     // [K]
     const float* sh_d;     // [L+1] diagonal factors
     const float* strato_lut;  // [STRATO_LUT_BINS + 1][W] stratospheric phase per sr on a uniform grid of u in [-1, 1]
+    const uint8_t* gsame;  // [ns] 1 when cell c + 1 (same height, next solar zenith) has c's ground directions, or null
 };
 
 constexpr int STRATO_LUT_BINS = 4096;
@@ -211,17 +212,6 @@ SOS_HD float legendre_phase(const Optics& o, float u, int w) {
     return val / C_4PI;
 }
 
-// Stratospheric phase by linear interpolation in its table (built from the same 33 Legendre moments in FP64), the
-// form the reference's CUDA path evaluates it in (kernel.cu strato_lut_build); used in the first-light ground sums.
-SOS_HD float legendre_phase_lut(const Optics& o, float u, int w) {
-    const float x = (clampf(u, -1.0f, 1.0f) + 1.0f) * (0.5f * STRATO_LUT_BINS);
-    int i = (int)x;
-    i = i > STRATO_LUT_BINS - 1 ? STRATO_LUT_BINS - 1 : i;
-    const float f = x - (float)i;
-    const float a = o.strato_lut[(size_t)i * o.W + w], b = o.strato_lut[(size_t)(i + 1) * o.W + w];
-    return a + f * (b - a);
-}
-
 SOS_HD float ftz_value(DS a) {
     float h = fabsf(a.h) < TRACE_MIN ? 0.0f : a.h;
     float l = fabsf(a.l) < TRACE_MIN ? 0.0f : a.l;
@@ -243,6 +233,9 @@ struct Node {
     float mu, exd, eyd;  // ray direction in the node's local frame (first light)
     Profile prof;
     float st_prof;
+    float fr[4];      // cos, sin of the interpolated cell angle; cos, sin of the node's longitude (frame inputs)
+    float ah, ac;     // bilinear fractions in height and solar zenith
+    int j;            // solar-zenith interval
 };
 
 struct RayConst {
@@ -269,33 +262,14 @@ SOS_HD float beta_at(const Optics& o, const RayConst& rc, DS t, int w) {
     return extinction(o, p, o.strato ? strato_profile(o, h) : 0.0f, w);
 }
 
-SOS_HD void sample_node(const Optics& o, const RayConst& rc, DS a, DS b, bool lower, DS u, DS wu, Node& n) {
-    DS length = ds_sub(b, a);
-    DS v = lower ? u : ds_sub(ds_make(1.0f), u);
-    DS tt = lower ? ds_add(a, ds_mul(length, ds_mul(u, u))) : ds_sub(b, ds_mul(length, ds_mul(v, v)));
-    n.t = tt;
-    n.ds = ds_val(ds_mul(ds_mul(length, v), wu)) * 2.0f;
-    DS q[3], q2[3], r;
-    path_point(rc, tt, q, q2, r);
-    n.r = r;
-    n.qz = q[2];
-    float h = path_height(o, r);
-    n.h = h;
-    DS xy = ds_sqrt(ds_add(q2[0], q2[1]));
-    float rho = ds_val(xy);
-    float cx = 1.0f, sx = 0.0f;
-    if (rho > 1e-12f) {
-        DS den = DS{fmaxf(xy.h, 1e-30f), xy.l};
-        cx = ds_val(ds_div(q[0], den));
-        sx = ds_val(ds_div(q[1], den));
-    }
-    float angle = atan2f(rho, ds_val(q[2]));
-    int ir = bracket(o.h, o.nh, h);
-    int j = bracket(o.chi, o.nc, angle);
-    float ah = clampf((h - o.h[ir]) / (o.h[ir + 1] - o.h[ir]), 0.0f, 1.0f);
-    float ac = clampf((angle - o.chi[j]) / (o.chi[j + 1] - o.chi[j]), 0.0f, 1.0f);
-    float ang = o.chi[j] + ac * (o.chi[j + 1] - o.chi[j]);
-    float sn = sinf(ang), cc = cosf(ang);
+// Rotation of the Rayleigh coherency tensor into the ray frame, the ray direction in the node's local frame and the
+// azimuth cosine, from the cos/sin of the node's interpolated cell angle (cc, sn) and of its longitude (cx, sx)
+// (numpy_reference.py:515-545).
+SOS_HD void node_frame(const RayConst& rc, float cc, float sn, float cx, float sx, Node& n) {
+    n.fr[0] = cc;
+    n.fr[1] = sn;
+    n.fr[2] = cx;
+    n.fr[3] = sx;
     // Q rows: local (east, north, up) of the node in global coordinates, columns indexed [k][j]
     float Q[3][3] = {{-cc * cx, sx, sn * cx}, {-cc * sx, -cx, sn * sx}, {sn, 0.0f, cc}};
     float A[3][3], dot[3];
@@ -325,6 +299,13 @@ SOS_HD void sample_node(const Optics& o, const RayConst& rc, DS a, DS b, bool lo
     n.exd = dot[0];
     n.eyd = dot[1];
     n.cp = rc.st > 1e-12f ? (rc.d32[0] * cx + rc.d32[1] * sx) / fmaxf(rc.st, 1e-30f) : 1.0f;
+}
+
+// Corner cells (ir, j), (ir, j+1), (ir+1, j), (ir+1, j+1) and their bilinear weights.
+SOS_HD void node_corners(const Optics& o, int ir, int j, float ah, float ac, Node& n) {
+    n.ah = ah;
+    n.ac = ac;
+    n.j = j;
     n.ir = ir;
     n.cell[0] = ir * o.nc + j;
     n.cell[1] = ir * o.nc + j + 1;
@@ -334,6 +315,36 @@ SOS_HD void sample_node(const Optics& o, const RayConst& rc, DS a, DS b, bool lo
     n.sw[1] = (1.0f - ah) * ac;
     n.sw[2] = ah * (1.0f - ac);
     n.sw[3] = ah * ac;
+}
+
+SOS_HD void sample_node(const Optics& o, const RayConst& rc, DS a, DS b, bool lower, DS u, DS wu, Node& n) {
+    DS length = ds_sub(b, a);
+    DS v = lower ? u : ds_sub(ds_make(1.0f), u);
+    DS tt = lower ? ds_add(a, ds_mul(length, ds_mul(u, u))) : ds_sub(b, ds_mul(length, ds_mul(v, v)));
+    n.t = tt;
+    n.ds = ds_val(ds_mul(ds_mul(length, v), wu)) * 2.0f;
+    DS q[3], q2[3], r;
+    path_point(rc, tt, q, q2, r);
+    n.r = r;
+    n.qz = q[2];
+    float h = path_height(o, r);
+    n.h = h;
+    DS xy = ds_sqrt(ds_add(q2[0], q2[1]));
+    float rho = ds_val(xy);
+    float cx = 1.0f, sx = 0.0f;
+    if (rho > 1e-12f) {
+        DS den = DS{fmaxf(xy.h, 1e-30f), xy.l};
+        cx = ds_val(ds_div(q[0], den));
+        sx = ds_val(ds_div(q[1], den));
+    }
+    float angle = atan2f(rho, ds_val(q[2]));
+    int ir = bracket(o.h, o.nh, h);
+    int j = bracket(o.chi, o.nc, angle);
+    float ah = clampf((h - o.h[ir]) / (o.h[ir + 1] - o.h[ir]), 0.0f, 1.0f);
+    float ac = clampf((angle - o.chi[j]) / (o.chi[j + 1] - o.chi[j]), 0.0f, 1.0f);
+    float ang = o.chi[j] + ac * (o.chi[j + 1] - o.chi[j]);
+    node_frame(rc, cosf(ang), sinf(ang), cx, sx, n);
+    node_corners(o, ir, j, ah, ac, n);
     n.prof = profile_at(o, h);
     n.st_prof = o.strato ? strato_profile(o, h) : 0.0f;
 }
@@ -476,11 +487,97 @@ struct LaneInputs {
     int first;
 };
 
+// Henyey-Greenstein phase (per sr) of the pair of scattering cosines (up, dn), averaged:
+// ((1 - g^2) / 4 pi) (den_up^-3/2 + den_dn^-3/2) / 2 with den = 1 + g^2 - 2 g u, by reciprocal square roots.
+struct HgPair {
+    float a, b, c;  // 1 + g^2, 2 g, (1 - g^2) / (8 pi)
+};
+
+SOS_HD HgPair hg_pair_constants(float g) { return HgPair{1.0f + g * g, 2.0f * g, (1.0f - g * g) / (2.0f * C_4PI)}; }
+
+SOS_HD float rsqrt_fast(float x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrtf(x);
+#else
+    return 1.0f / sqrtf(x);
+#endif
+}
+
+SOS_HD float hg_pair(const HgPair& k, float up, float dn) {
+    const float r1 = rsqrt_fast(fmaxf(1e-20f, k.a - k.b * up));
+    const float r2 = rsqrt_fast(fmaxf(1e-20f, k.a - k.b * dn));
+    return k.c * ((r1 * r1) * r1 + (r2 * r2) * r2);
+}
+
+// Stratospheric phase by linear interpolation in its table (built from the same 33 Legendre moments in FP64), the
+// form the reference's CUDA path evaluates it in (kernel.cu strato_lut_build); used in the first-light ground sums.
+// Position of u in the table: bin i and fraction f.
+SOS_HD void strato_lut_pos(float u, int& i, float& f) {
+    const float x = (clampf(u, -1.0f, 1.0f) + 1.0f) * (0.5f * STRATO_LUT_BINS);
+    i = (int)x;
+    i = i > STRATO_LUT_BINS - 1 ? STRATO_LUT_BINS - 1 : i;
+    f = x - (float)i;
+}
+
+SOS_HD float strato_lut_at(const Optics& o, int i, float f, int w) {
+    const float a = o.strato_lut[(size_t)i * o.W + w], b = o.strato_lut[(size_t)(i + 1) * o.W + w];
+    return a + f * (b - a);
+}
+
+// Light from the lit ground scattered at the node, wavelengths w0 .. w0 + nw - 1 (nw <= NW): for every ground
+// direction of every corner cell, the aerosol (Henyey-Greenstein) and stratospheric (table) phase of the pair of
+// cosines (m0 + m1, m0 - m1) weighted by the corner weight and the direction's ground value
+// (numpy_reference.py:548-566). Corner pairs (ir, j), (ir, j+1) whose cells share their ground directions evaluate
+// the phases once for both cells.
+template <int NW>
+SOS_HD void ground_sums(const Optics& o, const Node& n, int w0, int nw, float ground[NW], float sground[NW]) {
+    const int W = o.W;
+    const HgPair hk = hg_pair_constants(o.g);
+    const float aeyd = fabsf(n.eyd);
+    for (int w = 0; w < NW; ++w) ground[w] = sground[w] = 0.0f;
+    for (int pr = 0; pr < 2; ++pr) {
+        const int ca = n.cell[2 * pr], cb = n.cell[2 * pr + 1];
+        const float wa = n.sw[2 * pr], wb = n.sw[2 * pr + 1];
+        const bool merged = o.gsame != nullptr && o.gsame[ca] != 0;
+        for (int side = 0; side < (merged ? 1 : 2); ++side) {
+            const int cell = side ? cb : ca;
+            const float wc = side ? wb : wa;
+            const int g0 = o.goff[cell], g1 = o.goff[cell + 1];
+            const int shift = merged ? o.goff[cb] - g0 : 0;
+            for (int gi = g0; gi < g1; ++gi) {
+                const float* gd = o.gdir + 3 * gi;
+                const float m0 = n.mu * gd[2] + n.exd * gd[0];
+                const float m1 = aeyd * gd[1];
+                const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
+                const float ph = hg_pair(hk, up, dn);
+                int iu = 0, id = 0;
+                float fu = 0.0f, fd = 0.0f;
+                if (o.strato) {
+                    strato_lut_pos(up, iu, fu);
+                    strato_lut_pos(dn, id, fd);
+                }
+                for (int k = 0; k < NW; ++k) {
+                    if (k >= nw) break;
+                    const int w = w0 + k;
+                    float gv = wc * o.gval[(size_t)gi * W + w];
+                    if (merged) gv += wb * o.gval[(size_t)(gi + shift) * W + w];
+                    ground[k] += ph * gv;
+                    if (o.strato) {
+                        const float sph = (strato_lut_at(o, iu, fu, w) + strato_lut_at(o, id, fd, w)) * 0.5f;
+                        sground[k] += sph * gv;
+                    }
+                }
+            }
+        }
+    }
+}
+
 // First-light value of one node for wavelength w: single scattering of the attenuated sun (Rayleigh tensor,
-// aerosol and stratospheric phase), light from the lit ground through the cell ground directions, and the direct
-// ground Rayleigh moments of the four corners (numpy_reference.py:515-568,573-622 with first=True).
+// aerosol and stratospheric phase), light from the lit ground through the cell ground directions (ground, sground:
+// ground_sums for w), and the direct ground Rayleigh moments of the four corners (numpy_reference.py:515-568,573-622
+// with first=True).
 SOS_HD void first_light_value(const Optics& o, const RayConst& rc, const Node& n, int w, float phase, float sphase,
-                              float val[4]) {
+                              float ground, float sground, float val[4]) {
     const int W = o.W;
     const float mix = o.mix;
     float col[5], stc, lit;
@@ -489,24 +586,6 @@ SOS_HD void first_light_value(const Optics& o, const RayConst& rc, const Node& n
     for (int k = 0; k < 5; ++k) optical += col[k] * o.ext[k * W + w];
     if (o.strato) optical += stc * o.strato_ext[w];
     const float sun = expf(-optical) * lit;
-    float ground = 0.0f, sground = 0.0f;
-    const float aeyd = fabsf(n.eyd);
-    for (int c = 0; c < 4; ++c) {
-        const int cell = n.cell[c];
-        for (int gi = o.goff[cell]; gi < o.goff[cell + 1]; ++gi) {
-            const float* gd = o.gdir + 3 * gi;
-            const float m0 = n.mu * gd[2] + n.exd * gd[0];
-            const float m1 = aeyd * gd[1];
-            const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
-            const float gv = o.gval[(size_t)gi * W + w];
-            const float ph = (hg_phase(up, o.g) + hg_phase(dn, o.g)) / 2.0f;
-            ground += (n.sw[c] * ph) * gv;
-            if (o.strato) {
-                const float sph = (legendre_phase_lut(o, up, w) + legendre_phase_lut(o, dn, w)) / 2.0f;
-                sground += (n.sw[c] * sph) * gv;
-            }
-        }
-    }
     const float beam = (n.prof.v[1] * o.asca[w]) * (sun * phase + ground);
     const float ray_ = (sun * n.prof.v[0]) * o.ext[w];
     const float sbeam = o.strato ? (n.st_prof * o.strato_sca[w]) * (sun * sphase + sground) : 0.0f;
@@ -525,6 +604,13 @@ SOS_HD void first_light_value(const Optics& o, const RayConst& rc, const Node& n
             val[k] += n.sw[c] * (dens * (mix * rot + ((1.0f - mix) / 3.0f * trace) * rc.pu[k]));
         }
     }
+}
+
+SOS_HD void first_light_value(const Optics& o, const RayConst& rc, const Node& n, int w, float phase, float sphase,
+                              float val[4]) {
+    float ground[1], sground[1];
+    ground_sums<1>(o, n, w, 1, ground, sground);
+    first_light_value(o, rc, n, w, phase, sphase, ground[0], sground[0], val);
 }
 
 // Warm (multiple-scattering) value of one node for wavelength w from the current source: Rayleigh tensor of each

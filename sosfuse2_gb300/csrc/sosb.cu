@@ -42,10 +42,13 @@ struct BundleDev {
     int64_t nray = 0, nseg = 0;
     DevBuf cell_off, ray_cell, p, frame, dir, dir_lo, dloc, pcp, seg_off, seg, lower, end_j, end_col, hits;
     std::vector<int64_t> host_cell_off;
+    // node table (NodeTable): valid once a launch over the whole bundle wrote it; too_big: over the memory budget
+    DevBuf t_frame, t_misc, t_att;
+    bool t_valid = false, t_too_big = false;
 };
 
 // kernel classes timed by sosb_set_timing / sosb_get_timing
-enum { K_TRANSPORT = 0, K_PROJECT, K_PLANE, K_COMPOSE, K_BOXES, K_ANDERSON, K_OTHER, K_CLASSES };
+enum { K_TRANSPORT = 0, K_PROJECT, K_PLANE, K_COMPOSE, K_BOXES, K_ANDERSON, K_OTHER, K_TABLE, K_CLASSES };
 
 struct TimedLaunch {
     int cls;
@@ -65,7 +68,7 @@ struct sosb_state {
     bool have_constants = false;
     // constants
     DevBuf h, chi, hr, ha, ext, asca, table, sun_h, sun_col, gm, goff, gdir, gval, rf, af, ext0;
-    DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src, s_lut;
+    DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src, s_lut, gsame;
     DevBuf sh_a, sh_b, sh_d;
     DevBuf u_hi, u_lo, wu_hi, wu_lo, uq_hi, uq_lo, wuq_hi, wuq_lo, box_ww, solar;
     BundleDev cells, obs;
@@ -74,6 +77,7 @@ struct sosb_state {
     DevBuf fx, fg, fn, norms, partials, dots, mixw;
     DevBuf ring_g[4], ring_f[4];
     bool have_first = false;
+    bool tables = true;  // build and use node tables (sosb_set_node_tables)
     int64_t launches = 0;
 };
 
@@ -142,24 +146,43 @@ static int grid_for(long long n, int threads) {
 // ------------------------------------------------------------------------------------------------ kernels
 constexpr int TRANSPORT_THREADS = 128;
 
-__global__ void __launch_bounds__(TRANSPORT_THREADS)
-    transport_kernel(Optics o, Rays b, LaneInputs in, int ray0, int nray, int glog2, int wchunks, float4* rad) {
-    extern __shared__ float cache[];
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long grp = t >> glog2;
-    const int lane = (int)(t & ((1 << glog2) - 1));
-    const long long rr = grp / wchunks;
-    const int w = (int)(grp % wchunks) * 32 + lane;
-    if (rr >= nray || w >= o.W) return;
-    const int ray = ray0 + (int)rr;
-    float out[4];
-    transport_lane(o, b, in, ray, w, cache + threadIdx.x, blockDim.x, out);
-    rad[(size_t)ray * o.W + w] = make_float4(out[0], out[1], out[2], out[3]);
+// Per-node geometry and attenuation of one ray bundle (node id = segment * nq + step), written by the first launch
+// over the whole bundle after the bundle or the optics change and read by every later warm launch, which then skips
+// the double-single geometry, the profile lookups and the Simpson prefix. Null pointers: nothing is written.
+struct NodeTable {
+    float4* frame;  // [nodes] cos, sin of the interpolated cell angle; cos, sin of the node's longitude
+    float4* misc;   // [nodes] height fraction, solar-zenith fraction, azimuth cosine, bits of (ir << 16 | j)
+    float* att;     // [nodes][W] quadrature weight x attenuation from the ray's origin
+};
+
+__device__ __forceinline__ float4 table_misc(const Node& n) {
+    return make_float4(n.ah, n.ac, n.cp, __int_as_float((n.ir << 16) | n.j));
+}
+
+// Node of a table entry: frame rotation, corners and azimuth cosine (what warm_value and the SH synthesis read).
+__device__ __forceinline__ void table_node(const Optics& o, const RayConst& rc, const NodeTable& tab, long long id,
+                                           Node& n) {
+    const float4 fr = tab.frame[id];
+    const float4 ms = tab.misc[id];
+    node_frame(rc, fr.x, fr.y, fr.z, fr.w, n);
+    const int pk = __float_as_int(ms.w);
+    node_corners(o, pk >> 16, pk & 0xffff, ms.x, ms.y, n);
+    n.cp = ms.z;
 }
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
 static size_t warp_smem(int K) { return sizeof(float) * (size_t)K * (TRANSPORT_THREADS / 32); }
+
+// Shared words per warp of transport_table_kernel: basis, run cells, per-(run, corner, m, w) sums.
+SOS_HD int table_warp_words(int K, int L1, int W, int slots) { return K + slots + slots * 4 * L1 * W; }
+
+// Run slots of transport_table_kernel: as many as fit in 2048 words of sums per warp, 2 to 8.
+static int table_slots(int L, int W) { return std::max(2, std::min(8, 2048 / (4 * (L + 1) * W))); }
+
+static size_t table_smem(int K, int L, int W) {
+    return sizeof(float) * (size_t)table_warp_words(K, L + 1, W, table_slots(L, W)) * (TRANSPORT_THREADS / 32);
+}
 
 SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }
 
@@ -170,7 +193,7 @@ SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }
 // ray. Numerically this is transport_lane with the sums regrouped (panel and ray sums in tree order).
 template <int WM>
 __global__ void __launch_bounds__(TRANSPORT_THREADS)
-    transport_warp_kernel(Optics o, Rays b, LaneInputs in, int ray0, int nray, float4* rad) {
+    transport_warp_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, float4* rad) {
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= nray) return;  // the whole warp leaves together
@@ -288,13 +311,21 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
             S[w] = v;
         }
         if (act) {
+            const long long id = (long long)s0 * nq + i;
+            if (tab.frame) {
+                tab.frame[id] = make_float4(n.fr[0], n.fr[1], n.fr[2], n.fr[3]);
+                tab.misc[id] = table_misc(n);
+            }
+            float ground[WM], sground[WM];
+            if (first) ground_sums<WM>(o, n, 0, W, ground, sground);
 #pragma unroll
             for (int w = 0; w < WM; ++w) {
                 if (w >= W) continue;
                 const float att = n.ds * expf(-((carry[w] + S[w]) - close[w]));
+                if (tab.att) tab.att[id * W + w] = att;
                 float val[4];
                 if (first) {
-                    first_light_value(o, rc, n, w, phase, sphase[w], val);
+                    first_light_value(o, rc, n, w, phase, sphase[w], ground[w], sground[w], val);
                 } else {
                     float aero[4];
                     const float* pc[4];
@@ -367,7 +398,8 @@ SOS_HD void profile6(const Optics& o, const RayConst& rc, DS t, float* p6) {
 constexpr int WAVE_WARPS = 2;
 
 __global__ void __launch_bounds__(WAVE_WARPS * 32)
-    transport_wave_kernel(Optics o, Rays b, LaneInputs in, int ray0, int nray, int wchunks, float4* rad) {
+    transport_wave_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int wchunks,
+                          float4* rad) {
     extern __shared__ float wave_sm[];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -412,6 +444,11 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
             sample_node(o, rc, a, bb, b.lower[s0 + sl] != 0, DS{in.u_hi[step], in.u_lo[step]},
                         DS{in.wu_hi[step], in.wu_lo[step]}, n);
             tnode = n.t;
+            if (tab.frame) {
+                const long long id = (long long)s0 * nq + i;
+                tab.frame[id] = make_float4(n.fr[0], n.fr[1], n.fr[2], n.fr[3]);
+                tab.misc[id] = table_misc(n);
+            }
             R->r_h = n.r.h; R->r_l = n.r.l; R->qz_h = n.qz.h; R->qz_l = n.qz.l; R->h = n.h; R->ds = n.ds;
             R->cp = n.cp; R->mu = n.mu; R->exd = n.exd; R->eyd = n.eyd; R->st_prof = n.st_prof;
             for (int c = 0; c < 4; ++c) { R->sw[c] = n.sw[c]; R->cell[c] = n.cell[c]; }
@@ -459,6 +496,7 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
             acc = acc + R->wpan * ((beta0 + beta1) + 4.0f * ext6(o, R->pm, wl));
             beta0 = beta1;
             const float att = R->ds * expf(-((tau - tauc) + acc));
+            if (tab.att && wok) tab.att[((long long)s0 * nq + base + j) * o.W + w] = att;
             Node n;
             n.r = DS{R->r_h, R->r_l};
             n.qz = DS{R->qz_h, R->qz_l};
@@ -518,6 +556,215 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
 
 static size_t wave_smem(int L) {
     return sizeof(float) * (size_t)WAVE_WARPS * (32 * REC_WORDS + 4 * (L + 1) * 32 + (L + 1) * (L + 2) / 2);
+}
+
+// Warm pass from the node table, few wavelengths (W <= WM): one warp per ray, lane i takes nodes i, i + 32, ...
+// (the node-to-lane assignment and per-lane Kahan order of transport_warp_kernel). Consecutive nodes of a ray share
+// their corner cells, so per batch of 32 nodes the warp contracts each run of equal corner cells once: the lanes
+// split the (run, corner, m, wavelength) sums over l of Y_lm x plane into shared memory, and each node only adds its
+// azimuth series over m. Runs beyond `slots` synthesise their corners directly.
+template <int WM>
+__global__ void __launch_bounds__(TRANSPORT_THREADS)
+    transport_table_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int slots,
+                           float4* rad) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= nray) return;  // the whole warp leaves together
+    const int ray = ray0 + (int)warp;
+    const int W = o.W;
+    const int L1 = o.L + 1;
+    RayConst rc;
+    ray_constants(b, ray, rc);
+    const int nq = in.nq;
+    const int s0 = b.seg_off[ray];
+    const long long node0 = (long long)s0 * nq;
+    const int nn = (b.seg_off[ray + 1] - s0) * nq;
+    extern __shared__ float warp_sm[];
+    float* Y = warp_sm + (size_t)(threadIdx.x >> 5) * table_warp_words(o.K, L1, W, slots);
+    int* runs = reinterpret_cast<int*>(Y + o.K);
+    float* msum = Y + o.K + slots;  // [run][corner][m][w]
+    for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
+    float tot[WM][4], cmp[WM][4];
+#pragma unroll
+    for (int w = 0; w < WM; ++w)
+        for (int k = 0; k < 4; ++k) tot[w][k] = cmp[w][k] = 0.0f;
+    for (int base = 0; base < nn; base += 32) {
+        const int i = base + lane;
+        const bool act = i < nn;
+        const long long id = node0 + i;
+        Node n;
+        int key = -1;
+        if (act) {
+            table_node(o, rc, tab, id, n);
+            key = n.cell[0];
+        }
+        const int prev = __shfl_up_sync(FULL_MASK, key, 1);
+        const bool head = act && (lane == 0 || prev != key);
+        const unsigned heads = __ballot_sync(FULL_MASK, head);
+        const int run = __popc(heads & (FULL_MASK >> (31 - lane))) - 1;
+        const int nrun = min(__popc(heads), slots);
+        __syncwarp();  // the previous batch is done with runs and msum (and the basis is written)
+        if (head && run < slots) runs[run] = key;
+        __syncwarp();
+        const int items = nrun * 4 * L1 * W;
+        for (int it = lane; it < items; it += 32) {
+            const int w = it % W;
+            int r = it / W;
+            const int m = r % L1;
+            r /= L1;
+            const int c = r & 3;
+            r >>= 2;
+            const int cell = runs[r] + (c & 1) + (c >> 1) * o.nc;
+            const float* pl = in.plane + (size_t)cell * o.K * W + w;
+            float acc = 0.0f;
+            int k = m * (m + 1) / 2 + m;
+            for (int l = m; l <= o.L; ++l) {
+                acc += Y[k] * pl[(size_t)k * W];
+                k += l + 1;
+            }
+            msum[it] = acc;
+        }
+        __syncwarp();
+        if (act) {
+#pragma unroll
+            for (int w = 0; w < WM; ++w) {
+                if (w >= W) continue;
+                const float att = tab.att[id * W + w];
+                float aero[4];
+                if (run < slots) {
+                    for (int c = 0; c < 4; ++c)
+                        aero[c] = azimuth_sum(o.L, n.cp, msum + ((size_t)(run * 4 + c) * L1) * W + w, W);
+                } else {
+                    const float* pc[4];
+                    for (int c = 0; c < 4; ++c) pc[c] = in.plane + (size_t)n.cell[c] * o.K * W + w;
+                    sh_synth4(o.L, Y, n.cp, pc, W, aero);
+                }
+                float val[4];
+                warm_value(o, rc, n, in.field, w, aero, val);
+                for (int k = 0; k < 4; ++k) kahan(tot[w][k], cmp[w][k], val[k] * att);
+            }
+        }
+    }
+#pragma unroll
+    for (int w = 0; w < WM; ++w) {
+        float v[4];
+        for (int k = 0; k < 4; ++k) {
+            v[k] = tot[w][k] - cmp[w][k];
+#pragma unroll
+            for (int dd = 16; dd >= 1; dd >>= 1) v[k] += __shfl_xor_sync(FULL_MASK, v[k], dd);
+        }
+        if (lane == 0 && w < W) {
+            boundary_term(o, b, rc, in.boundary, ray, w, v);
+            rad[(size_t)ray * W + w] = make_float4(v[0], v[1], v[2], v[3]);
+        }
+    }
+}
+
+// Node record of the table wave kernel: what warm_value and the corner cache read.
+constexpr int TREC_WORDS = 27;  // odd stride: the 32 lanes write their records without bank conflicts
+struct TableRec {
+    float T[16];
+    float sw[4];
+    int cell[4];
+    int ir;
+    float cp;
+};
+static_assert(sizeof(TableRec) <= TREC_WORDS * 4, "table record exceeds its stride");
+
+// Warm pass from the node table, many wavelengths: one warp per (ray, chunk of 32 wavelengths). Lane j rebuilds
+// node base+j's record into shared memory; then lane = wavelength walks the records in order with its 4-slot corner
+// SH cache (the operation order of transport_wave_kernel's warm branch).
+__global__ void __launch_bounds__(WAVE_WARPS * 32)
+    transport_table_wave_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int wchunks,
+                                float4* rad) {
+    extern __shared__ float wave_sm[];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const long long warp = (long long)blockIdx.x * WAVE_WARPS + wid;
+    if (warp >= (long long)nray * wchunks) return;  // the whole warp leaves together
+    const int ray = ray0 + (int)(warp / wchunks);
+    const int w = (int)(warp % wchunks) * 32 + lane;
+    const bool wok = w < o.W;
+    const int wl = wok ? w : o.W - 1;  // idle lanes compute a valid wavelength and store nothing
+    const int L1 = o.L + 1;
+    float* recs = wave_sm + (size_t)wid * (32 * TREC_WORDS + 4 * L1 * 32 + o.K);
+    float* cache = recs + 32 * TREC_WORDS + lane;
+    float* Y = recs + 32 * TREC_WORDS + 4 * L1 * 32;
+    RayConst rc;
+    ray_constants(b, ray, rc);
+    for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
+    const int nq = in.nq;
+    const int s0 = b.seg_off[ray];
+    const long long node0 = (long long)s0 * nq;
+    const int nn = (b.seg_off[ray + 1] - s0) * nq;
+    float total[4] = {0, 0, 0, 0}, comp[4] = {0, 0, 0, 0};
+    int tag[4] = {-1, -1, -1, -1};
+    for (int base = 0; base < nn; base += 32) {
+        const int i = base + lane;
+        const int cnt = min(32, nn - base);
+        __syncwarp();
+        if (i < nn) {
+            TableRec* R = reinterpret_cast<TableRec*>(recs + lane * TREC_WORDS);
+            Node n;
+            table_node(o, rc, tab, node0 + i, n);
+            for (int k = 0; k < 4; ++k)
+                for (int u = 0; u < 4; ++u) R->T[4 * k + u] = n.T[k][u];
+            for (int c = 0; c < 4; ++c) {
+                R->sw[c] = n.sw[c];
+                R->cell[c] = n.cell[c];
+            }
+            R->ir = n.ir;
+            R->cp = n.cp;
+        }
+        __syncwarp();
+        for (int j = 0; j < cnt; ++j) {
+            const TableRec* R = reinterpret_cast<const TableRec*>(recs + j * TREC_WORDS);
+            const float att = tab.att[(node0 + base + j) * o.W + wl];
+            Node n;
+            for (int k = 0; k < 4; ++k)
+                for (int u = 0; u < 4; ++u) n.T[k][u] = R->T[4 * k + u];
+            for (int c = 0; c < 4; ++c) {
+                n.sw[c] = R->sw[c];
+                n.cell[c] = R->cell[c];
+            }
+            n.ir = R->ir;
+            n.cp = R->cp;
+            int slot_of[4];
+            unsigned used = 0;
+            for (int c = 0; c < 4; ++c) {
+                slot_of[c] = -1;
+                for (int q = 0; q < 4; ++q)
+                    if (tag[q] == n.cell[c] && !(used & (1u << q))) {
+                        slot_of[c] = q;
+                        used |= 1u << q;
+                        break;
+                    }
+            }
+            for (int c = 0; c < 4; ++c) {
+                if (slot_of[c] >= 0) continue;
+                int q = 0;
+                while (used & (1u << q)) ++q;
+                used |= 1u << q;
+                slot_of[c] = q;
+                tag[q] = n.cell[c];
+                sh_contract_basis(o.L, Y, in.plane + (size_t)n.cell[c] * o.K * o.W + wl, o.W,
+                                  cache + (size_t)q * L1 * 32, 32);
+            }
+            float aero[4];
+            for (int c = 0; c < 4; ++c) aero[c] = azimuth_sum(o.L, n.cp, cache + (size_t)slot_of[c] * L1 * 32, 32);
+            float val[4];
+            warm_value(o, rc, n, in.field, wl, aero, val);
+            for (int k = 0; k < 4; ++k) kahan(total[k], comp[k], val[k] * att);
+        }
+    }
+    if (wok) {
+        boundary_term(o, b, rc, in.boundary, ray, w, total);
+        rad[(size_t)ray * o.W + w] = make_float4(total[0], total[1], total[2], total[3]);
+    }
+}
+
+static size_t table_wave_smem(int L) {
+    return sizeof(float) * (size_t)WAVE_WARPS * (32 * TREC_WORDS + 4 * (L + 1) * 32 + (L + 1) * (L + 2) / 2);
 }
 
 __global__ void plane_kernel(const float* __restrict__ field, const float* __restrict__ ha,
@@ -842,6 +1089,7 @@ static Optics optics_of(const sosb_state* s) {
     o.sh_b = P<float>(s->sh_b);
     o.sh_d = P<float>(s->sh_d);
     o.strato_lut = P<float>(s->s_lut);
+    o.gsame = P<uint8_t>(s->gsame);
     return o;
 }
 
@@ -914,8 +1162,45 @@ static int collect_timing(sosb_state* s) {
     return 0;
 }
 
+// Node table of bundle `b` for a launch: `read` when a valid table serves a warm launch; `write` when this launch
+// covers the whole bundle and should build it (within half the free device memory).
+static int table_for(sosb_state* s, BundleDev& b, int nq, bool whole, int first, NodeTable& write, bool& read) {
+    write = NodeTable{nullptr, nullptr, nullptr};
+    read = false;
+    if (!s->tables || b.t_too_big) return 0;
+    if (b.t_valid) {
+        read = !first;
+        return 0;
+    }
+    if (!whole) return 0;
+    const sosb_dims& d = s->d;
+    if (d.nh > 32768 || d.nc > 65536) {  // (ir << 16 | j) packing
+        b.t_too_big = true;
+        return 0;
+    }
+    const size_t nodes = (size_t)b.nseg * nq;
+    const size_t need = nodes * (2 * sizeof(float4) + (size_t)d.W * sizeof(float));
+    const size_t have = b.t_frame.bytes + b.t_misc.bytes + b.t_att.bytes;
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if (need > have && need - have > (free_b + have) / 2) {
+        b.t_too_big = true;
+        return 0;
+    }
+    TRY(dalloc(s, b.t_frame, std::max<size_t>(nodes, 1) * sizeof(float4)));
+    TRY(dalloc(s, b.t_misc, std::max<size_t>(nodes, 1) * sizeof(float4)));
+    TRY(dalloc(s, b.t_att, std::max<size_t>(nodes * d.W, 1) * sizeof(float)));
+    write = NodeTable{P<float4>(b.t_frame), P<float4>(b.t_misc), P<float>(b.t_att)};
+    return 0;
+}
+
+static void invalidate_tables(BundleDev& b) {
+    b.t_valid = false;
+    b.t_too_big = false;
+}
+
 // transport of rays [ray0, ray0 + nray) of bundle `b` into s->rad
-static int run_transport(sosb_state* s, const BundleDev& b, int64_t ray0, int64_t nray, const float* field,
+static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray, const float* field,
                          const float* boundary, int first, bool query) {
     if (nray <= 0) return 0;
     const sosb_dims& d = s->d;
@@ -938,39 +1223,45 @@ static int run_transport(sosb_state* s, const BundleDev& b, int64_t ray0, int64_
         in.wu_lo = P<float>(s->wu_lo);
         in.nq = d.nq;
     }
+    NodeTable write;
+    bool read = false;
+    TRY(table_for(s, b, in.nq, ray0 == 0 && nray == b.nray, first, write, read));
+    const NodeTable table{P<float4>(b.t_frame), P<float4>(b.t_misc), P<float>(b.t_att)};
     if (d.W <= 4) {
         // sample-parallel: one warp per ray
         const long long blocks = (nray * 32 + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
-        Timer timer(s, K_TRANSPORT);
-        if (d.W == 1)
-            transport_warp_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, warp_smem(s->K), s->stream>>>(
-                optics_of(s), rays_of(b), in, (int)ray0, (int)nray, P<float4>(s->rad));
+        const size_t smem = warp_smem(s->K);
+        Timer timer(s, read ? K_TABLE : K_TRANSPORT);
+        const int slots = table_slots(d.L, d.W);
+        const size_t tsmem = table_smem(s->K, d.L, d.W);
+        if (read && d.W == 1)
+            transport_table_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, tsmem, s->stream>>>(
+                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, slots, P<float4>(s->rad));
+        else if (read)
+            transport_table_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, tsmem, s->stream>>>(
+                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, slots, P<float4>(s->rad));
+        else if (d.W == 1)
+            transport_warp_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
+                optics_of(s), rays_of(b), in, write, (int)ray0, (int)nray, P<float4>(s->rad));
         else
-            transport_warp_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, warp_smem(s->K), s->stream>>>(
-                optics_of(s), rays_of(b), in, (int)ray0, (int)nray, P<float4>(s->rad));
-        return launch_check(s);
-    }
-    {
+            transport_warp_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
+                optics_of(s), rays_of(b), in, write, (int)ray0, (int)nray, P<float4>(s->rad));
+    } else {
         // many wavelengths: one warp per (ray, chunk of 32 wavelengths), geometry shared through shared memory
         const int wchunks = (d.W + 31) / 32;
         const long long warps = (long long)nray * wchunks;
         const long long blocks = (warps + WAVE_WARPS - 1) / WAVE_WARPS;
-        Timer timer(s, K_TRANSPORT);
-        transport_wave_kernel<<<(unsigned)blocks, WAVE_WARPS * 32, wave_smem(d.L), s->stream>>>(
-            optics_of(s), rays_of(b), in, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
-        return launch_check(s);
+        Timer timer(s, read ? K_TABLE : K_TRANSPORT);
+        if (read)
+            transport_table_wave_kernel<<<(unsigned)blocks, WAVE_WARPS * 32, table_wave_smem(d.L), s->stream>>>(
+                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
+        else
+            transport_wave_kernel<<<(unsigned)blocks, WAVE_WARPS * 32, wave_smem(d.L), s->stream>>>(
+                optics_of(s), rays_of(b), in, write, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
     }
-    const int wchunk = std::min(d.W, 32);
-    int glog2 = 0;
-    while ((1 << glog2) < wchunk) ++glog2;
-    const int wchunks = (d.W + 31) / 32;
-    const long long threads = (long long)nray * wchunks << glog2;
-    const long long blocks = (threads + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
-    const size_t smem = sizeof(float) * 4 * (d.L + 1) * TRANSPORT_THREADS;
-    Timer timer(s, K_TRANSPORT);
-    transport_kernel<<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
-        optics_of(s), rays_of(b), in, (int)ray0, (int)nray, glog2, wchunks, P<float4>(s->rad));
-    return launch_check(s);
+    TRY(launch_check(s));
+    if (write.frame) b.t_valid = true;
+    return 0;
 }
 
 static int run_project(sosb_state* s, const BundleDev& b, int ncell, bool ground_only, float* moments, float* flux) {
@@ -1142,10 +1433,9 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
     }
     s->stream = s->own;
     {
-        const size_t t_smem = sizeof(float) * 4 * (d.L + 1) * TRANSPORT_THREADS;
         const size_t p_smem = project_smem((d.L + 1) * (d.L + 2) / 2, d.W);
-        if (cudaFuncSetAttribute(transport_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t_smem) !=
-                cudaSuccess ||
+        if (cudaFuncSetAttribute(transport_table_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)table_wave_smem(d.L)) != cudaSuccess ||
             cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_smem) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(transport_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1153,7 +1443,11 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
             cudaFuncSetAttribute(transport_warp_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
             cudaFuncSetAttribute(transport_warp_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess) {
+                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
+            cudaFuncSetAttribute(transport_table_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)table_smem((d.L + 1) * (d.L + 2) / 2, d.L, d.W)) != cudaSuccess ||
+            cudaFuncSetAttribute(transport_table_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)table_smem((d.L + 1) * (d.L + 2) / 2, d.L, d.W)) != cudaSuccess) {
             cudaStreamDestroy(s->own);
             delete s;
             return 5;
@@ -1175,7 +1469,7 @@ int sosb_destroy(sosb_handle s) {
     cudaStreamSynchronize(s->stream);
     DevBuf* bufs[] = {&s->h, &s->chi, &s->hr, &s->ha, &s->ext, &s->asca, &s->table, &s->sun_h, &s->sun_col, &s->gm,
                       &s->goff, &s->gdir, &s->gval, &s->rf, &s->af, &s->ext0, &s->s_ext, &s->s_sca, &s->s_chi,
-                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->s_lut, &s->sh_a, &s->sh_b, &s->sh_d,
+                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->s_lut, &s->gsame, &s->sh_a, &s->sh_b, &s->sh_d,
                       &s->u_hi, &s->u_lo, &s->wu_hi, &s->wu_lo, &s->uq_hi, &s->uq_lo, &s->wuq_hi, &s->wuq_lo,
                       &s->box_ww, &s->solar, &s->rad, &s->plane, &s->moments, &s->flux, &s->first_moments,
                       &s->first_flux, &s->boundary, &s->metrics, &s->boxes, &s->fx, &s->fg, &s->fn, &s->norms,
@@ -1184,7 +1478,8 @@ int sosb_destroy(sosb_handle s) {
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
-                        &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits};
+                        &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits,
+                        &bd->t_frame, &bd->t_misc, &bd->t_att};
         for (DevBuf* b : bb) dfree(s, *b);
     }
     collect_timing(s);
@@ -1212,6 +1507,14 @@ int sosb_get_timing(sosb_handle s, double* ms, int64_t* launches, int n) {
         ms[k] = s->timed_ms[k];
         launches[k] = s->timed_count[k];
     }
+    return 0;
+}
+
+int sosb_set_node_tables(sosb_handle s, int enable) {
+    if (!s) return 1;
+    s->tables = enable != 0;
+    invalidate_tables(s->cells);
+    invalidate_tables(s->obs);
     return 0;
 }
 
@@ -1273,6 +1576,18 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
         TRY(dalloc(s, s->gdir, 16));
         TRY(dalloc(s, s->gval, 16));
     }
+    {
+        // cells whose next solar-zenith neighbour (same height) has the same ground directions, bit for bit
+        std::vector<uint8_t> same(ns, 0);
+        for (int cell = 0; cell < ns; ++cell) {
+            if (cell % d.nc == d.nc - 1) continue;
+            const int n0 = goff[cell + 1] - goff[cell], n1 = goff[cell + 2] - goff[cell + 1];
+            same[cell] = n0 > 0 && n0 == n1 &&
+                         std::memcmp(c->gdir + 3 * (size_t)goff[cell], c->gdir + 3 * (size_t)goff[cell + 1],
+                                     (size_t)n0 * 3 * sizeof(float)) == 0;
+        }
+        TRY(dput_vec(s, s->gsame, same));
+    }
     TRY(dput(s, s->rf, c->rf, 6 * 4));
     TRY(dput(s, s->af, c->af, K * 4));
     TRY(dput(s, s->ext0, c->ext0, W * 4));
@@ -1307,6 +1622,8 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
     CK(cudaStreamSynchronize(s->stream));
     s->have_constants = true;
     s->have_first = false;
+    invalidate_tables(s->cells);
+    invalidate_tables(s->obs);
     return 0;
 }
 
@@ -1319,6 +1636,7 @@ int sosb_set_bundle(sosb_handle s, int which, const sosb_bundle* b) {
     const std::string msg = pack_bundle(b, s->d.nc, pk);
     if (!msg.empty()) return fail(s, "%s", msg.c_str());
     BundleDev& bd = which == SOSB_CELLS ? s->cells : s->obs;
+    invalidate_tables(bd);
     bd.ncell = pk.ncell;
     bd.nray = pk.nray;
     bd.nseg = pk.nseg;

@@ -65,6 +65,11 @@ class Kernel:
         st._keep.clear()
         self.state = st
 
+    def set_node_tables(self, enable):
+        """Store per-node geometry and attenuation at the first launch over a bundle and read them in warm launches
+        (default on); off: every launch recomputes them."""
+        self._check(self.lib.sosb_set_node_tables(self.h, int(bool(enable))))
+
     def _check(self, rc):
         if rc:
             msg = self.lib.sosb_last_error(self.h).decode()
