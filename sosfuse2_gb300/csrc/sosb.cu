@@ -76,6 +76,7 @@ struct sosb_state {
     DevBuf rad, plane, moments, flux, first_moments, first_flux, boundary, metrics, boxes;
     DevBuf fx, fg, fn, norms, partials, dots, mixw;
     DevBuf ring_g[4], ring_f[4];
+    DevBuf fl_val0, fl_coef, fl_dir, fl_g, fl_cnt, fl_off, fl_cursor, fl_entries;  // staged first light
     bool have_first = false;
     bool tables = true;  // build and use node tables (sosb_set_node_tables)
     int64_t launches = 0;
@@ -170,19 +171,21 @@ __device__ __forceinline__ void table_node(const Optics& o, const RayConst& rc, 
     n.cp = ms.z;
 }
 
+// First light of a cell bundle in stages (few wavelengths): a preparation launch stores per node the first-light
+// value without its ground-scattered part (val0), the factors that scale the ground sums into it (coef: aerosol
+// density x scattering, stratospheric profile x scattering) and the ray direction in the node's frame (dir); the
+// ground sums G (aerosol, stratospheric) of each corner pair are then computed over node pairs bucketed by corner
+// cell, and a last launch sums val0 + coef x G over each ray.
+struct FirstLightBufs {
+    float4* val0;  // [nodes][W]
+    float2* coef;  // [nodes][W]
+    float4* dir;   // [nodes] (mu, exd, |eyd|, 0)
+    float2* g;     // [nodes][2 pairs][W] (ground, stratospheric ground)
+};
+
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
 static size_t warp_smem(int K) { return sizeof(float) * (size_t)K * (TRANSPORT_THREADS / 32); }
-
-// Shared words per warp of transport_table_kernel: basis, run cells, per-(run, corner, m, w) sums.
-SOS_HD int table_warp_words(int K, int L1, int W, int slots) { return K + slots + slots * 4 * L1 * W; }
-
-// Run slots of transport_table_kernel: as many as fit in 2048 words of sums per warp, 2 to 8.
-static int table_slots(int L, int W) { return std::max(2, std::min(8, 2048 / (4 * (L + 1) * W))); }
-
-static size_t table_smem(int K, int L, int W) {
-    return sizeof(float) * (size_t)table_warp_words(K, L + 1, W, table_slots(L, W)) * (TRANSPORT_THREADS / 32);
-}
 
 SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }
 
@@ -191,9 +194,10 @@ SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }
 // (plus the segment's closing panel on its last node); a warp prefix sum of the panel integrals gives every node's
 // optical depth; each lane forms its node's value with the corner SH synthesised directly; a warp reduction sums the
 // ray. Numerically this is transport_lane with the sums regrouped (panel and ray sums in tree order).
-template <int WM>
+template <int WM, bool PREP>
 __global__ void __launch_bounds__(TRANSPORT_THREADS)
-    transport_warp_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, float4* rad) {
+    transport_warp_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, FirstLightBufs fl, int ray0, int nray,
+                          float4* rad) {
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= nray) return;  // the whole warp leaves together
@@ -316,14 +320,22 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
                 tab.frame[id] = make_float4(n.fr[0], n.fr[1], n.fr[2], n.fr[3]);
                 tab.misc[id] = table_misc(n);
             }
+            if (PREP) fl.dir[id] = make_float4(n.mu, n.exd, fabsf(n.eyd), 0.0f);
             float ground[WM], sground[WM];
-            if (first) ground_sums<WM>(o, n, 0, W, ground, sground);
+            if (first && !PREP) ground_sums<WM>(o, n, 0, W, ground, sground);
 #pragma unroll
             for (int w = 0; w < WM; ++w) {
                 if (w >= W) continue;
                 const float att = n.ds * expf(-((carry[w] + S[w]) - close[w]));
                 if (tab.att) tab.att[id * W + w] = att;
                 float val[4];
+                if (PREP) {
+                    first_light_value(o, rc, n, w, phase, sphase[w], 0.0f, 0.0f, val);
+                    fl.val0[id * W + w] = make_float4(val[0], val[1], val[2], val[3]);
+                    fl.coef[id * W + w] = make_float2(n.prof.v[1] * o.asca[w],
+                                                      o.strato ? n.st_prof * o.strato_sca[w] : 0.0f);
+                    continue;
+                }
                 if (first) {
                     first_light_value(o, rc, n, w, phase, sphase[w], ground[w], sground[w], val);
                 } else {
@@ -343,17 +355,19 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
         }
         carry_t = DS{__shfl_sync(FULL_MASK, n.t.h, 31), __shfl_sync(FULL_MASK, n.t.l, 31)};
     }
+    if constexpr (!PREP) {
 #pragma unroll
-    for (int w = 0; w < WM; ++w) {
-        float v[4];
-        for (int k = 0; k < 4; ++k) {
-            v[k] = tot[w][k] - cmp[w][k];
+        for (int w = 0; w < WM; ++w) {
+            float v[4];
+            for (int k = 0; k < 4; ++k) {
+                v[k] = tot[w][k] - cmp[w][k];
 #pragma unroll
-            for (int dd = 16; dd >= 1; dd >>= 1) v[k] += __shfl_xor_sync(FULL_MASK, v[k], dd);
-        }
-        if (lane == 0 && w < W) {
-            boundary_term(o, b, rc, in.boundary, ray, w, v);
-            rad[(size_t)ray * W + w] = make_float4(v[0], v[1], v[2], v[3]);
+                for (int dd = 16; dd >= 1; dd >>= 1) v[k] += __shfl_xor_sync(FULL_MASK, v[k], dd);
+            }
+            if (lane == 0 && w < W) {
+                boundary_term(o, b, rc, in.boundary, ray, w, v);
+                rad[(size_t)ray * W + w] = make_float4(v[0], v[1], v[2], v[3]);
+            }
         }
     }
 }
@@ -558,90 +572,177 @@ static size_t wave_smem(int L) {
     return sizeof(float) * (size_t)WAVE_WARPS * (32 * REC_WORDS + 4 * (L + 1) * 32 + (L + 1) * (L + 2) / 2);
 }
 
-// Warm pass from the node table, few wavelengths (W <= WM): one warp per ray, lane i takes nodes i, i + 32, ...
-// (the node-to-lane assignment and per-lane Kahan order of transport_warp_kernel). Consecutive nodes of a ray share
-// their corner cells, so per batch of 32 nodes the warp contracts each run of equal corner cells once: the lanes
-// split the (run, corner, m, wavelength) sums over l of Y_lm x plane into shared memory, and each node only adds its
-// azimuth series over m. Runs beyond `slots` synthesise their corners directly.
+// ------------------------------------------------------------------ staged first light (W <= 4)
+// Corner pair pr of a node (cells (ir + pr, j) and (ir + pr, j + 1)): its first cell, the key of its bucket.
+__device__ __forceinline__ int pair_cell(const Optics& o, float4 ms, int pr) {
+    const int pk = __float_as_int(ms.w);
+    return ((pk >> 16) + pr) * o.nc + (pk & 0xffff);
+}
+
+// Ground directions a pair visits: the first cell's, plus the second cell's unless the two share them.
+__device__ __forceinline__ int pair_work(const Optics& o, int ca) {
+    int n = o.goff[ca + 1] - o.goff[ca];
+    if (!(o.gsame != nullptr && o.gsame[ca])) n += o.goff[ca + 2] - o.goff[ca + 1];
+    return n;
+}
+
+// Bucket sizes: cnt[cell] += pairs with work whose first cell is `cell` (one atomic per group of equal keys in a
+// warp). With `cursor`, the second pass writes the pair codes (node * 2 + pr) into their buckets.
+__global__ void pair_bucket_kernel(Optics o, const float4* __restrict__ misc, long long nodes, int* cnt, int* cursor,
+                                   int* entries) {
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < nodes;
+         base += stride) {
+        const long long node = base + lane;
+        const bool ok = node < nodes;
+        const float4 ms = ok ? misc[node] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int pr = 0; pr < 2; ++pr) {
+            int key = -1;
+            if (ok) {
+                const int ca = pair_cell(o, ms, pr);
+                if (pair_work(o, ca) > 0) key = ca;
+            }
+            const unsigned peers = __match_any_sync(FULL_MASK, key);
+            const int leader = __ffs(peers) - 1;
+            if (key < 0) continue;
+            if (!cursor) {
+                if (lane == leader) atomicAdd(&cnt[key], __popc(peers));
+            } else {
+                int at = 0;
+                if (lane == leader) at = atomicAdd(&cursor[key], __popc(peers));
+                at = __shfl_sync(peers, at, leader);
+                const int rank = __popc(peers & ((1u << lane) - 1u));
+                entries[at + rank] = (int)(node * 2 + pr);
+            }
+        }
+    }
+}
+
+// Exclusive prefix sum of the bucket sizes (one block): off[0..n], and the scatter cursors.
+__global__ void bucket_scan_kernel(const int* __restrict__ cnt, int n, int* off, int* cursor) {
+    __shared__ int part[1024];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < n ? cnt[i] : 0;
+        part[threadIdx.x] = v;
+        __syncthreads();
+        for (int d = 1; d < 1024; d <<= 1) {
+            const int u = threadIdx.x >= d ? part[threadIdx.x - d] : 0;
+            __syncthreads();
+            part[threadIdx.x] += u;
+            __syncthreads();
+        }
+        if (i < n) {
+            off[i] = carry + part[threadIdx.x] - v;
+            cursor[i] = off[i];
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += part[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) off[n] = carry;
+}
+
+// Ground sums of the bucketed pairs: lane = pair, pairs of one bucket visit the same ground directions, so the
+// lanes of a warp run the same loop over warp-uniform direction loads (numpy_reference.py:548-566; the
+// per-direction arithmetic of ground_sums).
+template <int WM>
+__global__ void __launch_bounds__(256)
+    ground_pairs_kernel(Optics o, const float4* __restrict__ misc, const float4* __restrict__ dir,
+                        const int* __restrict__ entries, const int* __restrict__ total, float2* g) {
+    const int W = o.W;
+    const int n_entries = *total;
+    const HgPair hk = hg_pair_constants(o.g);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_entries; e += gridDim.x * blockDim.x) {
+        const int code = entries[e];
+        const long long node = code >> 1;
+        const int pr = code & 1;
+        const float4 ms = misc[node];
+        const float4 dv = dir[node];
+        const float ah = ms.x, ac = ms.y;
+        const float wa = pr ? ah * (1.0f - ac) : (1.0f - ah) * (1.0f - ac);
+        const float wb = pr ? ah * ac : (1.0f - ah) * ac;
+        const int ca = pair_cell(o, ms, pr), cb = ca + 1;
+        const bool merged = o.gsame != nullptr && o.gsame[ca] != 0;
+        float ground[WM], sground[WM];
+#pragma unroll
+        for (int w = 0; w < WM; ++w) ground[w] = sground[w] = 0.0f;
+        for (int side = 0; side < (merged ? 1 : 2); ++side) {
+            const int cell = side ? cb : ca;
+            const float wc = side ? wb : wa;
+            const int g0 = o.goff[cell], g1 = o.goff[cell + 1];
+            const int shift = merged ? o.goff[cb] - g0 : 0;
+            for (int gi = g0; gi < g1; ++gi) {
+                const float* gd = o.gdir + 3 * gi;
+                const float m0 = dv.x * gd[2] + dv.y * gd[0];
+                const float m1 = dv.z * gd[1];
+                const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
+                const float ph = hg_pair(hk, up, dn);
+                int iu = 0, id = 0;
+                float fu = 0.0f, fd = 0.0f;
+                if (o.strato) {
+                    strato_lut_pos(up, iu, fu);
+                    strato_lut_pos(dn, id, fd);
+                }
+#pragma unroll
+                for (int w = 0; w < WM; ++w) {
+                    if (w >= W) break;
+                    float gv = wc * o.gval[(size_t)gi * W + w];
+                    if (merged) gv += wb * o.gval[(size_t)(gi + shift) * W + w];
+                    ground[w] += ph * gv;
+                    if (o.strato) {
+                        const float sph = (strato_lut_at(o, iu, fu, w) + strato_lut_at(o, id, fd, w)) * 0.5f;
+                        sground[w] += sph * gv;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < WM; ++w)
+            if (w < W) g[((size_t)node * 2 + pr) * W + w] = make_float2(ground[w], sground[w]);
+    }
+}
+
+// Per-ray sum of the staged first light: val0 + coef x (G pair 0 + G pair 1), attenuated, in the node-to-lane
+// assignment and Kahan order of transport_warp_kernel.
 template <int WM>
 __global__ void __launch_bounds__(TRANSPORT_THREADS)
-    transport_table_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int slots,
+    first_light_sum_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, FirstLightBufs fl, int ray0, int nray,
                            float4* rad) {
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= nray) return;  // the whole warp leaves together
     const int ray = ray0 + (int)warp;
     const int W = o.W;
-    const int L1 = o.L + 1;
     RayConst rc;
     ray_constants(b, ray, rc);
     const int nq = in.nq;
     const int s0 = b.seg_off[ray];
     const long long node0 = (long long)s0 * nq;
     const int nn = (b.seg_off[ray + 1] - s0) * nq;
-    extern __shared__ float warp_sm[];
-    float* Y = warp_sm + (size_t)(threadIdx.x >> 5) * table_warp_words(o.K, L1, W, slots);
-    int* runs = reinterpret_cast<int*>(Y + o.K);
-    float* msum = Y + o.K + slots;  // [run][corner][m][w]
-    for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
     float tot[WM][4], cmp[WM][4];
 #pragma unroll
     for (int w = 0; w < WM; ++w)
         for (int k = 0; k < 4; ++k) tot[w][k] = cmp[w][k] = 0.0f;
-    for (int base = 0; base < nn; base += 32) {
-        const int i = base + lane;
-        const bool act = i < nn;
+    for (int i = lane; i < nn; i += 32) {
         const long long id = node0 + i;
-        Node n;
-        int key = -1;
-        if (act) {
-            table_node(o, rc, tab, id, n);
-            key = n.cell[0];
-        }
-        const int prev = __shfl_up_sync(FULL_MASK, key, 1);
-        const bool head = act && (lane == 0 || prev != key);
-        const unsigned heads = __ballot_sync(FULL_MASK, head);
-        const int run = __popc(heads & (FULL_MASK >> (31 - lane))) - 1;
-        const int nrun = min(__popc(heads), slots);
-        __syncwarp();  // the previous batch is done with runs and msum (and the basis is written)
-        if (head && run < slots) runs[run] = key;
-        __syncwarp();
-        const int items = nrun * 4 * L1 * W;
-        for (int it = lane; it < items; it += 32) {
-            const int w = it % W;
-            int r = it / W;
-            const int m = r % L1;
-            r /= L1;
-            const int c = r & 3;
-            r >>= 2;
-            const int cell = runs[r] + (c & 1) + (c >> 1) * o.nc;
-            const float* pl = in.plane + (size_t)cell * o.K * W + w;
-            float acc = 0.0f;
-            int k = m * (m + 1) / 2 + m;
-            for (int l = m; l <= o.L; ++l) {
-                acc += Y[k] * pl[(size_t)k * W];
-                k += l + 1;
-            }
-            msum[it] = acc;
-        }
-        __syncwarp();
-        if (act) {
 #pragma unroll
-            for (int w = 0; w < WM; ++w) {
-                if (w >= W) continue;
-                const float att = tab.att[id * W + w];
-                float aero[4];
-                if (run < slots) {
-                    for (int c = 0; c < 4; ++c)
-                        aero[c] = azimuth_sum(o.L, n.cp, msum + ((size_t)(run * 4 + c) * L1) * W + w, W);
-                } else {
-                    const float* pc[4];
-                    for (int c = 0; c < 4; ++c) pc[c] = in.plane + (size_t)n.cell[c] * o.K * W + w;
-                    sh_synth4(o.L, Y, n.cp, pc, W, aero);
-                }
-                float val[4];
-                warm_value(o, rc, n, in.field, w, aero, val);
-                for (int k = 0; k < 4; ++k) kahan(tot[w][k], cmp[w][k], val[k] * att);
+        for (int w = 0; w < WM; ++w) {
+            if (w >= W) continue;
+            const float att = tab.att[id * W + w];
+            const float4 v0 = fl.val0[id * W + w];
+            const float2 cf = fl.coef[id * W + w];
+            const float2 g0 = fl.g[(size_t)id * 2 * W + w], g1 = fl.g[((size_t)id * 2 + 1) * W + w];
+            const float ga = cf.x * (g0.x + g1.x), gs = cf.y * (g0.y + g1.y);
+            const float val[4] = {v0.x, v0.y, v0.z, v0.w};
+            for (int k = 0; k < 4; ++k) {
+                float v = val[k] + ga * rc.pu[k] / 2.0f;
+                if (o.strato) v += (gs * rc.pu[k]) / 2.0f;
+                kahan(tot[w][k], cmp[w][k], v * att);
             }
         }
     }
@@ -658,6 +759,87 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
             rad[(size_t)ray * W + w] = make_float4(v[0], v[1], v[2], v[3]);
         }
     }
+}
+
+// Warm pass from the node table, few wavelengths (W <= WM): `wpr` warps (1, 2 or 4) per ray, lane l of warp q takes
+// nodes 32 q + l, 32 (q + wpr) + l, ... with its own Kahan sums; the warps' sums are added in warp order. Each node's
+// corner SH is synthesised from the ray's basis. (Contracting runs of equal corner cells once per warp instead
+// measured slower on GB300: the per-batch ballots and the scattered (run, m) sums cost more than the direct
+// synthesis.) Several warps per ray serve bundles of long rays (observer rays) that would otherwise leave most SMs
+// idle.
+template <int WM>
+__global__ void __launch_bounds__(TRANSPORT_THREADS)
+    transport_table_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int wpr,
+                           float4* rad) {
+    constexpr int WARPS = TRANSPORT_THREADS / 32;
+    __shared__ float red[WARPS][WM][4];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int q = wid % wpr;
+    const long long rr = (long long)blockIdx.x * (WARPS / wpr) + wid / wpr;
+    const bool live = rr < nray;  // uniform over each warp
+    const int ray = ray0 + (int)(live ? rr : 0);
+    const int W = o.W;
+    RayConst rc;
+    float v[WM][4];
+    if (live) {
+        ray_constants(b, ray, rc);
+        const int nq = in.nq;
+        const int s0 = b.seg_off[ray];
+        const long long node0 = (long long)s0 * nq;
+        const int nn = (b.seg_off[ray + 1] - s0) * nq;
+        extern __shared__ float warp_sm[];
+        float* Y = warp_sm + wid * o.K;
+        for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
+        __syncwarp();
+        float tot[WM][4], cmp[WM][4];
+#pragma unroll
+        for (int w = 0; w < WM; ++w)
+            for (int k = 0; k < 4; ++k) tot[w][k] = cmp[w][k] = 0.0f;
+        for (int i = q * 32 + lane; i < nn; i += 32 * wpr) {
+            const long long id = node0 + i;
+            Node n;
+            table_node(o, rc, tab, id, n);
+#pragma unroll
+            for (int w = 0; w < WM; ++w) {
+                if (w >= W) continue;
+                const float att = tab.att[id * W + w];
+                float aero[4];
+                const float* pc[4];
+                for (int c = 0; c < 4; ++c) pc[c] = in.plane + (size_t)n.cell[c] * o.K * W + w;
+                sh_synth4(o.L, Y, n.cp, pc, W, aero);
+                float val[4];
+                warm_value(o, rc, n, in.field, w, aero, val);
+                for (int k = 0; k < 4; ++k) kahan(tot[w][k], cmp[w][k], val[k] * att);
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < WM; ++w)
+            for (int k = 0; k < 4; ++k) {
+                v[w][k] = tot[w][k] - cmp[w][k];
+#pragma unroll
+                for (int dd = 16; dd >= 1; dd >>= 1) v[w][k] += __shfl_xor_sync(FULL_MASK, v[w][k], dd);
+            }
+    }
+    if (wpr > 1) {
+        if (live && lane == 0)
+            for (int w = 0; w < WM; ++w)
+                for (int k = 0; k < 4; ++k) red[wid][w][k] = v[w][k];
+        __syncthreads();
+        if (live && q == 0 && lane == 0)
+            for (int w = 0; w < WM; ++w)
+                for (int k = 0; k < 4; ++k) {
+                    float t = red[wid][w][k];
+                    for (int u = 1; u < wpr; ++u) t += red[wid + u][w][k];
+                    v[w][k] = t;
+                }
+    }
+    if (live && q == 0 && lane == 0)
+        for (int w = 0; w < WM; ++w) {
+            if (w >= W) break;
+            boundary_term(o, b, rc, in.boundary, ray, w, v[w]);
+            rad[(size_t)ray * W + w] = make_float4(v[w][0], v[w][1], v[w][2], v[w][3]);
+        }
 }
 
 // Node record of the table wave kernel: what warm_value and the corner cache read.
@@ -963,60 +1145,81 @@ __global__ void boxes_kernel(const float4* __restrict__ rad, const double* __res
     out[i] = s * solar[w];
 }
 
-// Anderson residual features. norms[cell][w] = |g[cell, :, w]| (FP32), and the per-wavelength max in mx (bits).
-__global__ void norm_kernel(const float* __restrict__ g, int ns, int src, int W, float* __restrict__ norms,
-                            unsigned* __restrict__ mx) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (long long)ns * W;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int w = (int)(i % W);
-        const long long cell = i / W;
-        const float* p = g + (size_t)cell * src * W + w;
-        float s = 0.0f;
-        for (int k = 0; k < src; ++k) {
-            const float v = p[(size_t)k * W];
-            s += v * v;
+// Norm of each cell's source per wavelength, ||g[cell, :, w]||_2, one warp per cell: lanes split the slots
+// (kk = lane / Wc) and the wavelengths (lane % Wc, Wc = min(W, 32)), so the loads of a warp are contiguous; the kk
+// partial sums of a wavelength are added in lane order. mx[w] collects the maximum norm (bits of a non-negative
+// float order as unsigned integers).
+constexpr int NORM_WARPS = 8;
+
+__global__ void __launch_bounds__(NORM_WARPS * 32)
+    norm_kernel(const float* __restrict__ g, int ns, int src, int W, float* __restrict__ norms,
+                unsigned* __restrict__ mx) {
+    __shared__ float part[NORM_WARPS][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int Wc = min(W, 32), KL = 32 / Wc;
+    const int wl = lane % Wc, kk = lane / Wc;
+    for (long long cell = (long long)blockIdx.x * NORM_WARPS + wid; cell < ns;
+         cell += (long long)gridDim.x * NORM_WARPS) {
+        const float* row = g + (size_t)cell * src * W;
+        for (int w0 = 0; w0 < W; w0 += 32) {
+            const int w = w0 + wl;
+            float acc = 0.0f;
+            if (kk < KL && w < W)
+                for (int k = kk; k < src; k += KL) {
+                    const float v = row[(size_t)k * W + w];
+                    acc += v * v;
+                }
+            part[wid][lane] = acc;
+            __syncwarp();
+            if (lane < Wc && w < W) {  // here wl == lane and kk == 0
+                float t = 0.0f;
+                for (int q = 0; q < KL; ++q) t += part[wid][q * Wc + lane];
+                const float nv = sqrtf(t);
+                norms[cell * W + w] = nv;
+                atomicMax(&mx[w], __float_as_uint(nv));
+            }
+            __syncwarp();
         }
-        const float nv = sqrtf(s);
-        norms[i] = nv;
-        atomicMax(&mx[w], __float_as_uint(nv));
     }
 }
 
-// feature f = (g - x) / max(norm, 1e-8 max norm) written to ring slot `dst`; FP64 partial dots of f with the ring
-// slots listed in `slots` (nslot <= 4, including dst itself) per block: partials[block][j][w].
-__global__ void feature_kernel(const float* __restrict__ g, const float* __restrict__ x, const float* __restrict__ norms,
-                               const unsigned* __restrict__ mx, int src, int W, long long n, float* __restrict__ dst,
-                               const float* r0, const float* r1, const float* r2, const float* r3, int nslot,
-                               double* __restrict__ partials) {
-    extern __shared__ double sd[];  // [nslot][W]
-    for (int i = threadIdx.x; i < nslot * W; i += blockDim.x) sd[i] = 0.0;
-    __syncthreads();
+// Residual feature f = (g - x) / max(norm, 1e-8 max norm) into ring slot `dst`, and FP64 partial dots of f with
+// the ring slots (nslot <= 4, dst among them): partials[block][j][w]. Blocks walk whole cells; the block size is a
+// multiple of W, so thread t keeps wavelength t % W over all its elements, and the per-thread sums of a wavelength
+// are added in thread order at the end (no atomics: the dots are reproducible run to run).
+__global__ void feature_kernel(const float* __restrict__ g, const float* __restrict__ x,
+                               const float* __restrict__ norms, const unsigned* __restrict__ mx, long long ns, int src,
+                               int W, float* __restrict__ dst, const float* r0, const float* r1, const float* r2,
+                               const float* r3, int nslot, double* __restrict__ partials) {
+    extern __shared__ double sd[];  // [blockDim.x][4]
+    const int B = blockDim.x;
+    const int t = threadIdx.x;
+    const int w = t % W;
+    const int row = src * W;
     const float* ring[4] = {r0, r1, r2, r3};
-    double loc[4] = {0, 0, 0, 0};
-    int wl = -1;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int w = (int)(i % W);
-        const long long cell = i / W / src;
-        const float nv = norms[cell * W + w];
-        const float scale = fmaxf(nv, __uint_as_float(mx[w]) * 1e-8f);
-        const float f = (g[i] - x[i]) / scale;
-        dst[i] = f;
-        // the stride is a multiple of W when gridDim*blockDim % W == 0, so w is fixed per thread
-        if (wl != w) {
-            if (wl >= 0)
-                for (int j = 0; j < nslot; ++j) atomicAdd(&sd[j * W + wl], loc[j]);
-            for (int j = 0; j < 4; ++j) loc[j] = 0.0;
-            wl = w;
-        }
-        for (int j = 0; j < nslot; ++j) {
-            const float o = (ring[j] == dst) ? f : ring[j][i];
-            loc[j] += (double)f * (double)o;
+    const float floor_w = __uint_as_float(mx[w]) * 1e-8f;
+    double loc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long cell = blockIdx.x; cell < ns; cell += gridDim.x) {
+        const float scale = fmaxf(norms[cell * W + w], floor_w);
+        const size_t base = (size_t)cell * row;
+        for (int e = t; e < row; e += B) {
+            const size_t i = base + e;
+            const float f = (g[i] - x[i]) / scale;
+            dst[i] = f;
+            for (int j = 0; j < nslot; ++j) {
+                const float o = (ring[j] == dst) ? f : ring[j][i];
+                loc[j] += (double)f * (double)o;
+            }
         }
     }
-    if (wl >= 0)
-        for (int j = 0; j < nslot; ++j) atomicAdd(&sd[j * W + wl], loc[j]);
+    for (int j = 0; j < 4; ++j) sd[t * 4 + j] = loc[j];
     __syncthreads();
-    for (int i = threadIdx.x; i < nslot * W; i += blockDim.x) partials[(size_t)blockIdx.x * nslot * W + i] = sd[i];
+    for (int q = t; q < nslot * W; q += B) {
+        const int j = q / W, ww = q % W;
+        double acc = 0.0;
+        for (int u = ww; u < B; u += W) acc += sd[u * 4 + j];
+        partials[(size_t)blockIdx.x * nslot * W + q] = acc;
+    }
 }
 
 __global__ void sum_partials_kernel(const double* __restrict__ partials, int blocks, int n, double* out) {
@@ -1199,6 +1402,74 @@ static void invalidate_tables(BundleDev& b) {
     b.t_too_big = false;
 }
 
+// Staged first light of the whole cell bundle (W <= 4; FirstLightBufs). Returns 0 with `done` false when the
+// scratch does not fit, leaving the single-launch path to the caller.
+static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs& in, const NodeTable& table,
+                                  bool& done) {
+    done = false;
+    const sosb_dims& d = s->d;
+    const int W = d.W;
+    const long long nodes = (long long)b.nseg * in.nq;
+    if (nodes >= (1LL << 30)) return 0;  // pair codes node * 2 + pr are int
+    const size_t need = (size_t)nodes * ((size_t)W * (16 + 8 + 16) + 16 + 8) + (size_t)(3 * s->ns + 2) * 4;
+    const size_t have = s->fl_val0.bytes + s->fl_coef.bytes + s->fl_dir.bytes + s->fl_g.bytes + s->fl_entries.bytes;
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if (need > have && need - have > (free_b + have) / 2) return 0;
+    const size_t n1 = std::max<long long>(nodes, 1);
+    TRY(dalloc(s, s->fl_val0, n1 * W * sizeof(float4)));
+    TRY(dalloc(s, s->fl_coef, n1 * W * sizeof(float2)));
+    TRY(dalloc(s, s->fl_dir, n1 * sizeof(float4)));
+    TRY(dalloc(s, s->fl_g, n1 * 2 * W * sizeof(float2)));
+    TRY(dalloc(s, s->fl_entries, n1 * 2 * sizeof(int)));
+    TRY(dalloc(s, s->fl_cnt, (size_t)(s->ns + 1) * sizeof(int)));
+    TRY(dalloc(s, s->fl_off, (size_t)(s->ns + 1) * sizeof(int)));
+    TRY(dalloc(s, s->fl_cursor, (size_t)(s->ns + 1) * sizeof(int)));
+    const FirstLightBufs fl{P<float4>(s->fl_val0), P<float2>(s->fl_coef), P<float4>(s->fl_dir), P<float2>(s->fl_g)};
+    const Optics o = optics_of(s);
+    const Rays r = rays_of(b);
+    const long long blocks = (b.nray * 32 + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
+    const int nb = (int)std::min<long long>((nodes + 255) / 256, 152LL * 8);
+    Timer timer(s, K_TRANSPORT);
+    if (W == 1)
+        transport_warp_kernel<1, true><<<(unsigned)blocks, TRANSPORT_THREADS, warp_smem(s->K), s->stream>>>(
+            o, r, in, table, fl, 0, (int)b.nray, P<float4>(s->rad));
+    else
+        transport_warp_kernel<4, true><<<(unsigned)blocks, TRANSPORT_THREADS, warp_smem(s->K), s->stream>>>(
+            o, r, in, table, fl, 0, (int)b.nray, P<float4>(s->rad));
+    TRY(launch_check(s));
+    CK(cudaMemsetAsync(s->fl_cnt.p, 0, (size_t)(s->ns + 1) * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(s->fl_g.p, 0, (size_t)nodes * 2 * W * sizeof(float2), s->stream));
+    pair_bucket_kernel<<<std::max(nb, 1), 256, 0, s->stream>>>(o, table.misc, nodes, P<int>(s->fl_cnt), nullptr,
+                                                               nullptr);
+    TRY(launch_check(s));
+    bucket_scan_kernel<<<1, 1024, 0, s->stream>>>(P<int>(s->fl_cnt), s->ns, P<int>(s->fl_off), P<int>(s->fl_cursor));
+    TRY(launch_check(s));
+    pair_bucket_kernel<<<std::max(nb, 1), 256, 0, s->stream>>>(o, table.misc, nodes, nullptr, P<int>(s->fl_cursor),
+                                                               P<int>(s->fl_entries));
+    TRY(launch_check(s));
+    const int gb = (int)std::min<long long>((2 * nodes + 255) / 256, 152LL * 8);
+    if (W == 1)
+        ground_pairs_kernel<1><<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir, P<int>(s->fl_entries),
+                                                                       P<int>(s->fl_off) + s->ns, fl.g);
+    else
+        ground_pairs_kernel<4><<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir, P<int>(s->fl_entries),
+                                                                       P<int>(s->fl_off) + s->ns, fl.g);
+    TRY(launch_check(s));
+    if (W == 1)
+        first_light_sum_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, 0, s->stream>>>(o, r, in, table, fl, 0,
+                                                                                          (int)b.nray,
+                                                                                          P<float4>(s->rad));
+    else
+        first_light_sum_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, 0, s->stream>>>(o, r, in, table, fl, 0,
+                                                                                          (int)b.nray,
+                                                                                          P<float4>(s->rad));
+    TRY(launch_check(s));
+    b.t_valid = true;
+    done = true;
+    return 0;
+}
+
 // transport of rays [ray0, ray0 + nray) of bundle `b` into s->rad
 static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray, const float* field,
                          const float* boundary, int first, bool query) {
@@ -1227,25 +1498,33 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
     bool read = false;
     TRY(table_for(s, b, in.nq, ray0 == 0 && nray == b.nray, first, write, read));
     const NodeTable table{P<float4>(b.t_frame), P<float4>(b.t_misc), P<float>(b.t_att)};
+    if (first && !query && d.W <= 4 && ray0 == 0 && nray == b.nray && (write.frame || b.t_valid)) {
+        bool done = false;
+        TRY(run_first_light_staged(s, b, in, table, done));
+        if (done) return 0;
+    }
+    const FirstLightBufs no_fl{nullptr, nullptr, nullptr, nullptr};
     if (d.W <= 4) {
         // sample-parallel: one warp per ray
         const long long blocks = (nray * 32 + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
         const size_t smem = warp_smem(s->K);
         Timer timer(s, read ? K_TABLE : K_TRANSPORT);
-        const int slots = table_slots(d.L, d.W);
-        const size_t tsmem = table_smem(s->K, d.L, d.W);
+        // warps per ray from the bundle's mean nodes per ray
+        const double mean_nodes = (double)b.nseg * in.nq / std::max<int64_t>(b.nray, 1);
+        const int wpr = mean_nodes >= 96.0 ? 4 : (mean_nodes >= 48.0 ? 2 : 1);
+        const long long tblocks = (nray * wpr + TRANSPORT_THREADS / 32 - 1) / (TRANSPORT_THREADS / 32);
         if (read && d.W == 1)
-            transport_table_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, tsmem, s->stream>>>(
-                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, slots, P<float4>(s->rad));
+            transport_table_kernel<1><<<(unsigned)tblocks, TRANSPORT_THREADS, smem, s->stream>>>(
+                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, wpr, P<float4>(s->rad));
         else if (read)
-            transport_table_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, tsmem, s->stream>>>(
-                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, slots, P<float4>(s->rad));
+            transport_table_kernel<4><<<(unsigned)tblocks, TRANSPORT_THREADS, smem, s->stream>>>(
+                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, wpr, P<float4>(s->rad));
         else if (d.W == 1)
-            transport_warp_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
-                optics_of(s), rays_of(b), in, write, (int)ray0, (int)nray, P<float4>(s->rad));
+            transport_warp_kernel<1, false><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
+                optics_of(s), rays_of(b), in, write, no_fl, (int)ray0, (int)nray, P<float4>(s->rad));
         else
-            transport_warp_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
-                optics_of(s), rays_of(b), in, write, (int)ray0, (int)nray, P<float4>(s->rad));
+            transport_warp_kernel<4, false><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
+                optics_of(s), rays_of(b), in, write, no_fl, (int)ray0, (int)nray, P<float4>(s->rad));
     } else {
         // many wavelengths: one warp per (ray, chunk of 32 wavelengths), geometry shared through shared memory
         const int wchunks = (d.W + 31) / 32;
@@ -1440,14 +1719,18 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
                 cudaSuccess ||
             cudaFuncSetAttribute(transport_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)wave_smem(d.L)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_warp_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            cudaFuncSetAttribute(transport_warp_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_warp_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            cudaFuncSetAttribute(transport_warp_kernel<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
+            cudaFuncSetAttribute(transport_warp_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
+            cudaFuncSetAttribute(transport_warp_kernel<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
             cudaFuncSetAttribute(transport_table_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)table_smem((d.L + 1) * (d.L + 2) / 2, d.L, d.W)) != cudaSuccess ||
+                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
             cudaFuncSetAttribute(transport_table_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)table_smem((d.L + 1) * (d.L + 2) / 2, d.L, d.W)) != cudaSuccess) {
+                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess) {
             cudaStreamDestroy(s->own);
             delete s;
             return 5;
@@ -1474,7 +1757,8 @@ int sosb_destroy(sosb_handle s) {
                       &s->box_ww, &s->solar, &s->rad, &s->plane, &s->moments, &s->flux, &s->first_moments,
                       &s->first_flux, &s->boundary, &s->metrics, &s->boxes, &s->fx, &s->fg, &s->fn, &s->norms,
                       &s->partials, &s->dots, &s->mixw, &s->ring_g[0], &s->ring_g[1], &s->ring_g[2], &s->ring_g[3],
-                      &s->ring_f[0], &s->ring_f[1], &s->ring_f[2], &s->ring_f[3]};
+                      &s->ring_f[0], &s->ring_f[1], &s->ring_f[2], &s->ring_f[3], &s->fl_val0, &s->fl_coef,
+                      &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off, &s->fl_cursor, &s->fl_entries};
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
@@ -1815,18 +2099,9 @@ static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, 
     }
     TRY(dalloc(s, s->norms, (size_t)s->ns * W * sizeof(float)));
     TRY(dalloc(s, s->mixw, (size_t)(4 * W) * sizeof(float) + 64 * sizeof(int)));
-    const int fthreads = 256;
-    // the feature kernel's grid stride must be a multiple of W (one wavelength per thread)
-    int q_w = W;
-    for (int a = 256, b = W; b;) {
-        const int t = a % b;
-        a = b;
-        b = t;
-        if (!b) q_w = W / a;
-    }
-    // about 16 elements per thread; at most 8 blocks per SM
-    int fblocks = std::max(1, std::min(152 * 8, (int)((n + 256 * 16 - 1) / (256 * 16))));
-    fblocks = std::max(q_w, (fblocks / q_w) * q_w);
+    // feature kernel: blocks of a multiple of W threads (one wavelength per thread), whole cells per block
+    const int fthreads = W * std::max(1, 256 / W);
+    const int fblocks = (int)std::min<long long>(s->ns, 152LL * 4);
     TRY(dalloc(s, s->partials, (size_t)fblocks * 4 * W * sizeof(double)));
     TRY(dalloc(s, s->dots, (size_t)4 * W * sizeof(double)));
     if (x0)
@@ -1903,9 +2178,9 @@ static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, 
         CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
         {
             Timer t(s, K_ANDERSON);
-            norm_kernel<<<grid_for((long long)s->ns * W, 256), 256, 0, s->stream>>>(g, s->ns, s->src, W,
-                                                                                  P<float>(s->norms),
-                                                                                  P<unsigned>(s->metrics));
+            norm_kernel<<<(unsigned)std::min<long long>((s->ns + NORM_WARPS - 1) / NORM_WARPS, 152LL * 16),
+                          NORM_WARPS * 32, 0, s->stream>>>(g, s->ns, s->src, W, P<float>(s->norms),
+                                                           P<unsigned>(s->metrics));
         }
         TRY(launch_check(s));
         const int m = (int)order.size();
@@ -1915,8 +2190,8 @@ static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, 
         const int per = fthreads;
         {
             Timer t(s, K_ANDERSON);
-            feature_kernel<<<fb, per, (size_t)m * W * sizeof(double), s->stream>>>(
-                g, x, P<float>(s->norms), P<unsigned>(s->metrics), s->src, W, (long long)n, P<float>(s->ring_f[slot]),
+            feature_kernel<<<fb, per, (size_t)per * 4 * sizeof(double), s->stream>>>(
+                g, x, P<float>(s->norms), P<unsigned>(s->metrics), (long long)s->ns, s->src, W, P<float>(s->ring_f[slot]),
                 rp[0], rp[1], rp[2], rp[3], m, P<double>(s->partials));
         }
         TRY(launch_check(s));
