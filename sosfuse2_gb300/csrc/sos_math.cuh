@@ -19,6 +19,9 @@
 struct float4 {
     float x, y, z, w;
 };
+struct float2 {
+    float x, y;
+};
 #endif
 
 // Error-free transformations need every add and multiply rounded on its own: no contraction into FMA.
@@ -134,6 +137,8 @@ struct Optics {
     const float* sh_d;     // [L+1] diagonal factors
     const float* strato_lut;  // [STRATO_LUT_BINS + 1][W] stratospheric phase per sr on a uniform grid of u in [-1, 1]
     const uint8_t* gsame;  // [ns] 1 when cell c + 1 (same height, next solar zenith) has c's ground directions, or null
+    const float2* strato_lut2;  // [STRATO_LUT_BINS][W] (value, next value - value) of strato_lut, or null
+    const float4* gdir4;        // [*] gdir padded to 16 bytes, or null
 };
 
 constexpr int STRATO_LUT_BINS = 4096;
@@ -520,8 +525,20 @@ SOS_HD void strato_lut_pos(float u, int& i, float& f) {
 }
 
 SOS_HD float strato_lut_at(const Optics& o, int i, float f, int w) {
+    if (o.strato_lut2) {
+        const float2 p = o.strato_lut2[(size_t)i * o.W + w];
+        return p.x + f * p.y;
+    }
     const float a = o.strato_lut[(size_t)i * o.W + w], b = o.strato_lut[(size_t)(i + 1) * o.W + w];
     return a + f * (b - a);
+}
+
+// strato_lut_pos for u already in [-1, 1].
+SOS_HD void strato_lut_pos_clamped(float u, int& i, float& f) {
+    const float x = (u + 1.0f) * (0.5f * STRATO_LUT_BINS);
+    i = (int)x;
+    i = i > STRATO_LUT_BINS - 1 ? STRATO_LUT_BINS - 1 : i;
+    f = x - (float)i;
 }
 
 // Light from the lit ground scattered at the node, wavelengths w0 .. w0 + nw - 1 (nw <= NW): for every ground

@@ -68,7 +68,7 @@ struct sosb_state {
     bool have_constants = false;
     // constants
     DevBuf h, chi, hr, ha, ext, asca, table, sun_h, sun_col, gm, goff, gdir, gval, rf, af, ext0;
-    DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src, s_lut, gsame;
+    DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src, s_lut, s_lut2, gsame, gdir4;
     DevBuf sh_a, sh_b, sh_d;
     DevBuf u_hi, u_lo, wu_hi, wu_lo, uq_hi, uq_lo, wuq_hi, wuq_lo, box_ww, solar;
     BundleDev cells, obs;
@@ -676,17 +676,18 @@ __global__ void __launch_bounds__(256)
             const float wc = side ? wb : wa;
             const int g0 = o.goff[cell], g1 = o.goff[cell + 1];
             const int shift = merged ? o.goff[cb] - g0 : 0;
+#pragma unroll 2
             for (int gi = g0; gi < g1; ++gi) {
-                const float* gd = o.gdir + 3 * gi;
-                const float m0 = dv.x * gd[2] + dv.y * gd[0];
-                const float m1 = dv.z * gd[1];
+                const float4 gd = o.gdir4[gi];
+                const float m0 = dv.x * gd.z + dv.y * gd.x;
+                const float m1 = dv.z * gd.y;
                 const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
                 const float ph = hg_pair(hk, up, dn);
                 int iu = 0, id = 0;
                 float fu = 0.0f, fd = 0.0f;
                 if (o.strato) {
-                    strato_lut_pos(up, iu, fu);
-                    strato_lut_pos(dn, id, fd);
+                    strato_lut_pos_clamped(up, iu, fu);
+                    strato_lut_pos_clamped(dn, id, fd);
                 }
 #pragma unroll
                 for (int w = 0; w < WM; ++w) {
@@ -763,10 +764,11 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
 
 // Warm pass from the node table, few wavelengths (W <= WM): `wpr` warps (1, 2 or 4) per ray, lane l of warp q takes
 // nodes 32 q + l, 32 (q + wpr) + l, ... with its own Kahan sums; the warps' sums are added in warp order. Each node's
-// corner SH is synthesised from the ray's basis. (Contracting runs of equal corner cells once per warp instead
-// measured slower on GB300: the per-batch ballots and the scattered (run, m) sums cost more than the direct
-// synthesis.) Several warps per ray serve bundles of long rays (observer rays) that would otherwise leave most SMs
-// idle.
+// corner SH is synthesised from the ray's basis (sh_synth4). Several warps per ray serve bundles of long rays
+// (observer rays) that would otherwise leave most SMs idle. (Contracting each distinct corner cell of a batch once,
+// per-m sums in shared memory, measured 1.5-3x slower on GB300 in two forms: the per-batch ballots, deduplication
+// and serial per-cell sums leave the warp latency-bound, while the direct synthesis keeps 32 lanes x 4 independent
+// chains in flight.)
 template <int WM>
 __global__ void __launch_bounds__(TRANSPORT_THREADS)
     transport_table_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int wpr,
@@ -1214,20 +1216,29 @@ __global__ void feature_kernel(const float* __restrict__ g, const float* __restr
     }
     for (int j = 0; j < 4; ++j) sd[t * 4 + j] = loc[j];
     __syncthreads();
+    // thread t is member t / W of its wavelength's group of G = B / W; pairwise tree over the members
+    const int G = B / W, mem = t / W;
+    for (int h = 1; h < G; h <<= 1) {
+        if ((mem & (2 * h - 1)) == 0 && mem + h < G)
+            for (int j = 0; j < 4; ++j) sd[t * 4 + j] += sd[(t + h * W) * 4 + j];
+        __syncthreads();
+    }
     for (int q = t; q < nslot * W; q += B) {
         const int j = q / W, ww = q % W;
-        double acc = 0.0;
-        for (int u = ww; u < B; u += W) acc += sd[u * 4 + j];
-        partials[(size_t)blockIdx.x * nslot * W + q] = acc;
+        partials[(size_t)blockIdx.x * nslot * W + q] = sd[ww * 4 + j];
     }
 }
 
+// out[i] = sum over blocks of partials[block][i]: one warp per output, lanes over blocks, lane sums added by a fixed
+// shuffle tree (reproducible).
 __global__ void sum_partials_kernel(const double* __restrict__ partials, int blocks, int n, double* out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double s = 0.0;
-    for (int b = 0; b < blocks; ++b) s += partials[(size_t)b * n + i];
-    out[i] = s;
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;  // the whole warp leaves together
+    double acc = 0.0;
+    for (int b = lane; b < blocks; b += 32) acc += partials[(size_t)b * n + i];
+    for (int dd = 16; dd >= 1; dd >>= 1) acc += __shfl_xor_sync(FULL_MASK, acc, dd);
+    if (lane == 0) out[i] = acc;
 }
 
 // nxt[i] = sum_j c[j][w] ring_g[order j][i] for wavelengths with valid weights, else g[i].
@@ -1293,6 +1304,8 @@ static Optics optics_of(const sosb_state* s) {
     o.sh_d = P<float>(s->sh_d);
     o.strato_lut = P<float>(s->s_lut);
     o.gsame = P<uint8_t>(s->gsame);
+    o.strato_lut2 = P<float2>(s->s_lut2);
+    o.gdir4 = P<float4>(s->gdir4);
     return o;
 }
 
@@ -1448,7 +1461,7 @@ static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs&
     pair_bucket_kernel<<<std::max(nb, 1), 256, 0, s->stream>>>(o, table.misc, nodes, nullptr, P<int>(s->fl_cursor),
                                                                P<int>(s->fl_entries));
     TRY(launch_check(s));
-    const int gb = (int)std::min<long long>((2 * nodes + 255) / 256, 152LL * 8);
+    const int gb = (int)((2 * nodes + 255) / 256);  // one pair per thread at most
     if (W == 1)
         ground_pairs_kernel<1><<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir, P<int>(s->fl_entries),
                                                                        P<int>(s->fl_off) + s->ns, fl.g);
@@ -1752,7 +1765,7 @@ int sosb_destroy(sosb_handle s) {
     cudaStreamSynchronize(s->stream);
     DevBuf* bufs[] = {&s->h, &s->chi, &s->hr, &s->ha, &s->ext, &s->asca, &s->table, &s->sun_h, &s->sun_col, &s->gm,
                       &s->goff, &s->gdir, &s->gval, &s->rf, &s->af, &s->ext0, &s->s_ext, &s->s_sca, &s->s_chi,
-                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->s_lut, &s->gsame, &s->sh_a, &s->sh_b, &s->sh_d,
+                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->s_lut, &s->s_lut2, &s->gsame, &s->gdir4, &s->sh_a, &s->sh_b, &s->sh_d,
                       &s->u_hi, &s->u_lo, &s->wu_hi, &s->wu_lo, &s->uq_hi, &s->uq_lo, &s->wuq_hi, &s->wuq_lo,
                       &s->box_ww, &s->solar, &s->rad, &s->plane, &s->moments, &s->flux, &s->first_moments,
                       &s->first_flux, &s->boundary, &s->metrics, &s->boxes, &s->fx, &s->fg, &s->fn, &s->norms,
@@ -1855,9 +1868,13 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
     if (ng > 0) {
         if (!c->gdir || !c->gval) return fail(s, "E_CONSTANTS: missing ground directions");
         TRY(dput(s, s->gdir, c->gdir, (size_t)ng * 3 * 4));
+        std::vector<float4> g4(ng);
+        for (int i = 0; i < ng; ++i) g4[i] = make_float4(c->gdir[3 * i], c->gdir[3 * i + 1], c->gdir[3 * i + 2], 0.0f);
+        TRY(dput_vec(s, s->gdir4, g4));
         TRY(dput(s, s->gval, c->gval, (size_t)ng * W * 4));
     } else {
         TRY(dalloc(s, s->gdir, 16));
+        TRY(dalloc(s, s->gdir4, 16));
         TRY(dalloc(s, s->gval, 16));
     }
     {
@@ -1902,6 +1919,10 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
             }
         }
         TRY(dput_vec(s, s->s_lut, lut));
+        std::vector<float2> lut2((size_t)STRATO_LUT_BINS * W);
+        for (size_t i = 0; i < (size_t)STRATO_LUT_BINS * W; ++i)
+            lut2[i] = make_float2(lut[i], lut[i + W] - lut[i]);
+        TRY(dput_vec(s, s->s_lut2, lut2));
     }
     CK(cudaStreamSynchronize(s->stream));
     s->have_constants = true;
@@ -2197,8 +2218,8 @@ static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, 
         TRY(launch_check(s));
         {
             Timer t(s, K_ANDERSON);
-            sum_partials_kernel<<<(m * W + 127) / 128, 128, 0, s->stream>>>(P<double>(s->partials), fb, m * W,
-                                                                             P<double>(s->dots));
+            sum_partials_kernel<<<(m * W * 32 + 127) / 128, 128, 0, s->stream>>>(P<double>(s->partials), fb, m * W,
+                                                                                  P<double>(s->dots));
         }
         TRY(launch_check(s));
         CK(cudaMemcpyAsync(dots.data(), s->dots.p, (size_t)m * W * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
