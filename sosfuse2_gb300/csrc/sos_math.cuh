@@ -482,7 +482,8 @@ SOS_HD void kahan(float& total, float& comp, float value) {
 // Everything one lane needs that is shared by all rays of a launch.
 struct LaneInputs {
     const float* field;     // [ns][src][W] current source
-    const float* plane;     // [ns][K][W] aerosol (+ stratospheric) SH plane, already scaled by the cell density
+    const float* plane;     // aerosol (+ stratospheric) SH plane, already scaled by the cell density: [ns][K][W]
+                            // (kp = 0), or [ns][W][kp] rows padded to kp = K rounded up to 4 (few wavelengths)
     const float* boundary;  // [nc][W] ground flux at the surface nodes, or null
     const float* u_hi;      // quadrature nodes on [0, 1] and weights, double-single
     const float* u_lo;
@@ -490,6 +491,7 @@ struct LaneInputs {
     const float* wu_lo;
     int nq;
     int first;
+    int kp;
 };
 
 // Henyey-Greenstein phase (per sr) of the pair of scattering cosines (up, dn), averaged:
@@ -764,6 +766,58 @@ SOS_HD void sh_synth4(int L, const float* Y, float cp, const float* const pc[4],
         out[3] += cm * s3;
     }
 }
+
+// m of SH index k = l (l + 1) / 2 + m.
+SOS_HD constexpr int sh_m_of(int k) {
+    int l = 0;
+    while ((l + 1) * (l + 2) / 2 <= k) ++l;
+    return k - l * (l + 1) / 2;
+}
+
+#if defined(__CUDACC__)
+// acc[m] += Y[k] plane[k] over k = 4 V .. 4 V + 3 (< K), V = 0 .. ceil(K / 4) - 1: 16-byte loads of the basis and of
+// one plane row, per-m sums in registers (k ascending, so each m sums its l in ascending order, as sh_synth4 does).
+template <int L, int V>
+struct ShStep {
+    static __device__ __forceinline__ void run(const float4* y4, const float4* p4, float* acc) {
+        constexpr int K = (L + 1) * (L + 2) / 2;
+        const float4 y = y4[V];
+        const float4 p = p4[V];
+        if constexpr (4 * V + 0 < K) acc[sh_m_of(4 * V + 0)] += y.x * p.x;
+        if constexpr (4 * V + 1 < K) acc[sh_m_of(4 * V + 1)] += y.y * p.y;
+        if constexpr (4 * V + 2 < K) acc[sh_m_of(4 * V + 2)] += y.z * p.z;
+        if constexpr (4 * V + 3 < K) acc[sh_m_of(4 * V + 3)] += y.w * p.w;
+        // keep at most 8 loads of each operand in flight (registers), not the whole row
+        if constexpr (V % 8 == 7) asm volatile("" ::: "memory");
+        if constexpr (V + 1 < (K + 3) / 4) ShStep<L, V + 1>::run(y4, p4, acc);
+    }
+};
+
+// sh_synth4 for a compile-time order L with 16-byte aligned basis and plane rows (padded to a multiple of 4).
+template <int L>
+__device__ __forceinline__ void sh_synth4_fixed(const float* Y, float cp, const float* const pc[4], float out[4]) {
+    cp = clampf(cp, -1.0f, 1.0f);
+    const float4* y4 = reinterpret_cast<const float4*>(Y);
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        float acc[L + 1];
+#pragma unroll
+        for (int m = 0; m <= L; ++m) acc[m] = 0.0f;
+        ShStep<L, 0>::run(y4, reinterpret_cast<const float4*>(pc[c]), acc);
+        float c0 = 1.0f, c1 = cp;
+        float s = acc[0];
+        s += cp * acc[1];
+#pragma unroll
+        for (int m = 2; m <= L; ++m) {
+            const float c2 = (2.0f * cp) * c1 - c0;
+            s += c2 * acc[m];
+            c0 = c1;
+            c1 = c2;
+        }
+        out[c] = s;
+    }
+}
+#endif
 
 // Per-m sums of one cell from a shared basis (the cached form of sh_synth4).
 SOS_HD void sh_contract_basis(int L, const float* Y, const float* plane_cell, int wstride, float* cache, int cstride) {

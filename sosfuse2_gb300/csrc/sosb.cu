@@ -185,7 +185,8 @@ struct FirstLightBufs {
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
-static size_t warp_smem(int K) { return sizeof(float) * (size_t)K * (TRANSPORT_THREADS / 32); }
+// basis rows of the warps of a block, each padded to kp = K rounded up to 4
+static size_t warp_smem(int K) { return sizeof(float) * (size_t)((K + 3) & ~3) * (TRANSPORT_THREADS / 32); }
 
 SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }
 
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
     const int nsamp = (s1 - s0) * nq;
     const float phase = hg_phase(rc.d32[2], o.g);
     extern __shared__ float warp_sm[];
-    float* Y = warp_sm + (threadIdx.x >> 5) * o.K;  // this ray's SH basis, shared by the warp
+    float* Y = warp_sm + (threadIdx.x >> 5) * in.kp;  // this ray's SH basis, shared by the warp
     if (!first) {
         for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
         __syncwarp();
@@ -341,8 +342,8 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
                 } else {
                     float aero[4];
                     const float* pc[4];
-                    for (int c = 0; c < 4; ++c) pc[c] = in.plane + (size_t)n.cell[c] * o.K * W + w;
-                    sh_synth4(o.L, Y, n.cp, pc, W, aero);
+                    for (int c = 0; c < 4; ++c) pc[c] = in.plane + ((size_t)n.cell[c] * W + w) * in.kp;
+                    sh_synth4(o.L, Y, n.cp, pc, 1, aero);
                     warm_value(o, rc, n, in.field, w, aero, val);
                 }
                 for (int k = 0; k < 4; ++k) kahan(tot[w][k], cmp[w][k], val[k] * att);
@@ -764,12 +765,13 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
 
 // Warm pass from the node table, few wavelengths (W <= WM): `wpr` warps (1, 2 or 4) per ray, lane l of warp q takes
 // nodes 32 q + l, 32 (q + wpr) + l, ... with its own Kahan sums; the warps' sums are added in warp order. Each node's
-// corner SH is synthesised from the ray's basis (sh_synth4). Several warps per ray serve bundles of long rays
+// corner SH is synthesised from the ray's basis (sh_synth4; for L = 16 and 32, sh_synth4_fixed with 16-byte loads).
+// Several warps per ray serve bundles of long rays
 // (observer rays) that would otherwise leave most SMs idle. (Contracting each distinct corner cell of a batch once,
 // per-m sums in shared memory, measured 1.5-3x slower on GB300 in two forms: the per-batch ballots, deduplication
 // and serial per-cell sums leave the warp latency-bound, while the direct synthesis keeps 32 lanes x 4 independent
 // chains in flight.)
-template <int WM>
+template <int WM, int LT>
 __global__ void __launch_bounds__(TRANSPORT_THREADS)
     transport_table_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int wpr,
                            float4* rad) {
@@ -791,7 +793,7 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
         const long long node0 = (long long)s0 * nq;
         const int nn = (b.seg_off[ray + 1] - s0) * nq;
         extern __shared__ float warp_sm[];
-        float* Y = warp_sm + wid * o.K;
+        float* Y = warp_sm + wid * in.kp;
         for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
         __syncwarp();
         float tot[WM][4], cmp[WM][4];
@@ -808,8 +810,11 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
                 const float att = tab.att[id * W + w];
                 float aero[4];
                 const float* pc[4];
-                for (int c = 0; c < 4; ++c) pc[c] = in.plane + (size_t)n.cell[c] * o.K * W + w;
-                sh_synth4(o.L, Y, n.cp, pc, W, aero);
+                for (int c = 0; c < 4; ++c) pc[c] = in.plane + ((size_t)n.cell[c] * W + w) * in.kp;
+                if constexpr (LT > 0)
+                    sh_synth4_fixed<LT>(Y, n.cp, pc, aero);
+                else
+                    sh_synth4(o.L, Y, n.cp, pc, 1, aero);
                 float val[4];
                 warm_value(o, rc, n, in.field, w, aero, val);
                 for (int k = 0; k < 4; ++k) kahan(tot[w][k], cmp[w][k], val[k] * att);
@@ -951,14 +956,28 @@ static size_t table_wave_smem(int L) {
     return sizeof(float) * (size_t)WAVE_WARPS * (32 * TREC_WORDS + 4 * (L + 1) * 32 + (L + 1) * (L + 2) / 2);
 }
 
+// plane = SH slots x cell density (+ stratospheric slots x their density): [cell][k][w] (kp = 0), or
+// [cell][w][kp] with zero padding k = K .. kp - 1 (few wavelengths: 16-byte aligned rows for sh_synth4_fixed).
 __global__ void plane_kernel(const float* __restrict__ field, const float* __restrict__ ha,
-                             const float* __restrict__ sd, int nc, int K, int src, int W, int strato, long long n,
-                             float* __restrict__ plane) {
+                             const float* __restrict__ sd, int nc, int K, int src, int W, int strato, int kp,
+                             long long n, float* __restrict__ plane) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int w = (int)(i % W);
-        const long long r = i / W;
-        const int k = (int)(r % K);
-        const int cell = (int)(r / K);
+        int w, k, cell;
+        if (kp) {
+            k = (int)(i % kp);
+            const long long r = i / kp;
+            w = (int)(r % W);
+            cell = (int)(r / W);
+            if (k >= K) {
+                plane[i] = 0.0f;
+                continue;
+            }
+        } else {
+            w = (int)(i % W);
+            const long long r = i / W;
+            k = (int)(r % K);
+            cell = (int)(r / K);
+        }
         const int hi = cell / nc;
         const float* f = field + (size_t)cell * src * W + w;
         float v = f[(size_t)(10 + k) * W] * ha[hi];
@@ -1410,6 +1429,18 @@ static int table_for(sosb_state* s, BundleDev& b, int nq, bool whole, int first,
     return 0;
 }
 
+using TableKernel = void (*)(Optics, Rays, LaneInputs, NodeTable, int, int, int, float4*);
+
+// The table kernel instance for (W, L): one wavelength or up to four, the order unrolled for L = 16 and 32.
+static TableKernel table_kernel_for(int W, int L) {
+    if (W == 1) return L == 16 ? transport_table_kernel<1, 16> : (L == 32 ? transport_table_kernel<1, 32>
+                                                                          : transport_table_kernel<1, 0>);
+    return L == 16 ? transport_table_kernel<4, 16> : (L == 32 ? transport_table_kernel<4, 32> : transport_table_kernel<4, 0>);
+}
+
+// Row length of the padded plane layout (W <= 4), 0 for the wavelength-fastest layout of the wave kernels.
+static int plane_kp(const sosb_state* s) { return s->d.W <= 4 ? (s->K + 3) & ~3 : 0; }
+
 static void invalidate_tables(BundleDev& b) {
     b.t_valid = false;
     b.t_too_big = false;
@@ -1492,6 +1523,7 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
     LaneInputs in{};
     in.field = field;
     in.plane = P<float>(s->plane);
+    in.kp = plane_kp(s);
     in.boundary = boundary;
     in.first = first;
     if (query) {
@@ -1526,13 +1558,12 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
         const double mean_nodes = (double)b.nseg * in.nq / std::max<int64_t>(b.nray, 1);
         const int wpr = mean_nodes >= 96.0 ? 4 : (mean_nodes >= 48.0 ? 2 : 1);
         const long long tblocks = (nray * wpr + TRANSPORT_THREADS / 32 - 1) / (TRANSPORT_THREADS / 32);
-        if (read && d.W == 1)
-            transport_table_kernel<1><<<(unsigned)tblocks, TRANSPORT_THREADS, smem, s->stream>>>(
-                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, wpr, P<float4>(s->rad));
-        else if (read)
-            transport_table_kernel<4><<<(unsigned)tblocks, TRANSPORT_THREADS, smem, s->stream>>>(
-                optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, wpr, P<float4>(s->rad));
-        else if (d.W == 1)
+        if (read) {
+            auto kernel = table_kernel_for(d.W, d.L);
+            kernel<<<(unsigned)tblocks, TRANSPORT_THREADS, smem, s->stream>>>(optics_of(s), rays_of(b), in, table,
+                                                                             (int)ray0, (int)nray, wpr,
+                                                                             P<float4>(s->rad));
+        } else if (d.W == 1)
             transport_warp_kernel<1, false><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
                 optics_of(s), rays_of(b), in, write, no_fl, (int)ray0, (int)nray, P<float4>(s->rad));
         else
@@ -1576,11 +1607,12 @@ static int run_project(sosb_state* s, const BundleDev& b, int ncell, bool ground
 
 static int run_plane(sosb_state* s, const float* field) {
     const sosb_dims& d = s->d;
-    const long long n = (long long)s->ns * s->K * d.W;
+    const int kp = plane_kp(s);
+    const long long n = (long long)s->ns * (kp ? kp : s->K) * d.W;
     TRY(dalloc(s, s->plane, n * sizeof(float)));
     Timer timer(s, K_PLANE);
     plane_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(field, P<float>(s->ha), P<float>(s->s_density), d.nc, s->K,
-                                                          s->src, d.W, d.strato, n, P<float>(s->plane));
+                                                          s->src, d.W, d.strato, kp, n, P<float>(s->plane));
     return launch_check(s);
 }
 
@@ -1739,10 +1771,6 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
             cudaFuncSetAttribute(transport_warp_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
             cudaFuncSetAttribute(transport_warp_kernel<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_table_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_table_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess) {
             cudaStreamDestroy(s->own);
             delete s;
