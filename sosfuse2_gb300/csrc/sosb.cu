@@ -766,11 +766,10 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
 // Warm pass from the node table, few wavelengths (W <= WM): `wpr` warps (1, 2 or 4) per ray, lane l of warp q takes
 // nodes 32 q + l, 32 (q + wpr) + l, ... with its own Kahan sums; the warps' sums are added in warp order. Each node's
 // corner SH is synthesised from the ray's basis (sh_synth4; for L = 16 and 32, sh_synth4_fixed with 16-byte loads).
-// Several warps per ray serve bundles of long rays
-// (observer rays) that would otherwise leave most SMs idle. (Contracting each distinct corner cell of a batch once,
-// per-m sums in shared memory, measured 1.5-3x slower on GB300 in two forms: the per-batch ballots, deduplication
-// and serial per-cell sums leave the warp latency-bound, while the direct synthesis keeps 32 lanes x 4 independent
-// chains in flight.)
+// Several warps per ray serve bundles of long rays (observer rays) that would otherwise leave most SMs idle.
+// Contracting each distinct corner cell of a batch once
+// (per-m sums in shared memory) measured slower on the config-0 warm pass in three forms (0.30-1.3 ms against
+// 0.24 ms): the per-batch ballots, deduplication and synchronisation cost more than the 16-byte row loads they save.
 template <int WM, int LT>
 __global__ void __launch_bounds__(TRANSPORT_THREADS)
     transport_table_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int wpr,
