@@ -9,7 +9,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / 'csrc'
 OUT = PKG / '_lib' / 'libsosb.so'
 SOURCES = [CSRC / 'sosb.cu', CSRC / 'tc_gemm.cu']
-HEADERS = [CSRC / 'sos_math.cuh', CSRC / 'sos_pack.h', PKG.parent / 'include' / 'sosb.h']
+HEADERS = [CSRC / 'sos_math.cuh', CSRC / 'sos_pack.h', CSRC / 'tc_ptx.cuh', PKG.parent / 'include' / 'sosb.h']
 
 NVCC_FLAGS = [
     '-gencode', 'arch=compute_103a,code=sm_103a',

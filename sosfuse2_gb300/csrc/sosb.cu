@@ -9,6 +9,7 @@
 //   norm/feature/dot/mix kernels  Anderson depth-4 residual features, Gram columns (FP64) and the mixing
 // The fixed-point loop (sosb_solve) runs on the host thread over device-resident buffers; per evaluation it reads
 // back only per-wavelength scalars (metrics, box values, Gram columns).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +27,7 @@
 #include "sos_math.cuh"
 #include "sos_pack.h"
 #include "../../include/sosb.h"
+#include "tc_ptx.cuh"
 
 using namespace sos;
 
@@ -45,6 +47,9 @@ struct BundleDev {
     // node table (NodeTable): valid once a launch over the whole bundle wrote it; too_big: over the memory budget
     DevBuf t_frame, t_misc, t_att;
     bool t_valid = false, t_too_big = false;
+    // basis table of the tensor-core projection (BasisTable), built for projection mode b_mode (-1: none)
+    DevBuf b_hi, b_lo;
+    int b_mode = -1, b_kpad = 0, b_rpad = 0;
 };
 
 // kernel classes timed by sosb_set_timing / sosb_get_timing
@@ -79,6 +84,7 @@ struct sosb_state {
     DevBuf fl_val0, fl_coef, fl_dir, fl_g, fl_cnt, fl_off, fl_cursor, fl_entries;  // staged first light
     bool have_first = false;
     bool tables = true;  // build and use node tables (sosb_set_node_tables)
+    int proj_mode = 0;   // projection form (sosb_set_projection): PROJ_FP32, PROJ_BF16X3, PROJ_TF32, PROJ_BF16
     int64_t launches = 0;
 };
 
@@ -996,13 +1002,14 @@ static size_t project_smem(int K, int W) { return sizeof(float) * (size_t)PROJ_R
 // (numpy_reference.py:689-711: moments[0:4] = sum wt rad, moments[4+k] = sum (wt trace) (Y_k cos m phi),
 // flux = sum trace wt max(0, dloc_z) * albedo / pi).
 __global__ void __launch_bounds__(PROJ_THREADS)
-    project_kernel(Optics o, Rays b, const float4* __restrict__ rad, int cell0, int ground_only, int out_base,
-                   float* __restrict__ moments, float* __restrict__ flux, float flux_scale) {
+    project_kernel(Optics o, Rays b, const float4* __restrict__ rad, int cell0, int ground_only, int rayleigh_only,
+                   int out_base, float* __restrict__ moments, float* __restrict__ flux, float flux_scale) {
     extern __shared__ float sm[];
     const int W = o.W, K = o.K, L = o.L;
     const int cell = cell0 + blockIdx.x;
     const int r0 = b.cell_off[cell], r1 = b.cell_off[cell + 1];
     const int nout = (4 + K) * W;
+    const int nown = rayleigh_only ? 4 * W : nout;  // outputs this launch computes (the SH rows elsewhere)
     float* basis = sm;                    // [PROJ_RAYS][K]
     float* wtr = basis + PROJ_RAYS * K;   // [PROJ_RAYS][W]  weight * trace
     float* wr = wtr + PROJ_RAYS * W;      // [PROJ_RAYS][4][W] weight * radiance
@@ -1015,7 +1022,7 @@ __global__ void __launch_bounds__(PROJ_THREADS)
     for (int rb = r0; rb < r1; rb += PROJ_RAYS) {
         const int nr = min(PROJ_RAYS, r1 - rb);
         __syncthreads();
-        if (!ground_only) {
+        if (!ground_only && !rayleigh_only) {
             for (int it = threadIdx.x; it < nr * (L + 1); it += blockDim.x) {
                 const int r = it / (L + 1), m = it % (L + 1);
                 const int ray = rb + r;
@@ -1067,7 +1074,7 @@ __global__ void __launch_bounds__(PROJ_THREADS)
 #pragma unroll
             for (int i = 0; i < PROJ_OWN; ++i) {
                 const int oi = out_base + threadIdx.x + i * PROJ_THREADS;
-                if (oi < nout) {
+                if (oi < nown) {
                     const int slot = oi / W, w = oi % W;
                     float part = 0.0f;
                     if (slot < 4) {
@@ -1090,10 +1097,198 @@ __global__ void __launch_bounds__(PROJ_THREADS)
 #pragma unroll
         for (int i = 0; i < PROJ_OWN; ++i) {
             const int oi = out_base + threadIdx.x + i * PROJ_THREADS;
-            if (oi < nout) moments[(size_t)cell * nout + oi] = acc[i];
+            if (oi < nown) moments[(size_t)cell * nout + oi] = acc[i];
         }
     }
     if (do_flux) flux[(size_t)cell * W + threadIdx.x] = facc * flux_scale;
+}
+
+// ------------------------------------------------------------------ tensor-core projection
+// The SH rows of the projection as a dense contraction per cell: moments[4 + k][w] = sum_r B[k][r] V[r][w] with
+// B[k][r] = Y_k(mu_r) cos(m phi_r) (geometry only, a table built once per cell bundle) and V[r][w] = weight_r x
+// trace_r,w (from the radiance). One CTA per (cell, 128 rows of k): the tile of B (128 rows x one 128-byte chunk of
+// rays) and of V^T (N = W rounded up to 16 rows) are written to shared memory in the 128-byte swizzle, one thread
+// issues tcgen05.mma into an FP32 accumulator in tensor memory, the four warps read it back. Precision forms:
+// BF16 (one product), TF32 (kind::tf32), bf16x3 (B = Bh + Bl, V = Vh + Vl; Bh Vh + Bh Vl + Bl Vh).
+enum { PROJ_FP32 = 0, PROJ_BF16X3 = 1, PROJ_TF32 = 2, PROJ_BF16 = 3 };
+
+__device__ unsigned g_proj_error;  // bounded-wait flags of the tensor-core projection
+
+struct BasisTable {
+    void* hi;  // [cells][kpad][rpad]: BF16 (BF16, bf16x3) or FP32 (TF32)
+    void* lo;  // bf16x3: BF16 of (basis - hi)
+    int kpad, rpad;
+};
+
+// One thread per (ray, m): column m of the ray's basis row (the FP32 recurrences of project_kernel), stored at
+// [cell][k][ray - first ray of the cell].
+template <int MODE>
+__global__ void basis_table_kernel(Optics o, Rays b, BasisTable bt) {
+    const int L = o.L;
+    const long long n = (long long)b.nray * (L + 1);
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < n;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int ray = (int)(it / (L + 1)), m = (int)(it % (L + 1));
+        const int cell = b.ray_cell[ray];
+        const int j = ray - b.cell_off[cell];
+        const float4 dv = b.dir[ray];
+        const float mu = dv.z, st = dv.w;
+        const float cp = clampf(b.pcp[ray], -1.0f, 1.0f);
+        float c0 = 1.0f, c1 = cp, cm = 1.0f;
+        if (m == 1) cm = cp;
+        for (int q = 2; q <= m; ++q) {
+            const float c2 = (2.0f * cp) * c1 - c0;
+            c0 = c1;
+            c1 = c2;
+            cm = c2;
+        }
+        float pmm = 0.28209479177387814f;
+        for (int q = 1; q <= m; ++q) pmm = (pmm * o.sh_d[q]) * st;
+        const float scale = m ? 1.41421356237309515f : 1.0f;
+        const size_t base = (size_t)cell * bt.kpad * bt.rpad + j;
+        auto put = [&](int k, float v) {
+            const size_t at = base + (size_t)k * bt.rpad;
+            if (MODE == PROJ_TF32) {
+                static_cast<float*>(bt.hi)[at] = v;
+            } else {
+                const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                static_cast<__nv_bfloat16*>(bt.hi)[at] = h;
+                if (MODE == PROJ_BF16X3) static_cast<__nv_bfloat16*>(bt.lo)[at] = __float2bfloat16_rn(v - __bfloat162float(h));
+            }
+        };
+        float p0 = pmm;
+        put(m * (m + 1) / 2 + m, (scale * p0) * cm);
+        if (m < L) {
+            float p1 = (sqrtf(2.0f * m + 3.0f) * mu) * p0;
+            put((m + 1) * (m + 2) / 2 + m, (scale * p1) * cm);
+            for (int l = m + 2; l <= L; ++l) {
+                const int k = l * (l + 1) / 2 + m;
+                const float p2 = (o.sh_a[k] * mu) * p1 - o.sh_b[k] * p0;
+                put(k, (scale * p2) * cm);
+                p0 = p1;
+                p1 = p2;
+            }
+        }
+    }
+}
+
+static size_t project_tc_smem(int mode, int np) {
+    const int na = mode == PROJ_BF16X3 ? 2 : 1;
+    return 1024 + (size_t)na * 16384 + (size_t)na * np * 128 + 64;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128)
+    project_tc_kernel(BasisTable bt, Rays b, const float4* __restrict__ rad, int W, int K, int np, uint32_t idesc,
+                      uint32_t tmem_cols, float* __restrict__ moments) {
+    constexpr int ESZ = MODE == PROJ_TF32 ? 4 : 2;  // operand bytes
+    constexpr int CH = 128 / ESZ;                   // rays per 128-byte chunk
+    constexpr int NT = MODE == PROJ_BF16X3 ? 2 : 1; // operand tiles (high, low parts)
+    extern __shared__ uint8_t proj_raw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(proj_raw) + 1023) & ~(uintptr_t)1023);
+    uint8_t* at0 = sm;
+    uint8_t* at1 = sm + 16384;
+    uint8_t* vt0 = sm + NT * 16384;
+    uint8_t* vt1 = vt0 + np * 128;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(vt0 + NT * np * 128);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int cell = blockIdx.y, mt = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r0 = b.cell_off[cell], nr = b.cell_off[cell + 1] - r0;
+    if (threadIdx.x == 0) {
+        tcx::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tcx::tmem_alloc(tslot, tmem_cols);
+    tcx::fence_before();
+    __syncthreads();
+    tcx::fence_after();
+    const uint32_t tmem = *tslot;
+    const int nchunk = (nr + CH - 1) / CH;
+    bool ok = true;
+    for (int ch = 0; ch < nchunk && ok; ++ch) {
+        for (int pc = threadIdx.x; pc < 128 * 8; pc += 128) {  // basis tile: 128 rows x 8 pieces of 16 bytes
+            const int row = pc >> 3, piece = pc & 7;
+            const size_t src =
+                ((((size_t)cell * bt.kpad + mt * 128 + row) * bt.rpad) + (size_t)ch * CH) * ESZ + piece * 16;
+            *reinterpret_cast<uint4*>(at0 + tcx::sw128_offset(row, piece)) =
+                *reinterpret_cast<const uint4*>(static_cast<const uint8_t*>(bt.hi) + src);
+            if (NT == 2)
+                *reinterpret_cast<uint4*>(at1 + tcx::sw128_offset(row, piece)) =
+                    *reinterpret_cast<const uint4*>(static_cast<const uint8_t*>(bt.lo) + src);
+        }
+        for (int pc = threadIdx.x; pc < np * 8; pc += 128) {  // V^T tile: np rows (wavelengths) x 8 pieces
+            const int w = pc >> 3, piece = pc & 7;
+            constexpr int PER = 16 / ESZ;
+            float v[PER];
+#pragma unroll
+            for (int e = 0; e < PER; ++e) {
+                const int j = ch * CH + piece * PER + e;
+                v[e] = 0.0f;
+                if (w < W && j < nr) {
+                    const int ray = r0 + j;
+                    const float4 q = rad[(size_t)ray * W + w];
+                    v[e] = ((q.x + q.y) + q.z) * b.dir_lo[ray].w;
+                }
+            }
+            if (MODE == PROJ_TF32) {
+                *reinterpret_cast<float4*>(vt0 + tcx::sw128_offset(w, piece)) = make_float4(v[0], v[1], v[2], v[3]);
+            } else {
+                __align__(16) __nv_bfloat16 h[8], l[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    h[e] = __float2bfloat16_rn(v[e % PER]);
+                    l[e] = __float2bfloat16_rn(v[e % PER] - __bfloat162float(h[e]));
+                }
+                *reinterpret_cast<uint4*>(vt0 + tcx::sw128_offset(w, piece)) = *reinterpret_cast<const uint4*>(h);
+                if (NT == 2)
+                    *reinterpret_cast<uint4*>(vt1 + tcx::sw128_offset(w, piece)) = *reinterpret_cast<const uint4*>(l);
+            }
+        }
+        tcx::fence_proxy_async();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tcx::fence_after();
+            const uint32_t a0 = tcx::smem_u32(at0), a1 = tcx::smem_u32(at1);
+            const uint32_t v0 = tcx::smem_u32(vt0), v1 = tcx::smem_u32(vt1);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {  // four K steps of 32 bytes cover the chunk
+                const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
+                if (MODE == PROJ_TF32) {
+                    tcx::mma_tf32(tmem, tcx::sw128_desc(a0 + kk * 32), tcx::sw128_desc(v0 + kk * 32), idesc, acc);
+                } else {
+                    tcx::mma_f16(tmem, tcx::sw128_desc(a0 + kk * 32), tcx::sw128_desc(v0 + kk * 32), idesc, acc);
+                    if (NT == 2) {
+                        tcx::mma_f16(tmem, tcx::sw128_desc(a0 + kk * 32), tcx::sw128_desc(v1 + kk * 32), idesc, 1u);
+                        tcx::mma_f16(tmem, tcx::sw128_desc(a1 + kk * 32), tcx::sw128_desc(v0 + kk * 32), idesc, 1u);
+                    }
+                }
+            }
+            tcx::mma_commit(bar);
+        }
+        ok = tcx::mbar_wait(bar, ch & 1, 1u, &g_proj_error);  // the tiles may be overwritten once the MMAs are done
+        ok = __all_sync(FULL_MASK, ok);
+        tcx::fence_after();
+    }
+    const int k = mt * 128 + warp * 32 + lane;
+    if (ok) {
+        for (int c0 = 0; c0 < np; c0 += 16) {
+            float v[16];
+            if (nchunk > 0) {
+                tcx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = 0.0f;
+            }
+            if (k < K)
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (c0 + i < W) moments[((size_t)cell * (4 + K) + 4 + k) * W + c0 + i] = v[i];
+        }
+    }
+    tcx::fence_before();
+    __syncthreads();
+    if (warp == 0) tcx::tmem_dealloc(tmem, tmem_cols);
 }
 
 __global__ void add_kernel(const float* a, const float* b, float* out, int n) {
@@ -1586,10 +1781,50 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
     return 0;
 }
 
-static int run_project(sosb_state* s, const BundleDev& b, int ncell, bool ground_only, float* moments, float* flux) {
+// Basis table of the tensor-core projection for the cell bundle in the current projection mode.
+static int ensure_basis(sosb_state* s, BundleDev& b) {
+    const int mode = s->proj_mode;
+    if (b.b_mode == mode) return 0;
+    const sosb_dims& d = s->d;
+    const int esz = mode == PROJ_TF32 ? 4 : 2, ch = 128 / esz;
+    int64_t rmax = 0;
+    for (int c = 0; c < b.ncell; ++c) rmax = std::max(rmax, b.host_cell_off[c + 1] - b.host_cell_off[c]);
+    const int kpad = (s->K + 127) / 128 * 128;
+    const int rpad = (int)std::max<int64_t>(ch, (rmax + ch - 1) / ch * ch);
+    const size_t bytes = (size_t)b.ncell * kpad * rpad * esz;
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if (bytes * (mode == PROJ_BF16X3 ? 2 : 1) > (free_b + b.b_hi.bytes + b.b_lo.bytes) / 2)
+        return fail(s, "E_MEMORY: projection basis table of %zu bytes", bytes);
+    TRY(dalloc(s, b.b_hi, bytes));
+    CK(cudaMemsetAsync(b.b_hi.p, 0, bytes, s->stream));
+    if (mode == PROJ_BF16X3) {
+        TRY(dalloc(s, b.b_lo, bytes));
+        CK(cudaMemsetAsync(b.b_lo.p, 0, bytes, s->stream));
+    }
+    const BasisTable bt{b.b_hi.p, b.b_lo.p, kpad, rpad};
+    const int blocks = grid_for(b.nray * (int64_t)(d.L + 1), 256);
+    if (mode == PROJ_BF16X3)
+        basis_table_kernel<PROJ_BF16X3><<<blocks, 256, 0, s->stream>>>(optics_of(s), rays_of(b), bt);
+    else if (mode == PROJ_TF32)
+        basis_table_kernel<PROJ_TF32><<<blocks, 256, 0, s->stream>>>(optics_of(s), rays_of(b), bt);
+    else
+        basis_table_kernel<PROJ_BF16><<<blocks, 256, 0, s->stream>>>(optics_of(s), rays_of(b), bt);
+    TRY(launch_check(s));
+    b.b_mode = mode;
+    b.b_kpad = kpad;
+    b.b_rpad = rpad;
+    return 0;
+}
+
+// Moments of `ncell` cells from s->rad: Rayleigh rows and ground flux on the CUDA cores (compensated FP32); the SH
+// rows there too (PROJ_FP32) or on the tensor cores (the other projection forms).
+static int run_project(sosb_state* s, BundleDev& b, int ncell, bool ground_only, float* moments, float* flux) {
     if (ncell <= 0) return 0;
     const sosb_dims& d = s->d;
-    const int nout = (4 + s->K) * d.W;
+    const bool tc = s->proj_mode != PROJ_FP32 && !ground_only;
+    if (tc) TRY(ensure_basis(s, b));
+    const int nout = tc ? 4 * d.W : (4 + s->K) * d.W;
     const size_t smem = project_smem(s->K, d.W);
     const float flux_scale = (float)(d.albedo / M_PI);
     const int per_pass = PROJ_THREADS * PROJ_OWN;
@@ -1597,9 +1832,42 @@ static int run_project(sosb_state* s, const BundleDev& b, int ncell, bool ground
     for (int pass = 0; pass < passes; ++pass) {
         Timer timer(s, K_PROJECT);
         project_kernel<<<ncell, PROJ_THREADS, smem, s->stream>>>(optics_of(s), rays_of(b), P<float4>(s->rad), 0,
-                                                                 ground_only ? 1 : 0, pass * per_pass, moments,
-                                                                 pass == 0 ? flux : nullptr, flux_scale);
+                                                                 ground_only ? 1 : 0, tc ? 1 : 0, pass * per_pass,
+                                                                 moments, pass == 0 ? flux : nullptr, flux_scale);
         TRY(launch_check(s));
+    }
+    if (tc) {
+        const int np = (d.W + 15) / 16 * 16;
+        const uint32_t cols = np <= 32 ? 32u : 64u;
+        const uint32_t idesc = s->proj_mode == PROJ_TF32 ? tcx::idesc_tf32(128, np) : tcx::idesc_bf16(128, np);
+        const BasisTable bt{b.b_hi.p, b.b_lo.p, b.b_kpad, b.b_rpad};
+        const dim3 grid(b.b_kpad / 128, ncell);
+        const size_t tsm = project_tc_smem(s->proj_mode, np);
+        Timer timer(s, K_PROJECT);
+        if (s->proj_mode == PROJ_BF16X3)
+            project_tc_kernel<PROJ_BF16X3><<<grid, 128, tsm, s->stream>>>(bt, rays_of(b), P<float4>(s->rad), d.W,
+                                                                          s->K, np, idesc, cols, moments);
+        else if (s->proj_mode == PROJ_TF32)
+            project_tc_kernel<PROJ_TF32><<<grid, 128, tsm, s->stream>>>(bt, rays_of(b), P<float4>(s->rad), d.W, s->K,
+                                                                        np, idesc, cols, moments);
+        else
+            project_tc_kernel<PROJ_BF16><<<grid, 128, tsm, s->stream>>>(bt, rays_of(b), P<float4>(s->rad), d.W, s->K,
+                                                                        np, idesc, cols, moments);
+        TRY(launch_check(s));
+    }
+    return 0;
+}
+
+// Bounded waits of the tensor-core projection that ran out since the last check (synchronises the stream).
+static int proj_check(sosb_state* s) {
+    if (s->proj_mode == PROJ_FP32) return 0;
+    unsigned flags = 0;
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpyFromSymbol(&flags, g_proj_error, sizeof flags));
+    if (flags) {
+        const unsigned zero = 0;
+        CK(cudaMemcpyToSymbol(g_proj_error, &zero, sizeof zero));
+        return fail(s, "E_TC_TIMEOUT: a tensor-core projection wait ran out (flags %u)", flags);
     }
     return 0;
 }
@@ -1803,7 +2071,7 @@ int sosb_destroy(sosb_handle s) {
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
                         &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits,
-                        &bd->t_frame, &bd->t_misc, &bd->t_att};
+                        &bd->t_frame, &bd->t_misc, &bd->t_att, &bd->b_hi, &bd->b_lo};
         for (DevBuf* b : bb) dfree(s, *b);
     }
     collect_timing(s);
@@ -1831,6 +2099,27 @@ int sosb_get_timing(sosb_handle s, double* ms, int64_t* launches, int n) {
         ms[k] = s->timed_ms[k];
         launches[k] = s->timed_count[k];
     }
+    return 0;
+}
+
+int sosb_set_projection(sosb_handle s, int mode) {
+    if (!s) return 1;
+    if (mode < PROJ_FP32 || mode > PROJ_BF16) return fail(s, "E_PROJECTION: unknown form %d", mode);
+    if (mode != PROJ_FP32) {
+        const int np = (s->d.W + 15) / 16 * 16;
+        cudaError_t e = cudaSuccess;
+        if (mode == PROJ_BF16X3)
+            e = cudaFuncSetAttribute(project_tc_kernel<PROJ_BF16X3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)project_tc_smem(mode, np));
+        else if (mode == PROJ_TF32)
+            e = cudaFuncSetAttribute(project_tc_kernel<PROJ_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)project_tc_smem(mode, np));
+        else
+            e = cudaFuncSetAttribute(project_tc_kernel<PROJ_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)project_tc_smem(mode, np));
+        if (e != cudaSuccess) return fail(s, "E_CUDA: %s", cudaGetErrorString(e));
+    }
+    s->proj_mode = mode;
     return 0;
 }
 
@@ -1969,6 +2258,7 @@ int sosb_set_bundle(sosb_handle s, int which, const sosb_bundle* b) {
     if (!msg.empty()) return fail(s, "%s", msg.c_str());
     BundleDev& bd = which == SOSB_CELLS ? s->cells : s->obs;
     invalidate_tables(bd);
+    bd.b_mode = -1;
     bd.ncell = pk.ncell;
     bd.nray = pk.nray;
     bd.nseg = pk.nseg;
@@ -2001,7 +2291,7 @@ int sosb_evaluate(sosb_handle s, int phase, int first, const float* field_dev, c
     s->err.clear();
     TRY(evaluate_impl(s, phase, first, field_dev, boundary_dev, moments_dev, flux_dev, radiance_dev));
     CK(cudaStreamSynchronize(s->stream));
-    return 0;
+    return proj_check(s);
 }
 
 int sosb_apply(sosb_handle s, const float* field_dev, float* out_dev) {
@@ -2010,7 +2300,7 @@ int sosb_apply(sosb_handle s, const float* field_dev, float* out_dev) {
     s->err.clear();
     TRY(apply_impl(s, field_dev, out_dev, 0ull));
     CK(cudaStreamSynchronize(s->stream));
-    return 0;
+    return proj_check(s);
 }
 
 // ------------------------------------------------------------------------ allocation-free composition
@@ -2185,6 +2475,7 @@ static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, 
         TRY(apply_impl(s, x, g, mask));
         CK(cudaMemcpyAsync(met.data(), s->metrics.p, 3 * W * sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
+        TRY(proj_check(s));
         long long bad = 0;
         for (int w = 0; w < W; ++w) bad += met[w];
         if (bad) return fail(s, "E_NONFINITE_SOURCE: %lld values after evaluation %d", bad, it);

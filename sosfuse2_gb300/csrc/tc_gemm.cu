@@ -21,6 +21,7 @@
 #include <string>
 
 #include "../../include/sosb.h"
+#include "tc_ptx.cuh"
 
 namespace tc {
 
@@ -28,46 +29,22 @@ constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4;
 constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand tile
 constexpr int STAGE_BYTES = 2 * TILE_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr long long WAIT_CYCLES = 4000000000LL;  // about two seconds at the maximum SM clock
-
-// instruction descriptor, kind::f16: D = F32 (bits 4-5), A = BF16 (7-9), B = BF16 (10-12), both K-major,
-// N >> 3 (bits 17-22), M >> 4 (bits 24-28)
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t IDESC = tcx::idesc_bf16(BM, BN);
 
 __device__ unsigned g_error;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t* bar, unsigned parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
+using tcx::fence_after;
+using tcx::fence_before;
+using tcx::mbar_expect_tx;
+using tcx::mbar_init;
+using tcx::mma_commit;
+using tcx::smem_u32;
+using tcx::sw128_desc;
+using tcx::tmem_ld16;
 
 // Bounded wait on a barrier phase; false (with the error recorded) when the budget runs out.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned code) {
-    const long long t0 = clock64();
-    while (!mbar_try(bar, parity)) {
-        if (clock64() - t0 > WAIT_CYCLES) {
-            atomicOr(&g_error, code);
-            return false;
-        }
-    }
-    return true;
+    return tcx::mbar_wait(bar, parity, code, &g_error);
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
@@ -78,43 +55,8 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)1 << 16;              // leading byte offset (unused by swizzled K-major layouts)
-    d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset
-    d |= (uint64_t)1 << 46;              // descriptor version
-    d |= (uint64_t)2 << 61;              // 128-byte swizzle
-    return d;
-}
-
 __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-        "l"(a), "l"(b), "r"(IDESC), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    tcx::mma_f16(tmem, a, b, IDESC, accumulate);
 }
 
 __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
@@ -142,9 +84,7 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ 
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(BN));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        tcx::tmem_alloc(tmem_slot, BN);
     }
     fence_before();
     __syncthreads();
@@ -209,7 +149,7 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const __grid_constant__ 
     }
     fence_before();
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+    if (warp == 0) tcx::tmem_dealloc(tmem, BN);
 }
 
 // ------------------------------------------------------------------------------- elementwise kernels of the MLP
