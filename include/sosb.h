@@ -127,6 +127,16 @@ int sosb_set_node_tables(sosb_handle h, int enable);
  * tcgen05.mma against a basis table built once per cell bundle; the Rayleigh rows and the ground flux stay FP32.
  * E_PROJECTION for an unknown form; E_TC_TIMEOUT when a tensor-core wait ran out. */
 int sosb_set_projection(sosb_handle h, int mode);
+/* No reference counterpart. Evaluation graphs (default on): from the second evaluation of a solve, the evaluation's
+ * launches (Anderson mix, observer boxes, apply, residual feature and Gram column, report copy) are captured once into
+ * a CUDA graph and replayed, the changing ring slots and weights read from a device control block; the graph is
+ * dropped when constants, bundles or modes change. Timing (sosb_set_timing) runs the launches directly. 0: never. */
+int sosb_set_graphs(sosb_handle h, int enable);
+/* No reference counterpart. Autotuning (default on): the first table launch of each launch shape times 1, 2 and 4
+ * warps per ray (two runs each, CUDA events) and keeps the fastest for the process; off (or during a graph capture of
+ * an untuned shape): 4 warps from 96 nodes per ray, 2 from 48, else 1. Summation order follows the choice, so runs
+ * with autotuning may differ from runs without it by rounding. */
+int sosb_set_autotune(sosb_handle h, int enable);
 /* Replaces: Kernel.setup (source_solver.py:1243-1339) and constants_device (source_solver.py:2248). */
 int sosb_set_constants(sosb_handle h, const sosb_constants *c);
 /* Replaces: ray_geometry.upload_geometry / device_geometry (ray_geometry.py:205-287) of the cell bundle
@@ -177,9 +187,11 @@ int sosb_get_timing(sosb_handle h, double *ms, int64_t *launches, int n);
 int sosb_solve_warm(sosb_handle h, int max_eval, double tolerance, const float *x0_dev, double fallback_ss,
                     const float *fallback_dev, float *x_out, int x_out_is_device, sosb_stats *stats);
 /* Batched form of Solver.solve (no single counterpart in the reference, whose pipeline runs one state per process,
- * src/sosfuse2/jobs/pipeline_execution.py): n independent states, each its own handle and stream, solved concurrently
- * by `threads` host threads (0: one per state) so that their small launches overlap on the GPU. status[i] is state
- * i's sosb_solve result (its message in sosb_last_error(hs[i])); returns nonzero when any state failed. */
+ * src/sosfuse2/jobs/pipeline_execution.py): n independent states, each its own handle and stream, driven by one host
+ * thread with up to `threads` solves in flight (0: all); every round replays one evaluation graph per active state
+ * (sosb_set_graphs), so that their launches overlap on the GPU, then reads their reports; a finished solve hands its
+ * place to the next state. status[i] is state i's sosb_solve result (its message in sosb_last_error(hs[i]));
+ * returns nonzero when any state failed. */
 int sosb_solve_batch(sosb_handle *hs, int n, int max_eval, double tolerance, const float *const *x0_host,
                      float *const *x_out, int x_out_is_device, sosb_stats *stats, int *status, int threads);
 /* Tensor-core BF16 GEMM (tcgen05, TMA, TMEM; no counterpart in the reference, used by the learned warm start):
@@ -203,8 +215,9 @@ int sosb_mlp_adam(float *w, const float *g, float *m, float *v, long long n, flo
 int sosb_mlp_mse(const float *p, const float *y, long long n, float scale, float *d, float *partial, int blocks,
                  void *stream);
 int sosb_mlp_to_bf16(const float *in, long long n, void *out, void *stream);
-/* Batched forms of sosb_apply and sosb_solve_warm (no counterpart in the reference): n handles, each on its own
- * stream, run by `threads` host threads (0: one per handle); status[i] is handle i's result. */
+/* Batched forms of sosb_apply (n handles on `threads` host threads, 0: one per handle) and of sosb_solve_warm (the
+ * one-thread graph driver of sosb_solve_batch, `threads` solves in flight) (no counterpart in the reference);
+ * status[i] is handle i's result. */
 int sosb_apply_batch(sosb_handle *hs, int n, const float *const *fields_dev, float *const *outs_dev, int *status,
                      int threads);
 int sosb_solve_warm_batch(sosb_handle *hs, int n, int max_eval, double tolerance, const float *const *x0_dev,

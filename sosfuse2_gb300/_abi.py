@@ -70,6 +70,8 @@ SIGNATURES = {
     'sosb_set_stream': ([ctypes.c_void_p, ctypes.c_void_p], c_int),
     'sosb_set_node_tables': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_projection': ([ctypes.c_void_p, c_int], c_int),
+    'sosb_set_graphs': ([ctypes.c_void_p, c_int], c_int),
+    'sosb_set_autotune': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_constants': ([ctypes.c_void_p, ctypes.POINTER(Constants)], c_int),
     'sosb_set_bundle': ([ctypes.c_void_p, c_int, ctypes.POINTER(Bundle)], c_int),
     'sosb_evaluate': ([ctypes.c_void_p, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -18,8 +18,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <thread>
+#include <tuple>
 #include <atomic>
 #include <string>
 #include <vector>
@@ -60,6 +62,8 @@ struct TimedLaunch {
     cudaEvent_t a, b;
 };
 
+struct EvalCtrl;
+
 struct sosb_state {
     sosb_dims d{};
     bool timing = false;
@@ -79,11 +83,21 @@ struct sosb_state {
     BundleDev cells, obs;
     // work
     DevBuf rad, plane, moments, flux, first_moments, first_flux, boundary, metrics, boxes;
-    DevBuf fx, fg, fn, norms, partials, dots, mixw;
+    DevBuf fx, fg, norms, partials, dots;
     DevBuf ring_g[4], ring_f[4];
     DevBuf fl_val0, fl_coef, fl_dir, fl_g, fl_cnt, fl_off, fl_cursor, fl_entries;  // staged first light
     bool have_first = false;
     bool tables = true;  // build and use node tables (sosb_set_node_tables)
+    // fixed-point loop: evaluation control and report (device and pinned host copies), replayed evaluation graph
+    DevBuf ctrl_dev, report_dev;
+    EvalCtrl* ctrl_host = nullptr;
+    uint8_t* report_host = nullptr;
+    size_t report_bytes = 0;
+    int feat_blocks = 0, feat_threads = 0;
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_launches = 0;
+    bool graphs = true;  // replay evaluations from a captured CUDA graph (sosb_set_graphs)
+    bool autotune = true;  // time the table launch shapes once per shape (sosb_set_autotune)
     int proj_mode = 0;   // projection form (sosb_set_projection): PROJ_FP32, PROJ_BF16X3, PROJ_TF32, PROJ_BF16
     int64_t launches = 0;
 };
@@ -1301,8 +1315,10 @@ __global__ void compose_kernel(const float* __restrict__ warm, const float* __re
                                const float* __restrict__ rf, const float* __restrict__ af, const float* __restrict__ asca,
                                const float* __restrict__ ext0, const float* __restrict__ s_eigen,
                                const float* __restrict__ s_sca, int K, int src, int W, long long n,
-                               unsigned long long done_mask, float* __restrict__ out, unsigned* __restrict__ metrics) {
+                               unsigned long long done_mask, const unsigned long long* __restrict__ done_dev,
+                               float* __restrict__ out, unsigned* __restrict__ metrics) {
     __shared__ unsigned sm_bad[64], sm_mag[64], sm_dif[64];
+    if (done_dev) done_mask = *done_dev;  // frozen wavelengths from the evaluation control block
     for (int i = threadIdx.x; i < 64; i += blockDim.x) sm_bad[i] = sm_mag[i] = sm_dif[i] = 0u;
     __syncthreads();
     const int nm = 4 + K;
@@ -1398,20 +1414,41 @@ __global__ void __launch_bounds__(NORM_WARPS * 32)
     }
 }
 
-// Residual feature f = (g - x) / max(norm, 1e-8 max norm) into ring slot `dst`, and FP64 partial dots of f with
-// the ring slots (nslot <= 4, dst among them): partials[block][j][w]. Blocks walk whole cells; the block size is a
-// multiple of W, so thread t keeps wavelength t % W over all its elements, and the per-thread sums of a wavelength
-// are added in thread order at the end (no atomics: the dots are reproducible run to run).
+// Per-evaluation control of the fixed-point loop, written by the host (pinned) and copied to the device at the start
+// of every evaluation, so that one evaluation's launches are the same every time (a CUDA graph replays them).
+struct EvalCtrl {
+    int slot;      // ring slot receiving this evaluation's g and residual feature
+    int m;         // ring slots after adding it (1..4)
+    int order[4];  // those slots, oldest first
+    int mix;       // 1: x = Anderson mix of the previous ring (mix_m, mix_order, weights, use); 0: x as it is
+    int mix_m;
+    int mix_order[4];
+    int use[64];                 // per wavelength: 1 mix, 0 take g (frozen or no valid weights)
+    float weights[4 * 64];       // [j][w] over mix_order
+    unsigned long long done;     // converged wavelengths, frozen by the composition
+};
+
+struct Ring4 {
+    float* p[4];
+};
+
+// Residual feature f = (g - x) / max(norm, 1e-8 max norm) into ring slot ctrl->slot, and FP64 partial dots of f
+// with the ring slots ctrl->order[0 .. m-1] (the new slot among them): partials[block][j][w]. Blocks walk whole
+// cells; the block size is a multiple of W, so thread t keeps wavelength t % W over all its elements, and the
+// per-thread sums of a wavelength are added by a pairwise tree in thread order (no atomics: the dots are
+// reproducible run to run).
 __global__ void feature_kernel(const float* __restrict__ g, const float* __restrict__ x,
                                const float* __restrict__ norms, const unsigned* __restrict__ mx, long long ns, int src,
-                               int W, float* __restrict__ dst, const float* r0, const float* r1, const float* r2,
-                               const float* r3, int nslot, double* __restrict__ partials) {
+                               int W, Ring4 ring, const EvalCtrl* __restrict__ ctrl, double* __restrict__ partials) {
     extern __shared__ double sd[];  // [blockDim.x][4]
     const int B = blockDim.x;
     const int t = threadIdx.x;
     const int w = t % W;
     const int row = src * W;
-    const float* ring[4] = {r0, r1, r2, r3};
+    const int nslot = ctrl->m;
+    float* dst = ring.p[ctrl->slot];
+    const float* rj[4];
+    for (int j = 0; j < 4; ++j) rj[j] = ring.p[ctrl->order[j & 3]];
     const float floor_w = __uint_as_float(mx[w]) * 1e-8f;
     double loc[4] = {0.0, 0.0, 0.0, 0.0};
     for (long long cell = blockIdx.x; cell < ns; cell += gridDim.x) {
@@ -1422,7 +1459,7 @@ __global__ void feature_kernel(const float* __restrict__ g, const float* __restr
             const float f = (g[i] - x[i]) / scale;
             dst[i] = f;
             for (int j = 0; j < nslot; ++j) {
-                const float o = (ring[j] == dst) ? f : ring[j][i];
+                const float o = (rj[j] == dst) ? f : rj[j][i];
                 loc[j] += (double)f * (double)o;
             }
         }
@@ -1436,14 +1473,20 @@ __global__ void feature_kernel(const float* __restrict__ g, const float* __restr
             for (int j = 0; j < 4; ++j) sd[t * 4 + j] += sd[(t + h * W) * 4 + j];
         __syncthreads();
     }
-    for (int q = t; q < nslot * W; q += B) {
+    for (int q = t; q < 4 * W; q += B) {
         const int j = q / W, ww = q % W;
-        partials[(size_t)blockIdx.x * nslot * W + q] = sd[ww * 4 + j];
+        partials[(size_t)blockIdx.x * 4 * W + q] = j < nslot ? sd[ww * 4 + j] : 0.0;
     }
 }
 
-// out[i] = sum over blocks of partials[block][i]: one warp per output, lanes over blocks, lane sums added by a fixed
-// shuffle tree (reproducible).
+// ring.p[ctrl->slot] = g
+__global__ void ring_copy_kernel(const float* __restrict__ g, Ring4 ring, const EvalCtrl* __restrict__ ctrl,
+                                 long long n) {
+    float* dst = ring.p[ctrl->slot];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = g[i];
+}
+
 __global__ void sum_partials_kernel(const double* __restrict__ partials, int blocks, int n, double* out) {
     const int lane = threadIdx.x & 31;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1454,20 +1497,23 @@ __global__ void sum_partials_kernel(const double* __restrict__ partials, int blo
     if (lane == 0) out[i] = acc;
 }
 
-// nxt[i] = sum_j c[j][w] ring_g[order j][i] for wavelengths with valid weights, else g[i].
-__global__ void mix_kernel(const float* __restrict__ g, const float* q0, const float* q1, const float* q2,
-                           const float* q3, int m, const float* __restrict__ c, const int* __restrict__ use, int W,
-                           long long n, float* __restrict__ out) {
+// When ctrl->mix: x[i] = sum_j weights[j][w] ring[mix_order j][i] for wavelengths with valid weights, else g[i]
+// (the previous evaluation's g). Without ctrl->mix, x stays as it is.
+__global__ void mix_kernel(const float* __restrict__ g, Ring4 ring, const EvalCtrl* __restrict__ ctrl, int W,
+                           long long n, float* __restrict__ x) {
+    if (!ctrl->mix) return;
+    const int m = ctrl->mix_m;
+    const float* q[4];
+    for (int j = 0; j < 4; ++j) q[j] = ring.p[ctrl->mix_order[j]];
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int w = (int)(i % W);
-        if (!use[w]) {
-            out[i] = g[i];
+        if (!ctrl->use[w]) {
+            x[i] = g[i];
             continue;
         }
-        const float* q[4] = {q0, q1, q2, q3};
-        float s = c[w] * q[0][i];
-        for (int j = 1; j < m; ++j) s += c[j * W + w] * q[j][i];
-        out[i] = s;
+        float acc = ctrl->weights[w] * q[0][i];
+        for (int j = 1; j < m; ++j) acc += ctrl->weights[j * 64 + w] * q[j][i];
+        x[i] = acc;
     }
 }
 
@@ -1541,6 +1587,12 @@ static Rays rays_of(const BundleDev& b) {
     r.hits = P<uint8_t>(b.hits);
     r.pcp = P<float>(b.pcp);
     return r;
+}
+
+// Drops the captured evaluation graph (its launches hold the handle's constants, pointers and modes).
+static void graph_reset(sosb_state* s) {
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
 }
 
 static int launch_check(sosb_state* s) {
@@ -1638,6 +1690,70 @@ static int plane_kp(const sosb_state* s) { return s->d.W <= 4 ? (s->K + 3) & ~3 
 static void invalidate_tables(BundleDev& b) {
     b.t_valid = false;
     b.t_too_big = false;
+}
+
+// ------------------------------------------------------------------------------------------------ autotuner
+// Warps per ray of the table launches (1, 2 or 4): with autotuning on, the first table launch of a shape (rays of
+// the launch, segments, nodes per segment, W, L, cells) times each choice twice with CUDA events on the work stream
+// and keeps the fastest for the process; otherwise (or while a graph is being captured) the choice follows the mean
+// nodes per ray (4 warps from 96, 2 from 48). The launch that follows uses the chosen value, so results do not
+// depend on which candidate ran last.
+struct TuneKey {
+    int64_t nray, nseg;
+    int nq, W, L, ns;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(nray, nseg, nq, W, L, ns) < std::tie(o.nray, o.nseg, o.nq, o.W, o.L, o.ns);
+    }
+};
+static std::mutex g_tune_lock;
+static std::map<TuneKey, int> g_tuned;
+
+template <class Launch>
+static int tuned_wpr(sosb_state* s, const BundleDev& b, int nq, int64_t nray, Launch launch, int& wpr) {
+    const double mean_nodes = (double)b.nseg * nq / std::max<int64_t>(b.nray, 1);
+    wpr = mean_nodes >= 96.0 ? 4 : (mean_nodes >= 48.0 ? 2 : 1);
+    if (!s->autotune) return 0;
+    const TuneKey key{nray, b.nseg, nq, s->d.W, s->d.L, s->ns};
+    {
+        std::lock_guard<std::mutex> guard(g_tune_lock);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) {
+            wpr = it->second;
+            return 0;
+        }
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(s->stream, &cap));
+    if (cap != cudaStreamCaptureStatusNone) return 0;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_wpr = wpr;
+    for (int cand : {1, 2, 4}) {
+        float t = 1e30f;
+        for (int rep = 0; rep < 2; ++rep) {
+            CK(cudaEventRecord(e0, s->stream));
+            launch(cand);
+            CK(cudaGetLastError());
+            CK(cudaEventRecord(e1, s->stream));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            t = std::min(t, ms);
+        }
+        if (t < best) {
+            best = t;
+            best_wpr = cand;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s->launches += 6;
+    wpr = best_wpr;
+    std::lock_guard<std::mutex> guard(g_tune_lock);
+    g_tuned[key] = wpr;
+    return 0;
 }
 
 // Staged first light of the whole cell bundle (W <= 4; FirstLightBufs). Returns 0 with `done` false when the
@@ -1748,15 +1864,17 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
         const long long blocks = (nray * 32 + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
         const size_t smem = warp_smem(s->K);
         Timer timer(s, read ? K_TABLE : K_TRANSPORT);
-        // warps per ray from the bundle's mean nodes per ray
-        const double mean_nodes = (double)b.nseg * in.nq / std::max<int64_t>(b.nray, 1);
-        const int wpr = mean_nodes >= 96.0 ? 4 : (mean_nodes >= 48.0 ? 2 : 1);
-        const long long tblocks = (nray * wpr + TRANSPORT_THREADS / 32 - 1) / (TRANSPORT_THREADS / 32);
         if (read) {
-            auto kernel = table_kernel_for(d.W, d.L);
-            kernel<<<(unsigned)tblocks, TRANSPORT_THREADS, smem, s->stream>>>(optics_of(s), rays_of(b), in, table,
-                                                                             (int)ray0, (int)nray, wpr,
-                                                                             P<float4>(s->rad));
+            const TableKernel kernel = table_kernel_for(d.W, d.L);
+            auto launch = [&](int wpr) {
+                const long long tblocks = (nray * wpr + TRANSPORT_THREADS / 32 - 1) / (TRANSPORT_THREADS / 32);
+                kernel<<<(unsigned)tblocks, TRANSPORT_THREADS, smem, s->stream>>>(optics_of(s), rays_of(b), in, table,
+                                                                                 (int)ray0, (int)nray, wpr,
+                                                                                 P<float4>(s->rad));
+            };
+            int wpr = 0;
+            TRY(tuned_wpr(s, b, in.nq, nray, launch, wpr));
+            launch(wpr);
         } else if (d.W == 1)
             transport_warp_kernel<1, false><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
                 optics_of(s), rays_of(b), in, write, no_fl, (int)ray0, (int)nray, P<float4>(s->rad));
@@ -1928,7 +2046,8 @@ static int ensure_first(sosb_state* s) {
 }
 
 // Solver.apply: returns metrics on device in s->metrics (reset here)
-static int apply_impl(sosb_state* s, const float* field, float* out, unsigned long long done_mask) {
+static int apply_impl(sosb_state* s, const float* field, float* out, unsigned long long done_mask,
+                      const unsigned long long* done_dev = nullptr) {
     const sosb_dims& d = s->d;
     TRY(check_ready(s, false));
     TRY(ensure_first(s));
@@ -1954,12 +2073,14 @@ static int apply_impl(sosb_state* s, const float* field, float* out, unsigned lo
     Timer timer(s, K_COMPOSE);
     compose_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(
         P<float>(s->moments), P<float>(s->first_moments), field, P<float>(s->rf), P<float>(s->af), P<float>(s->asca),
-        P<float>(s->ext0), P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, done_mask, out,
+        P<float>(s->ext0), P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, done_mask, done_dev,
+        out,
         P<unsigned>(s->metrics));
     return launch_check(s);
 }
 
-static int boxes_impl(sosb_state* s, const float* field, double* out_host) {
+// Observer boxes of `field` into device memory (engine_core.Solver.boxes), no synchronisation.
+static int boxes_dev(sosb_state* s, const float* field, double* out_dev) {
     const sosb_dims& d = s->d;
     TRY(check_ready(s, true));
     if (s->obs.nray < (int64_t)d.n_monitor_rows * d.n_dirs * d.box_points)
@@ -1968,14 +2089,17 @@ static int boxes_impl(sosb_state* s, const float* field, double* out_host) {
     TRY(run_plane(s, field));
     TRY(run_transport(s, s->obs, 0, s->obs.nray, field, nullptr, 0, true));
     const int n = d.n_monitor_rows * d.n_dirs * d.W;
-    TRY(dalloc(s, s->boxes, n * sizeof(double)));
-    {
     Timer timer(s, K_BOXES);
     boxes_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(P<float4>(s->rad), P<double>(s->box_ww), P<double>(s->solar),
-                                                        d.n_monitor_rows, d.n_dirs, d.box_points, d.W,
-                                                        P<double>(s->boxes));
-    }
-    TRY(launch_check(s));
+                                                        d.n_monitor_rows, d.n_dirs, d.box_points, d.W, out_dev);
+    return launch_check(s);
+}
+
+static int boxes_impl(sosb_state* s, const float* field, double* out_host) {
+    const sosb_dims& d = s->d;
+    const int n = d.n_monitor_rows * d.n_dirs * d.W;
+    TRY(dalloc(s, s->boxes, n * sizeof(double)));
+    TRY(boxes_dev(s, field, P<double>(s->boxes)));
     CK(cudaMemcpyAsync(out_host, s->boxes.p, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return collect_timing(s);
@@ -2060,13 +2184,14 @@ int sosb_destroy(sosb_handle s) {
     cudaStreamSynchronize(s->stream);
     DevBuf* bufs[] = {&s->h, &s->chi, &s->hr, &s->ha, &s->ext, &s->asca, &s->table, &s->sun_h, &s->sun_col, &s->gm,
                       &s->goff, &s->gdir, &s->gval, &s->rf, &s->af, &s->ext0, &s->s_ext, &s->s_sca, &s->s_chi,
-                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->s_lut, &s->s_lut2, &s->gsame, &s->gdir4, &s->sh_a, &s->sh_b, &s->sh_d,
-                      &s->u_hi, &s->u_lo, &s->wu_hi, &s->wu_lo, &s->uq_hi, &s->uq_lo, &s->wuq_hi, &s->wuq_lo,
-                      &s->box_ww, &s->solar, &s->rad, &s->plane, &s->moments, &s->flux, &s->first_moments,
-                      &s->first_flux, &s->boundary, &s->metrics, &s->boxes, &s->fx, &s->fg, &s->fn, &s->norms,
-                      &s->partials, &s->dots, &s->mixw, &s->ring_g[0], &s->ring_g[1], &s->ring_g[2], &s->ring_g[3],
-                      &s->ring_f[0], &s->ring_f[1], &s->ring_f[2], &s->ring_f[3], &s->fl_val0, &s->fl_coef,
-                      &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off, &s->fl_cursor, &s->fl_entries};
+                      &s->s_density, &s->s_sun_col, &s->s_eigen, &s->s_sca_src, &s->s_lut, &s->s_lut2, &s->gsame,
+                      &s->gdir4, &s->sh_a, &s->sh_b, &s->sh_d, &s->u_hi, &s->u_lo, &s->wu_hi, &s->wu_lo, &s->uq_hi,
+                      &s->uq_lo, &s->wuq_hi, &s->wuq_lo, &s->box_ww, &s->solar, &s->rad, &s->plane, &s->moments,
+                      &s->flux, &s->first_moments, &s->first_flux, &s->boundary, &s->metrics, &s->boxes, &s->fx,
+                      &s->fg, &s->norms, &s->partials, &s->dots, &s->ctrl_dev, &s->report_dev, &s->ring_g[0],
+                      &s->ring_g[1], &s->ring_g[2], &s->ring_g[3], &s->ring_f[0], &s->ring_f[1], &s->ring_f[2],
+                      &s->ring_f[3], &s->fl_val0, &s->fl_coef, &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off,
+                      &s->fl_cursor, &s->fl_entries};
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
@@ -2075,6 +2200,9 @@ int sosb_destroy(sosb_handle s) {
         for (DevBuf* b : bb) dfree(s, *b);
     }
     collect_timing(s);
+    graph_reset(s);
+    if (s->ctrl_host) cudaFreeHost(s->ctrl_host);
+    if (s->report_host) cudaFreeHost(s->report_host);
     for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
     if (s->own) cudaStreamDestroy(s->own);
     delete s;
@@ -2120,6 +2248,7 @@ int sosb_set_projection(sosb_handle s, int mode) {
         if (e != cudaSuccess) return fail(s, "E_CUDA: %s", cudaGetErrorString(e));
     }
     s->proj_mode = mode;
+    graph_reset(s);
     return 0;
 }
 
@@ -2128,6 +2257,7 @@ int sosb_set_node_tables(sosb_handle s, int enable) {
     s->tables = enable != 0;
     invalidate_tables(s->cells);
     invalidate_tables(s->obs);
+    graph_reset(s);
     return 0;
 }
 
@@ -2245,6 +2375,7 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
     s->have_first = false;
     invalidate_tables(s->cells);
     invalidate_tables(s->obs);
+    graph_reset(s);
     return 0;
 }
 
@@ -2259,6 +2390,7 @@ int sosb_set_bundle(sosb_handle s, int which, const sosb_bundle* b) {
     BundleDev& bd = which == SOSB_CELLS ? s->cells : s->obs;
     invalidate_tables(bd);
     bd.b_mode = -1;
+    graph_reset(s);
     bd.ncell = pk.ncell;
     bd.nray = pk.nray;
     bd.nseg = pk.nseg;
@@ -2346,8 +2478,8 @@ int sosb_compose_static(sosb_handle s, const float* moments_dev, const float* fi
     const long long n = (long long)s->ns * s->src * d.W;
     compose_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(
         moments_dev, first_moments_dev, x_dev, P<float>(s->rf), P<float>(s->af), P<float>(s->asca), P<float>(s->ext0),
-        P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, (unsigned long long)done_mask, out_dev,
-        scratch);
+        P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, (unsigned long long)done_mask, nullptr,
+        out_dev, scratch);
     TRY(launch_check(s));
     unsigned words[3 * SOSB_STATIC_WAVES];
     CK(cudaMemcpyAsync(words, scratch, 3 * d.W * sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
@@ -2411,137 +2543,263 @@ static bool anderson_weights(int n, const double* G, float* out) {
     return true;
 }
 
-// The fixed-point loop. x0: NULL (zero start), a host (x0_device = 0) or device field. keep_first: reuse the
-// first-light moments already computed on this handle. fallback_dev: when the first evaluation's largest source
-// relative change exceeds fallback_ss, the iteration restarts from this device field.
-static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, int x0_device, bool keep_first,
-                      double fallback_ss, const float* fallback_dev, float* x_out, int x_out_is_device,
-                      sosb_stats* stats) {
-    if (!x_out) return fail(s, "E_FIELD: null output");
-    s->err.clear();
-    const auto t_start = std::chrono::steady_clock::now();
-    const int64_t launches0 = s->launches;
-    TRY(check_ready(s, true));
-    if (!keep_first) s->have_first = false;  // a solve includes its first-light pass unless told otherwise
-    int fell_back = 0;
-    const sosb_dims& d = s->d;
-    const int W = d.W;
-    const size_t n = (size_t)s->ns * s->src * W;
-    const size_t bytes = n * sizeof(float);
+// ------------------------------------------------------------------------------------------------ the fixed-point loop
+// Report of one evaluation (device, copied to pinned host memory at its end): composition metrics [3][64] u32,
+// observer boxes of x and of g [rows][dirs][W] f64 each, Gram columns [4][W] f64.
+struct ReportLayout {
+    size_t metrics, old_b, new_b, dots, bytes;
+};
+
+static ReportLayout report_layout(const sosb_state* s) {
+    const size_t nbox = (size_t)s->d.n_monitor_rows * s->d.n_dirs * s->d.W;
+    ReportLayout r;
+    r.metrics = 0;
+    r.old_b = 3 * 64 * sizeof(unsigned);
+    r.new_b = r.old_b + nbox * sizeof(double);
+    r.dots = r.new_b + nbox * sizeof(double);
+    r.bytes = r.dots + 4 * (size_t)s->d.W * sizeof(double);
+    return r;
+}
+
+// Buffers of the loop: iterate x and g, the Anderson rings, norms, Gram partials, control and report.
+static int loop_alloc(sosb_state* s) {
+    const int W = s->d.W;
+    const size_t bytes = (size_t)s->ns * s->src * W * sizeof(float);
     TRY(dalloc(s, s->fx, bytes));
     TRY(dalloc(s, s->fg, bytes));
-    TRY(dalloc(s, s->fn, bytes));
     for (int j = 0; j < 4; ++j) {
         TRY(dalloc(s, s->ring_g[j], bytes));
         TRY(dalloc(s, s->ring_f[j], bytes));
     }
     TRY(dalloc(s, s->norms, (size_t)s->ns * W * sizeof(float)));
-    TRY(dalloc(s, s->mixw, (size_t)(4 * W) * sizeof(float) + 64 * sizeof(int)));
     // feature kernel: blocks of a multiple of W threads (one wavelength per thread), whole cells per block
-    const int fthreads = W * std::max(1, 256 / W);
-    const int fblocks = (int)std::min<long long>(s->ns, 152LL * 4);
-    TRY(dalloc(s, s->partials, (size_t)fblocks * 4 * W * sizeof(double)));
+    s->feat_threads = W * std::max(1, 256 / W);
+    s->feat_blocks = (int)std::min<long long>(s->ns, 152LL * 4);
+    TRY(dalloc(s, s->partials, (size_t)s->feat_blocks * 4 * W * sizeof(double)));
     TRY(dalloc(s, s->dots, (size_t)4 * W * sizeof(double)));
-    if (x0)
-        CK(cudaMemcpyAsync(s->fx.p, x0, bytes, x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                           s->stream));
-    else
-        CK(cudaMemsetAsync(s->fx.p, 0, bytes, s->stream));
+    TRY(dalloc(s, s->metrics, 3 * 64 * sizeof(unsigned)));
+    TRY(dalloc(s, s->ctrl_dev, sizeof(EvalCtrl)));
+    const ReportLayout rl = report_layout(s);
+    TRY(dalloc(s, s->report_dev, rl.bytes));
+    if (!s->ctrl_host) CK(cudaMallocHost(&s->ctrl_host, sizeof(EvalCtrl)));
+    if (s->report_bytes < rl.bytes) {
+        if (s->report_host) CK(cudaFreeHost(s->report_host));
+        s->report_host = nullptr;
+        CK(cudaMallocHost(&s->report_host, rl.bytes));
+        s->report_bytes = rl.bytes;
+    }
+    return 0;
+}
+
+// One evaluation on the device, the same launches every time (the control block carries what changes):
+// x = Anderson mix of the previous ring (if ctrl.mix); boxes(x); g = apply(x) with the composition metrics; boxes(g);
+// g into the ring; residual feature and FP64 Gram column; the report copied to pinned host memory
+// (source_iteration.py:309-635, one evaluation of the loop).
+static int eval_body(sosb_state* s) {
+    const sosb_dims& d = s->d;
+    const int W = d.W;
+    const long long n = (long long)s->ns * s->src * W;
     float* x = P<float>(s->fx);
     float* g = P<float>(s->fg);
-    float* nxt = P<float>(s->fn);
-    const int rows = d.n_monitor_rows, stop = d.monitors, dirs = d.n_dirs;
-    const int nbox = rows * dirs * W;
-    std::vector<double> old_b(nbox), new_b(nbox);
-    std::vector<unsigned> met(3 * W);
-    std::vector<int> done(W, 0);
-    // ring bookkeeping shared by all active wavelengths: slots in age order (oldest first)
-    std::vector<int> order;
-    std::vector<double> gram(W * 16, 0.0);                 // [w][slot][slot]
-    std::vector<float> obs(4 * W * 64, 0.0f);               // [slot][w][stop*dirs]
-    std::vector<double> dots(4 * W);
-    std::vector<float> weights(4 * W);
-    std::vector<int> use(64);
-    const int nfeat_obs = stop * dirs;
-    const double obs_scale = std::sqrt((double)((size_t)s->ns * s->src) / (double)nfeat_obs);
-    int it = 0;
+    EvalCtrl* ctrl = P<EvalCtrl>(s->ctrl_dev);
+    uint8_t* rep = P<uint8_t>(s->report_dev);
+    const ReportLayout rl = report_layout(s);
+    const Ring4 rg{{P<float>(s->ring_g[0]), P<float>(s->ring_g[1]), P<float>(s->ring_g[2]), P<float>(s->ring_g[3])}};
+    const Ring4 rf{{P<float>(s->ring_f[0]), P<float>(s->ring_f[1]), P<float>(s->ring_f[2]), P<float>(s->ring_f[3])}};
+    CK(cudaMemcpyAsync(ctrl, s->ctrl_host, sizeof(EvalCtrl), cudaMemcpyHostToDevice, s->stream));
+    {
+        Timer t(s, K_ANDERSON);
+        mix_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(g, rg, ctrl, W, n, x);
+    }
+    TRY(launch_check(s));
+    TRY(boxes_dev(s, x, reinterpret_cast<double*>(rep + rl.old_b)));
+    TRY(apply_impl(s, x, g, 0ull, &ctrl->done));
+    CK(cudaMemcpyAsync(rep + rl.metrics, s->metrics.p, 3 * 64 * sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                       s->stream));
+    TRY(boxes_dev(s, g, reinterpret_cast<double*>(rep + rl.new_b)));
+    CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
+    {
+        Timer t(s, K_ANDERSON);
+        ring_copy_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(g, rg, ctrl, n);
+    }
+    TRY(launch_check(s));
+    {
+        Timer t(s, K_ANDERSON);
+        norm_kernel<<<(unsigned)std::min<long long>((s->ns + NORM_WARPS - 1) / NORM_WARPS, 152LL * 16),
+                      NORM_WARPS * 32, 0, s->stream>>>(g, s->ns, s->src, W, P<float>(s->norms),
+                                                       P<unsigned>(s->metrics));
+    }
+    TRY(launch_check(s));
+    {
+        Timer t(s, K_ANDERSON);
+        feature_kernel<<<s->feat_blocks, s->feat_threads, (size_t)s->feat_threads * 4 * sizeof(double),
+                         s->stream>>>(g, x, P<float>(s->norms), P<unsigned>(s->metrics), (long long)s->ns, s->src, W,
+                                      rf, ctrl, P<double>(s->partials));
+    }
+    TRY(launch_check(s));
+    {
+        Timer t(s, K_ANDERSON);
+        sum_partials_kernel<<<(4 * W * 32 + 127) / 128, 128, 0, s->stream>>>(P<double>(s->partials), s->feat_blocks,
+                                                                             4 * W, P<double>(s->dots));
+    }
+    TRY(launch_check(s));
+    CK(cudaMemcpyAsync(rep + rl.dots, s->dots.p, 4 * (size_t)W * sizeof(double), cudaMemcpyDeviceToDevice,
+                       s->stream));
+    CK(cudaMemcpyAsync(s->report_host, rep, rl.bytes, cudaMemcpyDeviceToHost, s->stream));
+    return 0;
+}
+
+// Enqueues one evaluation: a replay of the captured graph when graphs are on (captured at the second evaluation,
+// once buffers and tables exist), else the launches themselves. A capture that fails (an allocation or an
+// unsupported call inside it) turns graphs off for the handle and runs the launches directly.
+static int eval_issue(sosb_state* s, int it) {
+    if (!s->graphs || s->timing || it < 2) return eval_body(s);
+    if (!s->graph) {
+        const int64_t l0 = s->launches;
+        cudaGraph_t gph = nullptr;
+        const cudaError_t e0 = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+        const int rc = e0 == cudaSuccess ? eval_body(s) : 1;
+        const cudaError_t e1 = e0 == cudaSuccess ? cudaStreamEndCapture(s->stream, &gph) : e0;
+        cudaError_t e2 = cudaErrorUnknown;
+        if (rc == 0 && e1 == cudaSuccess && gph) e2 = cudaGraphInstantiate(&s->graph, gph, 0);
+        if (gph) cudaGraphDestroy(gph);
+        const int64_t captured = s->launches - l0;  // kernels recorded into the graph, counted while capturing
+        s->launches = l0;
+        if (e2 != cudaSuccess) {
+            cudaGetLastError();
+            s->graph = nullptr;
+            s->graphs = false;
+            s->err.clear();
+            return eval_body(s);
+        }
+        s->graph_launches = captured;
+    }
+    CK(cudaGraphLaunch(s->graph, s->stream));
+    s->launches += s->graph_launches;
+    return 0;
+}
+
+// Host side of one solve (Solver.solve, source_iteration.py:309-663): convergence test on the observer boxes and
+// the source metrics, Anderson depth 4 per wavelength (FP64 Gram and solve), the fallback restart of a warm start.
+struct SolveRun {
+    sosb_state* s = nullptr;
+    int max_eval = 0;
+    double tol = 0.0, fallback_ss = 0.0;
+    const float* fallback_dev = nullptr;
+    int it = 0, fell_back = 0;
     bool all_done = false;
-    std::vector<double> rr(W), ss(W);
-    for (it = 1; it <= max_eval; ++it) {
-        TRY(boxes_impl(s, x, old_b.data()));
+    std::vector<int> done, order, pending, use;
+    std::vector<double> gram, rr, ss;
+    std::vector<float> obs;
+    std::chrono::steady_clock::time_point t0;
+    int64_t launches0 = 0;
+
+    // Sets the start x (NULL: zero; host or device field) and resets the loop.
+    int begin(sosb_state* st, int max_eval_, double tol_, const float* x0, int x0_device, bool keep_first,
+              double fallback_ss_, const float* fallback_dev_) {
+        s = st;
+        max_eval = max_eval_;
+        tol = tol_;
+        fallback_ss = fallback_ss_;
+        fallback_dev = fallback_dev_;
+        s->err.clear();
+        t0 = std::chrono::steady_clock::now();
+        launches0 = s->launches;
+        TRY(check_ready(s, true));
+        if (!keep_first) s->have_first = false;  // a solve includes its first-light pass unless told otherwise
+        TRY(loop_alloc(s));
+        const int W = s->d.W;
+        const size_t bytes = (size_t)s->ns * s->src * W * sizeof(float);
+        if (x0)
+            CK(cudaMemcpyAsync(s->fx.p, x0, bytes, x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               s->stream));
+        else
+            CK(cudaMemsetAsync(s->fx.p, 0, bytes, s->stream));
+        done.assign(W, 0);
+        use.assign(64, 0);
+        gram.assign((size_t)W * 16, 0.0);
+        obs.assign((size_t)4 * W * 64, 0.0f);
+        rr.assign(W, 0.0);
+        ss.assign(W, 0.0);
+        order.clear();
+        std::memset(s->ctrl_host, 0, sizeof(EvalCtrl));
+        return 0;
+    }
+
+    // Enqueues evaluation it + 1 with its ring slot chosen (committed by finish() when the Anderson step runs).
+    int issue() {
+        ++it;
+        pending = order;
+        int slot;
+        if ((int)pending.size() < 4) {
+            slot = (int)pending.size();
+        } else {
+            slot = pending.front();
+            pending.erase(pending.begin());
+        }
+        pending.push_back(slot);
+        EvalCtrl& c = *s->ctrl_host;
+        c.slot = slot;
+        c.m = (int)pending.size();
+        for (int j = 0; j < 4; ++j) c.order[j] = j < c.m ? pending[j] : slot;
         unsigned long long mask = 0;
-        for (int w = 0; w < W; ++w)
+        for (int w = 0; w < s->d.W; ++w)
             if (done[w]) mask |= 1ull << w;
-        TRY(apply_impl(s, x, g, mask));
-        CK(cudaMemcpyAsync(met.data(), s->metrics.p, 3 * W * sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
-        CK(cudaStreamSynchronize(s->stream));
+        c.done = mask;
+        return eval_issue(s, it);
+    }
+
+    // After the stream finished the evaluation: 0 to continue, 1 when the loop ends (converged or out of budget).
+    int finish(int& stop) {
+        stop = 0;
+        const int W = s->d.W;
+        const sosb_dims& d = s->d;
         TRY(proj_check(s));
+        const ReportLayout rl = report_layout(s);
+        const unsigned* met = reinterpret_cast<const unsigned*>(s->report_host + rl.metrics);
+        const double* old_b = reinterpret_cast<const double*>(s->report_host + rl.old_b);
+        const double* new_b = reinterpret_cast<const double*>(s->report_host + rl.new_b);
+        const double* dots = reinterpret_cast<const double*>(s->report_host + rl.dots);
         long long bad = 0;
         for (int w = 0; w < W; ++w) bad += met[w];
         if (bad) return fail(s, "E_NONFINITE_SOURCE: %lld values after evaluation %d", bad, it);
-        TRY(boxes_impl(s, g, new_b.data()));
+        const int stop_rows = d.monitors, dirs = d.n_dirs;
+        const int nfeat_obs = stop_rows * dirs;
         for (int w = 0; w < W; ++w) {
             double r = 0.0;
-            for (int i = 0; i < stop * dirs; ++i) {
+            for (int i = 0; i < nfeat_obs; ++i) {
                 const double nv = new_b[i * W + w], ov = old_b[i * W + w];
                 r = std::max(r, std::fabs(nv - ov) / std::max(std::fabs(nv), 1e-30));
             }
             float mg, df;
-            std::memcpy(&mg, &met[W + w], 4);
-            std::memcpy(&df, &met[2 * W + w], 4);
+            std::memcpy(&mg, &met[64 + w], 4);
+            std::memcpy(&df, &met[128 + w], 4);
             rr[w] = r;
             ss[w] = (double)(df / std::max(mg, 1e-30f));
             if (it >= 2 && std::max(r, ss[w]) <= tol) done[w] = 1;
         }
+        EvalCtrl& c = *s->ctrl_host;
         if (it == 1 && fallback_dev && !fell_back && *std::max_element(ss.begin(), ss.end()) > fallback_ss) {
             // the supplied start is further from the fixed point than the fallback start: restart from it
-            CK(cudaMemcpyAsync(x, fallback_dev, bytes, cudaMemcpyDeviceToDevice, s->stream));
+            CK(cudaMemcpyAsync(s->fx.p, fallback_dev, (size_t)s->ns * s->src * W * sizeof(float),
+                               cudaMemcpyDeviceToDevice, s->stream));
             fell_back = 1;
-            continue;
+            order.clear();
+            c.mix = 0;
+            if (it >= max_eval) stop = 1;
+            return 0;
         }
         all_done = std::all_of(done.begin(), done.end(), [](int v) { return v != 0; });
         if (all_done) {
-            std::swap(x, g);
-            break;
+            stop = 1;
+            return 0;
         }
-        // Anderson: new ring slot for g and its residual feature
-        int slot;
-        if ((int)order.size() < 4) {
-            slot = (int)order.size();
-        } else {
-            slot = order.front();
-            order.erase(order.begin());
-        }
-        order.push_back(slot);
-        CK(cudaMemcpyAsync(s->ring_g[slot].p, g, bytes, cudaMemcpyDeviceToDevice, s->stream));
-        CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
-        {
-            Timer t(s, K_ANDERSON);
-            norm_kernel<<<(unsigned)std::min<long long>((s->ns + NORM_WARPS - 1) / NORM_WARPS, 152LL * 16),
-                          NORM_WARPS * 32, 0, s->stream>>>(g, s->ns, s->src, W, P<float>(s->norms),
-                                                           P<unsigned>(s->metrics));
-        }
-        TRY(launch_check(s));
+        // Anderson: this evaluation's g and residual feature are in ring slot c.slot
+        order = pending;
+        const int slot = c.slot;
         const int m = (int)order.size();
-        const float* rp[4] = {nullptr, nullptr, nullptr, nullptr};
-        for (int j = 0; j < m; ++j) rp[j] = P<float>(s->ring_f[order[j]]);
-        const int fb = fblocks;
-        const int per = fthreads;
-        {
-            Timer t(s, K_ANDERSON);
-            feature_kernel<<<fb, per, (size_t)per * 4 * sizeof(double), s->stream>>>(
-                g, x, P<float>(s->norms), P<unsigned>(s->metrics), (long long)s->ns, s->src, W, P<float>(s->ring_f[slot]),
-                rp[0], rp[1], rp[2], rp[3], m, P<double>(s->partials));
-        }
-        TRY(launch_check(s));
-        {
-            Timer t(s, K_ANDERSON);
-            sum_partials_kernel<<<(m * W * 32 + 127) / 128, 128, 0, s->stream>>>(P<double>(s->partials), fb, m * W,
-                                                                                  P<double>(s->dots));
-        }
-        TRY(launch_check(s));
-        CK(cudaMemcpyAsync(dots.data(), s->dots.p, (size_t)m * W * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-        CK(cudaStreamSynchronize(s->stream));
+        const double obs_scale = std::sqrt((double)((size_t)s->ns * s->src) / (double)nfeat_obs);
+        std::vector<float> weights(4 * W, 0.0f);
         for (int w = 0; w < W; ++w) {
             use[w] = 0;
             if (done[w]) continue;
@@ -2568,47 +2826,129 @@ static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, 
                 }
             }
         }
-        CK(cudaMemcpyAsync(s->mixw.p, weights.data(), 4 * W * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-        CK(cudaMemcpyAsync(P<char>(s->mixw) + 4 * W * sizeof(float), use.data(), W * sizeof(int), cudaMemcpyHostToDevice,
+        c.mix = 1;
+        c.mix_m = m;
+        for (int j = 0; j < 4; ++j) c.mix_order[j] = j < m ? order[j] : order[m - 1];
+        for (int w = 0; w < 64; ++w) c.use[w] = w < W ? use[w] : 0;
+        for (int j = 0; j < 4; ++j)
+            for (int w = 0; w < 64; ++w) c.weights[j * 64 + w] = w < W ? weights[j * W + w] : 0.0f;
+        if (it >= max_eval) stop = 1;
+        return 0;
+    }
+
+    // The result (g when converged, else the mixed x after the last evaluation) and the statistics.
+    int end(float* x_out, int x_out_is_device, sosb_stats* stats) {
+        const size_t bytes = (size_t)s->ns * s->src * s->d.W * sizeof(float);
+        float* result = P<float>(all_done ? s->fg : s->fx);
+        if (!all_done) {
+            // the mix the next evaluation would have started with (the reference leaves its last mix in x)
+            CK(cudaMemcpyAsync(P<EvalCtrl>(s->ctrl_dev), s->ctrl_host, sizeof(EvalCtrl), cudaMemcpyHostToDevice,
+                               s->stream));
+            const long long n = (long long)s->ns * s->src * s->d.W;
+            const Ring4 rg{{P<float>(s->ring_g[0]), P<float>(s->ring_g[1]), P<float>(s->ring_g[2]),
+                            P<float>(s->ring_g[3])}};
+            mix_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(P<float>(s->fg), rg, P<EvalCtrl>(s->ctrl_dev),
+                                                               s->d.W, n, result);
+            TRY(launch_check(s));
+        }
+        CK(cudaMemcpyAsync(x_out, result, bytes, x_out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                            s->stream));
-        const float* q[4] = {nullptr, nullptr, nullptr, nullptr};
-        for (int j = 0; j < m; ++j) q[j] = P<float>(s->ring_g[order[j]]);
-        {
-            Timer t(s, K_ANDERSON);
-            mix_kernel<<<grid_for((long long)n, 256), 256, 0, s->stream>>>(
-                g, q[0], q[1], q[2], q[3], m, P<float>(s->mixw),
-                reinterpret_cast<const int*>(P<char>(s->mixw) + 4 * W * sizeof(float)), W, (long long)n, nxt);
+        CK(cudaStreamSynchronize(s->stream));
+        if (stats) {
+            std::memset(stats, 0, sizeof *stats);
+            stats->evaluations = std::min(it, max_eval);
+            stats->converged = all_done ? 1 : 0;
+            stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            for (int w = 0; w < s->d.W; ++w) {
+                stats->observer_relative[w] = rr[w];
+                stats->source_relative[w] = ss[w];
+                stats->done[w] = done[w];
+            }
+            stats->kernel_launches = s->launches - launches0;
+            stats->start_fallback = fell_back;
         }
-        TRY(launch_check(s));
-        std::swap(x, nxt);
-    }
-    if (it > max_eval) it = max_eval;
-    if (x_out_is_device)
-        CK(cudaMemcpyAsync(x_out, x, bytes, cudaMemcpyDeviceToDevice, s->stream));
-    else
-        CK(cudaMemcpyAsync(x_out, x, bytes, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    if (stats) {
-        std::memset(stats, 0, sizeof *stats);
-        stats->evaluations = it;
-        stats->converged = all_done ? 1 : 0;
-        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-        for (int w = 0; w < W; ++w) {
-            stats->observer_relative[w] = rr[w];
-            stats->source_relative[w] = ss[w];
-            stats->done[w] = done[w];
+        if (!all_done) {
+            int nd = 0;
+            for (int w = 0; w < s->d.W; ++w) nd += done[w];
+            return fail(s, "E_NOT_CONVERGED: %d/%d within %g", nd, s->d.W, tol);
         }
-        stats->kernel_launches = s->launches - launches0;
-        stats->start_fallback = fell_back;
+        return 0;
     }
-    if (!all_done) {
-        int nd = 0;
-        for (int w = 0; w < W; ++w) nd += done[w];
-        return fail(s, "E_NOT_CONVERGED: %d/%d within %g", nd, W, tol);
+};
+
+// The fixed-point loop of one handle. x0: NULL (zero start), a host (x0_device = 0) or device field. keep_first:
+// reuse the first-light moments already computed on this handle. fallback_dev: when the first evaluation's largest
+// source relative change exceeds fallback_ss, the iteration restarts from this device field.
+static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, int x0_device, bool keep_first,
+                      double fallback_ss, const float* fallback_dev, float* x_out, int x_out_is_device,
+                      sosb_stats* stats) {
+    if (!x_out) return fail(s, "E_FIELD: null output");
+    if (max_eval < 1) return fail(s, "E_FIELD: max_eval %d", max_eval);
+    SolveRun run;
+    TRY(run.begin(s, max_eval, tol, x0, x0_device, keep_first, fallback_ss, fallback_dev));
+    for (;;) {
+        TRY(run.issue());
+        CK(cudaStreamSynchronize(s->stream));
+        int stop = 0;
+        TRY(run.finish(stop));
+        if (stop) break;
     }
-    return 0;
+    return run.end(x_out, x_out_is_device, stats);
 }
 
+// Many solves from one host thread: up to `concurrency` handles in flight, each evaluation a graph replay on the
+// handle's stream; every round enqueues one evaluation of every active solve, then reads their reports; a solve
+// that ends hands its place to the next one.
+static int batch_drive(sosb_handle* hs, int n, int max_eval, double tol, const float* const* x0, int x0_device,
+                       bool keep_first, double fallback_ss, const float* const* fallback_dev, float* const* x_out,
+                       int x_out_is_device, sosb_stats* stats, int* status, int concurrency) {
+    if (n <= 0) return 0;
+    const int cap = std::max(1, std::min(concurrency > 0 ? concurrency : n, n));
+    std::vector<SolveRun> runs(n);
+    std::vector<int> active;
+    int next = 0;
+    auto start = [&]() {
+        while (next < n && (int)active.size() < cap) {
+            const int i = next++;
+            if (!hs[i] || !x_out[i]) {
+                status[i] = 1;
+                continue;
+            }
+            if (keep_first && !hs[i]->have_first) {
+                status[i] = fail(hs[i], "E_STATE: no first light on this handle (run an apply first)");
+                continue;
+            }
+            status[i] = runs[i].begin(hs[i], max_eval, tol, x0 ? x0[i] : nullptr, x0_device, keep_first, fallback_ss,
+                                      fallback_dev ? fallback_dev[i] : nullptr);
+            if (status[i] == 0) active.push_back(i);
+        }
+    };
+    start();
+    while (!active.empty()) {
+        for (int i : active) status[i] = runs[i].issue();
+        std::vector<int> keep;
+        for (int i : active) {
+            if (status[i]) continue;  // failed to enqueue: out of the batch with its error
+            sosb_state* s = hs[i];
+            int stop = 0;
+            const cudaError_t e = cudaStreamSynchronize(s->stream);
+            if (e != cudaSuccess)
+                status[i] = fail(s, "E_CUDA: %s", cudaGetErrorString(e));
+            else
+                status[i] = runs[i].finish(stop);
+            if (status[i] == 0 && !stop) {
+                keep.push_back(i);
+                continue;
+            }
+            if (status[i] == 0) status[i] = runs[i].end(x_out[i], x_out_is_device, stats ? &stats[i] : nullptr);
+        }
+        active = keep;
+        start();
+    }
+    int failed = 0;
+    for (int i = 0; i < n; ++i) failed += status[i] != 0;
+    return failed ? 3 : 0;
+}
 
 int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, float* x_out, int x_out_is_device,
                sosb_stats* stats) {
@@ -2627,24 +2967,9 @@ int sosb_solve_warm(sosb_handle s, int max_eval, double tol, const float* x0_dev
 int sosb_solve_batch(sosb_handle* hs, int n, int max_eval, double tol, const float* const* x0_host,
                      float* const* x_out, int x_out_is_device, sosb_stats* stats, int* status, int threads) {
     if (!hs || !x_out || !status || n < 0) return 1;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 2;
-    const int nt = std::max(1, std::min(threads > 0 ? threads : n, n));
-    std::atomic<int> next(0);
-    auto work = [&]() {
-        cudaSetDevice(dev);
-        for (int i = next++; i < n; i = next++)
-            status[i] = sosb_solve(hs[i], max_eval, tol, x0_host ? x0_host[i] : nullptr, x_out[i], x_out_is_device,
-                                   stats ? &stats[i] : nullptr);
-    };
-    std::vector<std::thread> pool;
-    for (int t = 0; t < nt; ++t) pool.emplace_back(work);
-    for (auto& t : pool) t.join();
-    int failed = 0;
-    for (int i = 0; i < n; ++i) failed += status[i] != 0;
-    return failed ? 3 : 0;
+    return batch_drive(hs, n, max_eval, tol, x0_host, 0, false, 0.0, nullptr, x_out, x_out_is_device, stats, status,
+                       threads);
 }
-
 
 int sosb_apply_batch(sosb_handle* hs, int n, const float* const* fields, float* const* outs, int* status,
                      int threads) {
@@ -2659,13 +2984,21 @@ int sosb_solve_warm_batch(sosb_handle* hs, int n, int max_eval, double tol, cons
                           double fallback_ss, const float* const* fallback_dev, float* const* x_out,
                           int x_out_is_device, sosb_stats* stats, int* status, int threads) {
     if (!hs || !x0_dev || !x_out || !status || n < 0) return 1;
-    run_parallel(n, threads, [&](int i) {
-        status[i] = sosb_solve_warm(hs[i], max_eval, tol, x0_dev[i], fallback_ss,
-                                    fallback_dev ? fallback_dev[i] : nullptr, x_out[i], x_out_is_device,
-                                    stats ? &stats[i] : nullptr);
-    });
-    for (int i = 0; i < n; ++i)
-        if (status[i]) return 3;
+    return batch_drive(hs, n, max_eval, tol, x0_dev, 1, true, fallback_ss, fallback_dev, x_out, x_out_is_device,
+                       stats, status, threads);
+}
+
+int sosb_set_autotune(sosb_handle s, int enable) {
+    if (!s) return 1;
+    graph_reset(s);
+    s->autotune = enable != 0;
+    return 0;
+}
+
+int sosb_set_graphs(sosb_handle s, int enable) {
+    if (!s) return 1;
+    graph_reset(s);
+    s->graphs = enable != 0;
     return 0;
 }
 

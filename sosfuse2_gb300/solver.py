@@ -70,6 +70,14 @@ class Kernel:
         (default on); off: every launch recomputes them."""
         self._check(self.lib.sosb_set_node_tables(self.h, int(bool(enable))))
 
+    def set_projection(self, mode):
+        """Projection form: 0 FP32 CUDA cores, 1 bf16x3, 2 TF32, 3 BF16 tensor cores."""
+        self._check(self.lib.sosb_set_projection(self.h, int(mode)))
+
+    def set_graphs(self, enable):
+        """Replay each solve's evaluations from a captured CUDA graph (default on)."""
+        self._check(self.lib.sosb_set_graphs(self.h, int(bool(enable))))
+
     def _check(self, rc):
         if rc:
             msg = self.lib.sosb_last_error(self.h).decode()
@@ -206,8 +214,9 @@ class Solver:
 
 
 class BatchSolver:
-    """Many independent states solved together (sosb_solve_batch): each state has its own handle and stream, and the
-    library's host threads run their fixed-point loops concurrently so the GPU overlaps their launches."""
+    """Many independent states solved together (sosb_solve_batch): each state has its own handle and stream; one
+    library thread replays an evaluation graph per active state each round, so the GPU overlaps their launches, and
+    reads their reports (`threads`: solves in flight, 0 all)."""
 
     def __init__(self, states, device=None):
         self.kernels = [Kernel(st, device) for st in states]
