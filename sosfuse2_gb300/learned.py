@@ -318,9 +318,10 @@ def solve_warm(solver, start, fallback, fallback_ss, max_eval=64, tolerance=1e-3
 
 
 # ---------------------------------------------------------------------------------------------------- drivers
-def generate(family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3, log=None):
+def generate(family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3, log=None, slow=24):
     """Training data from plain solves of family states: inputs X, targets Y (FP32 device), and per state the plain
-    evaluation count and the single-scattering start's first source relative change."""
+    evaluation count and the single-scattering start's first source relative change. States the plain solve does
+    not converge on, or needs more than `slow` evaluations for, are skipped (generate.skipped)."""
     import torch
 
     from .solver import Kernel, Solver
@@ -344,6 +345,10 @@ def generate(family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3, log=No
         except RuntimeError as exc:  # states the plain iteration does not converge on teach nothing: skip them
             if not str(exc).startswith('E_NOT_CONVERGED'):
                 raise
+            skipped.append(seed)
+            continue
+        if stats['evaluations'] > slow:
+            # a slowly contracting iteration stops (at the tolerance) further from its fixed point: noisy targets
             skipped.append(seed)
             continue
         g2 = solver.apply(g1)
@@ -373,7 +378,8 @@ def train_warm_start(family, n_train=512, epochs=30, seed=10000, device='cuda:0'
     losses = ws.train(X, Y, epochs=epochs, lr=1e-3, log=log)
     t2 = time.perf_counter()
     ws.fallback_ss = float(np.quantile(ss1, 0.9))
-    return ws, dict(train_solves=n_train, not_converged=len(generate.skipped), rows=int(X.shape[0]), generate_seconds=t1 - t0, train_seconds=t2 - t1,
+    return ws, dict(train_solves=n_train, skipped_not_converged_or_slow=len(generate.skipped), rows=int(X.shape[0]),
+                    generate_seconds=t1 - t0, train_seconds=t2 - t1,
                     plain_evaluations_mean=float(evals.mean()), loss_first=losses[0], loss_last=losses[-1],
                     fallback_ss=ws.fallback_ss, gemm_launches=ws.mlp.gemm_launches)
 
