@@ -819,6 +819,32 @@ __device__ __forceinline__ void sh_synth4_fixed(const float* Y, float cp, const 
 }
 #endif
 
+#if defined(__CUDACC__)
+// sh_contract_basis for a compile-time order L (lane = wavelength, plane row stride W): rows l are unrolled by
+// template recursion and the m of a row by a compile-time loop, so the per-m sums stay in registers and the loads
+// of a row are issued together (instead of one dependent load per step); each m sums its l in ascending order, as
+// sh_contract_basis does.
+template <int L, int l>
+struct ShWaveRow {
+    static __device__ __forceinline__ void run(const float* Y, const float* plane_cell, int wstride, float* acc) {
+#pragma unroll
+        for (int m = 0; m <= l; ++m) {
+            const int k = l * (l + 1) / 2 + m;
+            acc[m] += Y[k] * plane_cell[(size_t)k * wstride];
+        }
+        // (no ordering barrier: a memory clobber would keep acc in local memory)
+        if constexpr (l < L) ShWaveRow<L, l + 1>::run(Y, plane_cell, wstride, acc);
+    }
+};
+
+template <int L>
+__device__ __forceinline__ void sh_contract_wave(const float* Y, const float* plane_cell, int wstride, float* acc) {
+#pragma unroll
+    for (int m = 0; m <= L; ++m) acc[m] = 0.0f;
+    ShWaveRow<L, 0>::run(Y, plane_cell, wstride, acc);
+}
+#endif
+
 // Per-m sums of one cell from a shared basis (the cached form of sh_synth4).
 SOS_HD void sh_contract_basis(int L, const float* Y, const float* plane_cell, int wstride, float* cache, int cstride) {
     for (int m = 0; m <= L; ++m) {

@@ -882,6 +882,7 @@ static_assert(sizeof(TableRec) <= TREC_WORDS * 4, "table record exceeds its stri
 // Warm pass from the node table, many wavelengths: one warp per (ray, chunk of 32 wavelengths). Lane j rebuilds
 // node base+j's record into shared memory; then lane = wavelength walks the records in order with its 4-slot corner
 // SH cache (the operation order of transport_wave_kernel's warm branch).
+template <int LT>
 __global__ void __launch_bounds__(WAVE_WARPS * 32)
     transport_table_wave_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int wchunks,
                                 float4* rad) {
@@ -955,8 +956,16 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
                 used |= 1u << q;
                 slot_of[c] = q;
                 tag[q] = n.cell[c];
-                sh_contract_basis(o.L, Y, in.plane + (size_t)n.cell[c] * o.K * o.W + wl, o.W,
-                                  cache + (size_t)q * L1 * 32, 32);
+                if constexpr (LT > 0) {
+                    float acc[LT + 1];
+                    sh_contract_wave<LT>(Y, in.plane + (size_t)n.cell[c] * o.K * o.W + wl, o.W, acc);
+                    float* cq = cache + (size_t)q * L1 * 32;
+#pragma unroll
+                    for (int m = 0; m <= LT; ++m) cq[m * 32] = acc[m];
+                } else {
+                    sh_contract_basis(o.L, Y, in.plane + (size_t)n.cell[c] * o.K * o.W + wl, o.W,
+                                      cache + (size_t)q * L1 * 32, 32);
+                }
             }
             float aero[4];
             for (int c = 0; c < 4; ++c) aero[c] = azimuth_sum(o.L, n.cp, cache + (size_t)slot_of[c] * L1 * 32, 32);
@@ -1887,10 +1896,12 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
         const long long warps = (long long)nray * wchunks;
         const long long blocks = (warps + WAVE_WARPS - 1) / WAVE_WARPS;
         Timer timer(s, read ? K_TABLE : K_TRANSPORT);
-        if (read)
-            transport_table_wave_kernel<<<(unsigned)blocks, WAVE_WARPS * 32, table_wave_smem(d.L), s->stream>>>(
+        if (read) {
+            auto kernel = d.L == 16 ? transport_table_wave_kernel<16>
+                                    : (d.L == 32 ? transport_table_wave_kernel<32> : transport_table_wave_kernel<0>);
+            kernel<<<(unsigned)blocks, WAVE_WARPS * 32, table_wave_smem(d.L), s->stream>>>(
                 optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
-        else
+        } else
             transport_wave_kernel<<<(unsigned)blocks, WAVE_WARPS * 32, wave_smem(d.L), s->stream>>>(
                 optics_of(s), rays_of(b), in, write, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
     }
@@ -2149,7 +2160,9 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
     s->stream = s->own;
     {
         const size_t p_smem = project_smem((d.L + 1) * (d.L + 2) / 2, d.W);
-        if (cudaFuncSetAttribute(transport_table_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        auto wave_table = d.L == 16 ? transport_table_wave_kernel<16>
+                                    : (d.L == 32 ? transport_table_wave_kernel<32> : transport_table_wave_kernel<0>);
+        if (cudaFuncSetAttribute(wave_table, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)table_wave_smem(d.L)) != cudaSuccess ||
             cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_smem) !=
                 cudaSuccess ||
