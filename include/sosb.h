@@ -137,6 +137,11 @@ int sosb_set_graphs(sosb_handle h, int enable);
  * an untuned shape): 4 warps from 96 nodes per ray, 2 from 48, else 1. Summation order follows the choice, so runs
  * with autotuning may differ from runs without it by rounding. */
 int sosb_set_autotune(sosb_handle h, int enable);
+/* No reference counterpart (its sos_vprod stage, kernel.cu:4568, contracts the same pairs). Pair contractions
+ * (default on, more than four wavelengths): with the node tables, the distinct (ray, corner cell) pairs of each bundle
+ * are listed once, every evaluation contracts each pair's plane row with the ray's basis once (per m and wavelength),
+ * and the nodes add their azimuth series over the pair sums instead of each lane caching its corners. 0: off. */
+int sosb_set_pairs(sosb_handle h, int enable);
 /* Replaces: Kernel.setup (source_solver.py:1243-1339) and constants_device (source_solver.py:2248). */
 int sosb_set_constants(sosb_handle h, const sosb_constants *c);
 /* Replaces: ray_geometry.upload_geometry / device_geometry (ray_geometry.py:205-287) of the cell bundle

@@ -72,6 +72,7 @@ SIGNATURES = {
     'sosb_set_projection': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_graphs': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_autotune': ([ctypes.c_void_p, c_int], c_int),
+    'sosb_set_pairs': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_constants': ([ctypes.c_void_p, ctypes.POINTER(Constants)], c_int),
     'sosb_set_bundle': ([ctypes.c_void_p, c_int, ctypes.POINTER(Bundle)], c_int),
     'sosb_evaluate': ([ctypes.c_void_p, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

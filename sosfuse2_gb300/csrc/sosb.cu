@@ -52,6 +52,11 @@ struct BundleDev {
     // basis table of the tensor-core projection (BasisTable), built for projection mode b_mode (-1: none)
     DevBuf b_hi, b_lo;
     int b_mode = -1, b_kpad = 0, b_rpad = 0;
+    // ray-cell pairs (PairTable): valid with the node table unless they exceed the memory budget; host copies of the
+    // pair offsets at the ground-pass end and at the end
+    DevBuf p_off, p_cell, p_ray, p_node, y_tab;
+    bool p_valid = false;
+    int64_t p_ground = 0, p_total = 0;
 };
 
 // kernel classes timed by sosb_set_timing / sosb_get_timing
@@ -86,6 +91,7 @@ struct sosb_state {
     DevBuf fx, fg, norms, partials, dots;
     DevBuf ring_g[4], ring_f[4];
     DevBuf fl_val0, fl_coef, fl_dir, fl_g, fl_cnt, fl_off, fl_cursor, fl_entries;  // staged first light
+    DevBuf pair_A;  // per-m pair contractions of the current plane (PairTable::A), shared by the bundles
     bool have_first = false;
     bool tables = true;  // build and use node tables (sosb_set_node_tables)
     // fixed-point loop: evaluation control and report (device and pinned host copies), replayed evaluation graph
@@ -98,6 +104,7 @@ struct sosb_state {
     int64_t graph_launches = 0;
     bool graphs = true;  // replay evaluations from a captured CUDA graph (sosb_set_graphs)
     bool autotune = true;  // time the table launch shapes once per shape (sosb_set_autotune)
+    bool pairs = true;     // corner SH by ray-cell pair contractions (sosb_set_pairs)
     int proj_mode = 0;   // projection form (sosb_set_projection): PROJ_FP32, PROJ_BF16X3, PROJ_TF32, PROJ_BF16
     int64_t launches = 0;
 };
@@ -593,6 +600,103 @@ static size_t wave_smem(int L) {
     return sizeof(float) * (size_t)WAVE_WARPS * (32 * REC_WORDS + 4 * (L + 1) * 32 + (L + 1) * (L + 2) / 2);
 }
 
+// ------------------------------------------------------------------ ray-cell pairs
+// The corner SH contraction by (ray, corner cell) pair, the form of the reference's sos_vprod, for many wavelengths:
+// for every distinct corner cell a ray's nodes touch, A[pair][m][w] = sum_l Y_lm(ray) plane[cell][k(l, m)][w] once
+// per evaluation (pair_contract_wave_kernel), and each node then adds its azimuth series over
+// A[pair(node, corner)][m][w] (transport_pair_wave_kernel). Pairs, the ray basis table and each node's four pair
+// indices are geometry and are built with the node table. With one to four wavelengths the per-node synthesis of
+// transport_table_kernel is faster (config 0 warm launch 0.24 ms against 0.32 ms for pairs), so pairs serve W > 4
+// (30 wavelengths, L=32: warm launch 8.6 -> 6.5 ms, observer 1.9 -> 1.1 ms, ground 0.9 -> 0.25 ms).
+constexpr int PAIR_WINDOW = 16;  // recent distinct corner cells a ray's new corners are matched against
+
+struct PairTable {
+    const int* off;     // [nray + 1] first pair of each ray
+    const int* cell;    // [pairs] corner cell
+    const int* ray;     // [pairs] ray
+    const int4* node;   // [nodes] pair index of each corner
+    const float* y;     // [nray][kp] the ray's SH basis Y_k(mu) at azimuth 0
+    float* A;           // [pairs][L + 1][W] per-m contractions of the current plane
+};
+
+// One thread per ray: the corner cells of the ray's nodes in node and corner order, each new one a pair unless it
+// is among the ray's last PAIR_WINDOW pairs (a ray passes its cells in sequence, so this finds nearly every repeat;
+// a repeat it misses costs one extra pair, not a wrong value). Pass 0 counts them (cnt[ray]), pass 1 writes the
+// pairs and each node's four pair indices.
+__global__ void pair_build_kernel(Optics o, Rays b, NodeTable tab, int nq, int pass, int* cnt, const int* off,
+                                  int* p_cell, int* p_ray, int4* p_node) {
+    for (int ray = blockIdx.x * blockDim.x + threadIdx.x; ray < b.nray; ray += gridDim.x * blockDim.x) {
+        const int s0 = b.seg_off[ray];
+        const long long node0 = (long long)s0 * nq;
+        const int nn = (b.seg_off[ray + 1] - s0) * nq;
+        const int base = pass == 1 ? off[ray] : 0;
+        int win_cell[PAIR_WINDOW], win_idx[PAIR_WINDOW];
+        int nwin = 0, head = 0, n = 0;
+        for (int i = 0; i < nn; ++i) {
+            const float4 ms = tab.misc[node0 + i];
+            const int pk = __float_as_int(ms.w);
+            const int cell0 = (pk >> 16) * o.nc + (pk & 0xffff);
+            int idx[4];
+            for (int c = 0; c < 4; ++c) {
+                const int cell = cell0 + (c & 1) + (c >> 1) * o.nc;
+                int f = -1;
+                for (int u = 0; u < nwin; ++u)
+                    if (win_cell[u] == cell) {
+                        f = win_idx[u];
+                        break;
+                    }
+                if (f < 0) {
+                    f = n++;
+                    win_cell[head] = cell;
+                    win_idx[head] = f;
+                    head = (head + 1) % PAIR_WINDOW;
+                    nwin = min(nwin + 1, PAIR_WINDOW);
+                    if (pass == 1) {
+                        p_cell[base + f] = cell;
+                        p_ray[base + f] = ray;
+                    }
+                }
+                idx[c] = f;
+            }
+            if (pass == 1) p_node[node0 + i] = make_int4(base + idx[0], base + idx[1], base + idx[2], base + idx[3]);
+        }
+        if (pass == 0) cnt[ray] = n;
+    }
+}
+
+// One warp per ray: its basis row into the table (lane m computes column m).
+__global__ void pair_basis_kernel(Optics o, Rays b, int kp, float* y_tab) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= b.nray) return;
+    const float4 d = b.dir[warp];
+    for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, d.z, d.w, m, y_tab + (size_t)warp * kp);
+}
+
+// Many wavelengths (plane [cell][K][W]): one warp per (pair, chunk of 32 wavelengths), lane = wavelength.
+template <int LT>
+__global__ void pair_contract_wave_kernel(Optics o, PairTable pt, const float* __restrict__ plane, int p0, int np,
+                                          int kp, int wchunks) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= (long long)np * wchunks) return;
+    const int p = p0 + (int)(warp / wchunks);
+    const int w = (int)(warp % wchunks) * 32 + lane;
+    if (w >= o.W) return;
+    const int W = o.W, L1 = o.L + 1;
+    const float* Y = pt.y + (size_t)pt.ray[p] * kp;
+    const float* P = plane + (size_t)pt.cell[p] * o.K * W + w;
+    float* out = pt.A + (size_t)p * L1 * W + w;
+    if constexpr (LT > 0) {
+        float acc[LT + 1];
+        sh_contract_wave<LT>(Y, P, W, acc);
+#pragma unroll
+        for (int m = 0; m <= LT; ++m) out[(size_t)m * W] = acc[m];
+    } else {
+        sh_contract_basis(o.L, Y, P, W, out, W);
+    }
+}
+
 // ------------------------------------------------------------------ staged first light (W <= 4)
 // Corner pair pr of a node (cells (ir + pr, j) and (ir + pr, j + 1)): its first cell, the key of its bucket.
 __device__ __forceinline__ int pair_cell(const Optics& o, float4 ms, int pr) {
@@ -977,6 +1081,83 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
     if (wok) {
         boundary_term(o, b, rc, in.boundary, ray, w, total);
         rad[(size_t)ray * o.W + w] = make_float4(total[0], total[1], total[2], total[3]);
+    }
+}
+
+// Warm pass from the node table and the pair contractions, many wavelengths: one warp per (ray, chunk of 32
+// wavelengths); lane j rebuilds node base+j's record (with its four pair indices) into shared memory, then lane =
+// wavelength walks the records in order reading the per-m contractions of its corner pairs (coalesced over lanes).
+constexpr int PREC_WORDS = 31;  // TableRec + 4 pair indices, odd stride
+constexpr int PAIR_WAVE_WARPS = 4;
+
+__global__ void __launch_bounds__(PAIR_WAVE_WARPS * 32)
+    transport_pair_wave_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, PairTable pt, int ray0, int nray,
+                               int wchunks, float4* rad) {
+    __shared__ float recs_all[PAIR_WAVE_WARPS][32 * PREC_WORDS];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const long long warp = (long long)blockIdx.x * PAIR_WAVE_WARPS + wid;
+    if (warp >= (long long)nray * wchunks) return;  // the whole warp leaves together
+    const int ray = ray0 + (int)(warp / wchunks);
+    const int w = (int)(warp % wchunks) * 32 + lane;
+    const bool wok = w < o.W;
+    const int wl = wok ? w : o.W - 1;  // idle lanes compute a valid wavelength and store nothing
+    const int W = o.W, L1 = o.L + 1;
+    float* recs = recs_all[wid];
+    RayConst rc;
+    ray_constants(b, ray, rc);
+    const int nq = in.nq;
+    const int s0 = b.seg_off[ray];
+    const long long node0 = (long long)s0 * nq;
+    const int nn = (b.seg_off[ray + 1] - s0) * nq;
+    float total[4] = {0, 0, 0, 0}, comp[4] = {0, 0, 0, 0};
+    for (int base = 0; base < nn; base += 32) {
+        const int i = base + lane;
+        const int cnt = min(32, nn - base);
+        __syncwarp();
+        if (i < nn) {
+            TableRec* R = reinterpret_cast<TableRec*>(recs + lane * PREC_WORDS);
+            Node n;
+            table_node(o, rc, tab, node0 + i, n);
+            for (int k = 0; k < 4; ++k)
+                for (int u = 0; u < 4; ++u) R->T[4 * k + u] = n.T[k][u];
+            for (int c = 0; c < 4; ++c) {
+                R->sw[c] = n.sw[c];
+                R->cell[c] = n.cell[c];
+            }
+            R->ir = n.ir;
+            R->cp = n.cp;
+            const int4 pn = pt.node[node0 + i];
+            int* pr = reinterpret_cast<int*>(recs + lane * PREC_WORDS + TREC_WORDS);
+            pr[0] = pn.x;
+            pr[1] = pn.y;
+            pr[2] = pn.z;
+            pr[3] = pn.w;
+        }
+        __syncwarp();
+        for (int j = 0; j < cnt; ++j) {
+            const TableRec* R = reinterpret_cast<const TableRec*>(recs + j * PREC_WORDS);
+            const int* pr = reinterpret_cast<const int*>(recs + j * PREC_WORDS + TREC_WORDS);
+            const float att = tab.att[(node0 + base + j) * W + wl];
+            Node n;
+            for (int k = 0; k < 4; ++k)
+                for (int u = 0; u < 4; ++u) n.T[k][u] = R->T[4 * k + u];
+            for (int c = 0; c < 4; ++c) {
+                n.sw[c] = R->sw[c];
+                n.cell[c] = R->cell[c];
+            }
+            n.ir = R->ir;
+            n.cp = R->cp;
+            float aero[4];
+            for (int c = 0; c < 4; ++c) aero[c] = azimuth_sum(o.L, n.cp, pt.A + (size_t)pr[c] * L1 * W + wl, W);
+            float val[4];
+            warm_value(o, rc, n, in.field, wl, aero, val);
+            for (int k = 0; k < 4; ++k) kahan(total[k], comp[k], val[k] * att);
+        }
+    }
+    if (wok) {
+        boundary_term(o, b, rc, in.boundary, ray, w, total);
+        rad[(size_t)ray * W + w] = make_float4(total[0], total[1], total[2], total[3]);
     }
 }
 
@@ -1696,9 +1877,62 @@ static TableKernel table_kernel_for(int W, int L) {
 // Row length of the padded plane layout (W <= 4), 0 for the wavelength-fastest layout of the wave kernels.
 static int plane_kp(const sosb_state* s) { return s->d.W <= 4 ? (s->K + 3) & ~3 : 0; }
 
-static void invalidate_tables(BundleDev& b) {
+// Node tables hold the optics (attenuation) and must be rebuilt when the constants change; the ray-cell pairs are
+// geometry only and survive new constants (`geometry` false).
+static void invalidate_tables(BundleDev& b, bool geometry = true) {
     b.t_valid = false;
     b.t_too_big = false;
+    if (geometry) b.p_valid = false;
+}
+
+// Ray-cell pairs of bundle b from its node table (geometry only): per-ray counts, offsets, the pairs, each node's
+// four pair indices and the ray basis table. Pairs over half the free memory leave the bundle on per-node synthesis.
+static int build_pairs(sosb_state* s, BundleDev& b, int nq) {
+    b.p_valid = false;
+    if (!s->pairs || b.nray == 0 || s->d.W <= 4) return 0;
+    const sosb_dims& d = s->d;
+    const int64_t nray = b.nray;
+    const size_t nodes = (size_t)b.nseg * nq;
+    const int kp = (s->K + 3) & ~3;
+    DevBuf cnt, cursor;
+    TRY(dalloc(s, cnt, (size_t)(nray + 1) * sizeof(int)));
+    TRY(dalloc(s, cursor, (size_t)(nray + 1) * sizeof(int)));
+    TRY(dalloc(s, b.p_off, (size_t)(nray + 1) * sizeof(int)));
+    const NodeTable tab{P<float4>(b.t_frame), P<float4>(b.t_misc), P<float>(b.t_att)};
+    const int blocks = grid_for(nray, 128);
+    pair_build_kernel<<<blocks, 128, 0, s->stream>>>(optics_of(s), rays_of(b), tab, nq, 0, P<int>(cnt), nullptr,
+                                                     nullptr, nullptr, nullptr);
+    TRY(launch_check(s));
+    bucket_scan_kernel<<<1, 1024, 0, s->stream>>>(P<int>(cnt), (int)nray, P<int>(b.p_off), P<int>(cursor));
+    TRY(launch_check(s));
+    int total = 0, ground = 0;
+    CK(cudaMemcpyAsync(&total, P<int>(b.p_off) + nray, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    const int64_t r_gnd = (int64_t)b.host_cell_off.size() > d.nc ? b.host_cell_off[d.nc] : 0;
+    CK(cudaMemcpyAsync(&ground, P<int>(b.p_off) + r_gnd, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    TRY(dfree(s, cnt));
+    TRY(dfree(s, cursor));
+    const size_t a_bytes = (size_t)total * (d.L + 1) * d.W * sizeof(float);
+    const size_t need = (size_t)total * 8 + nodes * sizeof(int4) + (size_t)nray * kp * sizeof(float) +
+                        (a_bytes > s->pair_A.bytes ? a_bytes - s->pair_A.bytes : 0);
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if (need > free_b / 2) return 0;
+    TRY(dalloc(s, b.p_cell, std::max<size_t>(total, 1) * sizeof(int)));
+    TRY(dalloc(s, b.p_ray, std::max<size_t>(total, 1) * sizeof(int)));
+    TRY(dalloc(s, b.p_node, std::max<size_t>(nodes, 1) * sizeof(int4)));
+    TRY(dalloc(s, b.y_tab, (size_t)nray * kp * sizeof(float)));
+    TRY(dalloc(s, s->pair_A, std::max<size_t>(a_bytes, 16)));
+    pair_build_kernel<<<blocks, 128, 0, s->stream>>>(optics_of(s), rays_of(b), tab, nq, 1, nullptr, P<int>(b.p_off),
+                                                     P<int>(b.p_cell), P<int>(b.p_ray), P<int4>(b.p_node));
+    TRY(launch_check(s));
+    pair_basis_kernel<<<(unsigned)((nray * 32 + 127) / 128), 128, 0, s->stream>>>(optics_of(s), rays_of(b), kp,
+                                                                                 P<float>(b.y_tab));
+    TRY(launch_check(s));
+    b.p_total = total;
+    b.p_ground = ground;
+    b.p_valid = true;
+    return 0;
 }
 
 // ------------------------------------------------------------------------------------------------ autotuner
@@ -1709,20 +1943,20 @@ static void invalidate_tables(BundleDev& b) {
 // depend on which candidate ran last.
 struct TuneKey {
     int64_t nray, nseg;
-    int nq, W, L, ns;
+    int nq, W, L, ns, kind;  // kind: 0 table kernel, 1 pair kernel
     bool operator<(const TuneKey& o) const {
-        return std::tie(nray, nseg, nq, W, L, ns) < std::tie(o.nray, o.nseg, o.nq, o.W, o.L, o.ns);
+        return std::tie(nray, nseg, nq, W, L, ns, kind) < std::tie(o.nray, o.nseg, o.nq, o.W, o.L, o.ns, o.kind);
     }
 };
 static std::mutex g_tune_lock;
 static std::map<TuneKey, int> g_tuned;
 
 template <class Launch>
-static int tuned_wpr(sosb_state* s, const BundleDev& b, int nq, int64_t nray, Launch launch, int& wpr) {
+static int tuned_wpr(sosb_state* s, const BundleDev& b, int nq, int64_t nray, int kind, Launch launch, int& wpr) {
     const double mean_nodes = (double)b.nseg * nq / std::max<int64_t>(b.nray, 1);
     wpr = mean_nodes >= 96.0 ? 4 : (mean_nodes >= 48.0 ? 2 : 1);
     if (!s->autotune) return 0;
-    const TuneKey key{nray, b.nseg, nq, s->d.W, s->d.L, s->ns};
+    const TuneKey key{nray, b.nseg, nq, s->d.W, s->d.L, s->ns, kind};
     {
         std::lock_guard<std::mutex> guard(g_tune_lock);
         auto it = g_tuned.find(key);
@@ -1829,6 +2063,7 @@ static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs&
                                                                                           P<float4>(s->rad));
     TRY(launch_check(s));
     b.t_valid = true;
+    if (!b.p_valid) TRY(build_pairs(s, b, in.nq));
     done = true;
     return 0;
 }
@@ -1882,7 +2117,7 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
                                                                                  P<float4>(s->rad));
             };
             int wpr = 0;
-            TRY(tuned_wpr(s, b, in.nq, nray, launch, wpr));
+            TRY(tuned_wpr(s, b, in.nq, nray, 0, launch, wpr));
             launch(wpr);
         } else if (d.W == 1)
             transport_warp_kernel<1, false><<<(unsigned)blocks, TRANSPORT_THREADS, smem, s->stream>>>(
@@ -1896,7 +2131,29 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
         const long long warps = (long long)nray * wchunks;
         const long long blocks = (warps + WAVE_WARPS - 1) / WAVE_WARPS;
         Timer timer(s, read ? K_TABLE : K_TRANSPORT);
-        if (read) {
+        const bool ground_launch = b.host_cell_off.size() > (size_t)d.nc && nray == b.host_cell_off[d.nc];
+        const int64_t np_launch = nray == b.nray ? b.p_total : (ground_launch ? b.p_ground : -1);
+        if (read && b.p_valid && np_launch >= 0) {
+            const PairTable pt{P<int>(b.p_off), P<int>(b.p_cell), P<int>(b.p_ray), P<int4>(b.p_node),
+                               P<float>(b.y_tab), P<float>(s->pair_A)};
+            const int kp = (s->K + 3) & ~3;
+            if (np_launch > 0) {
+                const unsigned cg = (unsigned)((np_launch * wchunks * 32 + 127) / 128);
+                if (d.L == 16)
+                    pair_contract_wave_kernel<16><<<cg, 128, 0, s->stream>>>(optics_of(s), pt, in.plane, 0,
+                                                                             (int)np_launch, kp, wchunks);
+                else if (d.L == 32)
+                    pair_contract_wave_kernel<32><<<cg, 128, 0, s->stream>>>(optics_of(s), pt, in.plane, 0,
+                                                                             (int)np_launch, kp, wchunks);
+                else
+                    pair_contract_wave_kernel<0><<<cg, 128, 0, s->stream>>>(optics_of(s), pt, in.plane, 0,
+                                                                            (int)np_launch, kp, wchunks);
+                TRY(launch_check(s));
+            }
+            const unsigned pb = (unsigned)((warps + PAIR_WAVE_WARPS - 1) / PAIR_WAVE_WARPS);
+            transport_pair_wave_kernel<<<pb, PAIR_WAVE_WARPS * 32, 0, s->stream>>>(
+                optics_of(s), rays_of(b), in, table, pt, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
+        } else if (read) {
             auto kernel = d.L == 16 ? transport_table_wave_kernel<16>
                                     : (d.L == 32 ? transport_table_wave_kernel<32> : transport_table_wave_kernel<0>);
             kernel<<<(unsigned)blocks, WAVE_WARPS * 32, table_wave_smem(d.L), s->stream>>>(
@@ -1906,7 +2163,10 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
                 optics_of(s), rays_of(b), in, write, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
     }
     TRY(launch_check(s));
-    if (write.frame) b.t_valid = true;
+    if (write.frame) {
+        b.t_valid = true;
+        if (!b.p_valid) TRY(build_pairs(s, b, in.nq));
+    }
     return 0;
 }
 
@@ -2204,12 +2464,13 @@ int sosb_destroy(sosb_handle s) {
                       &s->fg, &s->norms, &s->partials, &s->dots, &s->ctrl_dev, &s->report_dev, &s->ring_g[0],
                       &s->ring_g[1], &s->ring_g[2], &s->ring_g[3], &s->ring_f[0], &s->ring_f[1], &s->ring_f[2],
                       &s->ring_f[3], &s->fl_val0, &s->fl_coef, &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off,
-                      &s->fl_cursor, &s->fl_entries};
+                      &s->fl_cursor, &s->fl_entries, &s->pair_A};
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
                         &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits,
-                        &bd->t_frame, &bd->t_misc, &bd->t_att, &bd->b_hi, &bd->b_lo};
+                        &bd->t_frame, &bd->t_misc, &bd->t_att, &bd->b_hi, &bd->b_lo, &bd->p_off, &bd->p_cell,
+                        &bd->p_ray, &bd->p_node, &bd->y_tab};
         for (DevBuf* b : bb) dfree(s, *b);
     }
     collect_timing(s);
@@ -2386,8 +2647,8 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
     CK(cudaStreamSynchronize(s->stream));
     s->have_constants = true;
     s->have_first = false;
-    invalidate_tables(s->cells);
-    invalidate_tables(s->obs);
+    invalidate_tables(s->cells, false);
+    invalidate_tables(s->obs, false);
     graph_reset(s);
     return 0;
 }
@@ -2999,6 +3260,15 @@ int sosb_solve_warm_batch(sosb_handle* hs, int n, int max_eval, double tol, cons
     if (!hs || !x0_dev || !x_out || !status || n < 0) return 1;
     return batch_drive(hs, n, max_eval, tol, x0_dev, 1, true, fallback_ss, fallback_dev, x_out, x_out_is_device,
                        stats, status, threads);
+}
+
+int sosb_set_pairs(sosb_handle s, int enable) {
+    if (!s) return 1;
+    s->pairs = enable != 0;
+    invalidate_tables(s->cells);
+    invalidate_tables(s->obs);
+    graph_reset(s);
+    return 0;
 }
 
 int sosb_set_autotune(sosb_handle s, int enable) {

@@ -18,13 +18,14 @@ CASES = {
 }
 
 
-def _run(arrays, tables):
+def _run(arrays, tables, pairs=True):
     from sosfuse2_gb300.solver import Solver
     from sosfuse2_gb300.state import PackedState
 
     solver = Solver(PackedState(dict(arrays)), device='cuda:0')
     k = solver.kernel
     k.set_node_tables(tables)
+    k._check(k.lib.sosb_set_pairs(k.h, int(pairs)))
     x = k.field(np.zeros(solver.state.shape, np.float32))
     out = []
     for _ in range(2):                      # the first pass over each bundle builds the table, the second reads it
@@ -47,6 +48,18 @@ def test_tables_match_recompute(case):
     arrays = small_state(**CASES[case])
     on = _run(arrays, True)
     off = _run(arrays, False)
+    for i, (a, b) in enumerate(zip(on, off)):
+        ok, rel = _close(a, b)
+        assert ok, (case, i, rel)
+
+
+@pytest.mark.parametrize('case', sorted(CASES))
+def test_pairs_match_node_synthesis(case):
+    """Corner SH from the per-pair contractions (W > 4) against the per-lane corner cache (same sums); with W <= 4
+    pairs are not used and both runs take the per-node synthesis."""
+    arrays = small_state(**CASES[case])
+    on = _run(arrays, True, pairs=True)
+    off = _run(arrays, True, pairs=False)
     for i, (a, b) in enumerate(zip(on, off)):
         ok, rel = _close(a, b)
         assert ok, (case, i, rel)
