@@ -1566,41 +1566,35 @@ __global__ void boxes_kernel(const float4* __restrict__ rad, const double* __res
     out[i] = s * solar[w];
 }
 
-// Norm of each cell's source per wavelength, ||g[cell, :, w]||_2, one warp per cell: lanes split the slots
-// (kk = lane / Wc) and the wavelengths (lane % Wc, Wc = min(W, 32)), so the loads of a warp are contiguous; the kk
-// partial sums of a wavelength are added in lane order. mx[w] collects the maximum norm (bits of a non-negative
-// float order as unsigned integers).
-constexpr int NORM_WARPS = 8;
-
-__global__ void __launch_bounds__(NORM_WARPS * 32)
-    norm_kernel(const float* __restrict__ g, int ns, int src, int W, float* __restrict__ norms,
-                unsigned* __restrict__ mx) {
-    __shared__ float part[NORM_WARPS][32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int Wc = min(W, 32), KL = 32 / Wc;
-    const int wl = lane % Wc, kk = lane / Wc;
-    for (long long cell = (long long)blockIdx.x * NORM_WARPS + wid; cell < ns;
-         cell += (long long)gridDim.x * NORM_WARPS) {
+// Norm of each cell's source per wavelength, ||g[cell, :, w]||_2, one block per cell: the block size is a multiple
+// of W, thread t keeps wavelength t % W and, as member t / W of its wavelength's group of G, sums the squares of
+// the slots k = member, member + G, ... (contiguous loads across the block); the members' sums are added by a
+// pairwise tree in member order. mx[w] collects the maximum norm (bits of a non-negative float order as unsigned
+// integers).
+__global__ void norm_kernel(const float* __restrict__ g, long long ns, int src, int W, float* __restrict__ norms,
+                            unsigned* __restrict__ mx) {
+    extern __shared__ float part[];  // [blockDim.x]
+    const int B = blockDim.x, t = threadIdx.x;
+    const int w = t % W, G = B / W, mem = t / W;
+    for (long long cell = blockIdx.x; cell < ns; cell += gridDim.x) {
         const float* row = g + (size_t)cell * src * W;
-        for (int w0 = 0; w0 < W; w0 += 32) {
-            const int w = w0 + wl;
-            float acc = 0.0f;
-            if (kk < KL && w < W)
-                for (int k = kk; k < src; k += KL) {
-                    const float v = row[(size_t)k * W + w];
-                    acc += v * v;
-                }
-            part[wid][lane] = acc;
-            __syncwarp();
-            if (lane < Wc && w < W) {  // here wl == lane and kk == 0
-                float t = 0.0f;
-                for (int q = 0; q < KL; ++q) t += part[wid][q * Wc + lane];
-                const float nv = sqrtf(t);
-                norms[cell * W + w] = nv;
-                atomicMax(&mx[w], __float_as_uint(nv));
-            }
-            __syncwarp();
+        float acc = 0.0f;
+        for (int k = mem; k < src; k += G) {
+            const float v = row[(size_t)k * W + w];
+            acc += v * v;
         }
+        part[t] = acc;
+        __syncthreads();
+        for (int h = 1; h < G; h <<= 1) {
+            if ((mem & (2 * h - 1)) == 0 && mem + h < G) part[t] += part[t + h * W];
+            __syncthreads();
+        }
+        if (mem == 0) {
+            const float nv = sqrtf(part[w]);
+            norms[cell * W + w] = nv;
+            atomicMax(&mx[w], __float_as_uint(nv));
+        }
+        __syncthreads();
     }
 }
 
@@ -1624,9 +1618,9 @@ struct Ring4 {
 
 // Residual feature f = (g - x) / max(norm, 1e-8 max norm) into ring slot ctrl->slot, and FP64 partial dots of f
 // with the ring slots ctrl->order[0 .. m-1] (the new slot among them): partials[block][j][w]. Blocks walk whole
-// cells; the block size is a multiple of W, so thread t keeps wavelength t % W over all its elements, and the
-// per-thread sums of a wavelength are added by a pairwise tree in thread order (no atomics: the dots are
-// reproducible run to run).
+// cells; the block size is a multiple of W, so thread t keeps wavelength t % W over all its elements (FP32 products
+// in compensated FP32 sums), and the per-thread sums of a wavelength are added in FP64 by a pairwise tree in thread
+// order (no atomics: the dots are reproducible run to run).
 __global__ void feature_kernel(const float* __restrict__ g, const float* __restrict__ x,
                                const float* __restrict__ norms, const unsigned* __restrict__ mx, long long ns, int src,
                                int W, Ring4 ring, const EvalCtrl* __restrict__ ctrl, double* __restrict__ partials) {
@@ -1640,7 +1634,8 @@ __global__ void feature_kernel(const float* __restrict__ g, const float* __restr
     const float* rj[4];
     for (int j = 0; j < 4; ++j) rj[j] = ring.p[ctrl->order[j & 3]];
     const float floor_w = __uint_as_float(mx[w]) * 1e-8f;
-    double loc[4] = {0.0, 0.0, 0.0, 0.0};
+    // per-thread dots in compensated FP32 (FP32 products, Kahan sums), combined in FP64 below
+    float loc[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lcm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (long long cell = blockIdx.x; cell < ns; cell += gridDim.x) {
         const float scale = fmaxf(norms[cell * W + w], floor_w);
         const size_t base = (size_t)cell * row;
@@ -1650,11 +1645,11 @@ __global__ void feature_kernel(const float* __restrict__ g, const float* __restr
             dst[i] = f;
             for (int j = 0; j < nslot; ++j) {
                 const float o = (rj[j] == dst) ? f : rj[j][i];
-                loc[j] += (double)f * (double)o;
+                kahan(loc[j], lcm[j], f * o);
             }
         }
     }
-    for (int j = 0; j < 4; ++j) sd[t * 4 + j] = loc[j];
+    for (int j = 0; j < 4; ++j) sd[t * 4 + j] = (double)loc[j] - (double)lcm[j];
     __syncthreads();
     // thread t is member t / W of its wavelength's group of G = B / W; pairwise tree over the members
     const int G = B / W, mem = t / W;
@@ -2899,9 +2894,9 @@ static int eval_body(sosb_state* s) {
     TRY(launch_check(s));
     {
         Timer t(s, K_ANDERSON);
-        norm_kernel<<<(unsigned)std::min<long long>((s->ns + NORM_WARPS - 1) / NORM_WARPS, 152LL * 16),
-                      NORM_WARPS * 32, 0, s->stream>>>(g, s->ns, s->src, W, P<float>(s->norms),
-                                                       P<unsigned>(s->metrics));
+        norm_kernel<<<(unsigned)std::min<long long>(s->ns, 152LL * 16), s->feat_threads,
+                      (size_t)s->feat_threads * sizeof(float), s->stream>>>(g, (long long)s->ns, s->src, W,
+                                                                            P<float>(s->norms), P<unsigned>(s->metrics));
     }
     TRY(launch_check(s));
     {
