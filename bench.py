@@ -50,6 +50,8 @@ def args_():
     p.add_argument('--seed', type=int, default=0)
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--no-forms', action='store_true', help='plain single-state solve only')
+    p.add_argument('--precision-only', action='store_true',
+                   help='only the precision form (projection forms on a 30-wavelength state), one JSON line')
     p.add_argument('--batch', type=int, default=64, help='states per batched step')
     p.add_argument('--train-solves', type=int, default=512)
     p.add_argument('--epochs', type=int, default=30)
@@ -372,6 +374,10 @@ def run_gb300(a, rank, world):
     local = int(os.environ.get('LOCAL_RANK', 0))
     torch.cuda.set_device(local)
     device = f'cuda:{local}'
+    if a.precision_only:
+        if rank == 0:
+            print(json.dumps(dict(precision=_precision_form(device))), flush=True)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist  # noqa: F811

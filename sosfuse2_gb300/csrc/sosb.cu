@@ -439,9 +439,10 @@ SOS_HD void profile6(const Optics& o, const RayConst& rc, DS t, float* p6) {
 // 4-slot corner SH cache in shared memory.
 constexpr int WAVE_WARPS = 2;
 
+template <bool PREP>
 __global__ void __launch_bounds__(WAVE_WARPS * 32)
-    transport_wave_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, int ray0, int nray, int wchunks,
-                          float4* rad) {
+    transport_wave_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, FirstLightBufs fl, int ray0, int nray,
+                          int wchunks, float4* rad) {
     extern __shared__ float wave_sm[];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -491,6 +492,7 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
                 tab.frame[id] = make_float4(n.fr[0], n.fr[1], n.fr[2], n.fr[3]);
                 tab.misc[id] = table_misc(n);
             }
+            if (PREP) fl.dir[(long long)s0 * nq + i] = make_float4(n.mu, n.exd, fabsf(n.eyd), 0.0f);
             R->r_h = n.r.h; R->r_l = n.r.l; R->qz_h = n.qz.h; R->qz_l = n.qz.l; R->h = n.h; R->ds = n.ds;
             R->cp = n.cp; R->mu = n.mu; R->exd = n.exd; R->eyd = n.eyd; R->st_prof = n.st_prof;
             for (int c = 0; c < 4; ++c) { R->sw[c] = n.sw[c]; R->cell[c] = n.cell[c]; }
@@ -555,7 +557,15 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
                 for (int u = 0; u < 4; ++u) n.T[k][u] = R->T[4 * k + u];
             for (int k = 0; k < 5; ++k) n.prof.v[k] = R->prof[k];
             float val[4];
-            if (first) {
+            if (PREP) {
+                // staged first light: the value without its ground-scattered part, and the ground-sum factors
+                first_light_value(o, rc, n, wl, phase, sphase, 0.0f, 0.0f, val);
+                if (wok) {
+                    const long long id = ((long long)s0 * nq + base + j) * o.W + w;
+                    fl.val0[id] = make_float4(val[0], val[1], val[2], val[3]);
+                    fl.coef[id] = make_float2(n.prof.v[1] * o.asca[w], o.strato ? n.st_prof * o.strato_sca[w] : 0.0f);
+                }
+            } else if (first) {
                 first_light_value(o, rc, n, wl, phase, sphase, val);
             } else {
                 int slot_of[4];
@@ -590,7 +600,7 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
             }
         }
     }
-    if (wok) {
+    if (wok && !PREP) {
         boundary_term(o, b, rc, in.boundary, ray, w, total);
         rad[(size_t)ray * o.W + w] = make_float4(total[0], total[1], total[2], total[3]);
     }
@@ -885,6 +895,92 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
             rad[(size_t)ray * W + w] = make_float4(v[0], v[1], v[2], v[3]);
         }
     }
+}
+
+// Ground sums of the bucketed pairs, many wavelengths: one thread per (pair, wavelength), wavelengths fastest, so the
+// lanes of a warp share a pair (or two of one bucket) and run the same direction loop; each recomputes the pair's
+// phases (the arithmetic of ground_pairs_kernel) and adds its own wavelength's ground values and table phase.
+__global__ void __launch_bounds__(256)
+    ground_pairs_wave_kernel(Optics o, const float4* __restrict__ misc, const float4* __restrict__ dir,
+                             const int* __restrict__ entries, const int* __restrict__ total, float2* g) {
+    const int W = o.W;
+    const long long n_items = (long long)(*total) * W;
+    const HgPair hk = hg_pair_constants(o.g);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n_items;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int code = entries[t / W];
+        const int w = (int)(t % W);
+        const long long node = code >> 1;
+        const int pr = code & 1;
+        const float4 ms = misc[node];
+        const float4 dv = dir[node];
+        const float ah = ms.x, ac = ms.y;
+        const float wa = pr ? ah * (1.0f - ac) : (1.0f - ah) * (1.0f - ac);
+        const float wb = pr ? ah * ac : (1.0f - ah) * ac;
+        const int ca = pair_cell(o, ms, pr), cb = ca + 1;
+        const bool merged = o.gsame != nullptr && o.gsame[ca] != 0;
+        float ground = 0.0f, sground = 0.0f;
+        for (int side = 0; side < (merged ? 1 : 2); ++side) {
+            const int cell = side ? cb : ca;
+            const float wc = side ? wb : wa;
+            const int g0 = o.goff[cell], g1 = o.goff[cell + 1];
+            const int shift = merged ? o.goff[cb] - g0 : 0;
+            for (int gi = g0; gi < g1; ++gi) {
+                const float4 gd = o.gdir4[gi];
+                const float m0 = dv.x * gd.z + dv.y * gd.x;
+                const float m1 = dv.z * gd.y;
+                const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
+                float gv = wc * o.gval[(size_t)gi * W + w];
+                if (merged) gv += wb * o.gval[(size_t)(gi + shift) * W + w];
+                ground += hg_pair(hk, up, dn) * gv;
+                if (o.strato) {
+                    int iu, id;
+                    float fu, fd;
+                    strato_lut_pos_clamped(up, iu, fu);
+                    strato_lut_pos_clamped(dn, id, fd);
+                    const float sph = (strato_lut_at(o, iu, fu, w) + strato_lut_at(o, id, fd, w)) * 0.5f;
+                    sground += sph * gv;
+                }
+            }
+        }
+        g[((size_t)node * 2 + pr) * W + w] = make_float2(ground, sground);
+    }
+}
+
+// Per-ray sum of the staged first light, many wavelengths: one warp per (ray, chunk of 32 wavelengths), lane =
+// wavelength walking the ray's nodes in order (the Kahan order of transport_wave_kernel).
+__global__ void __launch_bounds__(128)
+    first_light_sum_wave_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, FirstLightBufs fl, int ray0,
+                                int nray, int wchunks, float4* rad) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= (long long)nray * wchunks) return;  // the whole warp leaves together
+    const int ray = ray0 + (int)(warp / wchunks);
+    const int w = (int)(warp % wchunks) * 32 + lane;
+    if (w >= o.W) return;
+    const int W = o.W;
+    RayConst rc;
+    ray_constants(b, ray, rc);
+    const int s0 = b.seg_off[ray];
+    const long long node0 = (long long)s0 * in.nq;
+    const int nn = (b.seg_off[ray + 1] - s0) * in.nq;
+    float total[4] = {0, 0, 0, 0}, comp[4] = {0, 0, 0, 0};
+    for (int i = 0; i < nn; ++i) {
+        const long long id = node0 + i;
+        const float att = tab.att[id * W + w];
+        const float4 v0 = fl.val0[id * W + w];
+        const float2 cf = fl.coef[id * W + w];
+        const float2 g0 = fl.g[(size_t)id * 2 * W + w], g1 = fl.g[((size_t)id * 2 + 1) * W + w];
+        const float ga = cf.x * (g0.x + g1.x), gs = cf.y * (g0.y + g1.y);
+        const float val[4] = {v0.x, v0.y, v0.z, v0.w};
+        for (int k = 0; k < 4; ++k) {
+            float v = val[k] + ga * rc.pu[k] / 2.0f;
+            if (o.strato) v += (gs * rc.pu[k]) / 2.0f;
+            kahan(total[k], comp[k], v * att);
+        }
+    }
+    boundary_term(o, b, rc, in.boundary, ray, w, total);
+    rad[(size_t)ray * W + w] = make_float4(total[0], total[1], total[2], total[3]);
 }
 
 // Warm pass from the node table, few wavelengths (W <= WM): `wpr` warps (1, 2 or 4) per ray, lane l of warp q takes
@@ -1994,8 +2090,8 @@ static int tuned_wpr(sosb_state* s, const BundleDev& b, int nq, int64_t nray, in
     return 0;
 }
 
-// Staged first light of the whole cell bundle (W <= 4; FirstLightBufs). Returns 0 with `done` false when the
-// scratch does not fit, leaving the single-launch path to the caller.
+// Staged first light of the whole cell bundle (FirstLightBufs). Returns 0 with `done` false when the scratch does
+// not fit, leaving the single-launch path to the caller.
 static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs& in, const NodeTable& table,
                                   bool& done) {
     done = false;
@@ -2022,13 +2118,18 @@ static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs&
     const Rays r = rays_of(b);
     const long long blocks = (b.nray * 32 + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
     const int nb = (int)std::min<long long>((nodes + 255) / 256, 152LL * 8);
+    const int wchunks = (W + 31) / 32;
+    const long long wave_blocks = (b.nray * wchunks + WAVE_WARPS - 1) / WAVE_WARPS;
     Timer timer(s, K_TRANSPORT);
     if (W == 1)
         transport_warp_kernel<1, true><<<(unsigned)blocks, TRANSPORT_THREADS, warp_smem(s->K), s->stream>>>(
             o, r, in, table, fl, 0, (int)b.nray, P<float4>(s->rad));
-    else
+    else if (W <= 4)
         transport_warp_kernel<4, true><<<(unsigned)blocks, TRANSPORT_THREADS, warp_smem(s->K), s->stream>>>(
             o, r, in, table, fl, 0, (int)b.nray, P<float4>(s->rad));
+    else
+        transport_wave_kernel<true><<<(unsigned)wave_blocks, WAVE_WARPS * 32, wave_smem(d.L), s->stream>>>(
+            o, r, in, table, fl, 0, (int)b.nray, wchunks, P<float4>(s->rad));
     TRY(launch_check(s));
     CK(cudaMemsetAsync(s->fl_cnt.p, 0, (size_t)(s->ns + 1) * sizeof(int), s->stream));
     CK(cudaMemsetAsync(s->fl_g.p, 0, (size_t)nodes * 2 * W * sizeof(float2), s->stream));
@@ -2040,22 +2141,33 @@ static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs&
     pair_bucket_kernel<<<std::max(nb, 1), 256, 0, s->stream>>>(o, table.misc, nodes, nullptr, P<int>(s->fl_cursor),
                                                                P<int>(s->fl_entries));
     TRY(launch_check(s));
-    const int gb = (int)((2 * nodes + 255) / 256);  // one pair per thread at most
-    if (W == 1)
-        ground_pairs_kernel<1><<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir, P<int>(s->fl_entries),
-                                                                       P<int>(s->fl_off) + s->ns, fl.g);
-    else
-        ground_pairs_kernel<4><<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir, P<int>(s->fl_entries),
-                                                                       P<int>(s->fl_off) + s->ns, fl.g);
+    if (W <= 4) {
+        const int gb = (int)((2 * nodes + 255) / 256);  // one pair per thread at most
+        if (W == 1)
+            ground_pairs_kernel<1><<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir,
+                                                                           P<int>(s->fl_entries),
+                                                                           P<int>(s->fl_off) + s->ns, fl.g);
+        else
+            ground_pairs_kernel<4><<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir,
+                                                                           P<int>(s->fl_entries),
+                                                                           P<int>(s->fl_off) + s->ns, fl.g);
+    } else {
+        const int gb = (int)std::min<long long>((2 * nodes * W + 255) / 256, 152LL * 64);
+        ground_pairs_wave_kernel<<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir, P<int>(s->fl_entries),
+                                                                         P<int>(s->fl_off) + s->ns, fl.g);
+    }
     TRY(launch_check(s));
     if (W == 1)
         first_light_sum_kernel<1><<<(unsigned)blocks, TRANSPORT_THREADS, 0, s->stream>>>(o, r, in, table, fl, 0,
                                                                                           (int)b.nray,
                                                                                           P<float4>(s->rad));
-    else
+    else if (W <= 4)
         first_light_sum_kernel<4><<<(unsigned)blocks, TRANSPORT_THREADS, 0, s->stream>>>(o, r, in, table, fl, 0,
                                                                                           (int)b.nray,
                                                                                           P<float4>(s->rad));
+    else
+        first_light_sum_wave_kernel<<<(unsigned)((b.nray * wchunks * 32 + 127) / 128), 128, 0, s->stream>>>(
+            o, r, in, table, fl, 0, (int)b.nray, wchunks, P<float4>(s->rad));
     TRY(launch_check(s));
     b.t_valid = true;
     if (!b.p_valid) TRY(build_pairs(s, b, in.nq));
@@ -2092,7 +2204,7 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
     bool read = false;
     TRY(table_for(s, b, in.nq, ray0 == 0 && nray == b.nray, first, write, read));
     const NodeTable table{P<float4>(b.t_frame), P<float4>(b.t_misc), P<float>(b.t_att)};
-    if (first && !query && d.W <= 4 && ray0 == 0 && nray == b.nray && (write.frame || b.t_valid)) {
+    if (first && !query && ray0 == 0 && nray == b.nray && (write.frame || b.t_valid)) {
         bool done = false;
         TRY(run_first_light_staged(s, b, in, table, done));
         if (done) return 0;
@@ -2154,8 +2266,8 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
             kernel<<<(unsigned)blocks, WAVE_WARPS * 32, table_wave_smem(d.L), s->stream>>>(
                 optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
         } else
-            transport_wave_kernel<<<(unsigned)blocks, WAVE_WARPS * 32, wave_smem(d.L), s->stream>>>(
-                optics_of(s), rays_of(b), in, write, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
+            transport_wave_kernel<false><<<(unsigned)blocks, WAVE_WARPS * 32, wave_smem(d.L), s->stream>>>(
+                optics_of(s), rays_of(b), in, write, no_fl, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
     }
     TRY(launch_check(s));
     if (write.frame) {
@@ -2421,7 +2533,9 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
                                  (int)table_wave_smem(d.L)) != cudaSuccess ||
             cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_smem) !=
                 cudaSuccess ||
-            cudaFuncSetAttribute(transport_wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            cudaFuncSetAttribute(transport_wave_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)wave_smem(d.L)) != cudaSuccess ||
+            cudaFuncSetAttribute(transport_wave_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)wave_smem(d.L)) != cudaSuccess ||
             cudaFuncSetAttribute(transport_warp_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
