@@ -55,8 +55,10 @@ struct BundleDev {
     // ray-cell pairs (PairTable): valid with the node table unless they exceed the memory budget; host copies of the
     // pair offsets at the ground-pass end and at the end
     DevBuf p_off, p_cell, p_ray, p_node, y_tab;
+    DevBuf pair_A;  // the per-m contractions of the pairs
     bool p_valid = false;
     int64_t p_ground = 0, p_total = 0;
+    int64_t a_version = -1;  // plane version pair_A was contracted from
 };
 
 // kernel classes timed by sosb_set_timing / sosb_get_timing
@@ -91,7 +93,7 @@ struct sosb_state {
     DevBuf fx, fg, norms, partials, dots;
     DevBuf ring_g[4], ring_f[4];
     DevBuf fl_val0, fl_coef, fl_dir, fl_g, fl_cnt, fl_off, fl_cursor, fl_entries;  // staged first light
-    DevBuf pair_A;  // per-m pair contractions of the current plane (PairTable::A), shared by the bundles
+    int64_t plane_version = 0;  // incremented by every plane rebuild (the pair contractions follow it)
     bool have_first = false;
     bool tables = true;  // build and use node tables (sosb_set_node_tables)
     // fixed-point loop: evaluation control and report (device and pinned host copies), replayed evaluation graph
@@ -612,12 +614,14 @@ static size_t wave_smem(int L) {
 
 // ------------------------------------------------------------------ ray-cell pairs
 // The corner SH contraction by (ray, corner cell) pair, the form of the reference's sos_vprod, for many wavelengths:
-// for every distinct corner cell a ray's nodes touch, A[pair][m][w] = sum_l Y_lm(ray) plane[cell][k(l, m)][w] once
-// per evaluation (pair_contract_wave_kernel), and each node then adds its azimuth series over
-// A[pair(node, corner)][m][w] (transport_pair_wave_kernel). Pairs, the ray basis table and each node's four pair
-// indices are geometry and are built with the node table. With one to four wavelengths the per-node synthesis of
-// transport_table_kernel is faster (config 0 warm launch 0.24 ms against 0.32 ms for pairs), so pairs serve W > 4
-// (30 wavelengths, L=32: warm launch 8.6 -> 6.5 ms, observer 1.9 -> 1.1 ms, ground 0.9 -> 0.25 ms).
+// for every distinct corner cell a ray's nodes touch, A[pair][m][w] = sum_l Y_lm(ray) plane[cell][k(l, m)][w], once
+// per plane and bundle (pair_contract_wave_kernel; the ground and the warm pass of one evaluation share them), and
+// each node then adds its azimuth series over A[pair(node, corner)][m][w] (transport_pair_wave_kernel). Pairs, the
+// ray basis table and each node's four pair indices are geometry and are built with the node table. With one to four
+// wavelengths the per-node synthesis of transport_table_kernel is faster: on config 0 the rays' nodes are spread
+// over long shell segments, so a node shares few corner cells with the ray's earlier nodes (1.53 M pairs for 0.51 M
+// nodes) and a contraction per pair costs more than the per-node one it replaces (measured with one thread per pair:
+// 55 us per node pass instead of 100 us, plus 80 us per contraction).
 constexpr int PAIR_WINDOW = 16;  // recent distinct corner cells a ray's new corners are matched against
 
 struct PairTable {
@@ -685,12 +689,12 @@ __global__ void pair_basis_kernel(Optics o, Rays b, int kp, float* y_tab) {
 
 // Many wavelengths (plane [cell][K][W]): one warp per (pair, chunk of 32 wavelengths), lane = wavelength.
 template <int LT>
-__global__ void pair_contract_wave_kernel(Optics o, PairTable pt, const float* __restrict__ plane, int p0, int np,
-                                          int kp, int wchunks) {
+__global__ void pair_contract_wave_kernel(Optics o, PairTable pt, const float* __restrict__ plane, int np, int kp,
+                                          int wchunks) {
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= (long long)np * wchunks) return;
-    const int p = p0 + (int)(warp / wchunks);
+    const int p = (int)(warp / wchunks);
     const int w = (int)(warp % wchunks) * 32 + lane;
     if (w >= o.W) return;
     const int W = o.W, L1 = o.L + 1;
@@ -1717,7 +1721,41 @@ struct Ring4 {
 // cells; the block size is a multiple of W, so thread t keeps wavelength t % W over all its elements (FP32 products
 // in compensated FP32 sums), and the per-thread sums of a wavelength are added in FP64 by a pairwise tree in thread
 // order (no atomics: the dots are reproducible run to run).
-__global__ void feature_kernel(const float* __restrict__ g, const float* __restrict__ x,
+// One cell's elements for thread t with NS ring slots dotted: four elements' loads are issued before any of them is
+// used (the kernel is latency-bound otherwise), and every element is summed in the same order as a plain loop.
+template <int NS>
+__device__ __forceinline__ void feature_cell(const float* __restrict__ g, const float* __restrict__ x, float* dst,
+                                             const float* const* rj, const bool* self, size_t base, int row, int t,
+                                             int B, float scale, float* loc, float* lcm) {
+    int e = t;
+    for (; e + 3 * B < row; e += 4 * B) {
+        float gv[4], xv[4], ov[NS > 0 ? NS : 1][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t i = base + e + u * B;
+            gv[u] = g[i];
+            xv[u] = x[i];
+#pragma unroll
+            for (int j = 0; j < NS; ++j) ov[j][u] = self[j] ? 0.0f : rj[j][i];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float f = (gv[u] - xv[u]) / scale;
+            dst[base + e + u * B] = f;
+#pragma unroll
+            for (int j = 0; j < NS; ++j) kahan(loc[j], lcm[j], f * (self[j] ? f : ov[j][u]));
+        }
+    }
+    for (; e < row; e += B) {
+        const size_t i = base + e;
+        const float f = (g[i] - x[i]) / scale;
+        dst[i] = f;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) kahan(loc[j], lcm[j], f * (self[j] ? f : rj[j][i]));
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) feature_kernel(const float* __restrict__ g, const float* __restrict__ x,
                                const float* __restrict__ norms, const unsigned* __restrict__ mx, long long ns, int src,
                                int W, Ring4 ring, const EvalCtrl* __restrict__ ctrl, double* __restrict__ partials) {
     extern __shared__ double sd[];  // [blockDim.x][4]
@@ -1728,21 +1766,22 @@ __global__ void feature_kernel(const float* __restrict__ g, const float* __restr
     const int nslot = ctrl->m;
     float* dst = ring.p[ctrl->slot];
     const float* rj[4];
-    for (int j = 0; j < 4; ++j) rj[j] = ring.p[ctrl->order[j & 3]];
+    bool self[4];
+    for (int j = 0; j < 4; ++j) {
+        rj[j] = ring.p[ctrl->order[j & 3]];
+        self[j] = rj[j] == dst;
+    }
     const float floor_w = __uint_as_float(mx[w]) * 1e-8f;
     // per-thread dots in compensated FP32 (FP32 products, Kahan sums), combined in FP64 below
     float loc[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lcm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (long long cell = blockIdx.x; cell < ns; cell += gridDim.x) {
         const float scale = fmaxf(norms[cell * W + w], floor_w);
         const size_t base = (size_t)cell * row;
-        for (int e = t; e < row; e += B) {
-            const size_t i = base + e;
-            const float f = (g[i] - x[i]) / scale;
-            dst[i] = f;
-            for (int j = 0; j < nslot; ++j) {
-                const float o = (rj[j] == dst) ? f : rj[j][i];
-                kahan(loc[j], lcm[j], f * o);
-            }
+        switch (nslot) {
+            case 1: feature_cell<1>(g, x, dst, rj, self, base, row, t, B, scale, loc, lcm); break;
+            case 2: feature_cell<2>(g, x, dst, rj, self, base, row, t, B, scale, loc, lcm); break;
+            case 3: feature_cell<3>(g, x, dst, rj, self, base, row, t, B, scale, loc, lcm); break;
+            default: feature_cell<4>(g, x, dst, rj, self, base, row, t, B, scale, loc, lcm); break;
         }
     }
     for (int j = 0; j < 4; ++j) sd[t * 4 + j] = (double)loc[j] - (double)lcm[j];
@@ -1780,21 +1819,56 @@ __global__ void sum_partials_kernel(const double* __restrict__ partials, int blo
 
 // When ctrl->mix: x[i] = sum_j weights[j][w] ring[mix_order j][i] for wavelengths with valid weights, else g[i]
 // (the previous evaluation's g). Without ctrl->mix, x stays as it is.
+// x[i] = sum_j weights[j][w] q_j[i] over M ring slots for the mixed wavelengths, g[i] for the others; four elements
+// a thread, loads issued first.
+template <int M>
+__device__ __forceinline__ void mix_elements(const float* __restrict__ g, const float* const* q,
+                                             const EvalCtrl* __restrict__ ctrl, int W, long long n,
+                                             float* __restrict__ x) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        float qv[M][4], gv[4];
+        int wv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long i = i0 + u * stride;
+            wv[u] = -1;
+            if (i >= n) continue;
+            wv[u] = (int)(i % W);
+            if (ctrl->use[wv[u]]) {
+#pragma unroll
+                for (int j = 0; j < M; ++j) qv[j][u] = q[j][i];
+            } else {
+                gv[u] = g[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int w = wv[u];
+            if (w < 0) continue;
+            const long long i = i0 + u * stride;
+            if (!ctrl->use[w]) {
+                x[i] = gv[u];
+                continue;
+            }
+            float acc = ctrl->weights[w] * qv[0][u];
+#pragma unroll
+            for (int j = 1; j < M; ++j) acc += ctrl->weights[j * 64 + w] * qv[j][u];
+            x[i] = acc;
+        }
+    }
+}
+
 __global__ void mix_kernel(const float* __restrict__ g, Ring4 ring, const EvalCtrl* __restrict__ ctrl, int W,
                            long long n, float* __restrict__ x) {
     if (!ctrl->mix) return;
-    const int m = ctrl->mix_m;
     const float* q[4];
     for (int j = 0; j < 4; ++j) q[j] = ring.p[ctrl->mix_order[j]];
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int w = (int)(i % W);
-        if (!ctrl->use[w]) {
-            x[i] = g[i];
-            continue;
-        }
-        float acc = ctrl->weights[w] * q[0][i];
-        for (int j = 1; j < m; ++j) acc += ctrl->weights[j * 64 + w] * q[j][i];
-        x[i] = acc;
+    switch (ctrl->mix_m) {
+        case 1: mix_elements<1>(g, q, ctrl, W, n, x); break;
+        case 2: mix_elements<2>(g, q, ctrl, W, n, x); break;
+        case 3: mix_elements<3>(g, q, ctrl, W, n, x); break;
+        default: mix_elements<4>(g, q, ctrl, W, n, x); break;
     }
 }
 
@@ -2005,21 +2079,22 @@ static int build_pairs(sosb_state* s, BundleDev& b, int nq) {
     TRY(dfree(s, cursor));
     const size_t a_bytes = (size_t)total * (d.L + 1) * d.W * sizeof(float);
     const size_t need = (size_t)total * 8 + nodes * sizeof(int4) + (size_t)nray * kp * sizeof(float) +
-                        (a_bytes > s->pair_A.bytes ? a_bytes - s->pair_A.bytes : 0);
+                        (a_bytes > b.pair_A.bytes ? a_bytes - b.pair_A.bytes : 0);
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     if (need > free_b / 2) return 0;
     TRY(dalloc(s, b.p_cell, std::max<size_t>(total, 1) * sizeof(int)));
     TRY(dalloc(s, b.p_ray, std::max<size_t>(total, 1) * sizeof(int)));
     TRY(dalloc(s, b.p_node, std::max<size_t>(nodes, 1) * sizeof(int4)));
-    TRY(dalloc(s, b.y_tab, (size_t)nray * kp * sizeof(float)));
-    TRY(dalloc(s, s->pair_A, std::max<size_t>(a_bytes, 16)));
+    TRY(dalloc(s, b.pair_A, std::max<size_t>(a_bytes, 16)));
     pair_build_kernel<<<blocks, 128, 0, s->stream>>>(optics_of(s), rays_of(b), tab, nq, 1, nullptr, P<int>(b.p_off),
                                                      P<int>(b.p_cell), P<int>(b.p_ray), P<int4>(b.p_node));
     TRY(launch_check(s));
+    TRY(dalloc(s, b.y_tab, (size_t)nray * kp * sizeof(float)));
     pair_basis_kernel<<<(unsigned)((nray * 32 + 127) / 128), 128, 0, s->stream>>>(optics_of(s), rays_of(b), kp,
                                                                                  P<float>(b.y_tab));
     TRY(launch_check(s));
+    b.a_version = -1;
     b.p_total = total;
     b.p_ground = ground;
     b.p_valid = true;
@@ -2034,7 +2109,7 @@ static int build_pairs(sosb_state* s, BundleDev& b, int nq) {
 // depend on which candidate ran last.
 struct TuneKey {
     int64_t nray, nseg;
-    int nq, W, L, ns, kind;  // kind: 0 table kernel, 1 pair kernel
+    int nq, W, L, ns, kind;  // kind: 0 table kernel
     bool operator<(const TuneKey& o) const {
         return std::tie(nray, nseg, nq, W, L, ns, kind) < std::tie(o.nray, o.nseg, o.nq, o.W, o.L, o.ns, o.kind);
     }
@@ -2238,24 +2313,22 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
         const long long warps = (long long)nray * wchunks;
         const long long blocks = (warps + WAVE_WARPS - 1) / WAVE_WARPS;
         Timer timer(s, read ? K_TABLE : K_TRANSPORT);
-        const bool ground_launch = b.host_cell_off.size() > (size_t)d.nc && nray == b.host_cell_off[d.nc];
-        const int64_t np_launch = nray == b.nray ? b.p_total : (ground_launch ? b.p_ground : -1);
-        if (read && b.p_valid && np_launch >= 0) {
+        if (read && b.p_valid) {
             const PairTable pt{P<int>(b.p_off), P<int>(b.p_cell), P<int>(b.p_ray), P<int4>(b.p_node),
-                               P<float>(b.y_tab), P<float>(s->pair_A)};
-            const int kp = (s->K + 3) & ~3;
-            if (np_launch > 0) {
-                const unsigned cg = (unsigned)((np_launch * wchunks * 32 + 127) / 128);
-                if (d.L == 16)
-                    pair_contract_wave_kernel<16><<<cg, 128, 0, s->stream>>>(optics_of(s), pt, in.plane, 0,
-                                                                             (int)np_launch, kp, wchunks);
-                else if (d.L == 32)
-                    pair_contract_wave_kernel<32><<<cg, 128, 0, s->stream>>>(optics_of(s), pt, in.plane, 0,
-                                                                             (int)np_launch, kp, wchunks);
-                else
-                    pair_contract_wave_kernel<0><<<cg, 128, 0, s->stream>>>(optics_of(s), pt, in.plane, 0,
-                                                                            (int)np_launch, kp, wchunks);
-                TRY(launch_check(s));
+                               P<float>(b.y_tab), P<float>(b.pair_A)};
+            if (b.a_version != s->plane_version) {
+                // contractions of every pair of the bundle against the current plane (reused by the launches that
+                // follow on the same plane: the ground and the warm pass of one apply)
+                const int kp = (s->K + 3) & ~3;
+                if (b.p_total > 0) {
+                    const unsigned cg = (unsigned)((b.p_total * wchunks * 32 + 127) / 128);
+                    const auto contract = d.L == 16 ? pair_contract_wave_kernel<16>
+                                                    : (d.L == 32 ? pair_contract_wave_kernel<32>
+                                                                 : pair_contract_wave_kernel<0>);
+                    contract<<<cg, 128, 0, s->stream>>>(optics_of(s), pt, in.plane, (int)b.p_total, kp, wchunks);
+                    TRY(launch_check(s));
+                }
+                b.a_version = s->plane_version;
             }
             const unsigned pb = (unsigned)((warps + PAIR_WAVE_WARPS - 1) / PAIR_WAVE_WARPS);
             transport_pair_wave_kernel<<<pb, PAIR_WAVE_WARPS * 32, 0, s->stream>>>(
@@ -2373,6 +2446,7 @@ static int run_plane(sosb_state* s, const float* field) {
     const int kp = plane_kp(s);
     const long long n = (long long)s->ns * (kp ? kp : s->K) * d.W;
     TRY(dalloc(s, s->plane, n * sizeof(float)));
+    ++s->plane_version;
     Timer timer(s, K_PLANE);
     plane_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(field, P<float>(s->ha), P<float>(s->s_density), d.nc, s->K,
                                                           s->src, d.W, d.strato, kp, n, P<float>(s->plane));
@@ -2573,13 +2647,13 @@ int sosb_destroy(sosb_handle s) {
                       &s->fg, &s->norms, &s->partials, &s->dots, &s->ctrl_dev, &s->report_dev, &s->ring_g[0],
                       &s->ring_g[1], &s->ring_g[2], &s->ring_g[3], &s->ring_f[0], &s->ring_f[1], &s->ring_f[2],
                       &s->ring_f[3], &s->fl_val0, &s->fl_coef, &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off,
-                      &s->fl_cursor, &s->fl_entries, &s->pair_A};
+                      &s->fl_cursor, &s->fl_entries};
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
                         &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits,
                         &bd->t_frame, &bd->t_misc, &bd->t_att, &bd->b_hi, &bd->b_lo, &bd->p_off, &bd->p_cell,
-                        &bd->p_ray, &bd->p_node, &bd->y_tab};
+                        &bd->p_ray, &bd->p_node, &bd->y_tab, &bd->pair_A};
         for (DevBuf* b : bb) dfree(s, *b);
     }
     collect_timing(s);
@@ -2957,7 +3031,9 @@ static int loop_alloc(sosb_state* s) {
     TRY(dalloc(s, s->norms, (size_t)s->ns * W * sizeof(float)));
     // feature kernel: blocks of a multiple of W threads (one wavelength per thread), whole cells per block
     s->feat_threads = W * std::max(1, 256 / W);
-    s->feat_blocks = (int)std::min<long long>(s->ns, 152LL * 4);
+    // cells of at least four elements a thread: one cell per block, up to 8 blocks an SM; smaller cells: 4 an SM
+    const bool long_rows = (long long)s->src * W >= 4LL * s->feat_threads;
+    s->feat_blocks = (int)std::min<long long>(s->ns, 152LL * (long_rows ? 8 : 4));
     TRY(dalloc(s, s->partials, (size_t)s->feat_blocks * 4 * W * sizeof(double)));
     TRY(dalloc(s, s->dots, (size_t)4 * W * sizeof(double)));
     TRY(dalloc(s, s->metrics, 3 * 64 * sizeof(unsigned)));

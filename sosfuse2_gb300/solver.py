@@ -97,6 +97,16 @@ class Kernel:
             pass
 
     # ------------------------------------------------------------------ reference Kernel surface
+    def set_observer(self, bundle):
+        """Replace the observer (phase-2) ray bundle by `bundle` (the packed-state bundle keys, without prefix); the
+        cell bundle and the constants stay. Node tables and pairs of the old observer bundle are dropped."""
+        arrays = {'query_' + k: v for k, v in bundle.items()}
+        arrays['meta'] = dict(self.state.meta)
+        st = PackedState(arrays)
+        self._check(self.lib.sosb_set_bundle(self.h, _abi.OBSERVER, ctypes.byref(st.abi_bundle('query'))))
+        st._keep.clear()
+        self.n_query = len(bundle['d'])
+
     def _stream(self):
         self.lib.sosb_set_stream(self.h, ctypes.c_void_p(self.torch.cuda.current_stream(self.device).cuda_stream))
 

@@ -426,6 +426,17 @@ class Family:
         self.query = build_bundle(qpts, qdirs, qw, self.chi, self.top, self.table, shape, with_ground_columns=False)
         self._ground_rays(ground_nmu, ground_nphi)
 
+    def view_bundle(self, hs, el, az):
+        """Rays of a radiance table (outputs/radiance_table.py:43-60 over solve/engine_core.py:208-226): for every
+        solar elevation hs[j] the observer at OBSERVER_KM under solar zenith 90 - hs[j] (one bundle cell), looking
+        along the (el, az) grid in meshgrid 'ij' order (elevation rows, azimuth columns), unit weights."""
+        ee, aa = np.meshgrid(np.asarray(el, float), np.asarray(az, float), indexing='ij')
+        e, z = np.deg2rad(ee.ravel()), np.deg2rad(aa.ravel())
+        loc = np.column_stack([np.cos(e) * np.cos(z), np.cos(e) * np.sin(z), np.sin(e)])
+        pts = [frame(R + OBSERVER_KM, np.deg2rad(90 - float(h))) for h in hs]
+        return build_bundle(pts, [loc] * len(pts), [np.ones(len(loc))] * len(pts), self.chi, self.top, self.table,
+                            self.shape, with_ground_columns=False)
+
     def _ground_rays(self, nmu, nphi):
         """Per cell: the directions of a ring quadrature without shadow rings, their weights, and for the downward
         ones the columns to the ground and from the ground point to the sun (solve/engine_core.py:103-147)."""

@@ -56,7 +56,9 @@ def test_tables_match_recompute(case):
 @pytest.mark.parametrize('case', sorted(CASES))
 def test_pairs_match_node_synthesis(case):
     """Corner SH from the per-pair contractions (W > 4) against the per-lane corner cache (same sums); with W <= 4
-    pairs are not used and both runs take the per-node synthesis."""
+    pairs are not used and both runs take the per-node synthesis. The cell bundle's contractions serve its ground and
+    warm passes and are redone for every new plane (the observer pass between two applications builds its own), so a
+    stale contraction would show here."""
     arrays = small_state(**CASES[case])
     on = _run(arrays, True, pairs=True)
     off = _run(arrays, True, pairs=False)
