@@ -10,6 +10,8 @@ meets the tolerance, Anderson mixing). `e2e` = the same through the public API w
 once with the shared geometry, every step uploading each state's constants from host arrays, solving and reading the
 fields back. The dominant kernel is timed with CUDA events recorded by the library on its own work stream;
 `roofline.achieved` is its algorithmic bytes per launch over its mean launch time.
+`forms` adds the plain and learned batched solves, the training report, the projection precision forms on a
+30-wavelength state and `make_table` on the reference's full table axes.
 `cpu_baseline` and the `--impl reference` arm time the CPU port of the reference algorithm (oracle/) on the host
 cores, one process per core, on a bounded sample of the same workload (first light plus one evaluation per process,
 extrapolated by the GPU run's evaluation count).
@@ -227,6 +229,29 @@ def cpu_baseline(arrays, evaluations, procs=None):
                        f'solve'), wall
 
 
+def whole_job(value, world, dist=None):
+    """Whole-job throughput of `world` replicas from this rank's own: the slowest rank's rate times the ranks (the
+    max-over-ranks time of equal work per rank)."""
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    if dist is not None and world > 1:
+        if dist.get_backend() == 'nccl':
+            t = t.cuda()
+        dist.all_reduce(t, op=dist.ReduceOp.MIN)
+    return float(t.item()) * world
+
+
+def bracket(dist):
+    """Barrier and device synchronisation on both sides of a timed region."""
+    import torch
+
+    if dist is not None:
+        dist.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
 # ------------------------------------------------------------------------------------------------ arms
 def run_reference(a, rank):
     if rank != 0:
@@ -267,8 +292,9 @@ def _batch_kernels(fam, seeds, device):
     return states, kernels
 
 
-def _time_batched(a, fam, ws, device, seeds):
-    """Plain and learned-start batched solves of the held-out family states: converged solves/s of each form."""
+def _time_batched(a, fam, ws, device, seeds, dist=None):
+    """Plain and learned-start batched solves of the held-out family states: converged solves/s of each form (each
+    step bracketed by a barrier over the ranks and a device synchronisation)."""
     import torch
 
     from sosfuse2_gb300 import _abi, learned
@@ -285,7 +311,7 @@ def _time_batched(a, fam, ws, device, seeds):
         for step in range(a.warmup + a.steps):
             for k, st in zip(kernels, states):
                 k.update(st)  # no first light carried between steps
-            torch.cuda.synchronize()
+            bracket(dist)
             t0 = time.perf_counter()
             if form == 'plain':
                 stats = (_abi.Stats * n)()
@@ -301,7 +327,7 @@ def _time_batched(a, fam, ws, device, seeds):
                 ev = [x[1]['evaluations'] for x in r if not isinstance(x, Exception)]
                 # warm solves + the apply(0) of every state (about a tenth of a solve's launches) + network GEMMs
                 nl = sum(x[1]['kernel_launches'] for x in r if not isinstance(x, Exception)) + ws.mlp.gemm_launches - g0
-            torch.cuda.synchronize()
+            bracket(dist)
             dt = time.perf_counter() - t0
             if step >= a.warmup:
                 times.append(dt)
@@ -363,6 +389,41 @@ def _precision_form(device):
                          f'against the fp32 form', forms=out)
 
 
+def _table_form(fam, device):
+    """make_table on the reference's full table axes (25 solar elevations +6..-18 deg, 100 x 180 views, one
+    wavelength) for the converged source of a config-0 family state: the call's seconds (view rays built on the host,
+    a handle, first-order and multiple-scattering phase-2 transports) and table entries per second."""
+    import torch
+
+    from sosfuse2_gb300.solver import Solver
+    from sosfuse2_gb300.state import PackedState
+    from sosfuse2_gb300.synth import family_state
+    from sosfuse2_gb300.table import axes, make_table
+
+    for seed in range(90001, 90017):  # the first held-out state the plain iteration converges on
+        state = PackedState(family_state(fam, seed))
+        solver = Solver(state, device=device)
+        try:
+            field, st = solver.solve(int(state.meta['max_eval']), float(state.meta['tolerance']), device_out=True)
+            break
+        except RuntimeError as exc:
+            solver.kernel.close()
+            if not str(exc).startswith('E_NOT_CONVERGED'):
+                raise
+    _, hs, el, az = axes(False)
+    make_table(solver, field, hs[:1], el[:4], az[:4], log=lambda m: None, family=fam)  # warm-up: module and handle
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    table, seconds = make_table(solver, field, hs, el, az, log=lambda m: None, family=fam)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    solver.kernel.close()
+    rays = len(hs) * len(el) * len(az)
+    return dict(workload=f'config-0 family state {seed} ({st["evaluations"]} evaluations), {len(hs)} solar elevations x '
+                         f'{len(el)} x {len(az)} views, W={state.W}', rays=rays, seconds=dt,
+                rays_per_s=rays / dt, batches=len(seconds))
+
+
 def run_gb300(a, rank, world):
     import torch
 
@@ -397,6 +458,7 @@ def run_gb300(a, rank, world):
     stream = torch.cuda.current_stream()
     clocks = Clocks(local)
     step_ms, evaluations, launches = [], [], 0
+    bracket(dist)
     for _ in range(a.steps):
         flush.fill_(1.0)  # L2 flush between timed solves, outside the events
         e0 = torch.cuda.Event(enable_timing=True)
@@ -408,6 +470,7 @@ def run_gb300(a, rank, world):
         step_ms.append(e0.elapsed_time(e1))
         evaluations.append(st['evaluations'])
         launches += st['kernel_launches']
+    bracket(dist)
     plain_ms = statistics.mean(step_ms)
     # per-class kernel times of one more solve with CUDA events around every launch (launched one by one: an event
     # pair per kernel, so this solve is not one of the timed steps)
@@ -427,19 +490,17 @@ def run_gb300(a, rank, world):
         ws, report = learned.train_warm_start(fam, n_train=a.train_solves, epochs=a.epochs, seed=10000, device=device)
         report['seconds'] = time.perf_counter() - t0
         seeds = list(range(90000, 90000 + a.batch))
-        forms = _time_batched(a, fam, ws, device, seeds)
+        forms = _time_batched(a, fam, ws, device, seeds, dist)
         forms['training'] = report
         forms['learned_vs_plain'] = forms['learned']['value'] / max(forms['plain']['value'], 1e-30)
         forms['precision'] = _precision_form(device)
+        forms['table'] = _table_form(fam, device)
         launches += forms['plain']['kernel_launches'] + forms['learned']['kernel_launches']
     clk = clocks.stop()
     value_plain = 1e3 / plain_ms
     value = forms['learned']['value'] if forms else value_plain
-    t = torch.tensor([value], device=k.device)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MIN)
-        dist.barrier()
-    value = float(t.item()) * world
+    value = whole_job(value, world, dist)
+    bracket(dist)
     # ---------------------------------------------------------------- end to end through the public API
     # The user's calls for states on one geometry: handles created once with the bundles (outside the timing); every
     # step uploads each state's constants from host arrays (Kernel.update), solves, and reads the fields back to the

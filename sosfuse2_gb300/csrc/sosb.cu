@@ -166,6 +166,10 @@ static T* P(const DevBuf& b) {
     return static_cast<T*>(b.p);
 }
 
+// Block size for element loops over [..][W] arrays: a multiple of W (at most 256), so that every thread of a
+// grid-stride loop keeps one wavelength.
+static int wave_threads(int W) { return W * std::max(1, 256 / std::max(W, 1)); }
+
 static int grid_for(long long n, int threads) {
     long long g = (n + threads - 1) / threads;
     if (g < 1) g = 1;
@@ -1265,27 +1269,47 @@ static size_t table_wave_smem(int L) {
     return sizeof(float) * (size_t)WAVE_WARPS * (32 * TREC_WORDS + 4 * (L + 1) * 32 + (L + 1) * (L + 2) / 2);
 }
 
+// Index (a, b, c) of element i of an [.][nb][nc] array for a grid-stride loop: set once by division, then advanced
+// by the stride's own (a, b, c) digits with carries, so that the loop divides nothing per element.
+struct StrideIndex {
+    long long a, da;
+    int b, c, db, dc, nb, nc;
+    __device__ StrideIndex(long long i, long long stride, int nb_, int nc_) : nb(nb_), nc(nc_) {
+        c = (int)(i % nc);
+        const long long r = i / nc;
+        b = (int)(r % nb);
+        a = r / nb;
+        dc = (int)(stride % nc);
+        const long long rs = stride / nc;
+        db = (int)(rs % nb);
+        da = rs / nb;
+    }
+    __device__ __forceinline__ void next() {
+        c += dc;
+        const int c1 = c >= nc;
+        c -= c1 ? nc : 0;
+        b += db + c1;
+        const int c2 = b >= nb;
+        b -= c2 ? nb : 0;
+        a += da + c2;
+    }
+};
+
 // plane = SH slots x cell density (+ stratospheric slots x their density): [cell][k][w] (kp = 0), or
 // [cell][w][kp] with zero padding k = K .. kp - 1 (few wavelengths: 16-byte aligned rows for sh_synth4_fixed).
 __global__ void plane_kernel(const float* __restrict__ field, const float* __restrict__ ha,
                              const float* __restrict__ sd, int nc, int K, int src, int W, int strato, int kp,
                              long long n, float* __restrict__ plane) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        int w, k, cell;
-        if (kp) {
-            k = (int)(i % kp);
-            const long long r = i / kp;
-            w = (int)(r % W);
-            cell = (int)(r / W);
-            if (k >= K) {
-                plane[i] = 0.0f;
-                continue;
-            }
-        } else {
-            w = (int)(i % W);
-            const long long r = i / W;
-            k = (int)(r % K);
-            cell = (int)(r / K);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    // kp: (cell, w, k) over [cell][W][kp]; otherwise (cell, k, w) over [cell][K][W]
+    StrideIndex ix(i, stride, kp ? W : K, kp ? kp : W);
+    for (; i < n; i += stride, ix.next()) {
+        const int cell = (int)ix.a;
+        const int w = kp ? ix.b : ix.c, k = kp ? ix.c : ix.b;
+        if (k >= K) {
+            plane[i] = 0.0f;
+            continue;
         }
         const int hi = cell / nc;
         const float* f = field + (size_t)cell * src * W + w;
@@ -1612,11 +1636,26 @@ __global__ void compose_kernel(const float* __restrict__ warm, const float* __re
     for (int i = threadIdx.x; i < 64; i += blockDim.x) sm_bad[i] = sm_mag[i] = sm_dif[i] = 0u;
     __syncthreads();
     const int nm = 4 + K;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int w = (int)(i % W);
-        const long long r = i / W;
-        const int slot = (int)(r % src);
-        const long long cell = r / src;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    StrideIndex ix(i, stride, src, W);  // (cell, slot, w)
+    // the metrics of this thread's elements, per wavelength it meets (one unless the stride is not a multiple of W)
+    unsigned bad = 0u, mag = 0u, dif = 0u;
+    int wcur = -1;
+    auto flush = [&]() {
+        if (wcur < 0) return;
+        if (bad) atomicAdd(&sm_bad[wcur], bad);
+        atomicMax(&sm_mag[wcur], mag);
+        atomicMax(&sm_dif[wcur], dif);
+        bad = mag = dif = 0u;
+    };
+    for (; i < n; i += stride, ix.next()) {
+        const int w = ix.c, slot = ix.b;
+        const long long cell = ix.a;
+        if (w != wcur) {
+            flush();
+            wcur = w;
+        }
         const size_t mb = ((size_t)cell * nm) * W + w;
         float v;
         if (slot < 4) {
@@ -1635,14 +1674,14 @@ __global__ void compose_kernel(const float* __restrict__ warm, const float* __re
             v = (m * s_eigen[k * W + w]) * s_sca[w];
         }
         if (fabsf(v) < TRACE_MIN) v = 0.0f;
-        const unsigned bad = isfinite(v) ? 0u : 1u;
+        bad += isfinite(v) ? 0u : 1u;
         const float xv = x ? x[i] : 0.0f;
         if ((done_mask >> w) & 1ull) v = xv;
         out[i] = v;
-        if (bad) atomicAdd(&sm_bad[w], 1u);
-        atomicMax(&sm_mag[w], __float_as_uint(fabsf(v)));
-        atomicMax(&sm_dif[w], __float_as_uint(fabsf(v - xv)));
+        mag = max(mag, __float_as_uint(fabsf(v)));
+        dif = max(dif, __float_as_uint(fabsf(v - xv)));
     }
+    flush();
     __syncthreads();
     for (int w = threadIdx.x; w < W; w += blockDim.x) {
         if (sm_bad[w]) atomicAdd(&metrics[w], sm_bad[w]);
@@ -1820,7 +1859,7 @@ __global__ void sum_partials_kernel(const double* __restrict__ partials, int blo
 // When ctrl->mix: x[i] = sum_j weights[j][w] ring[mix_order j][i] for wavelengths with valid weights, else g[i]
 // (the previous evaluation's g). Without ctrl->mix, x stays as it is.
 // x[i] = sum_j weights[j][w] q_j[i] over M ring slots for the mixed wavelengths, g[i] for the others; four elements
-// a thread, loads issued first.
+// a thread, loads issued first. The block size is a multiple of W, so a thread keeps one wavelength.
 template <int M>
 __device__ __forceinline__ void mix_elements(const float* __restrict__ g, const float* const* q,
                                              const EvalCtrl* __restrict__ ctrl, int W, long long n,
@@ -1834,7 +1873,7 @@ __device__ __forceinline__ void mix_elements(const float* __restrict__ g, const 
             const long long i = i0 + u * stride;
             wv[u] = -1;
             if (i >= n) continue;
-            wv[u] = (int)(i % W);
+            wv[u] = (int)(i0 % W);  // the stride is a multiple of W
             if (ctrl->use[wv[u]]) {
 #pragma unroll
                 for (int j = 0; j < M; ++j) qv[j][u] = q[j][i];
@@ -2523,7 +2562,7 @@ static int apply_impl(sosb_state* s, const float* field, float* out, unsigned lo
     CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
     const long long n = (long long)s->ns * s->src * d.W;
     Timer timer(s, K_COMPOSE);
-    compose_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(
+    compose_kernel<<<grid_for(n, wave_threads(d.W)), wave_threads(d.W), 0, s->stream>>>(
         P<float>(s->moments), P<float>(s->first_moments), field, P<float>(s->rf), P<float>(s->af), P<float>(s->asca),
         P<float>(s->ext0), P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, done_mask, done_dev,
         out,
@@ -2933,7 +2972,7 @@ int sosb_compose_static(sosb_handle s, const float* moments_dev, const float* fi
     // the scratch keeps the previous call's words: clear the part this call accumulates into
     CK(cudaMemsetAsync(scratch, 0, 3 * SOSB_STATIC_WAVES * sizeof(unsigned), s->stream));
     const long long n = (long long)s->ns * s->src * d.W;
-    compose_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(
+    compose_kernel<<<grid_for(n, wave_threads(d.W)), wave_threads(d.W), 0, s->stream>>>(
         moments_dev, first_moments_dev, x_dev, P<float>(s->rf), P<float>(s->af), P<float>(s->asca), P<float>(s->ext0),
         P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, (unsigned long long)done_mask, nullptr,
         out_dev, scratch);
@@ -3068,7 +3107,7 @@ static int eval_body(sosb_state* s) {
     CK(cudaMemcpyAsync(ctrl, s->ctrl_host, sizeof(EvalCtrl), cudaMemcpyHostToDevice, s->stream));
     {
         Timer t(s, K_ANDERSON);
-        mix_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(g, rg, ctrl, W, n, x);
+        mix_kernel<<<grid_for(n, wave_threads(W)), wave_threads(W), 0, s->stream>>>(g, rg, ctrl, W, n, x);
     }
     TRY(launch_check(s));
     TRY(boxes_dev(s, x, reinterpret_cast<double*>(rep + rl.old_b)));
@@ -3306,8 +3345,8 @@ struct SolveRun {
             const long long n = (long long)s->ns * s->src * s->d.W;
             const Ring4 rg{{P<float>(s->ring_g[0]), P<float>(s->ring_g[1]), P<float>(s->ring_g[2]),
                             P<float>(s->ring_g[3])}};
-            mix_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(P<float>(s->fg), rg, P<EvalCtrl>(s->ctrl_dev),
-                                                               s->d.W, n, result);
+            mix_kernel<<<grid_for(n, wave_threads(s->d.W)), wave_threads(s->d.W), 0, s->stream>>>(
+                P<float>(s->fg), rg, P<EvalCtrl>(s->ctrl_dev), s->d.W, n, result);
             TRY(launch_check(s));
         }
         CK(cudaMemcpyAsync(x_out, result, bytes, x_out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
