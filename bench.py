@@ -11,7 +11,8 @@ once with the shared geometry, every step uploading each state's constants from 
 fields back. The dominant kernel is timed with CUDA events recorded by the library on its own work stream;
 `roofline.achieved` is its algorithmic bytes per launch over its mean launch time.
 `forms` adds the plain and learned batched solves, the training report, the projection precision forms on a
-30-wavelength state and `make_table` on the reference's full table axes.
+30-wavelength state, `make_table` on the reference's full table axes and the per-state ground preparation on the host
+and on the device.
 `cpu_baseline` and the `--impl reference` arm time the CPU port of the reference algorithm (oracle/) on the host
 cores, one process per core, on a bounded sample of the same workload (first light plus one evaluation per process,
 extrapolated by the GPU run's evaluation count).
@@ -424,6 +425,38 @@ def _table_form(fam, device):
                 rays_per_s=rays / dt, batches=len(seconds))
 
 
+def _ground_form(fam, device):
+    """Per-state ground preparation (engine_core.Solver.prepare_ground) of a config-0 family state: the host form
+    (synth.Family.ground, NumPy FP64) against sosb_prepare_ground on the device (CUDA events not needed: the call
+    synchronises), each the mean of five calls after one untimed call."""
+    import torch
+
+    from sosfuse2_gb300.solver import Kernel
+    from sosfuse2_gb300.state import PackedState
+    from sosfuse2_gb300.synth import family_atmosphere
+
+    atm = family_atmosphere(fam, 90002)
+    ext = atm.ext()
+    fam.ground(atm, ext)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        fam.ground(atm, ext)
+    host_ms = (time.perf_counter() - t0) / 5 * 1e3
+    k = Kernel(PackedState(fam.state(atm, 90002, ground=False)), device)
+    rays = fam.ground_rays()
+    k.set_ground_rays(rays)
+    st_ext = atm.strato_ext if atm.strato else None
+    k.prepare_ground(atm.albedo, ext, st_ext)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        k.prepare_ground(atm.albedo, ext, st_ext)
+    dev_ms = (time.perf_counter() - t0) / 5 * 1e3
+    k.close()
+    return dict(workload=f'config-0 family state 90002: {len(rays["cell"])} ground rays over {fam.h.size * fam.chi.size} '
+                         f'cells, W={atm.W}', host_ms=host_ms, device_ms=dev_ms)
+
+
 def run_gb300(a, rank, world):
     import torch
 
@@ -495,6 +528,7 @@ def run_gb300(a, rank, world):
         forms['learned_vs_plain'] = forms['learned']['value'] / max(forms['plain']['value'], 1e-30)
         forms['precision'] = _precision_form(device)
         forms['table'] = _table_form(fam, device)
+        forms['ground'] = _ground_form(fam, device)
         launches += forms['plain']['kernel_launches'] + forms['learned']['kernel_launches']
     clk = clocks.stop()
     value_plain = 1e3 / plain_ms

@@ -185,6 +185,25 @@ int sosb_solve(sosb_handle h, int max_eval, double tolerance, const float *x0_ho
  * sosb_get_timing fills ms[k] and launches[k] for k < n. */
 int sosb_set_timing(sosb_handle h, int on);
 int sosb_get_timing(sosb_handle h, double *ms, int64_t *launches, int n);
+/* Ground-illumination rays of every cell, the geometry of engine_core.Solver.prepare_ground
+ * (src/sosfuse2/solve/engine_core.py:103-147) for the handle's grid: ray r belongs to cell[r] (ascending), arrives
+ * from the local direction loc[r][3] with quadrature weight weight[r]; cols[r][6] are its slant columns (five
+ * components and the stratospheric one) from the cell to the ground and on to the sun; cos_sun[r] = max(0, cosine
+ * of the solar zenith at its ground point); ok[r] = 1 when that point is lit and the ray reaches the ground. */
+typedef struct {
+    int64_t n;
+    const int32_t *cell;
+    const double *loc, *weight, *cols, *cos_sun;
+    const uint8_t *ok;
+} sosb_ground_rays;
+int sosb_set_ground_rays(sosb_handle h, const sosb_ground_rays *rays);
+/* Solver.prepare_ground on the device (engine_core.py:103-147) for a state's optics over the rays of
+ * sosb_set_ground_rays, replacing the ground arrays of sosb_set_constants (gm, goff, gdir, gval): per ray and
+ * wavelength value = albedo / pi * cos_sun * exp(-(cols[0:5] . ext[:, w] + cols[5] strato_ext[w])) * ok * weight
+ * in FP64; the rays with a positive value kept per cell in ray order; gm[cell][k][w] = sum over the cell's rays of
+ * factor_k(loc) * value times 2 C ext[0][w] (C = 3 / (16 pi)). ext: [5][W] FP64 extinction, strato_ext: [W] FP64
+ * (NULL without the stratospheric layer). */
+int sosb_prepare_ground(sosb_handle h, double albedo, const double *ext, const double *strato_ext);
 /* Warm-started Solver.solve (no counterpart in the reference; the learned start): iterate from the device field
  * x0_dev, reusing the first-light moments of the preceding sosb_apply on this handle. If the first evaluation's
  * largest source relative change max|g - x|/max|g| exceeds fallback_ss, the iteration restarts from fallback_dev

@@ -55,6 +55,13 @@ class Bundle(ctypes.Structure):
     ]
 
 
+class GroundRays(ctypes.Structure):
+    _fields_ = [
+        ('n', c_i64), ('cell', P_i32), ('loc', P_f64), ('weight', P_f64), ('cols', P_f64), ('cos_sun', P_f64),
+        ('ok', P_u8),
+    ]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ('evaluations', c_int), ('converged', c_int), ('seconds', c_dbl),
@@ -75,6 +82,8 @@ SIGNATURES = {
     'sosb_set_pairs': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_constants': ([ctypes.c_void_p, ctypes.POINTER(Constants)], c_int),
     'sosb_set_bundle': ([ctypes.c_void_p, c_int, ctypes.POINTER(Bundle)], c_int),
+    'sosb_set_ground_rays': ([ctypes.c_void_p, ctypes.POINTER(GroundRays)], c_int),
+    'sosb_prepare_ground': ([ctypes.c_void_p, c_dbl, P_f64, P_f64], c_int),
     'sosb_evaluate': ([ctypes.c_void_p, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                        ctypes.c_void_p, ctypes.c_void_p], c_int),
     'sosb_apply': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], c_int),

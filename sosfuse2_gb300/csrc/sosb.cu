@@ -93,6 +93,9 @@ struct sosb_state {
     DevBuf fx, fg, norms, partials, dots;
     DevBuf ring_g[4], ring_f[4];
     DevBuf fl_val0, fl_coef, fl_dir, fl_g, fl_cnt, fl_off, fl_cursor, fl_entries;  // staged first light
+    // ground-illumination rays of every cell (sosb_set_ground_rays) and the scratch of sosb_prepare_ground
+    DevBuf gr_off, gr_loc, gr_w, gr_cols, gr_cos, gr_ok, gr_value, gr_cnt, gr_cursor;
+    int64_t gr_n = 0;
     int64_t plane_version = 0;  // incremented by every plane rebuild (the pair contractions follow it)
     bool have_first = false;
     bool tables = true;  // build and use node tables (sosb_set_node_tables)
@@ -788,6 +791,108 @@ __global__ void bucket_scan_kernel(const int* __restrict__ cnt, int n, int* off,
         __syncthreads();
     }
     if (threadIdx.x == 0) off[n] = carry;
+}
+
+// ------------------------------------------------------------------ ground preparation on the device
+// engine_core.Solver.prepare_ground (src/sosfuse2/solve/engine_core.py:103-147) for a state's optics over the
+// ground-illumination rays of every cell: per ray r and wavelength w
+//   value = albedo / pi * cos_sun * exp(-(cols[0:5] . ext[:, w] + cols[5] strato_ext[w])) * ok * weight   (FP64),
+// the rays with a positive value in some wavelength kept per cell in ray order (goff, gdir, gval), and
+// gm[cell][k][w] = (sum over the cell's rays, in ray order, of factor_k(loc) value) * 2 C ext[0][w],
+// factor = ((1 - lx^2) / 2, (1 - ly^2) / 2, (1 - lz^2) / 2, -lx lz / 2), C = 3 / (16 pi).
+struct GroundRays {
+    const int* off;       // [cells + 1] first ray of each cell
+    const double* loc;    // [n][3]
+    const double* w;      // [n]
+    const double* cols;   // [n][6]
+    const double* cos;    // [n]
+    const uint8_t* ok;    // [n]
+    long long n;
+};
+
+// One thread per ray: its values for every wavelength and whether it is kept; cnt[cell] counts the kept rays.
+__global__ void ground_value_kernel(GroundRays g, int ns, int W, double albedo, const double* __restrict__ ext,
+                                    const double* __restrict__ strato_ext, double* __restrict__ value,
+                                    int* __restrict__ cnt, const int* __restrict__ ray_cell) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n) return;
+    const double* c = g.cols + r * 6;
+    bool take = false;
+    for (int w = 0; w < W; ++w) {
+        double od = c[0] * ext[w];
+        for (int k = 1; k < 5; ++k) od += c[k] * ext[k * W + w];
+        if (strato_ext) od += c[5] * strato_ext[w];
+        const double v = (((albedo / M_PI) * g.cos[r]) * exp(-od)) * (double)g.ok[r] * g.w[r];
+        value[r * W + w] = v;
+        take |= v > 0.0;
+    }
+    if (take) atomicAdd(&cnt[ray_cell[r]], 1);
+}
+
+// One block per cell: gm by threads (k, w) summing the cell's rays in order, then warp 0 writes the kept rays'
+// directions and values in ray order from goff[cell].
+__global__ void ground_cell_kernel(GroundRays g, int W, const double* __restrict__ ext0, const double* __restrict__ value,
+                                   const int* __restrict__ goff, float* __restrict__ gm, float* __restrict__ gdir,
+                                   float4* __restrict__ gdir4, float* __restrict__ gval) {
+    const int cell = blockIdx.x;
+    const int r0 = g.off[cell], r1 = g.off[cell + 1];
+    for (int q = threadIdx.x; q < 4 * W; q += blockDim.x) {
+        const int k = q / W, w = q % W;
+        double acc = 0.0;
+        for (int r = r0; r < r1; ++r) {
+            const double* l = g.loc + (size_t)r * 3;
+            double f;
+            if (k == 0) f = (1.0 - l[0] * l[0]) / 2.0;
+            else if (k == 1) f = (1.0 - l[1] * l[1]) / 2.0;
+            else if (k == 2) f = (1.0 - l[2] * l[2]) / 2.0;
+            else f = (-l[0] * l[2]) / 2.0;
+            acc += f * value[(size_t)r * W + w];
+        }
+        gm[((size_t)cell * 4 + k) * W + w] = (float)(acc * ((2.0 * (3.0 / (16.0 * M_PI))) * ext0[w]));
+    }
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    int pos = goff[cell];
+    for (int base = r0; base < r1; base += 32) {
+        const int r = base + lane;
+        bool take = false;
+        if (r < r1)
+            for (int w = 0; w < W; ++w) take |= value[(size_t)r * W + w] > 0.0;
+        const unsigned bal = __ballot_sync(FULL_MASK, take);
+        if (take) {
+            const int at = pos + __popc(bal & ((1u << lane) - 1u));
+            const double* l = g.loc + (size_t)r * 3;
+            const float x = (float)l[0], y = (float)l[1], z = (float)l[2];
+            gdir[(size_t)at * 3] = x;
+            gdir[(size_t)at * 3 + 1] = y;
+            gdir[(size_t)at * 3 + 2] = z;
+            gdir4[at] = make_float4(x, y, z, 0.0f);
+            for (int w = 0; w < W; ++w) gval[(size_t)at * W + w] = (float)value[(size_t)r * W + w];
+        }
+        pos += __popc(bal);
+    }
+}
+
+// gsame[cell]: the next solar-zenith cell of the same height keeps the same ground directions, bit for bit.
+__global__ void ground_same_kernel(const int* __restrict__ goff, const float* __restrict__ gdir, int ns, int nc,
+                                   uint8_t* __restrict__ same) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= ns) return;
+    uint8_t v = 0;
+    if (cell % nc != nc - 1) {
+        const int n0 = goff[cell + 1] - goff[cell], n1 = goff[cell + 2] - goff[cell + 1];
+        if (n0 > 0 && n0 == n1) {
+            v = 1;
+            const unsigned* a = reinterpret_cast<const unsigned*>(gdir) + (size_t)goff[cell] * 3;
+            const unsigned* b = reinterpret_cast<const unsigned*>(gdir) + (size_t)goff[cell + 1] * 3;
+            for (int i = 0; i < n0 * 3; ++i)
+                if (a[i] != b[i]) {
+                    v = 0;
+                    break;
+                }
+        }
+    }
+    same[cell] = v;
 }
 
 // Ground sums of the bucketed pairs: lane = pair, pairs of one bucket visit the same ground directions, so the
@@ -2686,7 +2791,8 @@ int sosb_destroy(sosb_handle s) {
                       &s->fg, &s->norms, &s->partials, &s->dots, &s->ctrl_dev, &s->report_dev, &s->ring_g[0],
                       &s->ring_g[1], &s->ring_g[2], &s->ring_g[3], &s->ring_f[0], &s->ring_f[1], &s->ring_f[2],
                       &s->ring_f[3], &s->fl_val0, &s->fl_coef, &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off,
-                      &s->fl_cursor, &s->fl_entries};
+                      &s->fl_cursor, &s->fl_entries, &s->gr_off, &s->gr_loc, &s->gr_w, &s->gr_cols, &s->gr_cos,
+                      &s->gr_ok, &s->gr_value, &s->gr_cnt, &s->gr_cursor};
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
@@ -2871,6 +2977,93 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
     s->have_first = false;
     invalidate_tables(s->cells, false);
     invalidate_tables(s->obs, false);
+    graph_reset(s);
+    return 0;
+}
+
+int sosb_set_ground_rays(sosb_handle s, const sosb_ground_rays* g) {
+    if (!s || !g) return 1;
+    if (g->n < 0 || (g->n > 0 && (!g->cell || !g->loc || !g->weight || !g->cols || !g->cos_sun || !g->ok)))
+        return fail(s, "E_GROUND: missing ground-ray array");
+    if (g->n >= (1LL << 31)) return fail(s, "E_GROUND: %lld ground rays", (long long)g->n);
+    std::vector<int> off((size_t)s->ns + 1, 0);
+    for (int64_t r = 0; r < g->n; ++r) {
+        const int c = g->cell[r];
+        if (c < 0 || c >= s->ns || (r > 0 && c < g->cell[r - 1]))
+            return fail(s, "E_GROUND: ground-ray cells must ascend within 0..%lld", (long long)s->ns - 1);
+        ++off[(size_t)c + 1];
+    }
+    for (int64_t c = 0; c < s->ns; ++c) off[c + 1] += off[c];
+    const size_t n = (size_t)std::max<int64_t>(g->n, 1);
+    TRY(dput_vec(s, s->gr_off, off));
+    TRY(dalloc(s, s->gr_loc, n * 3 * sizeof(double)));
+    TRY(dalloc(s, s->gr_w, n * sizeof(double)));
+    TRY(dalloc(s, s->gr_cols, n * 6 * sizeof(double)));
+    TRY(dalloc(s, s->gr_cos, n * sizeof(double)));
+    TRY(dalloc(s, s->gr_ok, n));
+    TRY(dalloc(s, s->gr_cursor, n * sizeof(int)));  // ray -> cell
+    if (g->n > 0) {
+        std::vector<int> cell(g->cell, g->cell + g->n);
+        CK(cudaMemcpyAsync(s->gr_loc.p, g->loc, (size_t)g->n * 3 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->gr_w.p, g->weight, (size_t)g->n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->gr_cols.p, g->cols, (size_t)g->n * 6 * sizeof(double), cudaMemcpyHostToDevice,
+                           s->stream));
+        CK(cudaMemcpyAsync(s->gr_cos.p, g->cos_sun, (size_t)g->n * sizeof(double), cudaMemcpyHostToDevice,
+                           s->stream));
+        CK(cudaMemcpyAsync(s->gr_ok.p, g->ok, (size_t)g->n, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->gr_cursor.p, cell.data(), cell.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->gr_n = g->n;
+    return 0;
+}
+
+int sosb_prepare_ground(sosb_handle s, double albedo, const double* ext, const double* strato_ext) {
+    if (!s || !ext) return 1;
+    if (!s->have_constants) return fail(s, "E_STATE: constants not set");
+    if (!s->gr_off.p) return fail(s, "E_STATE: ground rays not set");
+    if (s->d.strato && !strato_ext) return fail(s, "E_CONSTANTS: missing stratospheric extinction");
+    const int W = s->d.W, ns = s->ns;
+    const size_t n = (size_t)std::max<int64_t>(s->gr_n, 1);
+    DevBuf dext, dsext;
+    TRY(dput(s, dext, ext, 5 * (size_t)W * sizeof(double)));
+    if (s->d.strato) TRY(dput(s, dsext, strato_ext, (size_t)W * sizeof(double)));
+    TRY(dalloc(s, s->gr_value, n * W * sizeof(double)));
+    TRY(dalloc(s, s->gr_cnt, ((size_t)ns + 1) * sizeof(int)));
+    TRY(dalloc(s, s->gm, (size_t)ns * 4 * W * sizeof(float)));
+    TRY(dalloc(s, s->goff, ((size_t)ns + 1) * sizeof(int)));
+    TRY(dalloc(s, s->gdir, n * 3 * sizeof(float)));
+    TRY(dalloc(s, s->gdir4, n * sizeof(float4)));
+    TRY(dalloc(s, s->gval, n * W * sizeof(float)));
+    TRY(dalloc(s, s->gsame, (size_t)ns));
+    const GroundRays g{P<int>(s->gr_off), P<double>(s->gr_loc), P<double>(s->gr_w), P<double>(s->gr_cols),
+                       P<double>(s->gr_cos), P<uint8_t>(s->gr_ok), (long long)s->gr_n};
+    DevBuf cursor;
+    TRY(dalloc(s, cursor, ((size_t)ns + 1) * sizeof(int)));
+    CK(cudaMemsetAsync(s->gr_cnt.p, 0, ((size_t)ns + 1) * sizeof(int), s->stream));
+    {
+        Timer t(s, K_OTHER);
+        if (s->gr_n > 0)
+            ground_value_kernel<<<(unsigned)((s->gr_n + 127) / 128), 128, 0, s->stream>>>(
+                g, ns, W, albedo, P<double>(dext), s->d.strato ? P<double>(dsext) : nullptr, P<double>(s->gr_value),
+                P<int>(s->gr_cnt), P<int>(s->gr_cursor));
+        TRY(launch_check(s));
+        bucket_scan_kernel<<<1, 1024, 0, s->stream>>>(P<int>(s->gr_cnt), ns, P<int>(s->goff), P<int>(cursor));
+        TRY(launch_check(s));
+        ground_cell_kernel<<<ns, 256, 0, s->stream>>>(g, W, P<double>(dext), P<double>(s->gr_value), P<int>(s->goff),
+                                                      P<float>(s->gm), P<float>(s->gdir), P<float4>(s->gdir4),
+                                                      P<float>(s->gval));
+        TRY(launch_check(s));
+        ground_same_kernel<<<(ns + 127) / 128, 128, 0, s->stream>>>(P<int>(s->goff), P<float>(s->gdir), ns, s->d.nc,
+                                                                    P<uint8_t>(s->gsame));
+        TRY(launch_check(s));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    TRY(dfree(s, dext));
+    TRY(dfree(s, dsext));
+    TRY(dfree(s, cursor));
+    s->have_first = false;  // the first light's ground term uses these arrays
     graph_reset(s);
     return 0;
 }

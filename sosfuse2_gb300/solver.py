@@ -55,6 +55,8 @@ class Kernel:
         st._keep.clear()
         self.n_query = len(st['query_d'])
         self.n_rays = len(st['cell_d'])
+        self.ground_rays = None    # the rays of set_ground_rays
+        self.ground_optics = None  # (albedo, ext, strato_ext) of the last prepare_ground since the constants
 
     def update(self, state):
         """Replace the constants by those of another state with the same geometry (bundles stay on the device)."""
@@ -64,6 +66,7 @@ class Kernel:
         self._check(self.lib.sosb_set_constants(self.h, ctypes.byref(st.constants())))
         st._keep.clear()
         self.state = st
+        self.ground_optics = None  # the state's own ground arrays replaced any prepared on the device
 
     def set_node_tables(self, enable):
         """Store per-node geometry and attenuation at the first launch over a bundle and read them in warm launches
@@ -97,6 +100,31 @@ class Kernel:
             pass
 
     # ------------------------------------------------------------------ reference Kernel surface
+    def set_ground_rays(self, rays):
+        """Upload the ground-illumination rays of every cell (synth.Family.ground_rays(); the geometry of
+        engine_core.Solver.prepare_ground) for sosb_prepare_ground."""
+        keep = dict(cell=np.ascontiguousarray(rays['cell'], np.int32),
+                    loc=np.ascontiguousarray(rays['loc'], np.float64),
+                    weight=np.ascontiguousarray(rays['weight'], np.float64),
+                    cols=np.ascontiguousarray(rays['cols'], np.float64),
+                    cos_sun=np.ascontiguousarray(rays['cos_sun'], np.float64),
+                    ok=np.ascontiguousarray(rays['ok'], np.uint8))
+        g = _abi.GroundRays(n=len(keep['cell']))
+        for name, ct in _abi.GroundRays._fields_[1:]:
+            setattr(g, name, keep[name].ctypes.data_as(ct))
+        self._check(self.lib.sosb_set_ground_rays(self.h, ctypes.byref(g)))
+        self.ground_rays = keep
+
+    def prepare_ground(self, albedo, ext, strato_ext=None):
+        """Solver.prepare_ground on the device for a state's albedo and FP64 extinction ext [5, W] (and the
+        stratospheric extinction [W]); replaces the ground arrays of the constants until the next `update`."""
+        self._stream()
+        e = np.ascontiguousarray(ext, np.float64)
+        s = None if strato_ext is None else np.ascontiguousarray(strato_ext, np.float64)
+        self._check(self.lib.sosb_prepare_ground(self.h, float(albedo), e.ctypes.data_as(_abi.P_f64),
+                                                 None if s is None else s.ctypes.data_as(_abi.P_f64)))
+        self.ground_optics = (float(albedo), e, s)
+
     def set_observer(self, bundle):
         """Replace the observer (phase-2) ray bundle by `bundle` (the packed-state bundle keys, without prefix); the
         cell bundle and the constants stay. Node tables and pairs of the old observer bundle are dropped."""

@@ -473,6 +473,13 @@ class Family:
         self.g_factor = np.stack([(1 - lo[:, 0] ** 2) / 2, (1 - lo[:, 1] ** 2) / 2, (1 - lo[:, 2] ** 2) / 2,
                                   -lo[:, 0] * lo[:, 2] / 2], -1)
 
+    def ground_rays(self):
+        """The ground-illumination rays of every cell for sosb_set_ground_rays: cell, local direction, weight, the
+        six slant columns to the ground and on to the sun, the clipped solar cosine at the ground point and whether
+        that point is lit (the geometry `ground` combines with a state's optics)."""
+        return dict(cell=self.g_cell.astype(np.int32), loc=self.g_loc, weight=self.g_w, cols=self.g_cols,
+                    cos_sun=self.g_cos, ok=self.g_ok.astype(np.uint8))
+
     def ground(self, atm, ext):
         """gm [ns, 4, W], goff, gdir, gval of one atmosphere (vectorised over all ground rays)."""
         od = self.g_cols[:, :5] @ ext
@@ -489,12 +496,18 @@ class Family:
         goff = np.r_[0, np.cumsum(np.bincount(self.g_cell[take], minlength=ns))].astype(np.int64)
         return (gm.astype(np.float32), goff, self.g_loc[take].astype(np.float32), value[take].astype(np.float32))
 
-    def state(self, atm, seed=0):
-        """Packed-state arrays of atmosphere `atm` (same profile shapes as the family's)."""
+    def state(self, atm, seed=0, ground=True):
+        """Packed-state arrays of atmosphere `atm` (same profile shapes as the family's). ground=False leaves the
+        ground arrays empty for a handle that prepares them on the device (Kernel.prepare_ground)."""
         h, chi, L, W = self.h, self.chi, self.L, atm.W
         K = (L + 1) * (L + 2) // 2
         ext = atm.ext()
-        gm, goff, gdir, gval = self.ground(atm, ext)
+        if ground:
+            gm, goff, gdir, gval = self.ground(atm, ext)
+        else:
+            ns = len(h) * len(chi)
+            gm, goff = np.zeros((ns, 4, W), np.float32), np.zeros(ns + 1, np.int64)
+            gdir, gval = np.zeros((0, 3), np.float32), np.zeros((0, W), np.float32)
         u, wu = gauss01(self.path_n)
         uq, wuq = gauss01(self.query_n)
         step = 0.5
@@ -573,11 +586,15 @@ def random_amounts(seed):
                 ozone_du=float(rng.uniform(250, 400)), albedo=float(rng.uniform(0.05, 0.8)))
 
 
-def family_state(family, seed):
-    """A state of `family` with amounts random_amounts(seed)."""
+def family_atmosphere(family, seed):
+    """The atmosphere of `family` with amounts random_amounts(seed)."""
     a = random_amounts(seed)
-    atm = Atmosphere(family.shape.wl, seed=seed, top=family.top, scale_height=family.shape.H, **a)
-    return family.state(atm, seed)
+    return Atmosphere(family.shape.wl, seed=seed, top=family.top, scale_height=family.shape.H, **a)
+
+
+def family_state(family, seed, ground=True):
+    """A state of `family` with amounts random_amounts(seed) (ground=False: see Family.state)."""
+    return family.state(family_atmosphere(family, seed), seed, ground=ground)
 
 
 def config1(seed=0, nh=241, W=30, nmu=12, nphi=16, path_n=12, L=32, chi_deg=None, **kw):

@@ -66,6 +66,9 @@ def make_table(s, source, hs, el, az, group=32, batch=25, log=print, *, family):
             rays = family.view_bundle(hs[part], el, az)
             if kernel is None:
                 kernel = Kernel(st, k0.device)
+                if k0.ground_optics is not None:  # ground arrays prepared on the solver's handle: the same here
+                    kernel.set_ground_rays(k0.ground_rays)
+                    kernel.prepare_ground(*k0.ground_optics)
             kernel.set_observer(rays)
             one = _spectral(kernel.host(kernel.transport(None, True)), solar)
             multiple = _spectral(kernel.host(kernel.transport(field, False)), solar)
