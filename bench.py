@@ -55,6 +55,8 @@ def args_():
     p.add_argument('--no-forms', action='store_true', help='plain single-state solve only')
     p.add_argument('--precision-only', action='store_true',
                    help='only the precision form (projection forms on a 30-wavelength state), one JSON line')
+    p.add_argument('--ground-only', action='store_true',
+                   help='only the ground-preparation form (host against device, a config-0 family state)')
     p.add_argument('--batch', type=int, default=64, help='states per batched step')
     p.add_argument('--train-solves', type=int, default=512)
     p.add_argument('--epochs', type=int, default=30)
@@ -471,6 +473,10 @@ def run_gb300(a, rank, world):
     if a.precision_only:
         if rank == 0:
             print(json.dumps(dict(precision=_precision_form(device))), flush=True)
+        return
+    if a.ground_only:
+        if rank == 0:
+            print(json.dumps(dict(ground=_ground_form(synth.config0_family(), device))), flush=True)
         return
     dist = None
     if world > 1:

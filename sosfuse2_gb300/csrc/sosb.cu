@@ -829,17 +829,20 @@ __global__ void ground_value_kernel(GroundRays g, int ns, int W, double albedo, 
     if (take) atomicAdd(&cnt[ray_cell[r]], 1);
 }
 
-// One block per cell: gm by threads (k, w) summing the cell's rays in order, then warp 0 writes the kept rays'
-// directions and values in ray order from goff[cell].
-__global__ void ground_cell_kernel(GroundRays g, int W, const double* __restrict__ ext0, const double* __restrict__ value,
-                                   const int* __restrict__ goff, float* __restrict__ gm, float* __restrict__ gdir,
-                                   float4* __restrict__ gdir4, float* __restrict__ gval) {
+// One block per cell: warp j sums gm's (k, w) entries q = j, j + warps, ... over the cell's rays (lanes stride the
+// rays, FP64, then a shuffle tree; the order differs from a sequential sum only far below the FP32 result's last
+// bit), then warp 0 writes the kept rays' directions and values in ray order from goff[cell].
+__global__ void __launch_bounds__(256)
+    ground_cell_kernel(GroundRays g, int W, const double* __restrict__ ext0, const double* __restrict__ value,
+                       const int* __restrict__ goff, float* __restrict__ gm, float* __restrict__ gdir,
+                       float4* __restrict__ gdir4, float* __restrict__ gval) {
     const int cell = blockIdx.x;
     const int r0 = g.off[cell], r1 = g.off[cell + 1];
-    for (int q = threadIdx.x; q < 4 * W; q += blockDim.x) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int q = wid; q < 4 * W; q += nw) {
         const int k = q / W, w = q % W;
         double acc = 0.0;
-        for (int r = r0; r < r1; ++r) {
+        for (int r = r0 + lane; r < r1; r += 32) {
             const double* l = g.loc + (size_t)r * 3;
             double f;
             if (k == 0) f = (1.0 - l[0] * l[0]) / 2.0;
@@ -848,10 +851,11 @@ __global__ void ground_cell_kernel(GroundRays g, int W, const double* __restrict
             else f = (-l[0] * l[2]) / 2.0;
             acc += f * value[(size_t)r * W + w];
         }
-        gm[((size_t)cell * 4 + k) * W + w] = (float)(acc * ((2.0 * (3.0 / (16.0 * M_PI))) * ext0[w]));
+#pragma unroll
+        for (int dd = 16; dd >= 1; dd >>= 1) acc += __shfl_xor_sync(FULL_MASK, acc, dd);
+        if (lane == 0) gm[((size_t)cell * 4 + k) * W + w] = (float)(acc * ((2.0 * (3.0 / (16.0 * M_PI))) * ext0[w]));
     }
-    if (threadIdx.x >= 32) return;
-    const int lane = threadIdx.x;
+    if (wid != 0) return;
     int pos = goff[cell];
     for (int base = r0; base < r1; base += 32) {
         const int r = base + lane;
@@ -873,26 +877,25 @@ __global__ void ground_cell_kernel(GroundRays g, int W, const double* __restrict
     }
 }
 
-// gsame[cell]: the next solar-zenith cell of the same height keeps the same ground directions, bit for bit.
+// gsame[cell]: the next solar-zenith cell of the same height keeps the same ground directions, bit for bit (one
+// warp per cell comparing the two direction blocks).
 __global__ void ground_same_kernel(const int* __restrict__ goff, const float* __restrict__ gdir, int ns, int nc,
                                    uint8_t* __restrict__ same) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= ns) return;
-    uint8_t v = 0;
+    const int lane = threadIdx.x & 31;
+    const int cell = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (cell >= ns) return;  // the whole warp leaves together
+    bool v = false;
     if (cell % nc != nc - 1) {
         const int n0 = goff[cell + 1] - goff[cell], n1 = goff[cell + 2] - goff[cell + 1];
         if (n0 > 0 && n0 == n1) {
-            v = 1;
             const unsigned* a = reinterpret_cast<const unsigned*>(gdir) + (size_t)goff[cell] * 3;
             const unsigned* b = reinterpret_cast<const unsigned*>(gdir) + (size_t)goff[cell + 1] * 3;
-            for (int i = 0; i < n0 * 3; ++i)
-                if (a[i] != b[i]) {
-                    v = 0;
-                    break;
-                }
+            bool differ = false;
+            for (int i = lane; i < n0 * 3; i += 32) differ |= a[i] != b[i];
+            v = !__any_sync(FULL_MASK, differ);
         }
     }
-    same[cell] = v;
+    if (lane == 0) same[cell] = v ? 1 : 0;
 }
 
 // Ground sums of the bucketed pairs: lane = pair, pairs of one bucket visit the same ground directions, so the
@@ -3055,8 +3058,8 @@ int sosb_prepare_ground(sosb_handle s, double albedo, const double* ext, const d
                                                       P<float>(s->gm), P<float>(s->gdir), P<float4>(s->gdir4),
                                                       P<float>(s->gval));
         TRY(launch_check(s));
-        ground_same_kernel<<<(ns + 127) / 128, 128, 0, s->stream>>>(P<int>(s->goff), P<float>(s->gdir), ns, s->d.nc,
-                                                                    P<uint8_t>(s->gsame));
+        ground_same_kernel<<<(unsigned)(((long long)ns * 32 + 127) / 128), 128, 0, s->stream>>>(
+            P<int>(s->goff), P<float>(s->gdir), ns, s->d.nc, P<uint8_t>(s->gsame));
         TRY(launch_check(s));
     }
     CK(cudaStreamSynchronize(s->stream));
