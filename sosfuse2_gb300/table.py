@@ -34,13 +34,19 @@ def _spectral(rad, solar):
     return ((r[..., 0] + r[..., 1]) + r[..., 2]) * solar[None, :]
 
 
-def make_table(s, source, hs, el, az, group=32, batch=25, log=print, *, family):
-    """(table [len(hs), len(el), len(az), W] float32, seconds per batch) for the converged `source` of Solver `s`;
-    `family` is the synth.Family the state was built from (it builds the table's rays)."""
+def make_table(s, source, hs, el, az, group=32, batch=25, log=print, *, family=None, views=None):
+    """(table [len(hs), len(el), len(az), W] float32, seconds per batch) for the converged `source` of Solver `s`.
+    The view rays of a batch of solar elevations come from `views(hs_batch, el, az)` (a packed bundle, one cell per
+    solar elevation or per 64-ray pack, rays in (elevation, view elevation, azimuth) order), by default from
+    `family.view_bundle`, the synth.Family the state was built from."""
     if group < 1:
         raise ValueError('E_TABLE_GROUP: group must be positive')
     if batch < 1:
         raise ValueError('E_TABLE_BATCH: batch must be positive')
+    if views is None:
+        if family is None:
+            raise ValueError('E_TABLE_GEOMETRY: make_table needs the state family or a view-ray builder')
+        views = family.view_bundle
     st = s.state
     k0 = s.kernel
     torch = k0.torch
@@ -56,14 +62,16 @@ def make_table(s, source, hs, el, az, group=32, batch=25, log=print, *, family):
     hs, el, az = (np.asarray(v, np.float64).ravel() for v in (hs, el, az))
     solar = np.asarray(st['solar'], np.float64)
     table = np.empty((len(hs), len(el), len(az), st.W), np.float32)
-    views = len(el) * len(az)
+    views_n = len(el) * len(az)
     kernel = None
     seconds = []
     try:
         for b0 in range(0, len(hs), batch):
             t = time.monotonic()
             part = list(range(b0, min(b0 + batch, len(hs))))
-            rays = family.view_bundle(hs[part], el, az)
+            rays = views(hs[part], el, az)
+            if len(rays['d']) != len(part) * views_n:
+                raise ValueError(f'E_TABLE_GEOMETRY: {len(rays["d"])} view rays for {len(part)} x {views_n} entries')
             if kernel is None:
                 kernel = Kernel(st, k0.device)
                 if k0.ground_optics is not None:  # ground arrays prepared on the solver's handle: the same here
@@ -77,7 +85,7 @@ def make_table(s, source, hs, el, az, group=32, batch=25, log=print, *, family):
                 raise RuntimeError('E_RADIANCE_INVALID: nonfinite/negative')
             table[part] = spec.reshape(len(part), len(el), len(az), st.W)
             seconds.append(time.monotonic() - t)
-            log(f'TABLE_FAST sun={hs[part[0]]:+g}..{hs[part[-1]]:+g} rays={len(part) * views} '
+            log(f'TABLE_FAST sun={hs[part[0]]:+g}..{hs[part[-1]]:+g} rays={len(part) * views_n} '
                 f'seconds={seconds[-1]:.2f}')
     finally:
         if kernel is not None:

@@ -82,3 +82,26 @@ def test_table_rejects_bad_arguments():
     with pytest.raises(ValueError, match='E_SOURCE_SHAPE'):
         make_table(solver, good[:, :5], [-3.0], [45.0], [90.0], family=fam)
     solver.kernel.close()
+
+
+def test_table_matches_reference_golden():
+    """make_table over the reference's own view rays of the walkthrough state (tests/golden/table_walk1.npz) against
+    the reference's table (its make_table on the NumPy backend): the numeric gate, rtol 1e-3 on entries above 1e-6
+    of the largest."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from test_table_golden import table_state
+
+    from sosfuse2_gb300.solver import Solver
+    from sosfuse2_gb300.state import PackedState
+    from sosfuse2_gb300.table import make_table
+
+    arrays, bundle, source, ref, hs, el, az = table_state()
+    solver = Solver(PackedState(arrays), device='cuda:0')
+    table, _ = make_table(solver, source, hs, el, az, batch=len(hs), log=lambda m: None,
+                          views=lambda h, e, a: bundle)
+    big = np.abs(ref) > 1e-6 * np.abs(ref).max()
+    assert np.all(np.abs(table[big] - ref[big]) <= 1e-3 * np.abs(ref[big]))
+    solver.kernel.close()
