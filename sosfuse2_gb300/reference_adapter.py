@@ -138,3 +138,30 @@ def solve(s, geometry, scope, max_eval=64, tolerance=1e-3, device=None):
         return solver.solve(max_eval, tolerance)
     finally:
         solver.kernel.close()
+
+
+def view_rays(s, hs, el, az):
+    """The view rays of a radiance table of a reference-assembled state as one packed bundle per call: the packs
+    `Solver.query` builds for every solar elevation of `hs` over the (el, az) grid, captured without transport as
+    outputs/radiance_table.py:43-54 does, one bundle cell per 64-ray pack."""
+    from sosfuse2.outputs import radiance_table as tf
+
+    ee, aa = np.meshgrid(np.asarray(el, float), np.asarray(az, float), indexing='ij')
+    raws = [r for h in np.asarray(hs, float).ravel() for r in tf._capture(s, float(h), ee, aa, np.empty(0, 'f4'))]
+    cq = s.kernel.setup(s, raws[0]['nq'])
+    return _bundle(raws, cq, 'strato_ext' in cq)
+
+
+def make_table(s, source, hs, el, az, group=32, batch=25, log=print, *, geometry, scope, device=None):
+    """outputs/radiance_table.make_table (radiance_table.py:167-219) of a reference-assembled state on the GPU: the
+    reference's own view rays (view_rays), both phase-2 transports on the device, `query`'s reduction; returns
+    (table [len(hs), len(el), len(az), W] float32, seconds per batch) like the reference."""
+    from .solver import Solver
+    from .state import PackedState
+    from .table import make_table as table
+
+    solver = Solver(PackedState(pack_state(s, geometry, scope)), device=device)
+    try:
+        return table(solver, source, hs, el, az, group, batch, log, views=lambda h, e, a: view_rays(s, h, e, a))
+    finally:
+        solver.kernel.close()
