@@ -296,8 +296,9 @@ def _batch_kernels(fam, seeds, device):
 
 
 def _time_batched(a, fam, ws, device, seeds, dist=None):
-    """Plain and learned-start batched solves of the held-out family states: converged solves/s of each form (each
-    step bracketed by a barrier over the ranks and a device synchronisation)."""
+    """Plain and learned-start batched solves of the held-out family states, and the plain solves one state at a
+    time (`sequential`: the batch driver with one solve in flight): converged solves/s of each form (each step
+    bracketed by a barrier over the ranks and a device synchronisation)."""
     import torch
 
     from sosfuse2_gb300 import _abi, learned
@@ -309,17 +310,18 @@ def _time_batched(a, fam, ws, device, seeds, dist=None):
     outs = [k.field() for k in kernels]
     out_ptrs = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])
     res = {}
-    for form in ('plain', 'learned'):
+    for form in ('plain', 'learned', 'sequential'):
         times, conv, evals, launches = [], [], [], 0
         for step in range(a.warmup + a.steps):
             for k, st in zip(kernels, states):
                 k.update(st)  # no first light carried between steps
             bracket(dist)
             t0 = time.perf_counter()
-            if form == 'plain':
+            if form in ('plain', 'sequential'):
                 stats = (_abi.Stats * n)()
                 status = (ctypes.c_int32 * n)()
-                lib.sosb_solve_batch(handles, n, 64, 1e-3, None, out_ptrs, 1, stats, status, 0)
+                lib.sosb_solve_batch(handles, n, 64, 1e-3, None, out_ptrs, 1, stats, status,
+                                     1 if form == 'sequential' else 0)
                 ok = [not status[i] for i in range(n)]
                 ev = [stats[i].evaluations for i in range(n) if not status[i]]
                 nl = sum(stats[i].kernel_launches for i in range(n))
@@ -532,10 +534,12 @@ def run_gb300(a, rank, world):
         forms = _time_batched(a, fam, ws, device, seeds, dist)
         forms['training'] = report
         forms['learned_vs_plain'] = forms['learned']['value'] / max(forms['plain']['value'], 1e-30)
+        forms['learned_batched_vs_plain_sequential'] = (forms['learned']['value']
+                                                         / max(forms['sequential']['value'], 1e-30))
         forms['precision'] = _precision_form(device)
         forms['table'] = _table_form(fam, device)
         forms['ground'] = _ground_form(fam, device)
-        launches += forms['plain']['kernel_launches'] + forms['learned']['kernel_launches']
+        launches += sum(forms[f]['kernel_launches'] for f in ('plain', 'learned', 'sequential'))
     clk = clocks.stop()
     value_plain = 1e3 / plain_ms
     value = forms['learned']['value'] if forms else value_plain
