@@ -21,6 +21,11 @@ transport integrates). Rays are processed all at once, vectorised over rays, one
 arithmetic is the reference's, operation for operation, so the oracle agrees with the reference to FP32 rounding of
 the transcendental functions.
 
+Pins: tests/test_oracle_golden.py against the reference's outputs of tests/golden/{walk1,strato1,strato15}.npz
+(per-ray radiance, moments, apply, boxes, the converged field) and tests/test_table_golden.py against the reference's
+radiance table of the walkthrough state (tests/golden/table_walk1.npz). oracle/fp64.py evaluates the same operations
+in float64 for the per-pixel error report.
+
 Out of scope here (not on the fixtures' path): the extended top above 80 km, the tabulated tropospheric Mie phase,
 the two-layer aerosol profile and the combined SH plane.
 """
