@@ -53,7 +53,8 @@ def test_version_string(lib):
 
 
 @pytest.mark.parametrize('cname,pytype', [('sosb_dims', _abi.Dims), ('sosb_constants', _abi.Constants),
-                                           ('sosb_bundle', _abi.Bundle), ('sosb_stats', _abi.Stats)])
+                                           ('sosb_bundle', _abi.Bundle), ('sosb_stats', _abi.Stats),
+                                           ('sosb_ground_rays', _abi.GroundRays)])
 def test_struct_layout_matches_header(cname, pytype):
     assert header_struct_fields(cname) == [f[0] for f in pytype._fields_]
 
@@ -63,3 +64,13 @@ def test_null_handle_is_an_error(lib):
     lib.sosb_last_error.argtypes = [ctypes.c_void_p]
     assert lib.sosb_last_error(None).startswith(b'E_HANDLE')
     assert lib.sosb_destroy(None) == 0
+
+
+def test_ground_entry_points_reject_null_handles(lib):
+    lib.sosb_set_ground_rays.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.sosb_prepare_ground.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+    rays = _abi.GroundRays(n=0)
+    assert lib.sosb_set_ground_rays(None, ctypes.byref(rays)) == 1
+    ext = (ctypes.c_double * 5)()
+    assert lib.sosb_prepare_ground(None, 0.3, ext, None) == 1
+
