@@ -185,6 +185,25 @@ int sosb_solve(sosb_handle h, int max_eval, double tolerance, const float *x0_ho
  * sosb_get_timing fills ms[k] and launches[k] for k < n. */
 int sosb_set_timing(sosb_handle h, int on);
 int sosb_get_timing(sosb_handle h, double *ms, int64_t *launches, int n);
+/* Profile shapes of a synthetic atmosphere (sosfuse2_gb300.synth.Atmosphere) for sosb_column_table: air exp(-h/8),
+ * aerosol exp(-h/aerosol_height), ozone exp(1 - z - exp(-z)) * ozone_norm with z = (h - ozone_peak) / 5, NO2
+ * exp(-((h - no2_center) / 4)^2 / 2), O4 air^2, the first five on h clipped to [0, top]; the stratospheric layer
+ * exp(-((h - strato_center) / strato_sigma)^2 / 2) / strato_norm when strato is nonzero. */
+typedef struct {
+    double top, aerosol_height, ozone_peak, ozone_norm, no2_center;
+    int32_t strato;
+    double strato_center, strato_sigma, strato_norm;
+} sosb_profile_shape;
+/* Solar column table of a synthetic state family (host, no device work; the project's counterpart of the reference's
+ * sun geometry, src/sosfuse2/solve/engine_core.py:103-147): for every height h[i] and abscissa x[j] the six slant
+ * columns (five profile shapes and the stratospheric one) along the upward ray of zenith cosine
+ * mu = mg + (1 - mg) x^2 (mu = mg + 1e-9 at x = 0) into up[i][j][6] and along the downward ray
+ * mu = max(mg - (1 + mg) x^2, -1) (mg - 1e-9 at x = 0) into down[i][j][6], mg the horizon cosine at that height; each
+ * path cut at the shadow cylinder, the tangent point and the shells (at most 8) and integrated by the n_gl-point rule
+ * (gl_u, gl_w on [0, 1]). threads: host threads (0: all cores). */
+int sosb_column_table(int n_h, const double *h, int n_x, const double *x, const double *shells, int n_shells,
+                      const double *gl_u, const double *gl_w, int n_gl, const sosb_profile_shape *shape, double *up,
+                      double *down, int threads);
 /* Ground-illumination rays of every cell, the geometry of engine_core.Solver.prepare_ground
  * (src/sosfuse2/solve/engine_core.py:103-147) for the handle's grid: ray r belongs to cell[r] (ascending), arrives
  * from the local direction loc[r][3] with quadrature weight weight[r]; cols[r][6] are its slant columns (five

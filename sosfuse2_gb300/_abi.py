@@ -62,6 +62,12 @@ class GroundRays(ctypes.Structure):
     ]
 
 
+class ProfileShape(ctypes.Structure):
+    _fields_ = [('top', c_dbl), ('aerosol_height', c_dbl), ('ozone_peak', c_dbl), ('ozone_norm', c_dbl),
+                ('no2_center', c_dbl), ('strato', c_int), ('strato_center', c_dbl), ('strato_sigma', c_dbl),
+                ('strato_norm', c_dbl)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ('evaluations', c_int), ('converged', c_int), ('seconds', c_dbl),
@@ -84,6 +90,8 @@ SIGNATURES = {
     'sosb_set_bundle': ([ctypes.c_void_p, c_int, ctypes.POINTER(Bundle)], c_int),
     'sosb_set_ground_rays': ([ctypes.c_void_p, ctypes.POINTER(GroundRays)], c_int),
     'sosb_prepare_ground': ([ctypes.c_void_p, c_dbl, P_f64, P_f64], c_int),
+    'sosb_column_table': ([c_int, P_f64, c_int, P_f64, P_f64, c_int, P_f64, P_f64, c_int, ctypes.POINTER(ProfileShape),
+                           P_f64, P_f64, c_int], c_int),
     'sosb_evaluate': ([ctypes.c_void_p, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                        ctypes.c_void_p, ctypes.c_void_p], c_int),
     'sosb_apply': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], c_int),

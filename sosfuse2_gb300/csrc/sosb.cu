@@ -2984,6 +2984,100 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
     return 0;
 }
 
+// Slant columns of the solar column table (host; the synthetic family's counterpart of the reference's sun geometry,
+// src/sosfuse2/solve/engine_core.py:103-147 and S/precompute): from radius r0 along zenith cosine mu to the top of
+// the atmosphere or the ground, the path cut at the shadow cylinder, the tangent point and the shells, each piece
+// integrated by an n-point Gauss-Legendre rule of the five profile shapes (clipped to [0, top]) and the
+// stratospheric shape; the operations of the NumPy restatement in order, in FP64.
+static void column_along(double r0, double mu, const sosb_profile_shape& a, const double* shells, int nshell,
+                         const double* u, const double* wu, int n, double out[6]) {
+    const double R = 6371.0;
+    const double px = 0.0, py = 0.0, pz = r0;
+    const double dx = std::sqrt(std::max(1.0 - mu * mu, 0.0)), dy = 0.0, dz = mu;
+    const double b = (px * dx + py * dy) + pz * dz;
+    const double pp = (px * px + py * py) + pz * pz;
+    double end = -b + std::sqrt(std::max(b * b - pp + (R + a.top) * (R + a.top), 0.0));
+    const double disc = b * b - pp + R * R;
+    const double hit = -b - std::sqrt(std::max(disc, 0.0));
+    const bool ground = disc >= 0.0 && b < 0.0 && hit >= -1e-7;
+    end = std::max(ground ? std::max(hit, 0.0) : end, 0.0);
+    const double tangent = (-b > 0.0 && -b < end) ? -b : end;
+    const double aa = dx * dx + dy * dy, bb = px * dx + py * dy, cc = px * px + py * py - R * R;
+    const double ds = bb * bb - aa * cc;
+    double cols[5 + 2 * 8];
+    int nc = 0;
+    cols[nc++] = 0.0;
+    cols[nc++] = tangent;
+    cols[nc++] = end;
+    for (int sign = -1; sign <= 1; sign += 2) {
+        const double root = (-bb + sign * std::sqrt(std::max(ds, 0.0))) / std::max(aa, 1e-30);
+        const bool ok = aa > 1e-20 && ds >= 0.0 && root > 0.0 && root < end && pz + root * dz < 0.0;
+        cols[nc++] = ok ? root : end;
+    }
+    for (int k = 0; k < nshell && k < 8; ++k) {
+        const double disc2 = b * b - pp + (R + shells[k]) * (R + shells[k]);
+        for (int sign = -1; sign <= 1; sign += 2) {
+            const double root = -b + sign * std::sqrt(std::max(disc2, 0.0));
+            cols[nc++] = (disc2 > 0.0 && root > 0.0 && root < end) ? root : end;
+        }
+    }
+    std::sort(cols, cols + nc);
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    for (int k = 0; k + 1 < nc; ++k) {
+        const double s0 = cols[k], s1 = cols[k + 1];
+        double seg[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, sst = 0.0;
+        for (int q = 0; q < n; ++q) {
+            const double t = s0 + (s1 - s0) * u[q];
+            const double qx = px + t * dx, qy = py + t * dy, qz = pz + t * dz;
+            const double h = std::sqrt((qx * qx + qy * qy) + qz * qz) - R;
+            const double w = (s1 - s0) * wu[q];
+            const double hc = std::min(std::max(h, 0.0), a.top);
+            const double air = std::exp(-hc / 8.0);
+            const double z = (hc - a.ozone_peak) / 5.0;
+            const double no2 = (hc - a.no2_center) / 4.0;
+            const double prof[5] = {air, std::exp(-hc / a.aerosol_height), std::exp(1.0 - z - std::exp(-z)) * a.ozone_norm,
+                                    std::exp(-0.5 * (no2 * no2)), air * air};
+            for (int c = 0; c < 5; ++c) seg[c] += w * prof[c];
+            if (a.strato) {
+                const double v = (h - a.strato_center) / a.strato_sigma;
+                sst += w * (std::exp(-0.5 * (v * v)) / a.strato_norm);
+            }
+        }
+        for (int c = 0; c < 5; ++c) out[c] += seg[c];
+        out[5] += sst;
+    }
+}
+
+int sosb_column_table(int n_h, const double* h, int n_x, const double* x, const double* shells, int n_shells,
+                      const double* gl_u, const double* gl_w, int n_gl, const sosb_profile_shape* shape, double* up,
+                      double* down, int threads) {
+    if (n_h < 1 || n_x < 1 || !h || !x || !gl_u || !gl_w || n_gl < 1 || !shape || !up || !down) return 1;
+    if (n_shells < 0 || n_shells > 8 || (n_shells > 0 && !shells)) return 1;
+    const double R = 6371.0;
+    const sosb_profile_shape a = *shape;
+    auto row = [&](int i) {
+        const double r = R + h[i];
+        const double mg = -std::sqrt(std::max(0.0, 1.0 - (R / r) * (R / r)));
+        for (int j = 0; j < n_x; ++j) {
+            double mu = mg + (1.0 - mg) * (x[j] * x[j]);
+            if (j == 0) mu = mg + 1e-9;
+            column_along(r, mu, a, shells, n_shells, gl_u, gl_w, n_gl, up + ((size_t)i * n_x + j) * 6);
+            double mud = mg - (1.0 + mg) * (x[j] * x[j]);
+            if (j == 0) mud = mg - 1e-9;
+            column_along(r, std::max(mud, -1.0), a, shells, n_shells, gl_u, gl_w, n_gl, down + ((size_t)i * n_x + j) * 6);
+        }
+    };
+    const int nt = std::max(1, std::min(threads > 0 ? threads : (int)std::thread::hardware_concurrency(), n_h));
+    std::atomic<int> next(0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&]() {
+            for (int i = next++; i < n_h; i = next++) row(i);
+        });
+    for (auto& t : pool) t.join();
+    return 0;
+}
+
 int sosb_set_ground_rays(sosb_handle s, const sosb_ground_rays* g) {
     if (!s || !g) return 1;
     if (g->n < 0 || (g->n > 0 && (!g->cell || !g->loc || !g->weight || !g->cols || !g->cos_sun || !g->ok)))

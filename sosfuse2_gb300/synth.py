@@ -21,6 +21,7 @@ phase; optional stratospheric Gaussian layer with Henyey-Greenstein Legendre mom
 and O4 proportional to the squared air density; Lambertian ground. Spectral shapes are seeded smooth curves.
 """
 
+import ctypes
 import json
 import math
 
@@ -276,24 +277,55 @@ def _columns_along(r0, mu, atm, shells, n):
     return out, ground
 
 
+def column_rows(atm, shells, h, x, n=32):
+    """The (up, down) column tables [len(h), len(x), 6] by the NumPy restatement (_columns_along), row by row: the
+    reference the native sosb_column_table is checked against."""
+    up = np.empty((len(h), len(x), 6))
+    down = np.empty_like(up)
+    for i, hh in enumerate(h):
+        r = R + hh
+        mg = -math.sqrt(max(0.0, 1 - (R / r) ** 2))
+        mu = mg + (1 - mg) * x ** 2
+        mu[0] = mg + 1e-9
+        up[i] = _columns_along(r, mu, atm, shells, n)[0]
+        mud = mg - (1 + mg) * x ** 2
+        mud[0] = mg - 1e-9
+        down[i] = _columns_along(r, np.maximum(mud, -1.0), atm, shells, n)[0]
+    return up, down
+
+
+def native_column_table(atm, shells, h, x, n=32, threads=0):
+    """The same tables by libsosb's sosb_column_table (host threads; built in-tree on first use)."""
+    from . import _abi, build
+
+    lib = _abi.library(build.build())
+    atm.ozone_shape(0.0)  # sets the ozone normalisation
+    shape = _abi.ProfileShape(top=atm.top, aerosol_height=atm.H, ozone_peak=atm.ozone_peak, ozone_norm=atm._o3_norm,
+                              no2_center=atm.no2_center, strato=int(atm.strato),
+                              strato_center=atm.strato_center, strato_sigma=atm.strato_sigma,
+                              strato_norm=atm.strato_norm if atm.strato else 1.0)
+    h = np.ascontiguousarray(h, np.float64)
+    x = np.ascontiguousarray(x, np.float64)
+    sh = np.ascontiguousarray(shells, np.float64)
+    u, wu = (np.ascontiguousarray(v, np.float64) for v in gauss01(n))
+    up = np.empty((len(h), len(x), 6))
+    down = np.empty_like(up)
+    rc = lib.sosb_column_table(len(h), _abi.ptr(h, _abi.P_f64), len(x), _abi.ptr(x, _abi.P_f64),
+                               _abi.ptr(sh, _abi.P_f64), len(sh), _abi.ptr(u, _abi.P_f64), _abi.ptr(wu, _abi.P_f64), n,
+                               ctypes.byref(shape), _abi.ptr(up, _abi.P_f64), _abi.ptr(down, _abi.P_f64), int(threads))
+    if rc:
+        raise RuntimeError(f'E_COLUMN_TABLE: sosb_column_table returned {rc}')
+    return up, down
+
+
 class ColumnTable:
-    """Slant columns on a (height, x) grid for upward (sun) and downward (ground) rays."""
+    """Slant columns on a (height, x) grid for upward (sun) and downward (ground) rays (sosb_column_table)."""
 
     def __init__(self, atm, shells, scale=2, n=32):
         self.top = atm.top
         self.h = np.linspace(0, math.sqrt(atm.top), SUN_HEIGHT_INTERVALS * scale + 1) ** 2
         self.x = np.linspace(0, 1, 400 * scale + 1)
-        self.up = np.empty((len(self.h), len(self.x), 6))
-        self.down = np.empty_like(self.up)
-        for i, h in enumerate(self.h):
-            r = R + h
-            mg = -math.sqrt(max(0.0, 1 - (R / r) ** 2))
-            mu = mg + (1 - mg) * self.x ** 2
-            mu[0] = mg + 1e-9
-            self.up[i] = _columns_along(r, mu, atm, shells, n)[0]
-            mud = mg - (1 + mg) * self.x ** 2
-            mud[0] = mg - 1e-9
-            self.down[i] = _columns_along(r, np.maximum(mud, -1.0), atm, shells, n)[0]
+        self.up, self.down = native_column_table(atm, shells, self.h, self.x, n)
 
     def lookup(self, h, mu):
         """Columns [n, 6] and whether the ray escapes (mu >= horizon cosine)."""
