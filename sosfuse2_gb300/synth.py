@@ -146,6 +146,29 @@ def ring_quadrature(r, chi, nmu, nphi, heights, rings=True, a=4.0):
     return np.column_stack([st * np.cos(phi), st * np.sin(phi), mu]), np.concatenate(ws)
 
 
+def _quadrature_task(spec):
+    r, chi, nmu, nphi, heights, rings = spec
+    return ring_quadrature(r, chi, nmu, nphi, heights, rings=rings)
+
+
+# families at least this large compute their quadratures in a process pool ('spawn': safe after CUDA has started)
+POOL_CELLS = 4096
+
+
+def quadratures(specs, pool_min=None):
+    """ring_quadrature for every (r, chi, nmu, nphi, heights, rings) of `specs`, in order: serially for small grids,
+    else in a spawned process pool over the host cores (the same calls, so the same results)."""
+    pool_min = POOL_CELLS if pool_min is None else pool_min
+    if len(specs) < pool_min:
+        return [_quadrature_task(sp) for sp in specs]
+    import multiprocessing as mp
+    import os
+
+    workers = max(1, min(os.cpu_count() or 1, 32))
+    with mp.get_context('spawn').Pool(workers) as pool:
+        return pool.map(_quadrature_task, specs, chunksize=max(1, len(specs) // (8 * workers)))
+
+
 # ------------------------------------------------------------------------------------------------ segments
 def ray_edges(p, d, top, shells):
     """Sorted path coordinates of every crossing: start, tangent, shadow-cylinder roots, extra shells, end."""
@@ -436,13 +459,12 @@ class Family:
         shells = _shells(self.top)
         self.table = ColumnTable(shape, shells, scale=sun_scale)
         points, dirs, weights = [], [], []
-        for ih in range(len(self.h)):
-            for ic in range(len(self.chi)):
-                r = R + self.h[ih]
-                loc, w = ring_quadrature(r, self.chi[ic], nmu, nphi, _ring_heights(self.top))
-                points.append(frame(r, self.chi[ic]))
-                dirs.append(loc)
-                weights.append(w)
+        specs = [(R + self.h[ih], self.chi[ic], nmu, nphi, _ring_heights(self.top), True)
+                 for ih in range(len(self.h)) for ic in range(len(self.chi))]
+        for sp, (loc, w) in zip(specs, quadratures(specs)):
+            points.append(frame(sp[0], sp[1]))
+            dirs.append(loc)
+            weights.append(w)
         self.cells = build_bundle(points, dirs, weights, self.chi, self.top, self.table, shape)
         u4, w4 = np.polynomial.legendre.leggauss(4)
         self.box_ww = (w4[:, None] * w4[None, :] / 4).ravel()
@@ -474,10 +496,12 @@ class Family:
         ones the columns to the ground and from the ground point to the sun (solve/engine_core.py:103-147)."""
         table, h, chi = self.table, self.h, self.chi
         loc_all, w_all, col_all, sun_all, cos_all, ok_all, counts = [], [], [], [], [], [], []
+        quads = quadratures([(R + h[cell // len(chi)], chi[cell % len(chi)], nmu, nphi, (), False)
+                             for cell in range(len(h) * len(chi))])
         for cell in range(len(h) * len(chi)):
             ih, ic = divmod(cell, len(chi))
             r = R + h[ih]
-            loc, w = ring_quadrature(r, chi[ic], nmu, nphi, (), rings=False)
+            loc, w = quads[cell]
             p, up, ex = frame(r, chi[ic])
             ey = np.cross(up, ex)
             d = loc[:, 0, None] * ex + loc[:, 1, None] * ey + loc[:, 2, None] * up

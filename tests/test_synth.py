@@ -43,3 +43,13 @@ def test_config0_state_shapes():
     assert off[-1] == len(st['cell_seg_a']) and np.all(np.diff(off) >= 0)  # rays into the ground at h=0: none
     assert np.all(st['cell_seg_b'] - st['cell_seg_a'] > 1e-8)
     assert len(st['query_d']) == 5 * 7 * 16
+
+
+def test_pooled_quadratures_equal_serial():
+    """The process-pool path of synth.quadratures (large families) returns the serial calls' arrays bit for bit."""
+    specs = [(synth.R + hh, math.radians(c), 2, 4, (0.0, 1.2, 8.0, 25.0, 40.0, 80.0), rings)
+             for hh in (0.0, 3.0, 40.0) for c in (0.0, 88.0, 95.0) for rings in (True, False)]
+    serial = synth.quadratures(specs)
+    pooled = synth.quadratures(specs, pool_min=1)
+    for (a, wa), (b, wb) in zip(serial, pooled):
+        assert np.array_equal(a, b) and np.array_equal(wa, wb)
