@@ -204,6 +204,23 @@ typedef struct {
 int sosb_column_table(int n_h, const double *h, int n_x, const double *x, const double *shells, int n_shells,
                       const double *gl_u, const double *gl_w, int n_gl, const sosb_profile_shape *shape, double *up,
                       double *down, int threads);
+/* A solar column table (sosb_column_table's output with its grids) for lookups: heights h[n_h] (ascending, to
+ * top), abscissae x uniform on [0, 1] (n_x values), up/down [n_h][n_x][6]. */
+typedef struct {
+    int32_t n_h, n_x;
+    double top;
+    const double *h, *up, *down;
+} sosb_column_grid;
+/* Segments of n rays (the geometry CSR of a synthetic bundle, the project's counterpart of the reference's
+ * ray_geometry.pack, src/sosfuse2/solve/ray_geometry.py:28-82; host threads): per ray from p[r][3] along d[r][3], the
+ * 5 + 2 n_shells sorted cuts (edges[r][...], synth.ray_edges), for each consecutive pair whether it is a segment
+ * (b - a > 1e-8) and whether its start is the lower end, the end's solar-zenith interval j and fraction, whether the
+ * ray ends on the ground and, with a column table, the slant columns from the ray's start back to the ground along the
+ * ray (end_col[r][5], end_st[r]; zero for rays that do not hit the ground). table may be NULL (no ground columns). */
+int sosb_ray_segments(int64_t n, const double *p, const double *d, double top, const double *shells, int n_shells,
+                      int n_chi, const double *chi, const sosb_column_grid *table, double *edges, uint8_t *valid,
+                      uint8_t *lower, int32_t *end_j, double *end_f, float *end_col, float *end_st, uint8_t *hits,
+                      int threads);
 /* Ground-illumination rays of every cell, the geometry of engine_core.Solver.prepare_ground
  * (src/sosfuse2/solve/engine_core.py:103-147) for the handle's grid: ray r belongs to cell[r] (ascending), arrives
  * from the local direction loc[r][3] with quadrature weight weight[r]; cols[r][6] are its slant columns (five

@@ -68,6 +68,10 @@ class ProfileShape(ctypes.Structure):
                 ('strato_norm', c_dbl)]
 
 
+class ColumnGrid(ctypes.Structure):
+    _fields_ = [('n_h', c_int), ('n_x', c_int), ('top', c_dbl), ('h', P_f64), ('up', P_f64), ('down', P_f64)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ('evaluations', c_int), ('converged', c_int), ('seconds', c_dbl),
@@ -90,6 +94,8 @@ SIGNATURES = {
     'sosb_set_bundle': ([ctypes.c_void_p, c_int, ctypes.POINTER(Bundle)], c_int),
     'sosb_set_ground_rays': ([ctypes.c_void_p, ctypes.POINTER(GroundRays)], c_int),
     'sosb_prepare_ground': ([ctypes.c_void_p, c_dbl, P_f64, P_f64], c_int),
+    'sosb_ray_segments': ([c_i64, P_f64, P_f64, c_dbl, P_f64, c_int, c_int, P_f64, ctypes.POINTER(ColumnGrid), P_f64,
+                           P_u8, P_u8, P_i32, P_f64, P_f32, P_f32, P_u8, c_int], c_int),
     'sosb_column_table': ([c_int, P_f64, c_int, P_f64, P_f64, c_int, P_f64, P_f64, c_int, ctypes.POINTER(ProfileShape),
                            P_f64, P_f64, c_int], c_int),
     'sosb_evaluate': ([ctypes.c_void_p, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -2989,14 +2989,17 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
 // the atmosphere or the ground, the path cut at the shadow cylinder, the tangent point and the shells, each piece
 // integrated by an n-point Gauss-Legendre rule of the five profile shapes (clipped to [0, top]) and the
 // stratospheric shape; the operations of the NumPy restatement in order, in FP64.
-static void column_along(double r0, double mu, const sosb_profile_shape& a, const double* shells, int nshell,
-                         const double* u, const double* wu, int n, double out[6]) {
+// Sorted path coordinates where a ray from p along d is cut (synth.ray_edges): start, tangent point, the shadow
+// cylinder's two roots, the shells' crossings, and the end at the top or the ground (each absent cut repeats the end).
+// Returns the count (5 + 2 nshell) and whether the ray ends on the ground.
+constexpr int MAX_CUTS = 5 + 2 * 8;
+static int ray_cuts(const double p[3], const double d[3], double top, const double* shells, int nshell,
+                    double cols[MAX_CUTS], bool* ground_out) {
     const double R = 6371.0;
-    const double px = 0.0, py = 0.0, pz = r0;
-    const double dx = std::sqrt(std::max(1.0 - mu * mu, 0.0)), dy = 0.0, dz = mu;
+    const double px = p[0], py = p[1], pz = p[2], dx = d[0], dy = d[1], dz = d[2];
     const double b = (px * dx + py * dy) + pz * dz;
     const double pp = (px * px + py * py) + pz * pz;
-    double end = -b + std::sqrt(std::max(b * b - pp + (R + a.top) * (R + a.top), 0.0));
+    double end = -b + std::sqrt(std::max(b * b - pp + (R + top) * (R + top), 0.0));
     const double disc = b * b - pp + R * R;
     const double hit = -b - std::sqrt(std::max(disc, 0.0));
     const bool ground = disc >= 0.0 && b < 0.0 && hit >= -1e-7;
@@ -3004,7 +3007,6 @@ static void column_along(double r0, double mu, const sosb_profile_shape& a, cons
     const double tangent = (-b > 0.0 && -b < end) ? -b : end;
     const double aa = dx * dx + dy * dy, bb = px * dx + py * dy, cc = px * px + py * py - R * R;
     const double ds = bb * bb - aa * cc;
-    double cols[5 + 2 * 8];
     int nc = 0;
     cols[nc++] = 0.0;
     cols[nc++] = tangent;
@@ -3022,6 +3024,18 @@ static void column_along(double r0, double mu, const sosb_profile_shape& a, cons
         }
     }
     std::sort(cols, cols + nc);
+    if (ground_out) *ground_out = ground;
+    return nc;
+}
+
+static void column_along(double r0, double mu, const sosb_profile_shape& a, const double* shells, int nshell,
+                         const double* u, const double* wu, int n, double out[6]) {
+    const double R = 6371.0;
+    const double px = 0.0, py = 0.0, pz = r0;
+    const double dx = std::sqrt(std::max(1.0 - mu * mu, 0.0)), dy = 0.0, dz = mu;
+    const double pv[3] = {px, py, pz}, dv[3] = {dx, dy, dz};
+    double cols[MAX_CUTS];
+    const int nc = ray_cuts(pv, dv, a.top, shells, nshell, cols, nullptr);
     for (int k = 0; k < 6; ++k) out[k] = 0.0;
     for (int k = 0; k + 1 < nc; ++k) {
         const double s0 = cols[k], s1 = cols[k + 1];
@@ -3073,6 +3087,96 @@ int sosb_column_table(int n_h, const double* h, int n_x, const double* x, const 
     for (int t = 0; t < nt; ++t)
         pool.emplace_back([&]() {
             for (int i = next++; i < n_h; i = next++) row(i);
+        });
+    for (auto& t : pool) t.join();
+    return 0;
+}
+
+// Bilinear lookup of a solar column table (synth.ColumnTable.lookup): columns [6] at height h (clipped to [0, top])
+// along zenith cosine mu from the up table when the ray escapes (mu >= the horizon cosine), else the down table.
+static void column_lookup(const sosb_column_grid& t, double h, double mu, double out[6]) {
+    const double R = 6371.0;
+    h = std::min(std::max(h, 0.0), t.top);
+    const double r = R + h;
+    const double rr = std::max(r, R);
+    const double mg = -std::sqrt(std::max(0.0, 1.0 - (R / rr) * (R / rr)));
+    const bool escape = mu >= mg;
+    const double x = escape ? std::sqrt(std::min(std::max((mu - mg) / (1.0 - mg), 0.0), 1.0))
+                            : std::sqrt(std::min(std::max((mg - mu) / (1.0 + mg), 0.0), 1.0));
+    // i = clip(searchsorted(h_grid, h, 'right') - 1, 0, n_h - 2)
+    int i = (int)(std::upper_bound(t.h, t.h + t.n_h, h) - t.h) - 1;
+    i = std::min(std::max(i, 0), t.n_h - 2);
+    const double a = (h - t.h[i]) / (t.h[i + 1] - t.h[i]);
+    const double f = x * (double)(t.n_x - 1);
+    const int j = std::min(std::max((int)f, 0), t.n_x - 2);
+    const double bb = f - (double)j;
+    const double* tab = escape ? t.up : t.down;
+    const double* t00 = tab + ((size_t)i * t.n_x + j) * 6;
+    const double* t10 = tab + ((size_t)(i + 1) * t.n_x + j) * 6;
+    const double* t01 = t00 + 6;
+    const double* t11 = t10 + 6;
+    for (int k = 0; k < 6; ++k)
+        out[k] = (((1.0 - a) * (1.0 - bb) * t00[k] + a * (1.0 - bb) * t10[k]) + (1.0 - a) * bb * t01[k]) +
+                 a * bb * t11[k];
+}
+
+int sosb_ray_segments(int64_t n, const double* p, const double* d, double top, const double* shells, int n_shells,
+                      int n_chi, const double* chi, const sosb_column_grid* table, double* edges, uint8_t* valid,
+                      uint8_t* lower, int32_t* end_j, double* end_f, float* end_col, float* end_st, uint8_t* hits,
+                      int threads) {
+    if (n < 0 || (n > 0 && (!p || !d || !edges || !valid || !lower || !end_j || !end_f || !hits)) || n_chi < 2 ||
+        !chi || n_shells < 0 || n_shells > 8 || (n_shells > 0 && !shells))
+        return 1;
+    if (table && (!end_col || !end_st || table->n_h < 2 || table->n_x < 2)) return 1;
+    const double R = 6371.0;
+    const int ncut = 5 + 2 * n_shells;
+    auto ray = [&](int64_t r) {
+        const double* pr = p + r * 3;
+        const double* dr = d + r * 3;
+        double* e = edges + r * ncut;
+        ray_cuts(pr, dr, top, shells, n_shells, e, nullptr);
+        for (int k = 0; k + 1 < ncut; ++k) {
+            const double a = e[k], b = e[k + 1];
+            valid[r * (ncut - 1) + k] = (b - a) > 1e-8;
+            double qa[3], qb[3];
+            for (int c = 0; c < 3; ++c) {
+                qa[c] = pr[c] + a * dr[c];
+                qb[c] = pr[c] + b * dr[c];
+            }
+            lower[r * (ncut - 1) + k] =
+                ((qa[0] * qa[0] + qa[1] * qa[1]) + qa[2] * qa[2]) <= ((qb[0] * qb[0] + qb[1] * qb[1]) + qb[2] * qb[2]);
+        }
+        const double end = e[ncut - 1];
+        double qe[3];
+        for (int c = 0; c < 3; ++c) qe[c] = pr[c] + end * dr[c];
+        const double re = std::sqrt((qe[0] * qe[0] + qe[1] * qe[1]) + qe[2] * qe[2]);
+        const double ch = std::acos(std::min(std::max(qe[2] / re, -1.0), 1.0));
+        int j = (int)(std::upper_bound(chi, chi + n_chi, ch) - chi) - 1;
+        j = std::min(std::max(j, 0), n_chi - 2);
+        end_j[r] = j;
+        end_f[r] = std::min(std::max((ch - chi[j]) / (chi[j + 1] - chi[j]), 0.0), 1.0);
+        const bool hit = re < R + 1e-5;
+        hits[r] = hit;
+        if (table) {
+            double cols[6] = {0, 0, 0, 0, 0, 0};
+            if (hit) {
+                const double r0 = std::sqrt((pr[0] * pr[0] + pr[1] * pr[1]) + pr[2] * pr[2]);
+                const double mu = ((pr[0] * dr[0] + pr[1] * dr[1]) + pr[2] * dr[2]) / r0;
+                column_lookup(*table, r0 - R, mu, cols);
+            }
+            for (int k = 0; k < 5; ++k) end_col[r * 5 + k] = (float)cols[k];
+            end_st[r] = (float)cols[5];
+        }
+    };
+    const int64_t chunk = 4096;
+    const int64_t nchunk = (n + chunk - 1) / chunk;
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(threads > 0 ? threads : (int)std::thread::hardware_concurrency(), nchunk));
+    std::atomic<int64_t> next(0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&]() {
+            for (int64_t c = next++; c < nchunk; c = next++)
+                for (int64_t r = c * chunk; r < std::min(n, (c + 1) * chunk); ++r) ray(r);
         });
     for (auto& t : pool) t.join();
     return 0;

@@ -383,6 +383,45 @@ def _ring_heights(top):
 
 
 def _ray_block(p, d, chi_grid, top, table, with_ground_columns):
+    """The segments and ray-end quantities of a block of rays by libsosb's sosb_ray_segments (host threads)."""
+    from . import _abi, build
+
+    lib = _abi.library(build.build())
+    shells = np.ascontiguousarray(_shells(top), np.float64)
+    p = np.ascontiguousarray(p, np.float64)
+    d = np.ascontiguousarray(d, np.float64)
+    chi = np.ascontiguousarray(chi_grid, np.float64)
+    n, ncut = len(d), 5 + 2 * len(shells)
+    edges = np.empty((n, ncut))
+    valid = np.empty((n, ncut - 1), np.uint8)
+    lower = np.empty((n, ncut - 1), np.uint8)
+    end_j = np.empty(n, np.int32)
+    end_f = np.empty(n)
+    end_col = np.zeros((n, 5), np.float32)
+    end_st = np.zeros(n, np.float32)
+    hits = np.empty(n, np.uint8)
+    grid = None
+    if with_ground_columns:
+        keep = [np.ascontiguousarray(table.h, np.float64), np.ascontiguousarray(table.up, np.float64),
+                np.ascontiguousarray(table.down, np.float64)]
+        grid = _abi.ColumnGrid(n_h=len(table.h), n_x=len(table.x), top=table.top, h=_abi.ptr(keep[0], _abi.P_f64),
+                               up=_abi.ptr(keep[1], _abi.P_f64), down=_abi.ptr(keep[2], _abi.P_f64))
+    rc = lib.sosb_ray_segments(n, _abi.ptr(p, _abi.P_f64), _abi.ptr(d, _abi.P_f64), float(top),
+                               _abi.ptr(shells, _abi.P_f64), len(shells), len(chi), _abi.ptr(chi, _abi.P_f64),
+                               None if grid is None else ctypes.byref(grid), _abi.ptr(edges, _abi.P_f64),
+                               _abi.ptr(valid, _abi.P_u8), _abi.ptr(lower, _abi.P_u8), _abi.ptr(end_j, _abi.P_i32),
+                               _abi.ptr(end_f, _abi.P_f64), _abi.ptr(end_col, _abi.P_f32), _abi.ptr(end_st, _abi.P_f32),
+                               _abi.ptr(hits, _abi.P_u8), 0)
+    if rc:
+        raise RuntimeError(f'E_SEGMENTS: sosb_ray_segments returned {rc}')
+    v = valid.astype(bool)
+    return dict(seg_off=np.r_[0, np.cumsum(v.sum(1))].astype(np.int64), seg_a=edges[:, :-1][v], seg_b=edges[:, 1:][v],
+                seg_lower=lower[v], end_j=end_j, end_f=end_f, end_col=end_col, end_st=end_st, hits=hits)
+
+
+def ray_block_numpy(p, d, chi_grid, top, table, with_ground_columns):
+    """The NumPy restatement of _ray_block (ray_edges, compact_segments and the end quantities), the reference the
+    native sosb_ray_segments is checked against."""
     shells = _shells(top)
     edges, ground = ray_edges(p, d, top, shells)
     seg_off, seg_a, seg_b, seg_lower = compact_segments(p, d, edges)
