@@ -54,7 +54,9 @@ def test_version_string(lib):
 
 @pytest.mark.parametrize('cname,pytype', [('sosb_dims', _abi.Dims), ('sosb_constants', _abi.Constants),
                                            ('sosb_bundle', _abi.Bundle), ('sosb_stats', _abi.Stats),
-                                           ('sosb_ground_rays', _abi.GroundRays)])
+                                           ('sosb_ground_rays', _abi.GroundRays),
+                                           ('sosb_profile_shape', _abi.ProfileShape),
+                                           ('sosb_column_grid', _abi.ColumnGrid)])
 def test_struct_layout_matches_header(cname, pytype):
     assert header_struct_fields(cname) == [f[0] for f in pytype._fields_]
 
