@@ -41,6 +41,16 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// A device buffer owned by one host function: freed on every return, the error paths included.
+struct LocalBuf : DevBuf {
+    LocalBuf() = default;
+    LocalBuf(const LocalBuf&) = delete;
+    LocalBuf& operator=(const LocalBuf&) = delete;
+    ~LocalBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
 struct BundleDev {
     int ncell = 0;
     int64_t nray = 0, nseg = 0;
@@ -2206,7 +2216,7 @@ static int build_pairs(sosb_state* s, BundleDev& b, int nq) {
     const int64_t nray = b.nray;
     const size_t nodes = (size_t)b.nseg * nq;
     const int kp = (s->K + 3) & ~3;
-    DevBuf cnt, cursor;
+    LocalBuf cnt, cursor;
     TRY(dalloc(s, cnt, (size_t)(nray + 1) * sizeof(int)));
     TRY(dalloc(s, cursor, (size_t)(nray + 1) * sizeof(int)));
     TRY(dalloc(s, b.p_off, (size_t)(nray + 1) * sizeof(int)));
@@ -3227,7 +3237,7 @@ int sosb_prepare_ground(sosb_handle s, double albedo, const double* ext, const d
     if (s->d.strato && !strato_ext) return fail(s, "E_CONSTANTS: missing stratospheric extinction");
     const int W = s->d.W, ns = s->ns;
     const size_t n = (size_t)std::max<int64_t>(s->gr_n, 1);
-    DevBuf dext, dsext;
+    LocalBuf dext, dsext;
     TRY(dput(s, dext, ext, 5 * (size_t)W * sizeof(double)));
     if (s->d.strato) TRY(dput(s, dsext, strato_ext, (size_t)W * sizeof(double)));
     TRY(dalloc(s, s->gr_value, n * W * sizeof(double)));
@@ -3240,7 +3250,7 @@ int sosb_prepare_ground(sosb_handle s, double albedo, const double* ext, const d
     TRY(dalloc(s, s->gsame, (size_t)ns));
     const GroundRays g{P<int>(s->gr_off), P<double>(s->gr_loc), P<double>(s->gr_w), P<double>(s->gr_cols),
                        P<double>(s->gr_cos), P<uint8_t>(s->gr_ok), (long long)s->gr_n};
-    DevBuf cursor;
+    LocalBuf cursor;
     TRY(dalloc(s, cursor, ((size_t)ns + 1) * sizeof(int)));
     CK(cudaMemsetAsync(s->gr_cnt.p, 0, ((size_t)ns + 1) * sizeof(int), s->stream));
     {
