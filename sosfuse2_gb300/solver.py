@@ -240,13 +240,18 @@ class Solver:
         self.last_stats = stats
         k._check(rc)
         W = k.W
+        obs = [float(stats.observer_relative[w]) for w in range(W)]
+        src = [float(stats.source_relative[w]) for w in range(W)]
         return out, dict(
             seconds=seconds,
             evaluations=int(stats.evaluations),
             tolerance=tolerance,
             converged=[bool(stats.done[w]) for w in range(W)],
-            observer_relative=[float(stats.observer_relative[w]) for w in range(W)],
-            source_relative=[float(stats.source_relative[w]) for w in range(W)],
+            observer_relative=obs,
+            source_relative=src,
+            # the reference's consumers read the last entry of its per-evaluation history
+            # (jobs/run_state.py:99-104, jobs/walkthrough.py:296); the device loop reports the final evaluation's
+            history=[dict(observer_relative=obs, source_relative=src)],
             kernel_launches=int(stats.kernel_launches),
         )
 
