@@ -221,6 +221,15 @@ int sosb_ray_segments(int64_t n, const double *p, const double *d, double top, c
                       int n_chi, const double *chi, const sosb_column_grid *table, double *edges, uint8_t *valid,
                       uint8_t *lower, int32_t *end_j, double *end_f, float *end_col, float *end_st, uint8_t *hits,
                       int threads);
+/* Incoming-direction quadratures of n_cells cells (host threads; the project's restatement of the reference's ring
+ * rule, src/sosfuse2/rays/incoming_rings.py): cell c at radius r[c] and solar zenith chi[c], nphi + 1 azimuth
+ * planes, in each a sinh-mapped (a) Gauss-Legendre rule (u, wu on [0, 1], nmu nodes) between the cuts at the
+ * horizon, the shadow boundary, the forward direction and, with rings, the shadow rings of the n_heights shells.
+ * counts[c] receives each cell's direction count; with loc (and w) not NULL the directions (local ex, ey, up) and
+ * weights of all cells follow one another in cell order (capacity: directions loc and w can hold; 2 when short). */
+int sosb_ring_quadrature(int n_cells, const double *r, const double *chi, int nmu, int nphi, const double *heights,
+                         int n_heights, int rings, double a, const double *u, const double *wu, int64_t *counts,
+                         double *loc, double *w, int64_t capacity, int threads);
 /* Ground-illumination rays of every cell, the geometry of engine_core.Solver.prepare_ground
  * (src/sosfuse2/solve/engine_core.py:103-147) for the handle's grid: ray r belongs to cell[r] (ascending), arrives
  * from the local direction loc[r][3] with quadrature weight weight[r]; cols[r][6] are its slant columns (five

@@ -3192,6 +3192,142 @@ int sosb_ray_segments(int64_t n, const double* p, const double* d, double top, c
     return 0;
 }
 
+// Incoming-direction quadrature of one cell (synth.ring_quadrature, the reference's ring rule restated: per azimuth
+// plane a sinh-mapped Gauss-Legendre rule in mu between the cuts at the horizon, the shadow boundary and the shells'
+// shadow rings). Writes the directions (local ex, ey, up) and weights when loc is not NULL; returns the count.
+static int64_t ring_cell(double r, double chi, int nmu, int nphi, const double* heights, int nh, bool rings, double a,
+                         const double* u, const double* wu, double* loc, double* wout) {
+    const double R = 6371.0, PI = 3.141592653589793;
+    const double mg = -std::sqrt(std::max(0.0, 1.0 - (R / r) * (R / r)));
+    const double sa = std::sinh(a);
+    const double sinchi = std::sin(chi), coschi = std::cos(chi);
+    const double rp = r * sinchi;
+    const double up[3] = {sinchi, 0.0, coschi}, ex[3] = {-coschi, 0.0, sinchi};
+    const double p[3] = {r * up[0], r * up[1], r * up[2]};
+    const double ey[3] = {up[1] * ex[2] - up[2] * ex[1], up[2] * ex[0] - up[0] * ex[2], up[0] * ex[1] - up[1] * ex[0]};
+    const double step = PI / (double)nphi;
+    int64_t count = 0;
+    std::vector<double> edges, tt;
+    for (int j = 0; j <= nphi; ++j) {
+        const double phi = j == nphi ? PI : (double)j * step;
+        const double cphi = std::cos(phi), sphi = std::sin(phi);
+        edges.assign({-1.0, 1.0, mg, 0.0, mg - 0.05234, mg + 0.05234, mg - 0.0061, mg + 0.0061});
+        if (rp > R + 1e-8 && std::fabs(sinchi) > 1e-8) {
+            const double kk = R / std::sqrt(rp * rp - R * R);
+            for (int sign = -1; sign <= 1; sign += 2) {
+                const double t = cphi * coschi / sinchi + sign * sphi / (kk * sinchi);
+                const double mu = t / std::sqrt(1.0 + t * t);
+                const double st = std::sqrt(1.0 - mu * mu);
+                const double dx = mu * sinchi - st * cphi * coschi;
+                const double dy = -st * sphi;
+                const double dz = mu * coschi + st * cphi * sinchi;
+                const double tmin = -rp * dx / std::max(dx * dx + dy * dy, 1e-25);
+                if (std::fabs(dx) + std::fabs(dy) < 1e-10 || (tmin > 0.0 && r * coschi + tmin * dz < 0.0))
+                    edges.push_back(mu);
+            }
+        }
+        if (phi < PI / 6.0) {
+            const double mu = coschi / std::sqrt(coschi * coschi + cphi * cphi * (sinchi * sinchi) + 1e-300);
+            edges.push_back(mu);
+            edges.push_back(mu - 0.012);
+            edges.push_back(mu + 0.012);
+        }
+        if (rings) {
+            double hz[3];
+            for (int c = 0; c < 3; ++c) hz[c] = cphi * ex[c] + sphi * ey[c];
+            const double nrm[3] = {up[1] * hz[2] - up[2] * hz[1], up[2] * hz[0] - up[0] * hz[2],
+                                   up[0] * hz[1] - up[1] * hz[0]};
+            const double amp = R * std::hypot(nrm[0], nrm[1]);
+            if (amp >= 1e-10) {
+                const double angle = std::atan2(nrm[1], nrm[0]);
+                for (int k = 0; k < nh; ++k) {
+                    const double z = -std::sqrt(std::max(0.0, (R + heights[k]) * (R + heights[k]) - R * R));
+                    const double target = -nrm[2] * z / amp;
+                    if (std::fabs(target) > 1.0) continue;
+                    const double delta = std::acos(target);
+                    for (int side = 0; side < 2; ++side) {
+                        const double az = side == 0 ? angle - delta : angle + delta;
+                        double d[3] = {R * std::cos(az) - p[0], R * std::sin(az) - p[1], z - p[2]};
+                        const double length = std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+                        if (length < 1e-8) continue;
+                        for (int c = 0; c < 3; ++c) d[c] /= length;
+                        if ((d[0] * hz[0] + d[1] * hz[1]) + d[2] * hz[2] <= 1e-10) continue;
+                        const double b = (p[0] * d[0] + p[1] * d[1]) + p[2] * d[2];
+                        const double disc = b * b - r * r + R * R;
+                        const double hit = -b - std::sqrt(std::max(0.0, disc));
+                        if (disc >= 0.0 && b < 0.0 && hit >= -1e-7 && hit < length - 1e-5) continue;
+                        edges.push_back((d[0] * up[0] + d[1] * up[1]) + d[2] * up[2]);
+                    }
+                }
+            }
+        }
+        for (double& e : edges) e = std::min(std::max(e, -1.0), 1.0);
+        std::sort(edges.begin(), edges.end());
+        edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
+        tt.resize(edges.size());
+        for (size_t k = 0; k < edges.size(); ++k) {
+            const double dl = edges[k] - mg;
+            const double sg = dl > 0.0 ? 1.0 : (dl < 0.0 ? -1.0 : 0.0);
+            tt[k] = sg * std::asinh(std::fabs(dl) / (dl < 0.0 ? 1.0 + mg : 1.0 - mg) * sa) / a;
+        }
+        const double half = (j == 0 || j == nphi) ? 0.5 : 1.0;
+        for (size_t k = 0; k + 1 < tt.size(); ++k) {
+            const double left = tt[k], right = tt[k + 1];
+            if (!(right - left >= 1e-10)) continue;
+            for (int q = 0; q < nmu; ++q) {
+                if (loc) {
+                    const double t = left + (right - left) * u[q];
+                    const double den = t < 0.0 ? 1.0 + mg : 1.0 - mg;
+                    const double sg = t > 0.0 ? 1.0 : (t < 0.0 ? -1.0 : 0.0);
+                    const double mu = mg + sg * den * std::sinh(a * std::fabs(t)) / sa;
+                    const double st = std::sqrt(std::max(0.0, 1.0 - mu * mu));
+                    loc[count * 3] = st * cphi;
+                    loc[count * 3 + 1] = st * sphi;
+                    loc[count * 3 + 2] = mu;
+                    wout[count] = (right - left) * wu[q] * den * a * std::cosh(a * std::fabs(t)) / sa *
+                                  (2.0 * PI / (double)nphi) * half;
+                }
+                ++count;
+            }
+        }
+    }
+    return count;
+}
+
+int sosb_ring_quadrature(int n_cells, const double* r, const double* chi, int nmu, int nphi, const double* heights,
+                         int n_heights, int rings, double a, const double* u, const double* wu, int64_t* counts,
+                         double* loc, double* w, int64_t capacity, int threads) {
+    if (n_cells < 0 || (n_cells > 0 && (!r || !chi || !counts)) || nmu < 1 || nphi < 1 || !u || !wu ||
+        n_heights < 0 || (n_heights > 0 && !heights) || (loc && !w))
+        return 1;
+    auto run = [&](bool fill, const std::vector<int64_t>& off) {
+        const int nt = std::max(1, std::min(threads > 0 ? threads : (int)std::thread::hardware_concurrency(),
+                                            std::max(n_cells, 1)));
+        std::atomic<int> next(0);
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back([&]() {
+                for (int c = next++; c < n_cells; c = next++) {
+                    if (fill)
+                        ring_cell(r[c], chi[c], nmu, nphi, heights, n_heights, rings != 0, a, u, wu, loc + off[c] * 3,
+                                  w + off[c]);
+                    else
+                        counts[c] = ring_cell(r[c], chi[c], nmu, nphi, heights, n_heights, rings != 0, a, u, wu,
+                                              nullptr, nullptr);
+                }
+            });
+        for (auto& th : pool) th.join();
+    };
+    const std::vector<int64_t> none;
+    run(false, none);
+    if (!loc) return 0;
+    std::vector<int64_t> off((size_t)n_cells + 1, 0);
+    for (int c = 0; c < n_cells; ++c) off[c + 1] = off[c] + counts[c];
+    if (off[n_cells] > capacity) return 2;
+    run(true, off);
+    return 0;
+}
+
 int sosb_set_ground_rays(sosb_handle s, const sosb_ground_rays* g) {
     if (!s || !g) return 1;
     if (g->n < 0 || (g->n > 0 && (!g->cell || !g->loc || !g->weight || !g->cols || !g->cos_sun || !g->ok)))

@@ -146,27 +146,35 @@ def ring_quadrature(r, chi, nmu, nphi, heights, rings=True, a=4.0):
     return np.column_stack([st * np.cos(phi), st * np.sin(phi), mu]), np.concatenate(ws)
 
 
-def _quadrature_task(spec):
-    r, chi, nmu, nphi, heights, rings = spec
-    return ring_quadrature(r, chi, nmu, nphi, heights, rings=rings)
+def quadratures(specs):
+    """The ring quadrature (loc, w) of every (r, chi, nmu, nphi, heights, rings) of `specs`, in order, by libsosb's
+    sosb_ring_quadrature (host threads; the same rule as ring_quadrature). The specs of one call share nmu, nphi,
+    heights and rings."""
+    from . import _abi, build
 
-
-# families at least this large compute their quadratures in a process pool ('spawn': safe after CUDA has started)
-POOL_CELLS = 4096
-
-
-def quadratures(specs, pool_min=None):
-    """ring_quadrature for every (r, chi, nmu, nphi, heights, rings) of `specs`, in order: serially for small grids,
-    else in a spawned process pool over the host cores (the same calls, so the same results)."""
-    pool_min = POOL_CELLS if pool_min is None else pool_min
-    if len(specs) < pool_min:
-        return [_quadrature_task(sp) for sp in specs]
-    import multiprocessing as mp
-    import os
-
-    workers = max(1, min(os.cpu_count() or 1, 32))
-    with mp.get_context('spawn').Pool(workers) as pool:
-        return pool.map(_quadrature_task, specs, chunksize=max(1, len(specs) // (8 * workers)))
+    if not specs:
+        return []
+    nmu, nphi, heights, rings = specs[0][2:]
+    if any(sp[2:] != (nmu, nphi, heights, rings) for sp in specs):
+        raise ValueError('E_SYNTH: one quadrature rule per call')
+    lib = _abi.library(build.build())
+    r = np.ascontiguousarray([sp[0] for sp in specs], np.float64)
+    chi = np.ascontiguousarray([sp[1] for sp in specs], np.float64)
+    hh = np.ascontiguousarray(heights, np.float64)
+    u, wu = (np.ascontiguousarray(v, np.float64) for v in gauss01(nmu))
+    counts = np.zeros(len(specs), np.int64)
+    args = (len(specs), _abi.ptr(r, _abi.P_f64), _abi.ptr(chi, _abi.P_f64), int(nmu), int(nphi),
+            _abi.ptr(hh, _abi.P_f64) if len(hh) else None, len(hh), int(bool(rings)), 4.0, _abi.ptr(u, _abi.P_f64),
+            _abi.ptr(wu, _abi.P_f64), _abi.ptr(counts, _abi.P_i64))
+    if lib.sosb_ring_quadrature(*args, None, None, 0, 0):
+        raise RuntimeError('E_SYNTH: sosb_ring_quadrature failed')
+    total = int(counts.sum())
+    loc = np.empty((total, 3))
+    w = np.empty(total)
+    if lib.sosb_ring_quadrature(*args, _abi.ptr(loc, _abi.P_f64), _abi.ptr(w, _abi.P_f64), total, 0):
+        raise RuntimeError('E_SYNTH: sosb_ring_quadrature failed')
+    off = np.r_[0, np.cumsum(counts)]
+    return [(loc[off[i]:off[i + 1]], w[off[i]:off[i + 1]]) for i in range(len(specs))]
 
 
 # ------------------------------------------------------------------------------------------------ segments
