@@ -166,9 +166,10 @@ int sosb_apply(sosb_handle h, const float *field_dev, float *out_dev);
  * plus first_moments_dev (first light) are composed into out_dev [cells][slots][W]; wavelengths whose bit is set in
  * done_mask keep x_dev's values. Per wavelength it returns the count of non-finite composed values and
  * max|g - x| / max|g|. It calls no cudaMalloc, cudaFree or allocating library routine: its reduction scratch is a
- * file-scope device array of 3 x 64 words (W <= 64; larger W is rejected with E_SHAPE). The first call on each device
- * looks that array's address up (cudaGetSymbolAddress) with the device current, so make the first call before any
- * stream capture. Every call shares the array and clears it first: calls that overlap on the GPU race. */
+ * file-scope device array of 3 x 64 words (W <= 64; larger W is rejected with E_SHAPE). Every call looks that array's
+ * address up (cudaGetSymbolAddress) with the calling device current, so a device reset leaves no stale address; the
+ * first call on a device may load the library's device code, so make it before any stream capture. Every call shares
+ * the array and clears it first: calls that overlap on the GPU race. */
 int sosb_compose_static(sosb_handle h, const float *moments_dev, const float *first_moments_dev, const float *x_dev,
                         uint64_t done_mask, float *out_dev, int64_t *nonfinite_host, double *source_relative_host);
 /* Replaces: Solver.boxes (source_iteration.py:218-222): observer values [n_monitor_rows][n_dirs][W] to host. */
@@ -178,6 +179,11 @@ int sosb_boxes(sosb_handle h, const float *field_dev, double *out_host);
  * Returns nonzero with E_NOT_CONVERGED or E_NONFINITE_SOURCE like the reference. */
 int sosb_solve(sosb_handle h, int max_eval, double tolerance, const float *x0_host, float *x_out,
                int x_out_is_device, sosb_stats *stats);
+/* Replaces: the `history` list in the stats of Solver.solve (source_iteration.py:381-391): the per-evaluation
+ * observer_relative and source_relative of the last solve on this handle (sosb_solve, sosb_solve_warm or a batch
+ * member), row e = evaluation e + 1, [count][W] each. *count receives the evaluations recorded; at most `capacity`
+ * rows are copied. */
+int sosb_history(sosb_handle h, int capacity, int32_t *count, double *observer_relative, double *source_relative);
 /* Kernel timing with CUDA events on the work stream (no counterpart in the reference's ABI; its Kernel.timed_launch,
  * source_solver.py:1478-1523, keeps a per-kind launch log). Classes: 0 transport with its geometry (first light,
  * node-table builds), 1 projection, 2 SH plane, 3 composition, 4 observer boxes, 5 Anderson, 6 other, 7 transport

@@ -677,11 +677,12 @@ class Oracle:
     def boxes(self, field):
         return boxes(self.pk, field)
 
-    def solve(self, max_eval=None, tolerance=None, initial=None):
+    def solve(self, max_eval=None, tolerance=None, initial=None, log=None):
         pk = self.pk
         return anderson_solve(self.apply, self.boxes, (pk.ns, pk.source_size, pk.W),
                               pk.meta['max_eval'] if max_eval is None else max_eval,
-                              pk.meta['tolerance'] if tolerance is None else tolerance, initial)
+                              pk.meta['tolerance'] if tolerance is None else tolerance, initial,
+                              monitors=int(pk.meta.get('monitors', 5)), log=log)
 
 
 def compose(pk, moment):

@@ -106,6 +106,7 @@ SIGNATURES = {
     'sosb_boxes': ([ctypes.c_void_p, ctypes.c_void_p, P_f64], c_int),
     'sosb_solve': ([ctypes.c_void_p, c_int, c_dbl, ctypes.c_void_p, ctypes.c_void_p, c_int, ctypes.POINTER(Stats)],
                    c_int),
+    'sosb_history': ([ctypes.c_void_p, c_int, P_i32, P_f64, P_f64], c_int),
     'sosb_compose_static': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                              ctypes.c_void_p, P_i64, P_f64], c_int),
     'sosb_solve_warm': ([ctypes.c_void_p, c_int, c_dbl, ctypes.c_void_p, c_dbl, ctypes.c_void_p, ctypes.c_void_p, c_int,

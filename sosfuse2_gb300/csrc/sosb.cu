@@ -122,6 +122,8 @@ struct sosb_state {
     bool pairs = true;     // corner SH by ray-cell pair contractions (sosb_set_pairs)
     int proj_mode = 0;   // projection form (sosb_set_projection): PROJ_FP32, PROJ_BF16X3, PROJ_TF32, PROJ_BF16
     int64_t launches = 0;
+    // per-evaluation history of the last solve on this handle: [evaluation][W] observer and source relative changes
+    std::vector<double> hist_obs, hist_src;
 };
 
 static int fail(sosb_state* s, const char* fmt, ...) {
@@ -3478,22 +3480,13 @@ int sosb_apply(sosb_handle s, const float* field_dev, float* out_dev) {
 #define SOSB_STATIC_WAVES 64
 static __device__ __align__(256) unsigned g_compose_scratch[3 * SOSB_STATIC_WAVES];
 
-// The array's name is only a host-side stand-in for it; the device address is looked up once per device, with that
-// device current, and kept here.
-static std::mutex g_compose_scratch_lock;
-static unsigned* g_compose_scratch_dev[256] = {nullptr};
-
+// The array's name is only a host-side stand-in for it; its device address is looked up on every call, with the
+// calling device current, so that a context torn down and created again (cudaDeviceReset) never leaves a stale
+// address behind. The lookup is a host-side query next to the kernel's cost.
 static int compose_scratch_address(sosb_state* s, unsigned** out) {
-    int dev = -1;
-    CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 256) return fail(s, "E_DEVICE: device ordinal %d out of range", dev);
-    std::lock_guard<std::mutex> guard(g_compose_scratch_lock);
-    if (!g_compose_scratch_dev[dev]) {
-        void* ptr = nullptr;
-        CK(cudaGetSymbolAddress(&ptr, g_compose_scratch));
-        g_compose_scratch_dev[dev] = static_cast<unsigned*>(ptr);
-    }
-    *out = g_compose_scratch_dev[dev];
+    void* ptr = nullptr;
+    CK(cudaGetSymbolAddress(&ptr, g_compose_scratch));
+    *out = static_cast<unsigned*>(ptr);
     return 0;
 }
 
@@ -3759,6 +3752,8 @@ struct SolveRun {
         obs.assign((size_t)4 * W * 64, 0.0f);
         rr.assign(W, 0.0);
         ss.assign(W, 0.0);
+        s->hist_obs.clear();
+        s->hist_src.clear();
         order.clear();
         std::memset(s->ctrl_host, 0, sizeof(EvalCtrl));
         return 0;
@@ -3809,13 +3804,16 @@ struct SolveRun {
                 const double nv = new_b[i * W + w], ov = old_b[i * W + w];
                 r = std::max(r, std::fabs(nv - ov) / std::max(std::fabs(nv), 1e-30));
             }
+            // compose_kernel's layout: [0][W] nonfinite counts, [1][W] max |g| bits, [2][W] max |g - x| bits
             float mg, df;
-            std::memcpy(&mg, &met[64 + w], 4);
-            std::memcpy(&df, &met[128 + w], 4);
+            std::memcpy(&mg, &met[W + w], 4);
+            std::memcpy(&df, &met[2 * W + w], 4);
             rr[w] = r;
             ss[w] = (double)(df / std::max(mg, 1e-30f));
             if (it >= 2 && std::max(r, ss[w]) <= tol) done[w] = 1;
         }
+        s->hist_obs.insert(s->hist_obs.end(), rr.begin(), rr.end());
+        s->hist_src.insert(s->hist_src.end(), ss.begin(), ss.end());
         EvalCtrl& c = *s->ctrl_host;
         if (it == 1 && fallback_dev && !fell_back && *std::max_element(ss.begin(), ss.end()) > fallback_ss) {
             // the supplied start is further from the fixed point than the fallback start: restart from it
@@ -3992,6 +3990,19 @@ int sosb_solve(sosb_handle s, int max_eval, double tol, const float* x0_host, fl
                sosb_stats* stats) {
     if (!s) return 1;
     return solve_impl(s, max_eval, tol, x0_host, 0, false, 0.0, nullptr, x_out, x_out_is_device, stats);
+}
+
+int sosb_history(sosb_handle s, int capacity, int32_t* count, double* observer_relative, double* source_relative) {
+    if (!s) return 1;
+    if (!count) return fail(s, "E_FIELD: null pointer");
+    const int W = s->d.W;
+    const int n = W ? (int)(s->hist_obs.size() / W) : 0;
+    *count = n;
+    const int m = std::min(n, std::max(capacity, 0));
+    if (m && (!observer_relative || !source_relative)) return fail(s, "E_FIELD: null pointer");
+    std::copy(s->hist_obs.begin(), s->hist_obs.begin() + (size_t)m * W, observer_relative);
+    std::copy(s->hist_src.begin(), s->hist_src.begin() + (size_t)m * W, source_relative);
+    return 0;
 }
 
 int sosb_solve_warm(sosb_handle s, int max_eval, double tol, const float* x0_dev, double fallback_ss,

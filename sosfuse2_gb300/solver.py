@@ -249,11 +249,24 @@ class Solver:
             converged=[bool(stats.done[w]) for w in range(W)],
             observer_relative=obs,
             source_relative=src,
-            # the reference's consumers read the last entry of its per-evaluation history
-            # (jobs/run_state.py:99-104, jobs/walkthrough.py:296); the device loop reports the final evaluation's
-            history=[dict(observer_relative=obs, source_relative=src)],
+            # the reference's per-evaluation history (source_iteration.py:381-391); its consumers read the last entry
+            # (jobs/run_state.py:99-104, jobs/walkthrough.py:296)
+            history=self.history(),
             kernel_launches=int(stats.kernel_launches),
         )
+
+    def history(self):
+        """Per-evaluation history of the last solve on this kernel: [{evaluation, observer_relative, source_relative}]."""
+        k = self.kernel
+        count = ctypes.c_int32()
+        k._check(k.lib.sosb_history(k.h, 0, ctypes.byref(count), None, None))
+        n, W = int(count.value), k.W
+        obs = np.zeros((max(n, 1), W))
+        src = np.zeros((max(n, 1), W))
+        k._check(k.lib.sosb_history(k.h, n, ctypes.byref(count), obs.ctypes.data_as(_abi.P_f64),
+                                    src.ctypes.data_as(_abi.P_f64)))
+        return [dict(evaluation=e + 1, observer_relative=obs[e].tolist(), source_relative=src[e].tolist())
+                for e in range(n)]
 
 
 class BatchSolver:

@@ -15,7 +15,7 @@ def pytest_configure(config):
 
 
 def fixture_names():
-    return [n for n in ('walk1', 'strato1', 'strato15') if (GOLDEN / f'{n}.npz').exists()]
+    return [n for n in ('walk1', 'strato1', 'strato15', 'slow1') if (GOLDEN / f'{n}.npz').exists()]
 
 
 @pytest.fixture(scope='session')
@@ -58,3 +58,8 @@ def rel_l2_per_wave(a, b):
 def ray_index(state, cells):
     off = state['cell_cell_off']
     return np.concatenate([np.arange(off[i], off[i + 1]) for i in cells])
+
+
+def reference_history(meta):
+    """The reference solve's per-evaluation (observer_relative, source_relative) arrays [evaluations, W]."""
+    return np.asarray(meta['history_observer'], np.float64), np.asarray(meta['history_source'], np.float64)

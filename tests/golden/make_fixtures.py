@@ -19,9 +19,12 @@ The solar column table is stored only where the transport can read it (every bil
 first-light sample, dilated by two nodes in each direction) so the fixture stays small.
 """
 
+import contextlib
 import copy
+import io
 import json
 import os
+import re
 import sys
 import tempfile
 import time
@@ -30,7 +33,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REFERENCE_SRC = Path('/root/reference/src')
+REFERENCE_SRC = Path(os.environ.get('SOSFUSE2_REFERENCE_SRC', '/root/reference/src'))
 
 FIXTURES = dict(
     # the walkthrough state: clear_34 parameters, exp8 air / triangle ozone, O4 off, no stratospheric layer
@@ -40,6 +43,10 @@ FIXTURES = dict(
     # the stratospheric state over one 15-wavelength chunk, 450-730 nm (the reference kernel takes 1 or 15
     # wavelengths; its solve of this state does not converge within 64 evaluations below 400 nm)
     strato15=dict(strato=True, wavelengths=(450.0 + 20.0 * np.arange(15)).tolist()),
+    # a forward-scattering, hazy variant of the walkthrough state (AOD 0.3, g 0.78): the amounts of the synthetic
+    # family members whose iteration keeps a large source change; records whether the reference converges and its
+    # per-evaluation history either way
+    slow1=dict(strato=False, wavelengths=[550.0], parameters=dict(aod550=0.3, g=0.78)),
 )
 
 
@@ -106,6 +113,7 @@ def make(name, spec, out_dir=HERE):
     production_only()
     a = SimpleNamespace(reduced=True, settings_json=None, stratosphere=None)
     st = wt.example_state()
+    st['parameters'].update(spec.get('parameters', {}))
     if spec['strato']:
         st['stratosphere'] = dict(status='enabled', profile='gaussian', center_km=21.0, sigma_km=3.0, g=0.63, ssa=1.0)
     state = rs.effective_state(st, a)
@@ -171,10 +179,19 @@ def make(name, spec, out_dir=HERE):
     arrays['pin_project_flux'] = proj_f
 
     t2 = time.time()
+    printed = io.StringIO()
     try:
-        x, stats = Solver(s, geometry, fixed_boxes=False).solve(64, cfg['anderson_tol'])
+        with contextlib.redirect_stdout(printed):
+            x, stats = Solver(s, geometry, fixed_boxes=False).solve(64, cfg['anderson_tol'])
     except RuntimeError as exc:  # the reference's own outcome (E_NOT_CONVERGED) is recorded, not hidden
-        x, stats = None, dict(evaluations=64, converged=[], history=[], error=str(exc))
+        # its history is then only in the per-evaluation lines it prints (source_iteration.py:392-394)
+        hist = [re.search(r'obs=(\S+) source=(\S+)', line) for line in printed.getvalue().splitlines()
+                if line.startswith('SOSFUSE EVAL')]
+        stats = dict(evaluations=64, converged=[], error=str(exc),
+                     history=[dict(observer_relative=[float(h.group(1))], source_relative=[float(h.group(2))])
+                              for h in hist if h])
+        x = None
+    sys.stdout.write(printed.getvalue())
     solve_seconds = time.time() - t2
     if x is not None:
         arrays['solve_x'] = np.asarray(x, 'f4')

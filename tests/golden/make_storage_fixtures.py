@@ -9,6 +9,7 @@ It writes source.npz, moment.npz and table.npz with the reference's `write_sourc
 with `sosfuse2_gb300.storage` and compares keys, dtypes, shapes and values.
 """
 
+import os
 import sys
 import tempfile
 from pathlib import Path
@@ -16,7 +17,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REFERENCE_SRC = Path('/root/reference/src')
+REFERENCE_SRC = Path(os.environ.get('SOSFUSE2_REFERENCE_SRC', '/root/reference/src'))
 
 
 def inputs():

@@ -1,5 +1,5 @@
 """CUDA path against the oracle on small synthetic states that exercise the many-wavelength transport (W > 4), SH
-orders other than 16, two wavelength chunks (W > 32), and an 80-120 km extended grid. Same tolerances as
+orders other than 16 up to L = 48, two wavelength chunks (W > 32), and an 80-120 km extended grid. Same tolerances as
 tests/test_gpu_parity.py (moments/sources relative L2 per wavelength <= 1e-4, observer radiance rtol 1e-3)."""
 
 import numpy as np
@@ -13,6 +13,9 @@ CASES = {
     'w8_l24': dict(W=8, L=24, top=80.0, nh=6),
     'w33_l16': dict(W=33, L=16, top=80.0, nh=5),
     'w3_l32_top120': dict(W=3, L=32, top=120.0, nh=7),
+    # the largest SH order of the batched configuration (L = 48, K = 1225), on the warp path and the wavelength path
+    'w1_l48': dict(W=1, L=48, top=80.0, nh=5),
+    'w12_l48_top120': dict(W=12, L=48, top=120.0, nh=5),
 }
 
 

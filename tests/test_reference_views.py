@@ -12,7 +12,7 @@ import pytest
 
 from conftest import GOLDEN
 
-REFERENCE = Path('/root/reference/src')
+REFERENCE = Path(os.environ.get('SOSFUSE2_REFERENCE_SRC', '/root/reference/src'))
 
 
 @pytest.mark.skipif(not REFERENCE.exists() or not (GOLDEN / 'table_walk1.npz').exists(),

@@ -2,6 +2,7 @@
 importable in this environment), its weights, and the packed state it writes."""
 
 import math
+import os
 import sys
 from pathlib import Path
 
@@ -11,7 +12,7 @@ import pytest
 from sosfuse2_gb300 import synth
 from sosfuse2_gb300.state import PackedState
 
-REFERENCE = Path('/root/reference/src')
+REFERENCE = Path(os.environ.get('SOSFUSE2_REFERENCE_SRC', '/root/reference/src'))
 
 
 @pytest.mark.parametrize('h,chi,nmu,nphi,err', [(0.0, 60.0, 1, 2, 0.3), (40.0, 100.0, 3, 8, 1e-2),
