@@ -145,21 +145,22 @@ def sh_basis(mu, L):
     return out
 
 
-def cos_multiples(cp):
-    """cos(m phi), m = 0..32, by the Chebyshev recurrence in FP32."""
+def cos_multiples(cp, n=33):
+    """cos(m phi), m = 0..n-1 (the reference's table has n = 33, L <= 32), by the Chebyshev recurrence in FP32."""
     cp = np.clip(cp, F(-1), F(1)).astype(F)
-    out = np.empty((len(cp), 33), F)
+    out = np.empty((len(cp), n), F)
     out[:, 0] = F(1)
     out[:, 1] = cp
-    for m in range(2, 33):
+    for m in range(2, n):
         out[:, m] = (F(2) * cp) * out[:, m - 1] - out[:, m - 2]
     return out
 
 
 def lane_tree_sum(x):
-    """Sum over m = 0..32 as a 32-lane shuffle-down tree with m = 32 folded into lane 0 first."""
+    """Sum over m = 0..32 as a 32-lane shuffle-down tree with m = 32 folded into lane 0 first (orders above 32, which
+    the reference does not take, are folded into lanes m - 32 the same way)."""
     x = x.copy()
-    x[:, 0] = x[:, 0] + x[:, 32]
+    x[:, : x.shape[1] - 32] = x[:, : x.shape[1] - 32] + x[:, 32:]
     x = x[:, :32]
     for stride in (16, 8, 4, 2, 1):
         old = x.copy()
@@ -386,7 +387,7 @@ def sample(rays, seg, u, wu, pk):
     cells = np.stack([ir * nc + j, ir * nc + j + 1, (ir + 1) * nc + j, (ir + 1) * nc + j + 1], -1)
     sw = np.stack([(F(1) - ah) * (F(1) - ac), (F(1) - ah) * ac, ah * (F(1) - ac), ah * ac], -1)
     prof = profile_at(h, pk)
-    return dict(h=h, ds=dsl, cells=cells, sw=sw, ir=ir, T=T, cm=cos_multiples(cp), prof=prof,
+    return dict(h=h, ds=dsl, cells=cells, sw=sw, ir=ir, T=T, cm=cos_multiples(cp, max(33, pk.L + 1)), prof=prof,
                 st_prof=strato_profile(h, pk) if pk.strato else None, Q=Q, r=r, qz=(q[0][:, 2], q[1][:, 2]), t=tt)
 
 
@@ -565,8 +566,8 @@ def _sample_value(pk, r, q, field, first, phase, sphase, g, mix, hr, ha):
             aero = np.zeros((n, W), F)
             density = q['prof'][:, 0]
         else:
-            cache = np.zeros((n, 33, W), F)
-            scache = np.zeros((n, 33, W), F) if strat else None
+            cache = np.zeros((n, max(33, L + 1), W), F)
+            scache = np.zeros((n, max(33, L + 1), W), F) if strat else None
             for l in range(L + 1):
                 for m in range(l + 1):
                     k = l * (l + 1) // 2 + m
@@ -618,7 +619,7 @@ def _project(pk, b, rad, ground_only):
     Y = sh_basis(d[:, 2], L)
     st = np.sqrt(np.maximum(0.0, 1 - d[:, 2] ** 2))
     cp = np.where(st > 1e-12, d[:, 0] / np.maximum(st, 1e-30), 1.0).astype(F)
-    cm = cos_multiples(cp)
+    cm = cos_multiples(cp, max(33, L + 1))
     weight = b['weight'].astype(F)
     trace = (rad[:, :, 0] + rad[:, :, 1]) + rad[:, :, 2]
     weighted = trace * weight[:, None]

@@ -80,6 +80,7 @@ struct TimedLaunch {
 };
 
 struct EvalCtrl;
+struct LoopDev;
 
 struct sosb_state {
     sosb_dims d{};
@@ -110,13 +111,15 @@ struct sosb_state {
     bool have_first = false;
     bool tables = true;  // build and use node tables (sosb_set_node_tables)
     // fixed-point loop: evaluation control and report (device and pinned host copies), replayed evaluation graph
-    DevBuf ctrl_dev, report_dev;
+    // and loop state on the device (the control kernel's), the observer boxes of x and g, the residual's observer
+    // features, the Gram matrices, the history and the norm maxima
+    DevBuf ctrl_dev, loop_dev, box_old, box_new, obs_feat, gram, hist_dev, normmax;
     EvalCtrl* ctrl_host = nullptr;
-    uint8_t* report_host = nullptr;
-    size_t report_bytes = 0;
+    LoopDev* loop_host = nullptr;
     int feat_blocks = 0, feat_threads = 0;
-    cudaGraphExec_t graph = nullptr;
-    int64_t graph_launches = 0;
+    cudaGraphExec_t graph = nullptr;  // the solve graph: gate kernel, then a WHILE node over one evaluation
+    cudaGraphConditionalHandle cond = 0;
+    int64_t graph_launches = 0;       // kernels in one evaluation of the solve graph
     bool graphs = true;  // replay evaluations from a captured CUDA graph (sosb_set_graphs)
     bool autotune = true;  // time the table launch shapes once per shape (sosb_set_autotune)
     bool pairs = true;     // corner SH by ray-cell pair contractions (sosb_set_pairs)
@@ -1869,6 +1872,8 @@ struct EvalCtrl {
     int use[64];                 // per wavelength: 1 mix, 0 take g (frozen or no valid weights)
     float weights[4 * 64];       // [j][w] over mix_order
     unsigned long long done;     // converged wavelengths, frozen by the composition
+    int restart;                 // 1: x = *fallback (the warm start's fallback), no mix
+    const float* fallback;       // the fallback start of a warm-started solve (device field), or null
 };
 
 struct Ring4 {
@@ -2020,6 +2025,12 @@ __device__ __forceinline__ void mix_elements(const float* __restrict__ g, const 
 
 __global__ void mix_kernel(const float* __restrict__ g, Ring4 ring, const EvalCtrl* __restrict__ ctrl, int W,
                            long long n, float* __restrict__ x) {
+    if (ctrl->restart) {
+        const float* __restrict__ f = ctrl->fallback;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            x[i] = f[i];
+        return;
+    }
     if (!ctrl->mix) return;
     const float* q[4];
     for (int j = 0; j < 4; ++j) q[j] = ring.p[ctrl->mix_order[j]];
@@ -2803,7 +2814,8 @@ int sosb_destroy(sosb_handle s) {
                       &s->gdir4, &s->sh_a, &s->sh_b, &s->sh_d, &s->u_hi, &s->u_lo, &s->wu_hi, &s->wu_lo, &s->uq_hi,
                       &s->uq_lo, &s->wuq_hi, &s->wuq_lo, &s->box_ww, &s->solar, &s->rad, &s->plane, &s->moments,
                       &s->flux, &s->first_moments, &s->first_flux, &s->boundary, &s->metrics, &s->boxes, &s->fx,
-                      &s->fg, &s->norms, &s->partials, &s->dots, &s->ctrl_dev, &s->report_dev, &s->ring_g[0],
+                      &s->fg, &s->norms, &s->partials, &s->dots, &s->ctrl_dev, &s->loop_dev, &s->box_old, &s->box_new,
+                      &s->obs_feat, &s->gram, &s->hist_dev, &s->normmax, &s->ring_g[0],
                       &s->ring_g[1], &s->ring_g[2], &s->ring_g[3], &s->ring_f[0], &s->ring_f[1], &s->ring_f[2],
                       &s->ring_f[3], &s->fl_val0, &s->fl_coef, &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off,
                       &s->fl_cursor, &s->fl_entries, &s->gr_off, &s->gr_loc, &s->gr_w, &s->gr_cols, &s->gr_cos,
@@ -2819,7 +2831,7 @@ int sosb_destroy(sosb_handle s) {
     collect_timing(s);
     graph_reset(s);
     if (s->ctrl_host) cudaFreeHost(s->ctrl_host);
-    if (s->report_host) cudaFreeHost(s->report_host);
+    if (s->loop_host) cudaFreeHost(s->loop_host);
     for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
     if (s->own) cudaStreamDestroy(s->own);
     delete s;
@@ -3531,12 +3543,12 @@ int sosb_boxes(sosb_handle s, const float* field_dev, double* out_host) {
 }
 
 // Solve the regularised Gram system (FP64, partial pivoting); weights normalised to sum 1 and rejected unless finite
-// with max |w| < 8 (source_iteration.py:25-33). Returns false when singular or rejected.
-static bool anderson_weights(int n, const double* G, float* out) {
+// with max |w| < 8 (source_iteration.py:25-33). Returns false when singular or rejected. One thread per wavelength.
+__device__ bool anderson_weights(int n, const double* G, float* out) {
     double A[4][5];
     double tr = 0.0;
     for (int i = 0; i < n; ++i) tr += G[i * n + i];
-    const double reg = std::max(tr * 1e-10, 1e-30);
+    const double reg = fmax(tr * 1e-10, 1e-30);
     for (int i = 0; i < n; ++i) {
         for (int j = 0; j < n; ++j) A[i][j] = G[i * n + j] + (i == j ? reg : 0.0);
         A[i][n] = 1.0;
@@ -3544,10 +3556,14 @@ static bool anderson_weights(int n, const double* G, float* out) {
     for (int c = 0; c < n; ++c) {
         int piv = c;
         for (int r = c + 1; r < n; ++r)
-            if (std::fabs(A[r][c]) > std::fabs(A[piv][c])) piv = r;
+            if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
         if (A[piv][c] == 0.0) return false;
         if (piv != c)
-            for (int j = 0; j <= n; ++j) std::swap(A[c][j], A[piv][j]);
+            for (int j = 0; j <= n; ++j) {
+                const double t = A[c][j];
+                A[c][j] = A[piv][j];
+                A[piv][j] = t;
+            }
         for (int r = c + 1; r < n; ++r) {
             const double f = A[r][c] / A[c][c];
             for (int j = c; j <= n; ++j) A[r][j] -= f * A[c][j];
@@ -3564,8 +3580,8 @@ static bool anderson_weights(int n, const double* G, float* out) {
     double mx = 0.0;
     for (int i = 0; i < n; ++i) {
         x[i] /= sum;
-        if (!std::isfinite(x[i])) return false;
-        mx = std::max(mx, std::fabs(x[i]));
+        if (!isfinite(x[i])) return false;
+        mx = fmax(mx, fabs(x[i]));
     }
     if (!(mx < 8.0)) return false;
     for (int i = 0; i < n; ++i) out[i] = (float)x[i];
@@ -3573,27 +3589,203 @@ static bool anderson_weights(int n, const double* G, float* out) {
 }
 
 // ------------------------------------------------------------------------------------------------ the fixed-point loop
-// Report of one evaluation (device, copied to pinned host memory at its end): composition metrics [3][64] u32,
-// observer boxes of x and of g [rows][dirs][W] f64 each, Gram columns [4][W] f64.
-struct ReportLayout {
-    size_t metrics, old_b, new_b, dots, bytes;
+// Loop state of one solve on the device (Solver.solve, source_iteration.py:309-663): the evaluation count, the stop
+// flag and outcome, the per-wavelength convergence marks and measures, and the Anderson ring order. The control
+// kernel at the end of every evaluation updates it and the evaluation control block, so that one evaluation follows
+// another without a host round trip; a CUDA graph's WHILE node replays the evaluation until the control kernel
+// clears its condition.
+enum { LOOP_RUNNING = 0, LOOP_CONVERGED = 1, LOOP_BUDGET = 2, LOOP_NONFINITE = 3 };
+
+struct LoopDev {
+    int it;        // evaluations completed
+    int max_eval;
+    int go;        // 1 while another evaluation follows
+    int status;    // LOOP_*
+    int fell_back; // the supplied start was replaced by the fallback start
+    int has_fallback;
+    int norder;    // ring slots of the Anderson history, oldest first
+    int order[4];
+    int nfeat;     // observer features of the residual: stop rows x directions
+    int W;
+    unsigned long long bad;  // non-finite composed values of the last evaluation
+    double tol, fallback_ss, obs_scale;
+    int done[64];
+    double rr[64], ss[64];
 };
 
-static ReportLayout report_layout(const sosb_state* s) {
-    const size_t nbox = (size_t)s->d.n_monitor_rows * s->d.n_dirs * s->d.W;
-    ReportLayout r;
-    r.metrics = 0;
-    r.old_b = 3 * 64 * sizeof(unsigned);
-    r.new_b = r.old_b + nbox * sizeof(double);
-    r.dots = r.new_b + nbox * sizeof(double);
-    r.bytes = r.dots + 4 * (size_t)s->d.W * sizeof(double);
-    return r;
+// End of one evaluation (64 threads, thread w = wavelength w): the observer change rr = max |new - old| / |new| over
+// the stop rows' boxes and the source change ss = max |g - x| / max |g| from the composition's metrics ([0][W]
+// non-finite counts, [1][W] max |g| bits, [2][W] max |g - x| bits); a wavelength is done from the second evaluation on
+// when max(rr, ss) <= tol (source_iteration.py:353-376); the history row; the warm start's fallback check after the
+// first evaluation; then per active wavelength the observer part of the residual feature, the new Gram row and column
+// (FP64: the feature kernel's dots plus the observer products) and the Anderson weights of the next mix
+// (source_iteration.py:401-635); last, the ring slot of the next evaluation (the oldest slot once four are held) and
+// the condition of the enclosing WHILE node.
+__global__ void __launch_bounds__(64) control_kernel(LoopDev* __restrict__ L, EvalCtrl* __restrict__ ctrl,
+                                                     const unsigned* __restrict__ met, const double* __restrict__ old_b,
+                                                     const double* __restrict__ new_b,
+                                                     const double* __restrict__ dots, float* __restrict__ obs,
+                                                     double* __restrict__ gram, double* __restrict__ hist,
+                                                     unsigned* __restrict__ normmax, cudaGraphConditionalHandle cond,
+                                                     int set_cond) {
+    __shared__ double s_ss[64];
+    __shared__ unsigned long long s_bad;
+    __shared__ int s_anderson, s_restart, s_stop;
+    const int t = threadIdx.x;
+    const int W = L->W;
+    const int it = L->it + 1;
+    const int nobs = L->nfeat;
+    if (t == 0) s_bad = 0ull;
+    s_ss[t] = 0.0;
+    __syncthreads();
+    if (t < W) {
+        double r = 0.0;
+        for (int i = 0; i < nobs; ++i) {
+            const double nv = new_b[i * W + t], ov = old_b[i * W + t];
+            r = fmax(r, fabs(nv - ov) / fmax(fabs(nv), 1e-30));
+        }
+        const float mg = __uint_as_float(met[W + t]), df = __uint_as_float(met[2 * W + t]);
+        const double ss = (double)(df / fmaxf(mg, 1e-30f));
+        L->rr[t] = r;
+        L->ss[t] = ss;
+        s_ss[t] = ss;
+        if (it >= 2 && fmax(r, ss) <= L->tol) L->done[t] = 1;
+        if (it <= L->max_eval) {
+            hist[((size_t)(it - 1) * 2) * W + t] = r;
+            hist[((size_t)(it - 1) * 2 + 1) * W + t] = ss;
+        }
+        if (met[t]) atomicAdd(&s_bad, (unsigned long long)met[t]);
+    }
+    __syncthreads();
+    if (t == 0) {
+        L->it = it;
+        L->bad = s_bad;
+        int stop = 0, anderson = 0, restart = 0;
+        if (s_bad) {
+            L->status = LOOP_NONFINITE;
+            stop = 1;
+        } else {
+            double mx = 0.0;
+            for (int w = 0; w < W; ++w) mx = fmax(mx, s_ss[w]);
+            if (it == 1 && L->has_fallback && !L->fell_back && mx > L->fallback_ss) {
+                // the supplied start is further from the fixed point than the fallback start: restart from it
+                L->fell_back = 1;
+                L->norder = 0;
+                restart = 1;
+                if (it >= L->max_eval) {
+                    stop = 1;
+                    L->status = LOOP_BUDGET;
+                }
+            } else {
+                int all = 1;
+                for (int w = 0; w < W; ++w) all &= L->done[w] != 0;
+                if (all) {
+                    stop = 1;
+                    L->status = LOOP_CONVERGED;
+                } else {
+                    anderson = 1;
+                }
+            }
+        }
+        s_anderson = anderson;
+        s_restart = restart;
+        s_stop = stop;
+    }
+    __syncthreads();
+    if (s_anderson) {
+        // this evaluation's g and residual feature are in ring slot ctrl->slot; the ring order after it is the
+        // order its evaluation was issued with (ctrl->order[0 .. ctrl->m - 1])
+        const int m = ctrl->m, slot = ctrl->slot;
+        const int w = t;
+        int use = 0;
+        float wt[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (w < W && !L->done[w]) {
+            float* ob = obs + ((size_t)slot * W + w) * nobs;
+            for (int i = 0; i < nobs; ++i) {
+                const double nv = new_b[i * W + w], ov = old_b[i * W + w];
+                ob[i] = (float)((nv - ov) / fmax(fabs(nv), 1e-20) * L->obs_scale);
+            }
+            double* gw = gram + (size_t)w * 16;
+            for (int j = 0; j < m; ++j) {
+                const int oj = ctrl->order[j];
+                const float* q = obs + ((size_t)oj * W + w) * nobs;
+                double v = dots[j * W + w];
+                for (int i = 0; i < nobs; ++i) v += (double)ob[i] * (double)q[i];
+                gw[slot * 4 + oj] = v;
+                gw[oj * 4 + slot] = v;
+            }
+            if (m > 1) {
+                double G[16];
+                for (int i = 0; i < m; ++i)
+                    for (int j = 0; j < m; ++j) G[i * m + j] = gw[ctrl->order[i] * 4 + ctrl->order[j]];
+                use = anderson_weights(m, G, wt) ? 1 : 0;
+            }
+        }
+        ctrl->use[w] = use;
+        for (int j = 0; j < 4; ++j) ctrl->weights[j * 64 + w] = (use && j < m) ? wt[j] : 0.0f;
+    }
+    __syncthreads();
+    if (t == 0) {
+        int stop = s_stop;
+        if (s_anderson) {
+            const int m = ctrl->m;
+            L->norder = m;
+            for (int j = 0; j < 4; ++j) L->order[j] = ctrl->order[j];
+            ctrl->mix = 1;
+            ctrl->mix_m = m;
+            for (int j = 0; j < 4; ++j) ctrl->mix_order[j] = j < m ? ctrl->order[j] : ctrl->order[m - 1];
+            if (it >= L->max_eval) {
+                stop = 1;
+                L->status = LOOP_BUDGET;
+            }
+        } else if (s_restart) {
+            ctrl->mix = 0;
+        }
+        ctrl->restart = s_restart;
+        if (!stop) {
+            // the next evaluation's ring slot: a new one while fewer than four are held, else the oldest
+            int pend[4], np = L->norder;
+            for (int j = 0; j < 4; ++j) pend[j] = L->order[j];
+            int nslot;
+            if (np < 4) {
+                nslot = np;
+            } else {
+                nslot = pend[0];
+                for (int j = 0; j < 3; ++j) pend[j] = pend[j + 1];
+                np = 3;
+            }
+            pend[np++] = nslot;
+            ctrl->slot = nslot;
+            ctrl->m = np;
+            for (int j = 0; j < 4; ++j) ctrl->order[j] = j < np ? pend[j] : nslot;
+            unsigned long long mask = 0ull;
+            for (int v = 0; v < W; ++v)
+                if (L->done[v]) mask |= 1ull << v;
+            ctrl->done = mask;
+        }
+        L->go = stop ? 0 : 1;
+        if (set_cond) cudaGraphSetConditional(cond, stop ? 0u : 1u);
+    }
+    normmax[t] = 0u;  // the next evaluation's norm pass collects its maxima from zero
 }
 
-// Buffers of the loop: iterate x and g, the Anderson rings, norms, Gram partials, control and report.
-static int loop_alloc(sosb_state* s) {
+// First node of a solve graph: the WHILE node runs while the eager first evaluation left the loop going.
+__global__ void gate_kernel(const LoopDev* __restrict__ L, cudaGraphConditionalHandle cond) {
+    cudaGraphSetConditional(cond, L->go ? 1u : 0u);
+}
+
+// Buffers of the loop: iterate x and g, the Anderson rings, norms, Gram partials and dots, the observer boxes of x
+// and g, the residual's observer features and the Gram matrices, the history, control and loop state. A buffer
+// that moves drops the captured solve graph.
+static int loop_alloc(sosb_state* s, int max_eval) {
     const int W = s->d.W;
     const size_t bytes = (size_t)s->ns * s->src * W * sizeof(float);
+    DevBuf* bufs[] = {&s->fx, &s->fg, &s->ring_g[0], &s->ring_g[1], &s->ring_g[2], &s->ring_g[3], &s->ring_f[0],
+                      &s->ring_f[1], &s->ring_f[2], &s->ring_f[3], &s->norms, &s->partials, &s->dots, &s->box_old,
+                      &s->box_new, &s->obs_feat, &s->gram, &s->hist_dev, &s->normmax, &s->metrics, &s->ctrl_dev,
+                      &s->loop_dev};
+    void* before[sizeof bufs / sizeof bufs[0]];
+    for (size_t i = 0; i < sizeof bufs / sizeof bufs[0]; ++i) before[i] = bufs[i]->p;
     TRY(dalloc(s, s->fx, bytes));
     TRY(dalloc(s, s->fg, bytes));
     for (int j = 0; j < 4; ++j) {
@@ -3608,47 +3800,49 @@ static int loop_alloc(sosb_state* s) {
     s->feat_blocks = (int)std::min<long long>(s->ns, 152LL * (long_rows ? 8 : 4));
     TRY(dalloc(s, s->partials, (size_t)s->feat_blocks * 4 * W * sizeof(double)));
     TRY(dalloc(s, s->dots, (size_t)4 * W * sizeof(double)));
+    const size_t nbox = (size_t)s->d.n_monitor_rows * s->d.n_dirs * W;
+    TRY(dalloc(s, s->box_old, nbox * sizeof(double)));
+    TRY(dalloc(s, s->box_new, nbox * sizeof(double)));
+    const int nfeat = s->d.monitors * s->d.n_dirs;
+    TRY(dalloc(s, s->obs_feat, (size_t)4 * W * std::max(nfeat, 1) * sizeof(float)));
+    TRY(dalloc(s, s->gram, (size_t)W * 16 * sizeof(double)));
+    TRY(dalloc(s, s->hist_dev, (size_t)std::max(max_eval, 64) * 2 * W * sizeof(double)));
+    TRY(dalloc(s, s->normmax, 64 * sizeof(unsigned)));
     TRY(dalloc(s, s->metrics, 3 * 64 * sizeof(unsigned)));
     TRY(dalloc(s, s->ctrl_dev, sizeof(EvalCtrl)));
-    const ReportLayout rl = report_layout(s);
-    TRY(dalloc(s, s->report_dev, rl.bytes));
+    TRY(dalloc(s, s->loop_dev, sizeof(LoopDev)));
     if (!s->ctrl_host) CK(cudaMallocHost(&s->ctrl_host, sizeof(EvalCtrl)));
-    if (s->report_bytes < rl.bytes) {
-        if (s->report_host) CK(cudaFreeHost(s->report_host));
-        s->report_host = nullptr;
-        CK(cudaMallocHost(&s->report_host, rl.bytes));
-        s->report_bytes = rl.bytes;
-    }
+    if (!s->loop_host) CK(cudaMallocHost(&s->loop_host, sizeof(LoopDev)));
+    for (size_t i = 0; i < sizeof bufs / sizeof bufs[0]; ++i)
+        if (before[i] != bufs[i]->p) {
+            graph_reset(s);
+            break;
+        }
     return 0;
 }
 
-// One evaluation on the device, the same launches every time (the control block carries what changes):
-// x = Anderson mix of the previous ring (if ctrl.mix); boxes(x); g = apply(x) with the composition metrics; boxes(g);
-// g into the ring; residual feature and FP64 Gram column; the report copied to pinned host memory
-// (source_iteration.py:309-635, one evaluation of the loop).
-static int eval_body(sosb_state* s) {
+// One evaluation on the device, the same launches every time (the control block and the loop state carry what
+// changes): x = Anderson mix of the previous ring (or the fallback start after a restart); boxes(x); g = apply(x)
+// with the composition metrics; boxes(g); g into the ring; residual feature and FP64 Gram column; the control kernel
+// (source_iteration.py:309-635, one evaluation of the loop). set_cond: the control kernel sets the enclosing WHILE
+// node's condition.
+static int eval_body(sosb_state* s, bool set_cond) {
     const sosb_dims& d = s->d;
     const int W = d.W;
     const long long n = (long long)s->ns * s->src * W;
     float* x = P<float>(s->fx);
     float* g = P<float>(s->fg);
     EvalCtrl* ctrl = P<EvalCtrl>(s->ctrl_dev);
-    uint8_t* rep = P<uint8_t>(s->report_dev);
-    const ReportLayout rl = report_layout(s);
     const Ring4 rg{{P<float>(s->ring_g[0]), P<float>(s->ring_g[1]), P<float>(s->ring_g[2]), P<float>(s->ring_g[3])}};
     const Ring4 rf{{P<float>(s->ring_f[0]), P<float>(s->ring_f[1]), P<float>(s->ring_f[2]), P<float>(s->ring_f[3])}};
-    CK(cudaMemcpyAsync(ctrl, s->ctrl_host, sizeof(EvalCtrl), cudaMemcpyHostToDevice, s->stream));
     {
         Timer t(s, K_ANDERSON);
         mix_kernel<<<grid_for(n, wave_threads(W)), wave_threads(W), 0, s->stream>>>(g, rg, ctrl, W, n, x);
     }
     TRY(launch_check(s));
-    TRY(boxes_dev(s, x, reinterpret_cast<double*>(rep + rl.old_b)));
+    TRY(boxes_dev(s, x, P<double>(s->box_old)));
     TRY(apply_impl(s, x, g, 0ull, &ctrl->done));
-    CK(cudaMemcpyAsync(rep + rl.metrics, s->metrics.p, 3 * 64 * sizeof(unsigned), cudaMemcpyDeviceToDevice,
-                       s->stream));
-    TRY(boxes_dev(s, g, reinterpret_cast<double*>(rep + rl.new_b)));
-    CK(cudaMemsetAsync(s->metrics.p, 0, 3 * 64 * sizeof(unsigned), s->stream));
+    TRY(boxes_dev(s, g, P<double>(s->box_new)));
     {
         Timer t(s, K_ANDERSON);
         ring_copy_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(g, rg, ctrl, n);
@@ -3658,13 +3852,13 @@ static int eval_body(sosb_state* s) {
         Timer t(s, K_ANDERSON);
         norm_kernel<<<(unsigned)std::min<long long>(s->ns, 152LL * 16), s->feat_threads,
                       (size_t)s->feat_threads * sizeof(float), s->stream>>>(g, (long long)s->ns, s->src, W,
-                                                                            P<float>(s->norms), P<unsigned>(s->metrics));
+                                                                            P<float>(s->norms), P<unsigned>(s->normmax));
     }
     TRY(launch_check(s));
     {
         Timer t(s, K_ANDERSON);
         feature_kernel<<<s->feat_blocks, s->feat_threads, (size_t)s->feat_threads * 4 * sizeof(double),
-                         s->stream>>>(g, x, P<float>(s->norms), P<unsigned>(s->metrics), (long long)s->ns, s->src, W,
+                         s->stream>>>(g, x, P<float>(s->norms), P<unsigned>(s->normmax), (long long)s->ns, s->src, W,
                                       rf, ctrl, P<double>(s->partials));
     }
     TRY(launch_check(s));
@@ -3674,71 +3868,100 @@ static int eval_body(sosb_state* s) {
                                                                              4 * W, P<double>(s->dots));
     }
     TRY(launch_check(s));
-    CK(cudaMemcpyAsync(rep + rl.dots, s->dots.p, 4 * (size_t)W * sizeof(double), cudaMemcpyDeviceToDevice,
-                       s->stream));
-    CK(cudaMemcpyAsync(s->report_host, rep, rl.bytes, cudaMemcpyDeviceToHost, s->stream));
-    return 0;
-}
-
-// Enqueues one evaluation: a replay of the captured graph when graphs are on (captured at the second evaluation,
-// once buffers and tables exist), else the launches themselves. A capture that fails (an allocation or an
-// unsupported call inside it) turns graphs off for the handle and runs the launches directly.
-static int eval_issue(sosb_state* s, int it) {
-    if (!s->graphs || s->timing || it < 2) return eval_body(s);
-    if (!s->graph) {
-        const int64_t l0 = s->launches;
-        cudaGraph_t gph = nullptr;
-        const cudaError_t e0 = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
-        const int rc = e0 == cudaSuccess ? eval_body(s) : 1;
-        const cudaError_t e1 = e0 == cudaSuccess ? cudaStreamEndCapture(s->stream, &gph) : e0;
-        cudaError_t e2 = cudaErrorUnknown;
-        if (rc == 0 && e1 == cudaSuccess && gph) e2 = cudaGraphInstantiate(&s->graph, gph, 0);
-        if (gph) cudaGraphDestroy(gph);
-        const int64_t captured = s->launches - l0;  // kernels recorded into the graph, counted while capturing
-        s->launches = l0;
-        if (e2 != cudaSuccess) {
-            cudaGetLastError();
-            s->graph = nullptr;
-            s->graphs = false;
-            s->err.clear();
-            return eval_body(s);
-        }
-        s->graph_launches = captured;
+    {
+        Timer t(s, K_ANDERSON);
+        control_kernel<<<1, 64, 0, s->stream>>>(P<LoopDev>(s->loop_dev), ctrl, P<unsigned>(s->metrics),
+                                                P<double>(s->box_old), P<double>(s->box_new), P<double>(s->dots),
+                                                P<float>(s->obs_feat), P<double>(s->gram), P<double>(s->hist_dev),
+                                                P<unsigned>(s->normmax), s->cond, set_cond ? 1 : 0);
     }
-    CK(cudaGraphLaunch(s->graph, s->stream));
-    s->launches += s->graph_launches;
+    return launch_check(s);
+}
+
+// The solve graph of the handle: a gate kernel (the condition from the loop state) and a WHILE node whose body is
+// one evaluation (eval_body with its control kernel). Built after an eager first evaluation, once tables, pair
+// lists and launch shapes exist; dropped when constants, bundles, modes or loop buffers change. A capture that fails
+// (an allocation, or a call that a conditional body cannot hold) turns graphs off for the handle.
+static int build_solve_graph(sosb_state* s) {
+    if (s->graph) return 0;
+    cudaGraph_t gph = nullptr;
+    cudaError_t e = cudaGraphCreate(&gph, 0);
+    cudaGraphConditionalHandle cond = 0;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&cond, gph, 0, 0);
+    cudaGraphNode_t gate = nullptr, loop = nullptr;
+    cudaGraph_t body = nullptr;
+    const LoopDev* ld = P<LoopDev>(s->loop_dev);
+    if (e == cudaSuccess) {
+        cudaKernelNodeParams kp{};
+        void* args[] = {(void*)&ld, (void*)&cond};
+        kp.func = (void*)gate_kernel;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(1);
+        kp.kernelParams = args;
+        e = cudaGraphAddKernelNode(&gate, gph, nullptr, 0, &kp);
+    }
+    if (e == cudaSuccess) {
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        e = cudaGraphAddNode(&loop, gph, &gate, nullptr, 1, &np);
+        if (e == cudaSuccess) body = np.conditional.phGraph_out[0];
+    }
+    int rc = 1;
+    int64_t captured = 0;
+    if (e == cudaSuccess) {
+        s->cond = cond;
+        const int64_t l0 = s->launches;
+        e = cudaStreamBeginCaptureToGraph(s->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            rc = eval_body(s, true);
+            cudaGraph_t out = nullptr;
+            const cudaError_t e1 = cudaStreamEndCapture(s->stream, &out);
+            if (e1 != cudaSuccess) e = e1;
+        }
+        captured = s->launches - l0;  // kernels recorded into the body, counted while capturing
+        s->launches = l0;
+    }
+    cudaGraphExec_t exec = nullptr;
+    if (rc == 0 && e == cudaSuccess) e = cudaGraphInstantiate(&exec, gph, 0);
+    if (gph) cudaGraphDestroy(gph);
+    if (rc != 0 || e != cudaSuccess || !exec) {
+        cudaGetLastError();
+        if (exec) cudaGraphExecDestroy(exec);
+        s->graphs = false;
+        s->err.clear();
+        return 0;
+    }
+    s->graph = exec;
+    s->graph_launches = captured;
     return 0;
 }
 
-// Host side of one solve (Solver.solve, source_iteration.py:309-663): convergence test on the observer boxes and
-// the source metrics, Anderson depth 4 per wavelength (FP64 Gram and solve), the fallback restart of a warm start.
+// Host side of one solve (Solver.solve, source_iteration.py:309-663). The loop itself runs on the device: begin()
+// sets the start and the loop state, first() enqueues the first evaluation directly (it builds node tables, pair
+// lists and tunes launch shapes), rest() enqueues the solve graph (the WHILE node runs the remaining evaluations
+// until the control kernel stops it) or, with graphs off, one evaluation at a time with a read of the stop flag,
+// and end() reads the outcome, the statistics and the history back once.
 struct SolveRun {
     sosb_state* s = nullptr;
     int max_eval = 0;
-    double tol = 0.0, fallback_ss = 0.0;
-    const float* fallback_dev = nullptr;
-    int it = 0, fell_back = 0;
-    bool all_done = false;
-    std::vector<int> done, order, pending, use;
-    std::vector<double> gram, rr, ss;
-    std::vector<float> obs;
     std::chrono::steady_clock::time_point t0;
     int64_t launches0 = 0;
+    bool graphed = false;
 
-    // Sets the start x (NULL: zero; host or device field) and resets the loop.
-    int begin(sosb_state* st, int max_eval_, double tol_, const float* x0, int x0_device, bool keep_first,
-              double fallback_ss_, const float* fallback_dev_) {
+    // Sets the start x (NULL: zero; host or device field), the control block and the loop state.
+    int begin(sosb_state* st, int max_eval_, double tol, const float* x0, int x0_device, bool keep_first,
+              double fallback_ss, const float* fallback_dev) {
         s = st;
         max_eval = max_eval_;
-        tol = tol_;
-        fallback_ss = fallback_ss_;
-        fallback_dev = fallback_dev_;
         s->err.clear();
         t0 = std::chrono::steady_clock::now();
         launches0 = s->launches;
         TRY(check_ready(s, true));
         if (!keep_first) s->have_first = false;  // a solve includes its first-light pass unless told otherwise
-        TRY(loop_alloc(s));
+        TRY(loop_alloc(s, max_eval));
         const int W = s->d.W;
         const size_t bytes = (size_t)s->ns * s->src * W * sizeof(float);
         if (x0)
@@ -3746,145 +3969,79 @@ struct SolveRun {
                                s->stream));
         else
             CK(cudaMemsetAsync(s->fx.p, 0, bytes, s->stream));
-        done.assign(W, 0);
-        use.assign(64, 0);
-        gram.assign((size_t)W * 16, 0.0);
-        obs.assign((size_t)4 * W * 64, 0.0f);
-        rr.assign(W, 0.0);
-        ss.assign(W, 0.0);
-        s->hist_obs.clear();
-        s->hist_src.clear();
-        order.clear();
-        std::memset(s->ctrl_host, 0, sizeof(EvalCtrl));
+        // evaluation 1: ring slot 0, no mix (x is the start)
+        EvalCtrl& c = *s->ctrl_host;
+        std::memset(&c, 0, sizeof c);
+        c.slot = 0;
+        c.m = 1;
+        c.fallback = fallback_dev;
+        LoopDev& L = *s->loop_host;
+        std::memset(&L, 0, sizeof L);
+        L.max_eval = max_eval;
+        L.go = 1;
+        L.has_fallback = fallback_dev ? 1 : 0;
+        L.nfeat = s->d.monitors * s->d.n_dirs;
+        L.W = W;
+        L.tol = tol;
+        L.fallback_ss = fallback_ss;
+        L.obs_scale = std::sqrt((double)((size_t)s->ns * s->src) / (double)std::max(L.nfeat, 1));
+        CK(cudaMemcpyAsync(s->ctrl_dev.p, &c, sizeof c, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->loop_dev.p, &L, sizeof L, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemsetAsync(s->gram.p, 0, (size_t)W * 16 * sizeof(double), s->stream));
+        CK(cudaMemsetAsync(s->normmax.p, 0, 64 * sizeof(unsigned), s->stream));
         return 0;
     }
 
-    // Enqueues evaluation it + 1 with its ring slot chosen (committed by finish() when the Anderson step runs).
-    int issue() {
-        ++it;
-        pending = order;
-        int slot;
-        if ((int)pending.size() < 4) {
-            slot = (int)pending.size();
-        } else {
-            slot = pending.front();
-            pending.erase(pending.begin());
-        }
-        pending.push_back(slot);
-        EvalCtrl& c = *s->ctrl_host;
-        c.slot = slot;
-        c.m = (int)pending.size();
-        for (int j = 0; j < 4; ++j) c.order[j] = j < c.m ? pending[j] : slot;
-        unsigned long long mask = 0;
-        for (int w = 0; w < s->d.W; ++w)
-            if (done[w]) mask |= 1ull << w;
-        c.done = mask;
-        return eval_issue(s, it);
-    }
+    int first() { return eval_body(s, false); }
 
-    // After the stream finished the evaluation: 0 to continue, 1 when the loop ends (converged or out of budget).
-    int finish(int& stop) {
-        stop = 0;
-        const int W = s->d.W;
-        const sosb_dims& d = s->d;
-        TRY(proj_check(s));
-        const ReportLayout rl = report_layout(s);
-        const unsigned* met = reinterpret_cast<const unsigned*>(s->report_host + rl.metrics);
-        const double* old_b = reinterpret_cast<const double*>(s->report_host + rl.old_b);
-        const double* new_b = reinterpret_cast<const double*>(s->report_host + rl.new_b);
-        const double* dots = reinterpret_cast<const double*>(s->report_host + rl.dots);
-        long long bad = 0;
-        for (int w = 0; w < W; ++w) bad += met[w];
-        if (bad) return fail(s, "E_NONFINITE_SOURCE: %lld values after evaluation %d", bad, it);
-        const int stop_rows = d.monitors, dirs = d.n_dirs;
-        const int nfeat_obs = stop_rows * dirs;
-        for (int w = 0; w < W; ++w) {
-            double r = 0.0;
-            for (int i = 0; i < nfeat_obs; ++i) {
-                const double nv = new_b[i * W + w], ov = old_b[i * W + w];
-                r = std::max(r, std::fabs(nv - ov) / std::max(std::fabs(nv), 1e-30));
-            }
-            // compose_kernel's layout: [0][W] nonfinite counts, [1][W] max |g| bits, [2][W] max |g - x| bits
-            float mg, df;
-            std::memcpy(&mg, &met[W + w], 4);
-            std::memcpy(&df, &met[2 * W + w], 4);
-            rr[w] = r;
-            ss[w] = (double)(df / std::max(mg, 1e-30f));
-            if (it >= 2 && std::max(r, ss[w]) <= tol) done[w] = 1;
-        }
-        s->hist_obs.insert(s->hist_obs.end(), rr.begin(), rr.end());
-        s->hist_src.insert(s->hist_src.end(), ss.begin(), ss.end());
-        EvalCtrl& c = *s->ctrl_host;
-        if (it == 1 && fallback_dev && !fell_back && *std::max_element(ss.begin(), ss.end()) > fallback_ss) {
-            // the supplied start is further from the fixed point than the fallback start: restart from it
-            CK(cudaMemcpyAsync(s->fx.p, fallback_dev, (size_t)s->ns * s->src * W * sizeof(float),
-                               cudaMemcpyDeviceToDevice, s->stream));
-            fell_back = 1;
-            order.clear();
-            c.mix = 0;
-            if (it >= max_eval) stop = 1;
+    // The remaining evaluations: the solve graph (no host round trip), or the launches one evaluation at a time.
+    int rest() {
+        graphed = false;
+        if (s->graphs && !s->timing) TRY(build_solve_graph(s));
+        if (s->graph && s->graphs && !s->timing) {
+            CK(cudaGraphLaunch(s->graph, s->stream));
+            graphed = true;
             return 0;
         }
-        all_done = std::all_of(done.begin(), done.end(), [](int v) { return v != 0; });
-        if (all_done) {
-            stop = 1;
-            return 0;
-        }
-        // Anderson: this evaluation's g and residual feature are in ring slot c.slot
-        order = pending;
-        const int slot = c.slot;
-        const int m = (int)order.size();
-        const double obs_scale = std::sqrt((double)((size_t)s->ns * s->src) / (double)nfeat_obs);
-        std::vector<float> weights(4 * W, 0.0f);
-        for (int w = 0; w < W; ++w) {
-            use[w] = 0;
-            if (done[w]) continue;
-            float* ob = &obs[((size_t)slot * W + w) * 64];
-            for (int i = 0; i < nfeat_obs; ++i) {
-                const double nv = new_b[i * W + w], ov = old_b[i * W + w];
-                ob[i] = (float)((nv - ov) / std::max(std::fabs(nv), 1e-20) * obs_scale);
-            }
-            for (int j = 0; j < m; ++j) {
-                const float* oj = &obs[((size_t)order[j] * W + w) * 64];
-                double v = dots[j * W + w];
-                for (int i = 0; i < nfeat_obs; ++i) v += (double)ob[i] * (double)oj[i];
-                gram[w * 16 + slot * 4 + order[j]] = v;
-                gram[w * 16 + order[j] * 4 + slot] = v;
-            }
-            if (m > 1) {
-                double G[16];
-                for (int i = 0; i < m; ++i)
-                    for (int j = 0; j < m; ++j) G[i * m + j] = gram[w * 16 + order[i] * 4 + order[j]];
-                float wt[4];
-                if (anderson_weights(m, G, wt)) {
-                    use[w] = 1;
-                    for (int j = 0; j < m; ++j) weights[j * W + w] = wt[j];
-                }
-            }
-        }
-        c.mix = 1;
-        c.mix_m = m;
-        for (int j = 0; j < 4; ++j) c.mix_order[j] = j < m ? order[j] : order[m - 1];
-        for (int w = 0; w < 64; ++w) c.use[w] = w < W ? use[w] : 0;
-        for (int j = 0; j < 4; ++j)
-            for (int w = 0; w < 64; ++w) c.weights[j * 64 + w] = w < W ? weights[j * W + w] : 0.0f;
-        if (it >= max_eval) stop = 1;
-        return 0;
-    }
-
-    // The result (g when converged, else the mixed x after the last evaluation) and the statistics.
-    int end(float* x_out, int x_out_is_device, sosb_stats* stats) {
-        const size_t bytes = (size_t)s->ns * s->src * s->d.W * sizeof(float);
-        float* result = P<float>(all_done ? s->fg : s->fx);
-        if (!all_done) {
-            // the mix the next evaluation would have started with (the reference leaves its last mix in x)
-            CK(cudaMemcpyAsync(P<EvalCtrl>(s->ctrl_dev), s->ctrl_host, sizeof(EvalCtrl), cudaMemcpyHostToDevice,
+        for (;;) {
+            CK(cudaMemcpyAsync(&s->loop_host->go, &P<LoopDev>(s->loop_dev)->go, sizeof(int), cudaMemcpyDeviceToHost,
                                s->stream));
-            const long long n = (long long)s->ns * s->src * s->d.W;
+            CK(cudaStreamSynchronize(s->stream));
+            if (!s->loop_host->go) return 0;
+            TRY(eval_body(s, false));
+        }
+    }
+
+    // The result (g when converged, else the mix the next evaluation would have started with: the reference leaves
+    // its last mix in x), the statistics and the history; the reference's error codes.
+    int end(float* x_out, int x_out_is_device, sosb_stats* stats) {
+        CK(cudaMemcpyAsync(s->loop_host, s->loop_dev.p, sizeof(LoopDev), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        TRY(proj_check(s));
+        const LoopDev& L = *s->loop_host;
+        const int W = s->d.W;
+        const int n_it = std::min(L.it, max_eval);
+        if (graphed) s->launches += 1 + s->graph_launches * std::max(L.it - 1, 0);
+        std::vector<double> h((size_t)n_it * 2 * W);
+        if (n_it) CK(cudaMemcpy(h.data(), s->hist_dev.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        s->hist_obs.assign((size_t)n_it * W, 0.0);
+        s->hist_src.assign((size_t)n_it * W, 0.0);
+        for (int e = 0; e < n_it; ++e)
+            for (int w = 0; w < W; ++w) {
+                s->hist_obs[(size_t)e * W + w] = h[((size_t)e * 2) * W + w];
+                s->hist_src[(size_t)e * W + w] = h[((size_t)e * 2 + 1) * W + w];
+            }
+        if (L.status == LOOP_NONFINITE)
+            return fail(s, "E_NONFINITE_SOURCE: %llu values after evaluation %d", L.bad, L.it);
+        const bool converged = L.status == LOOP_CONVERGED;
+        const size_t bytes = (size_t)s->ns * s->src * W * sizeof(float);
+        float* result = P<float>(converged ? s->fg : s->fx);
+        if (!converged) {
+            const long long n = (long long)s->ns * s->src * W;
             const Ring4 rg{{P<float>(s->ring_g[0]), P<float>(s->ring_g[1]), P<float>(s->ring_g[2]),
                             P<float>(s->ring_g[3])}};
-            mix_kernel<<<grid_for(n, wave_threads(s->d.W)), wave_threads(s->d.W), 0, s->stream>>>(
-                P<float>(s->fg), rg, P<EvalCtrl>(s->ctrl_dev), s->d.W, n, result);
+            mix_kernel<<<grid_for(n, wave_threads(W)), wave_threads(W), 0, s->stream>>>(
+                P<float>(s->fg), rg, P<EvalCtrl>(s->ctrl_dev), W, n, result);
             TRY(launch_check(s));
         }
         CK(cudaMemcpyAsync(x_out, result, bytes, x_out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
@@ -3892,21 +4049,21 @@ struct SolveRun {
         CK(cudaStreamSynchronize(s->stream));
         if (stats) {
             std::memset(stats, 0, sizeof *stats);
-            stats->evaluations = std::min(it, max_eval);
-            stats->converged = all_done ? 1 : 0;
+            stats->evaluations = n_it;
+            stats->converged = converged ? 1 : 0;
             stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-            for (int w = 0; w < s->d.W; ++w) {
-                stats->observer_relative[w] = rr[w];
-                stats->source_relative[w] = ss[w];
-                stats->done[w] = done[w];
+            for (int w = 0; w < W; ++w) {
+                stats->observer_relative[w] = L.rr[w];
+                stats->source_relative[w] = L.ss[w];
+                stats->done[w] = L.done[w];
             }
             stats->kernel_launches = s->launches - launches0;
-            stats->start_fallback = fell_back;
+            stats->start_fallback = L.fell_back;
         }
-        if (!all_done) {
+        if (!converged) {
             int nd = 0;
-            for (int w = 0; w < s->d.W; ++w) nd += done[w];
-            return fail(s, "E_NOT_CONVERGED: %d/%d within %g", nd, s->d.W, tol);
+            for (int w = 0; w < W; ++w) nd += L.done[w] != 0;
+            return fail(s, "E_NOT_CONVERGED: %d/%d within %g", nd, W, L.tol);
         }
         return 0;
     }
@@ -3922,19 +4079,15 @@ static int solve_impl(sosb_state* s, int max_eval, double tol, const float* x0, 
     if (max_eval < 1) return fail(s, "E_FIELD: max_eval %d", max_eval);
     SolveRun run;
     TRY(run.begin(s, max_eval, tol, x0, x0_device, keep_first, fallback_ss, fallback_dev));
-    for (;;) {
-        TRY(run.issue());
-        CK(cudaStreamSynchronize(s->stream));
-        int stop = 0;
-        TRY(run.finish(stop));
-        if (stop) break;
-    }
+    TRY(run.first());
+    TRY(run.rest());
     return run.end(x_out, x_out_is_device, stats);
 }
 
-// Many solves from one host thread: up to `concurrency` handles in flight, each evaluation a graph replay on the
-// handle's stream; every round enqueues one evaluation of every active solve, then reads their reports; a solve
-// that ends hands its place to the next one.
+// Many solves from one host thread: every state's first evaluation and then its solve graph are enqueued on the
+// state's own stream, up to `concurrency` states in flight; the thread only waits for streams to finish (no
+// per-evaluation round trip), and a finished state hands its place to the next one. With graphs off, every state
+// runs its evaluations one at a time (SolveRun::rest).
 static int batch_drive(sosb_handle* hs, int n, int max_eval, double tol, const float* const* x0, int x0_device,
                        bool keep_first, double fallback_ss, const float* const* fallback_dev, float* const* x_out,
                        int x_out_is_device, sosb_stats* stats, int* status, int concurrency) {
@@ -3956,30 +4109,30 @@ static int batch_drive(sosb_handle* hs, int n, int max_eval, double tol, const f
             }
             status[i] = runs[i].begin(hs[i], max_eval, tol, x0 ? x0[i] : nullptr, x0_device, keep_first, fallback_ss,
                                       fallback_dev ? fallback_dev[i] : nullptr);
+            if (status[i] == 0) status[i] = runs[i].first();
+            if (status[i] == 0) status[i] = runs[i].rest();
             if (status[i] == 0) active.push_back(i);
         }
     };
     start();
     while (!active.empty()) {
-        for (int i : active) status[i] = runs[i].issue();
         std::vector<int> keep;
+        bool finished = false;
         for (int i : active) {
-            if (status[i]) continue;  // failed to enqueue: out of the batch with its error
-            sosb_state* s = hs[i];
-            int stop = 0;
-            const cudaError_t e = cudaStreamSynchronize(s->stream);
-            if (e != cudaSuccess)
-                status[i] = fail(s, "E_CUDA: %s", cudaGetErrorString(e));
-            else
-                status[i] = runs[i].finish(stop);
-            if (status[i] == 0 && !stop) {
+            const cudaError_t q = cudaStreamQuery(hs[i]->stream);
+            if (q == cudaErrorNotReady) {
                 keep.push_back(i);
                 continue;
             }
-            if (status[i] == 0) status[i] = runs[i].end(x_out[i], x_out_is_device, stats ? &stats[i] : nullptr);
+            finished = true;
+            if (q != cudaSuccess)
+                status[i] = fail(hs[i], "E_CUDA: %s", cudaGetErrorString(q));
+            else
+                status[i] = runs[i].end(x_out[i], x_out_is_device, stats ? &stats[i] : nullptr);
         }
         active = keep;
         start();
+        if (!finished) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
     int failed = 0;
     for (int i = 0; i < n; ++i) failed += status[i] != 0;

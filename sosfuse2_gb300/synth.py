@@ -494,7 +494,7 @@ class Family:
     depth), so `state()` costs a fraction of a second."""
 
     def __init__(self, h, chi_deg, L, nmu, nphi, path_n, shape, query_n=24, sun_scale=2, tolerance=1e-3, max_eval=64,
-                 name='synthetic', ground_nmu=3, ground_nphi=32):
+                 name='synthetic', ground_nmu=3, ground_nphi=32, monitor_elevations=MONITOR_ELEVATIONS):
         self.h = np.asarray(h, float)
         self.chi = np.deg2rad(np.asarray(chi_deg, float))
         self.top = float(self.h[-1])
@@ -503,6 +503,7 @@ class Family:
         self.L, self.path_n, self.query_n, self.name = L, path_n, query_n, name
         self.tolerance, self.max_eval = tolerance, max_eval
         self.shape = shape
+        self.monitor_elevations = tuple(float(e) for e in monitor_elevations)
         shells = _shells(self.top)
         self.table = ColumnTable(shape, shells, scale=sun_scale)
         points, dirs, weights = [], [], []
@@ -516,7 +517,7 @@ class Family:
         u4, w4 = np.polynomial.legendre.leggauss(4)
         self.box_ww = (w4[:, None] * w4[None, :] / 4).ravel()
         qpts, qdirs, qw = [], [], []
-        for hs in MONITOR_ELEVATIONS:
+        for hs in self.monitor_elevations:
             el = np.array([e + de for e, z in DIRS for de in u4 for dz in u4])
             az = np.array([z + dz for e, z in DIRS for de in u4 for dz in u4])
             e, zz = np.deg2rad(el), np.deg2rad(az)
@@ -623,7 +624,7 @@ class Family:
             ns=len(h) * len(chi), source_size=10 + K * (2 if atm.strato else 1), strato=atm.strato, g=atm.g,
             mix=(1 - 0.03) / (1 + 0.015), height=atm.H, albedo=atm.albedo, top_km=self.top, profile_step_km=step,
             density_mask=2, air_surface=1.0, tolerance=self.tolerance, max_eval=self.max_eval,
-            monitors=len(MONITOR_ELEVATIONS), n_dirs=len(DIRS), box_points=16, wavelengths_nm=atm.wl.tolist(),
+            monitors=len(self.monitor_elevations), n_dirs=len(DIRS), box_points=16, wavelengths_nm=atm.wl.tolist(),
             seed=seed, C=3 / (16 * math.pi), rays=int(len(self.cells['d'])), segments=int(len(self.cells['seg_a'])),
             query_rays=int(len(self.query['d'])),
             amounts=dict(aod=atm.aod, ssa=atm.ssa, g=atm.g, ozone_du=atm.ozone_du, albedo=atm.albedo,
@@ -709,3 +710,48 @@ def config1(seed=0, nh=241, W=30, nmu=12, nphi=16, path_n=12, L=32, chi_deg=None
     chi = production_chi_deg() if chi_deg is None else np.asarray(chi_deg, float)
     return make_state(np.linspace(0.0, 120.0, nh), chi, wl, L, nmu, nphi, path_n, atm, seed=seed, name='config1',
                       **kw)
+
+
+# the batched configuration: 64 seeded states (seeds 1000 + i) of uneven sizes
+CONFIG3_STATES = 64
+CONFIG3_TOP = 120.0
+
+
+def config3_spec(i):
+    """Sizes and amounts of batched state i (seed 1000 + i): height levels U{121..481} on 0-120 km, wavelengths
+    U{8..64} linear on 400-700 nm, L in {16, 24, 32, 48}, observer solar elevations +6 to -18 deg in 1 or 2 deg steps
+    (the stop rows), and the amounts of random_amounts (AOD U(0.02, 0.5), g U(0.5, 0.8), ozone U(250, 400) DU, albedo
+    U(0.05, 0.8)). The rest follows the reduced configuration (10-node solar-zenith grid, nmu 1, nphi 2, path_n 4)
+    and the full-table atmosphere (NO2 layer at 25 km, O4)."""
+    seed = 1000 + int(i)
+    rng = np.random.default_rng(seed)
+    amounts = dict(aod=float(rng.uniform(0.02, 0.5)), g=float(rng.uniform(0.5, 0.8)),
+                   ozone_du=float(rng.uniform(250, 400)), albedo=float(rng.uniform(0.05, 0.8)))  # random_amounts(seed)
+    nh = int(rng.integers(121, 482))
+    W = int(rng.integers(8, 65))
+    L = int(rng.choice([16, 24, 32, 48]))
+    step = int(rng.choice([1, 2]))
+    return dict(index=int(i), seed=seed, nh=nh, W=W, L=L, solar_step=step, **amounts)
+
+
+def config3_family(i):
+    """The geometry of batched state i (its grid, bundles, observer rows and ground rays)."""
+    sp = config3_spec(i)
+    wl = np.linspace(400.0, 700.0, sp['W'])
+    shape = Atmosphere(wl, seed=sp['seed'], top=CONFIG3_TOP, no2_column=5e15, o4=True)
+    elevations = np.arange(6.0, -18.0 - 1e-9, -float(sp['solar_step']))
+    return Family(np.linspace(0.0, CONFIG3_TOP, sp['nh']), REDUCED_CHI_DEG, sp['L'], 1, 2, 4, shape,
+                  name=f'config3-{i}', monitor_elevations=elevations)
+
+
+def config3(i, family=None, ground=True):
+    """Packed-state arrays of batched state i (seed 1000 + i; see config3_spec)."""
+    sp = config3_spec(i)
+    fam = family or config3_family(i)
+    a = {k: sp[k] for k in ('aod', 'g', 'ozone_du', 'albedo')}
+    atm = Atmosphere(fam.shape.wl, seed=sp['seed'], top=CONFIG3_TOP, no2_column=5e15, o4=True, **a)
+    arrays = fam.state(atm, sp['seed'], ground=ground)
+    meta = json.loads(arrays['meta'])
+    meta.update(config3=sp)
+    arrays['meta'] = json.dumps(meta)
+    return arrays

@@ -31,10 +31,10 @@ def close(a, ref, rtol=1e-3, floor=1e-6, overall=1e-5):
     assert not bad.any(), f'{bad.sum()} elements beyond rtol {rtol}'
 
 
-def close_field(a, ref):
+def close_field(a, ref, floor=1e-4):
     """Moments [cells, slots, W] and source fields."""
-    close(a, ref, floor=1e-4)
-    assert np.all(rel_l2_per_wave(a, ref) <= 1e-4)
+    assert np.all(rel_l2_per_wave(a, ref) <= 1e-4), rel_l2_per_wave(a, ref)
+    close(a, ref, floor=floor)
 
 
 @pytest.fixture(scope='module', params=fixture_names())

@@ -15,7 +15,7 @@ CASES = {
     'w3_l32_top120': dict(W=3, L=32, top=120.0, nh=7),
     # the largest SH order of the batched configuration (L = 48, K = 1225), on the warp path and the wavelength path
     'w1_l48': dict(W=1, L=48, top=80.0, nh=5),
-    'w12_l48_top120': dict(W=12, L=48, top=120.0, nh=5),
+    'w6_l48_top120': dict(W=6, L=48, top=120.0, nh=4),
 }
 
 
