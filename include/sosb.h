@@ -127,10 +127,12 @@ int sosb_set_node_tables(sosb_handle h, int enable);
  * tcgen05.mma against a basis table built once per cell bundle; the Rayleigh rows and the ground flux stay FP32.
  * E_PROJECTION for an unknown form; E_TC_TIMEOUT when a tensor-core wait ran out. */
 int sosb_set_projection(sosb_handle h, int mode);
-/* No reference counterpart. Evaluation graphs (default on): from the second evaluation of a solve, the evaluation's
- * launches (Anderson mix, observer boxes, apply, residual feature and Gram column, report copy) are captured once into
- * a CUDA graph and replayed, the changing ring slots and weights read from a device control block; the graph is
- * dropped when constants, bundles or modes change. Timing (sosb_set_timing) runs the launches directly. 0: never. */
+/* No reference counterpart. Solve graphs (default on): a solve runs its first evaluation directly (it builds the node
+ * tables and pair lists and tunes the launch shapes), then launches one CUDA graph whose WHILE node replays one
+ * evaluation (Anderson mix, observer boxes, apply, residual feature and Gram column, and a control kernel that takes
+ * the stop decision, the Gram solve and the next ring slot on the device) until the control kernel stops it: no host
+ * round trip per evaluation. The graph is rebuilt when constants, bundles, modes or loop buffers change. Timing
+ * (sosb_set_timing) or 0 here: the evaluations are launched one at a time, with the stop flag read after each. */
 int sosb_set_graphs(sosb_handle h, int enable);
 /* No reference counterpart. Autotuning (default on): the first table launch of each launch shape times 1, 2 and 4
  * warps per ray (two runs each, CUDA events) and keeps the fastest for the process; off (or during a graph capture of
@@ -263,10 +265,10 @@ int sosb_solve_warm(sosb_handle h, int max_eval, double tolerance, const float *
                     const float *fallback_dev, float *x_out, int x_out_is_device, sosb_stats *stats);
 /* Batched form of Solver.solve (no single counterpart in the reference, whose pipeline runs one state per process,
  * src/sosfuse2/jobs/pipeline_execution.py): n independent states, each its own handle and stream, driven by one host
- * thread with up to `threads` solves in flight (0: all); every round replays one evaluation graph per active state
- * (sosb_set_graphs), so that their launches overlap on the GPU, then reads their reports; a finished solve hands its
- * place to the next state. status[i] is state i's sosb_solve result (its message in sosb_last_error(hs[i]));
- * returns nonzero when any state failed. */
+ * thread with up to `threads` solves in flight (0: all); each state's first evaluation and then its solve graph
+ * (sosb_set_graphs) are enqueued on its stream, so that the states' evaluations overlap on the GPU with no host round
+ * trip; a finished solve hands its place to the next state. status[i] is state i's sosb_solve result (its message
+ * in sosb_last_error(hs[i])); returns nonzero when any state failed. */
 int sosb_solve_batch(sosb_handle *hs, int n, int max_eval, double tolerance, const float *const *x0_host,
                      float *const *x_out, int x_out_is_device, sosb_stats *stats, int *status, int threads);
 /* Tensor-core BF16 GEMM (tcgen05, TMA, TMEM; no counterpart in the reference, used by the learned warm start):
