@@ -3613,43 +3613,55 @@ struct LoopDev {
     double rr[64], ss[64];
 };
 
-// End of one evaluation (64 threads, thread w = wavelength w): the observer change rr = max |new - old| / |new| over
-// the stop rows' boxes and the source change ss = max |g - x| / max |g| from the composition's metrics ([0][W]
-// non-finite counts, [1][W] max |g| bits, [2][W] max |g - x| bits); a wavelength is done from the second evaluation on
-// when max(rr, ss) <= tol (source_iteration.py:353-376); the history row; the warm start's fallback check after the
-// first evaluation; then per active wavelength the observer part of the residual feature, the new Gram row and column
-// (FP64: the feature kernel's dots plus the observer products) and the Anderson weights of the next mix
-// (source_iteration.py:401-635); last, the ring slot of the next evaluation (the oldest slot once four are held) and
-// the condition of the enclosing WHILE node.
-__global__ void __launch_bounds__(64) control_kernel(LoopDev* __restrict__ L, EvalCtrl* __restrict__ ctrl,
-                                                     const unsigned* __restrict__ met, const double* __restrict__ old_b,
-                                                     const double* __restrict__ new_b,
-                                                     const double* __restrict__ dots, float* __restrict__ obs,
-                                                     double* __restrict__ gram, double* __restrict__ hist,
-                                                     unsigned* __restrict__ normmax, cudaGraphConditionalHandle cond,
-                                                     int set_cond) {
+// End of one evaluation (one block of CONTROL_THREADS): the observer change rr = max |new - old| / |new| over the stop
+// rows' boxes and the source change ss = max |g - x| / max |g| from the composition's metrics ([0][W] non-finite
+// counts, [1][W] max |g| bits, [2][W] max |g - x| bits); a wavelength is done from the second evaluation on when
+// max(rr, ss) <= tol (source_iteration.py:353-376); the history row; the warm start's fallback check after the first
+// evaluation; then per active wavelength the observer part of the residual feature, the new Gram row and column
+// (FP64: the feature kernel's dots plus the observer products, one warp per entry with a fixed shuffle tree) and the
+// Anderson weights of the next mix (source_iteration.py:401-635); last, the ring slot of the next evaluation (the
+// oldest slot once four are held) and the condition of the enclosing WHILE node. The (feature, wavelength) loops are
+// spread over the block; the per-wavelength decisions take one thread each.
+constexpr int CONTROL_THREADS = 256;
+
+__global__ void __launch_bounds__(CONTROL_THREADS)
+control_kernel(LoopDev* __restrict__ L, EvalCtrl* __restrict__ ctrl, const unsigned* __restrict__ met,
+               const double* __restrict__ old_b, const double* __restrict__ new_b, const double* __restrict__ dots,
+               float* __restrict__ obs, double* __restrict__ gram, double* __restrict__ hist,
+               unsigned* __restrict__ normmax, cudaGraphConditionalHandle cond, int set_cond) {
+    __shared__ unsigned long long s_rr[64];  // bits of non-negative doubles order as unsigned integers
     __shared__ double s_ss[64];
+    __shared__ int s_done[64];
     __shared__ unsigned long long s_bad;
-    __shared__ int s_anderson, s_restart, s_stop;
+    __shared__ int s_anderson, s_restart, s_stop, s_m, s_slot, s_order[4];
     const int t = threadIdx.x;
     const int W = L->W;
     const int it = L->it + 1;
     const int nobs = L->nfeat;
+    if (t < 64) {
+        s_rr[t] = 0ull;
+        s_ss[t] = 0.0;
+        s_done[t] = t < W ? L->done[t] : 1;
+    }
     if (t == 0) s_bad = 0ull;
-    s_ss[t] = 0.0;
+    __syncthreads();
+    for (int q = t; q < nobs * W; q += CONTROL_THREADS) {
+        const double nv = new_b[q], ov = old_b[q];  // [feature][W], q = i * W + w
+        const double r = fabs(nv - ov) / fmax(fabs(nv), 1e-30);
+        atomicMax(&s_rr[q % W], (unsigned long long)__double_as_longlong(r));
+    }
     __syncthreads();
     if (t < W) {
-        double r = 0.0;
-        for (int i = 0; i < nobs; ++i) {
-            const double nv = new_b[i * W + t], ov = old_b[i * W + t];
-            r = fmax(r, fabs(nv - ov) / fmax(fabs(nv), 1e-30));
-        }
+        const double r = __longlong_as_double((long long)s_rr[t]);
         const float mg = __uint_as_float(met[W + t]), df = __uint_as_float(met[2 * W + t]);
         const double ss = (double)(df / fmaxf(mg, 1e-30f));
         L->rr[t] = r;
         L->ss[t] = ss;
         s_ss[t] = ss;
-        if (it >= 2 && fmax(r, ss) <= L->tol) L->done[t] = 1;
+        if (it >= 2 && fmax(r, ss) <= L->tol) {
+            L->done[t] = 1;
+            s_done[t] = 1;
+        }
         if (it <= L->max_eval) {
             hist[((size_t)(it - 1) * 2) * W + t] = r;
             hist[((size_t)(it - 1) * 2 + 1) * W + t] = ss;
@@ -3678,7 +3690,7 @@ __global__ void __launch_bounds__(64) control_kernel(LoopDev* __restrict__ L, Ev
                 }
             } else {
                 int all = 1;
-                for (int w = 0; w < W; ++w) all &= L->done[w] != 0;
+                for (int w = 0; w < W; ++w) all &= s_done[w];
                 if (all) {
                     stop = 1;
                     L->status = LOOP_CONVERGED;
@@ -3690,50 +3702,64 @@ __global__ void __launch_bounds__(64) control_kernel(LoopDev* __restrict__ L, Ev
         s_anderson = anderson;
         s_restart = restart;
         s_stop = stop;
+        // this evaluation's g and residual feature are in ring slot ctrl->slot; the ring order after it is the order
+        // its evaluation was issued with (ctrl->order[0 .. ctrl->m - 1])
+        s_m = ctrl->m;
+        s_slot = ctrl->slot;
+        for (int j = 0; j < 4; ++j) s_order[j] = ctrl->order[j];
     }
     __syncthreads();
     if (s_anderson) {
-        // this evaluation's g and residual feature are in ring slot ctrl->slot; the ring order after it is the
-        // order its evaluation was issued with (ctrl->order[0 .. ctrl->m - 1])
-        const int m = ctrl->m, slot = ctrl->slot;
-        const int w = t;
-        int use = 0;
-        float wt[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        if (w < W && !L->done[w]) {
-            float* ob = obs + ((size_t)slot * W + w) * nobs;
-            for (int i = 0; i < nobs; ++i) {
-                const double nv = new_b[i * W + w], ov = old_b[i * W + w];
-                ob[i] = (float)((nv - ov) / fmax(fabs(nv), 1e-20) * L->obs_scale);
-            }
-            double* gw = gram + (size_t)w * 16;
-            for (int j = 0; j < m; ++j) {
-                const int oj = ctrl->order[j];
-                const float* q = obs + ((size_t)oj * W + w) * nobs;
-                double v = dots[j * W + w];
-                for (int i = 0; i < nobs; ++i) v += (double)ob[i] * (double)q[i];
-                gw[slot * 4 + oj] = v;
-                gw[oj * 4 + slot] = v;
-            }
-            if (m > 1) {
-                double G[16];
-                for (int i = 0; i < m; ++i)
-                    for (int j = 0; j < m; ++j) G[i * m + j] = gw[ctrl->order[i] * 4 + ctrl->order[j]];
-                use = anderson_weights(m, G, wt) ? 1 : 0;
+        const int m = s_m, slot = s_slot;
+        for (int q = t; q < nobs * W; q += CONTROL_THREADS) {
+            const int i = q / W, w = q - i * W;
+            if (s_done[w]) continue;
+            const double nv = new_b[q], ov = old_b[q];
+            obs[((size_t)slot * W + w) * nobs + i] = (float)((nv - ov) / fmax(fabs(nv), 1e-20) * L->obs_scale);
+        }
+        __syncthreads();
+        const int lane = t & 31, warp = t >> 5;
+        for (int e = warp; e < W * m; e += CONTROL_THREADS / 32) {
+            const int w = e / m, j = e - w * m;
+            if (s_done[w]) continue;  // the whole warp skips
+            const int oj = s_order[j];
+            const float* a = obs + ((size_t)slot * W + w) * nobs;
+            const float* q = obs + ((size_t)oj * W + w) * nobs;
+            double acc = 0.0;
+            for (int i = lane; i < nobs; i += 32) acc += (double)a[i] * (double)q[i];
+            for (int dd = 16; dd >= 1; dd >>= 1) acc += __shfl_xor_sync(FULL_MASK, acc, dd);
+            if (lane == 0) {
+                const double v = dots[j * W + w] + acc;
+                gram[(size_t)w * 16 + slot * 4 + oj] = v;
+                gram[(size_t)w * 16 + oj * 4 + slot] = v;
             }
         }
-        ctrl->use[w] = use;
-        for (int j = 0; j < 4; ++j) ctrl->weights[j * 64 + w] = (use && j < m) ? wt[j] : 0.0f;
+        __syncthreads();
+        if (t < 64) {
+            const int w = t;
+            int use = 0;
+            float wt[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (w < W && !s_done[w] && m > 1) {
+                const double* gw = gram + (size_t)w * 16;
+                double G[16];
+                for (int i = 0; i < m; ++i)
+                    for (int j = 0; j < m; ++j) G[i * m + j] = gw[s_order[i] * 4 + s_order[j]];
+                use = anderson_weights(m, G, wt) ? 1 : 0;
+            }
+            ctrl->use[w] = use;
+            for (int j = 0; j < 4; ++j) ctrl->weights[j * 64 + w] = (use && j < m) ? wt[j] : 0.0f;
+        }
     }
     __syncthreads();
     if (t == 0) {
         int stop = s_stop;
         if (s_anderson) {
-            const int m = ctrl->m;
+            const int m = s_m;
             L->norder = m;
-            for (int j = 0; j < 4; ++j) L->order[j] = ctrl->order[j];
+            for (int j = 0; j < 4; ++j) L->order[j] = s_order[j];
             ctrl->mix = 1;
             ctrl->mix_m = m;
-            for (int j = 0; j < 4; ++j) ctrl->mix_order[j] = j < m ? ctrl->order[j] : ctrl->order[m - 1];
+            for (int j = 0; j < 4; ++j) ctrl->mix_order[j] = j < m ? s_order[j] : s_order[m - 1];
             if (it >= L->max_eval) {
                 stop = 1;
                 L->status = LOOP_BUDGET;
@@ -3760,13 +3786,13 @@ __global__ void __launch_bounds__(64) control_kernel(LoopDev* __restrict__ L, Ev
             for (int j = 0; j < 4; ++j) ctrl->order[j] = j < np ? pend[j] : nslot;
             unsigned long long mask = 0ull;
             for (int v = 0; v < W; ++v)
-                if (L->done[v]) mask |= 1ull << v;
+                if (s_done[v]) mask |= 1ull << v;
             ctrl->done = mask;
         }
         L->go = stop ? 0 : 1;
         if (set_cond) cudaGraphSetConditional(cond, stop ? 0u : 1u);
     }
-    normmax[t] = 0u;  // the next evaluation's norm pass collects its maxima from zero
+    if (t < 64) normmax[t] = 0u;  // the next evaluation's norm pass collects its maxima from zero
 }
 
 // First node of a solve graph: the WHILE node runs while the eager first evaluation left the loop going.
@@ -3870,7 +3896,7 @@ static int eval_body(sosb_state* s, bool set_cond) {
     TRY(launch_check(s));
     {
         Timer t(s, K_ANDERSON);
-        control_kernel<<<1, 64, 0, s->stream>>>(P<LoopDev>(s->loop_dev), ctrl, P<unsigned>(s->metrics),
+        control_kernel<<<1, CONTROL_THREADS, 0, s->stream>>>(P<LoopDev>(s->loop_dev), ctrl, P<unsigned>(s->metrics),
                                                 P<double>(s->box_old), P<double>(s->box_new), P<double>(s->dots),
                                                 P<float>(s->obs_feat), P<double>(s->gram), P<double>(s->hist_dev),
                                                 P<unsigned>(s->normmax), s->cond, set_cond ? 1 : 0);

@@ -146,6 +146,23 @@ def ring_quadrature(r, chi, nmu, nphi, heights, rings=True, a=4.0):
     return np.column_stack([st * np.cos(phi), st * np.sin(phi), mu]), np.concatenate(ws)
 
 
+_NATIVE = True
+
+
+class numpy_geometry:
+    """Context in which the geometry builders (ring quadratures, solar column tables, ray segments) run their NumPy
+    restatements instead of libsosb's host code, so that no native library is loaded (the CPU baseline's workload)."""
+
+    def __enter__(self):
+        global _NATIVE
+        self.previous, _NATIVE = _NATIVE, False
+        return self
+
+    def __exit__(self, *exc):
+        global _NATIVE
+        _NATIVE = self.previous
+
+
 def quadratures(specs):
     """The ring quadrature (loc, w) of every (r, chi, nmu, nphi, heights, rings) of `specs`, in order, by libsosb's
     sosb_ring_quadrature (host threads; the same rule as ring_quadrature). The specs of one call share nmu, nphi,
@@ -154,6 +171,8 @@ def quadratures(specs):
 
     if not specs:
         return []
+    if not _NATIVE:
+        return [ring_quadrature(*sp) for sp in specs]
     nmu, nphi, heights, rings = specs[0][2:]
     if any(sp[2:] != (nmu, nphi, heights, rings) for sp in specs):
         raise ValueError('E_SYNTH: one quadrature rule per call')
@@ -356,7 +375,8 @@ class ColumnTable:
         self.top = atm.top
         self.h = np.linspace(0, math.sqrt(atm.top), SUN_HEIGHT_INTERVALS * scale + 1) ** 2
         self.x = np.linspace(0, 1, 400 * scale + 1)
-        self.up, self.down = native_column_table(atm, shells, self.h, self.x, n)
+        build = native_column_table if _NATIVE else column_rows
+        self.up, self.down = build(atm, shells, self.h, self.x, n)
 
     def lookup(self, h, mu):
         """Columns [n, 6] and whether the ray escapes (mu >= horizon cosine)."""
@@ -474,7 +494,8 @@ def build_bundle(points, dirs_local, weights, chi_grid, top, table, atm, with_gr
     parts = []
     for r0 in range(0, len(d), block):
         r1 = min(r0 + block, len(d))
-        parts.append(_ray_block(P[ray_cell[r0:r1]], d[r0:r1], chi_grid, top, table, with_ground_columns))
+        block_fn = _ray_block if _NATIVE else ray_block_numpy
+        parts.append(block_fn(P[ray_cell[r0:r1]], d[r0:r1], chi_grid, top, table, with_ground_columns))
     seg_off = [np.zeros(1, np.int64)]
     base = 0
     for part in parts:
@@ -494,7 +515,8 @@ class Family:
     depth), so `state()` costs a fraction of a second."""
 
     def __init__(self, h, chi_deg, L, nmu, nphi, path_n, shape, query_n=24, sun_scale=2, tolerance=1e-3, max_eval=64,
-                 name='synthetic', ground_nmu=3, ground_nphi=32, monitor_elevations=MONITOR_ELEVATIONS):
+                 name='synthetic', ground_nmu=3, ground_nphi=32, monitor_elevations=MONITOR_ELEVATIONS, cells=None,
+                 table=None):
         self.h = np.asarray(h, float)
         self.chi = np.deg2rad(np.asarray(chi_deg, float))
         self.top = float(self.h[-1])
@@ -505,10 +527,14 @@ class Family:
         self.shape = shape
         self.monitor_elevations = tuple(float(e) for e in monitor_elevations)
         shells = _shells(self.top)
-        self.table = ColumnTable(shape, shells, scale=sun_scale)
+        # the solar column table depends only on the profile shapes and the top: `table` reuses one built before
+        self.table = table if table is not None else ColumnTable(shape, shells, scale=sun_scale)
+        # the cells whose bundles are built (all by default; a subset for a timing sample), in cell order
+        ncell = len(self.h) * len(self.chi)
+        self.cell_ids = np.arange(ncell) if cells is None else np.unique(np.asarray(cells, int))
         points, dirs, weights = [], [], []
-        specs = [(R + self.h[ih], self.chi[ic], nmu, nphi, _ring_heights(self.top), True)
-                 for ih in range(len(self.h)) for ic in range(len(self.chi))]
+        specs = [(R + self.h[c // len(self.chi)], self.chi[c % len(self.chi)], nmu, nphi, _ring_heights(self.top), True)
+                 for c in self.cell_ids]
         for sp, (loc, w) in zip(specs, quadratures(specs)):
             points.append(frame(sp[0], sp[1]))
             dirs.append(loc)
@@ -545,11 +571,11 @@ class Family:
         table, h, chi = self.table, self.h, self.chi
         loc_all, w_all, col_all, sun_all, cos_all, ok_all, counts = [], [], [], [], [], [], []
         quads = quadratures([(R + h[cell // len(chi)], chi[cell % len(chi)], nmu, nphi, (), False)
-                             for cell in range(len(h) * len(chi))])
-        for cell in range(len(h) * len(chi)):
-            ih, ic = divmod(cell, len(chi))
+                             for cell in self.cell_ids])
+        for q_index, cell in enumerate(self.cell_ids):
+            ih, ic = divmod(int(cell), len(chi))
             r = R + h[ih]
-            loc, w = quads[cell]
+            loc, w = quads[q_index]
             p, up, ex = frame(r, chi[ic])
             ey = np.cross(up, ex)
             d = loc[:, 0, None] * ex + loc[:, 1, None] * ey + loc[:, 2, None] * up
@@ -572,7 +598,7 @@ class Family:
         self.g_cols = np.concatenate(col_all) + np.concatenate(sun_all)
         self.g_cos = np.maximum(0, np.concatenate(cos_all))
         self.g_ok = np.concatenate(ok_all)
-        self.g_cell = np.repeat(np.arange(len(counts)), counts)
+        self.g_cell = np.repeat(self.cell_ids, counts)
         lo = self.g_loc
         self.g_factor = np.stack([(1 - lo[:, 0] ** 2) / 2, (1 - lo[:, 1] ** 2) / 2, (1 - lo[:, 2] ** 2) / 2,
                                   -lo[:, 0] * lo[:, 2] / 2], -1)
@@ -734,14 +760,21 @@ def config3_spec(i):
     return dict(index=int(i), seed=seed, nh=nh, W=W, L=L, solar_step=step, **amounts)
 
 
-def config3_family(i):
-    """The geometry of batched state i (its grid, bundles, observer rows and ground rays)."""
+def config3_family(i, cells=None, table=None):
+    """The geometry of batched state i (its grid, bundles, observer rows and ground rays); `cells`: only those
+    cells' bundles and ground rays (a timing sample); `table`: a column table of config3_table() to reuse."""
     sp = config3_spec(i)
     wl = np.linspace(400.0, 700.0, sp['W'])
     shape = Atmosphere(wl, seed=sp['seed'], top=CONFIG3_TOP, no2_column=5e15, o4=True)
     elevations = np.arange(6.0, -18.0 - 1e-9, -float(sp['solar_step']))
     return Family(np.linspace(0.0, CONFIG3_TOP, sp['nh']), REDUCED_CHI_DEG, sp['L'], 1, 2, 4, shape,
-                  name=f'config3-{i}', monitor_elevations=elevations)
+                  name=f'config3-{i}', monitor_elevations=elevations, cells=cells, table=table)
+
+
+def config3_table():
+    """The solar column table shared by every batched state (same profile shapes and top)."""
+    shape = Atmosphere([550.0], seed=1000, top=CONFIG3_TOP, no2_column=5e15, o4=True)
+    return ColumnTable(shape, _shells(CONFIG3_TOP))
 
 
 def config3(i, family=None, ground=True):

@@ -42,10 +42,7 @@ def test_config0_first_light(config0):
     oracle, solver = config0
     oracle.initialize()
     m, f, _ = solver.kernel.launch(0, True)
-    # 157 moment rows of 1,010 cells: the high SH orders are sums with cancellation (FP64 in the oracle, compensated
-    # FP32 on the device), so the element-wise bound starts at 1e-3 of the largest moment here (2 of 77,338 entries
-    # between 1e-4 and 1e-3 of it differ by slightly more than 1e-3 relative); the relative L2 bound is unchanged
-    close_field(m.cpu().numpy(), oracle.first_moments, floor=1e-3)
+    close_field(m.cpu().numpy(), oracle.first_moments)
     close(f.cpu().numpy(), oracle.first_flux)
 
 

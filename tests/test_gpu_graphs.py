@@ -1,7 +1,8 @@
-"""Evaluation graphs and the one-thread batch driver: a solve whose evaluations replay a captured CUDA graph gives the
-field, evaluation count and statistics of the same solve launched kernel by kernel (the same kernels on the same
-inputs, so bit for bit), including a warm start that falls back and a solve that runs out of evaluations; the batch
-driver with two solves in flight gives every state's single-solve result."""
+"""Solve graphs and the one-thread batch driver: a solve whose evaluations after the first run inside one CUDA graph
+(a WHILE node that the device's control kernel stops) gives the field, evaluation count and statistics of the same
+solve launched kernel by kernel with the stop flag read after each evaluation (the same kernels on the same inputs,
+so bit for bit), including a warm start that falls back and a solve that runs out of evaluations; the batch driver
+with two solves in flight gives every state's single-solve result."""
 
 import ctypes
 
@@ -43,7 +44,7 @@ def test_graph_solve_equals_direct(case):
     assert eg is None and ed is None
     assert sg['evaluations'] == sd['evaluations']
     assert np.array_equal(xg, xd)
-    assert lg == ld  # the replayed graph counts its kernels
+    assert lg == ld + 1  # the solve graph counts its kernels, and its gate kernel is one more
 
 
 def test_graph_budget_exhausted_equals_direct():
