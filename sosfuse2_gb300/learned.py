@@ -436,9 +436,24 @@ def evaluate(ws, family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3):
     return out
 
 
+def train_config3(orders=(16, 24, 32, 48), n_train=64, epochs=30, seed=10000, device='cuda:0', log=None):
+    """One network per SH order of the batched configuration (the network's input and output are the source slots,
+    10 + 2K of them), each trained on n_train solves of synth.config3_training_family(L) (seeds seed, seed + 1, ...);
+    returns ({L: WarmStart}, {L: report})."""
+    from .synth import config3_table, config3_training_family
+
+    table = config3_table()
+    nets, reports = {}, {}
+    for L in orders:
+        fam = config3_training_family(L, table)
+        nets[L], reports[L] = train_warm_start(fam, n_train=n_train, epochs=epochs, seed=seed, device=device, log=log)
+    return nets, reports
+
+
 def solve_batch(ws, kernels, states, max_eval=64, tolerance=1e-3, threads=0):
-    """Learned-start batched solves: apply(0) on every handle concurrently, one network pass over all states' rows,
-    then the warm-started solves concurrently. Returns [(field, stats) or RuntimeError] per state."""
+    """Learned-start batched solves: apply(0) on every handle concurrently, one network pass over the rows of the
+    states of each SH order, then the warm-started solves concurrently. `ws`: one WarmStart, or {L: WarmStart}.
+    Returns [(field, stats) or RuntimeError] per state."""
     import torch
 
     n = len(kernels)
@@ -453,26 +468,32 @@ def solve_batch(ws, kernels, states, max_eval=64, tolerance=1e-3, threads=0):
     for i in range(n):
         if status[i]:
             raise RuntimeError(lib.sosb_last_error(kernels[i].h).decode())
-    rows, norms, counts = [], [], []
-    for st, g in zip(states, g1):
-        X, norm = ws.rows(st, g)
-        rows.append(X)
-        norms.append(norm)
-        counts.append(X.shape[0])
-    X = torch.cat(rows)
-    pred = ws.mlp.predict(ws._pad_in(X))[:X.shape[0], :ws.n_slots] * ws.y_std + ws.y_mean
-    starts, r0 = [], 0
-    for st, g, norm, c in zip(states, g1, norms, counts):
-        p = pred[r0:r0 + c] * ws.lit(norm)[:, None]
-        r0 += c
-        ns, slots, W = g.shape
-        x0 = g.permute(0, 2, 1).reshape(-1, slots) + norm * p
-        starts.append(x0.reshape(ns, W, slots).permute(0, 2, 1).contiguous())
+    nets = ws if isinstance(ws, dict) else None
+    starts = [None] * n
+    for L in sorted({st.L for st in states}):
+        net = nets[L] if nets is not None else ws
+        idx = [i for i, st in enumerate(states) if st.L == L]
+        rows, norms, counts = [], [], []
+        for i in idx:
+            X, norm = net.rows(states[i], g1[i])
+            rows.append(X)
+            norms.append(norm)
+            counts.append(X.shape[0])
+        X = torch.cat(rows)
+        pred = net.mlp.predict(net._pad_in(X))[:X.shape[0], :net.n_slots] * net.y_std + net.y_mean
+        r0 = 0
+        for i, norm, c in zip(idx, norms, counts):
+            p = pred[r0:r0 + c] * net.lit(norm)[:, None]
+            r0 += c
+            ns, slots, W = g1[i].shape
+            x0 = g1[i].permute(0, 2, 1).reshape(-1, slots) + norm * p
+            starts[i] = x0.reshape(ns, W, slots).permute(0, 2, 1).contiguous()
     outs = [torch.empty_like(g) for g in g1]
     stats = (_abi.Stats * n)()
     torch.cuda.synchronize()
+    fallback_ss = min(w.fallback_ss for w in nets.values()) if nets is not None else ws.fallback_ss
     lib.sosb_solve_warm_batch(handles, n, int(max_eval), float(tolerance),
-                              (ctypes.c_void_p * n)(*[x.data_ptr() for x in starts]), float(ws.fallback_ss),
+                              (ctypes.c_void_p * n)(*[x.data_ptr() for x in starts]), float(fallback_ss),
                               (ctypes.c_void_p * n)(*[g.data_ptr() for g in g1]),
                               (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs]), 1, stats, status, int(threads))
     res = []

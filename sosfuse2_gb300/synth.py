@@ -719,7 +719,8 @@ def random_amounts(seed):
 def family_atmosphere(family, seed):
     """The atmosphere of `family` with amounts random_amounts(seed)."""
     a = random_amounts(seed)
-    return Atmosphere(family.shape.wl, seed=seed, top=family.top, scale_height=family.shape.H, **a)
+    return Atmosphere(family.shape.wl, seed=seed, top=family.top, scale_height=family.shape.H,
+                      no2_column=family.shape.no2_column, o4=family.shape.o4, **a)
 
 
 def family_state(family, seed, ground=True):
@@ -788,3 +789,12 @@ def config3(i, family=None, ground=True):
     meta.update(config3=sp)
     arrays['meta'] = json.dumps(meta)
     return arrays
+
+
+def config3_training_family(L, table=None):
+    """The geometry the learned start of the batched configuration trains on for SH order L: the smallest grid of
+    the batched ranges (121 heights on 0-120 km, 8 wavelengths 400-700 nm, observer rows every 2 deg), the batched
+    states' atmosphere shapes; its states draw their amounts like the batched states (family_state, seeds 10000+)."""
+    shape = Atmosphere(np.linspace(400.0, 700.0, 8), seed=10000, top=CONFIG3_TOP, no2_column=5e15, o4=True)
+    return Family(np.linspace(0.0, CONFIG3_TOP, 121), REDUCED_CHI_DEG, int(L), 1, 2, 4, shape,
+                  name=f'config3-train-L{L}', monitor_elevations=np.arange(6.0, -18.0 - 1e-9, -2.0), table=table)

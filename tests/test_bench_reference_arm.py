@@ -1,5 +1,6 @@
-"""bench.py's reference arm on the host cores (the CPU port of the reference algorithm): one bounded step prints the
-contract's JSON line (impl, metric, value, unit, cpu_baseline with kind/cores/sample, e2e without copies)."""
+"""bench.py's reference arm on the host cores (the CPU port of the reference algorithm): one bounded step (a sample of
+one batched state) prints the contract's JSON line (impl, metric, value, unit, cpu_baseline with kind/cores/sample,
+e2e without copies) and loads no native library of this repository."""
 
 import json
 import subprocess
@@ -19,3 +20,5 @@ def test_reference_arm_prints_its_line():
     cb = line['cpu_baseline']
     assert cb['kind'] == 'port' and cb['cores'] >= 1 and cb['value'] == line['value'] and cb['sample']
     assert line['e2e'] == dict(value=line['value'], unit='solves/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0)
+    assert cb['native_libraries_loaded'] == []  # the CPU arm builds its geometry with the NumPy restatements
+    assert cb['nproc'] >= cb['cores'] >= 1
