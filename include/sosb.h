@@ -144,6 +144,14 @@ int sosb_set_autotune(sosb_handle h, int enable);
  * are listed once, every evaluation contracts each pair's plane row with the ray's basis once (per m and wavelength),
  * and the nodes add their azimuth series over the pair sums instead of each lane caching its corners. 0: off. */
 int sosb_set_pairs(sosb_handle h, int enable);
+/* No reference counterpart (its sos_vprod stage, kernel.cu:4568, computes the same corner sums on CUDA cores). Corner
+ * values on the tensor cores (default on, more than four wavelengths; takes precedence over the pair form): with the
+ * node tables, every node's four (node, corner cell) entries are bucketed by corner cell once per geometry; once per
+ * plane, tiles of 128 entries of one cell form [128 x K] x [K x W] products of the nodes' basis rows
+ * (Y_k(ray) cos(m phi_node)) with the cell's SH plane on tcgen05 (BF16 high and low parts, three products, FP32
+ * accumulation in tensor memory), and the node pass reads each node's four corner values. 0: off (pair form).
+ * E_TC_TIMEOUT when a tensor-core wait ran out. */
+int sosb_set_corner_mma(sosb_handle h, int enable);
 /* Replaces: Kernel.setup (source_solver.py:1243-1339) and constants_device (source_solver.py:2248). */
 int sosb_set_constants(sosb_handle h, const sosb_constants *c);
 /* Replaces: ray_geometry.upload_geometry / device_geometry (ray_geometry.py:205-287) of the cell bundle

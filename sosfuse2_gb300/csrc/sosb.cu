@@ -69,10 +69,16 @@ struct BundleDev {
     bool p_valid = false;
     int64_t p_ground = 0, p_total = 0;
     int64_t a_version = -1;  // plane version pair_A was contracted from
+    // (node, corner) entries bucketed by corner cell for the tensor-core corner values (CornerEntries), valid with
+    // the node table unless over the memory budget; cv the corner values of plane version c_version
+    DevBuf c_ray, c_cp, c_slot, c_tile, cv;
+    bool c_valid = false;
+    int c_ntiles = 0;
+    int64_t c_version = -1;
 };
 
 // kernel classes timed by sosb_set_timing / sosb_get_timing
-enum { K_TRANSPORT = 0, K_PROJECT, K_PLANE, K_COMPOSE, K_BOXES, K_ANDERSON, K_OTHER, K_TABLE, K_CLASSES };
+enum { K_TRANSPORT = 0, K_PROJECT, K_PLANE, K_COMPOSE, K_BOXES, K_ANDERSON, K_OTHER, K_TABLE, K_CORNER, K_CLASSES };
 
 struct TimedLaunch {
     int cls;
@@ -123,6 +129,8 @@ struct sosb_state {
     bool graphs = true;  // replay evaluations from a captured CUDA graph (sosb_set_graphs)
     bool autotune = true;  // time the table launch shapes once per shape (sosb_set_autotune)
     bool pairs = true;     // corner SH by ray-cell pair contractions (sosb_set_pairs)
+    bool corner_mma = true;  // corner SH values on the tensor cores, more than four wavelengths (sosb_set_corner_mma)
+    bool corner_used = false;  // a corner GEMM ran since the last check of its bounded waits
     int proj_mode = 0;   // projection form (sosb_set_projection): PROJ_FP32, PROJ_BF16X3, PROJ_TF32, PROJ_BF16
     int64_t launches = 0;
     // per-evaluation history of the last solve on this handle: [evaluation][W] observer and source relative changes
@@ -1742,6 +1750,265 @@ __global__ void __launch_bounds__(128)
     if (warp == 0) tcx::tmem_dealloc(tmem, tmem_cols);
 }
 
+// ------------------------------------------------------------------ corner SH values on the tensor cores (W > 4)
+// The corner SH value of a node at one of its four corner cells c is
+//     V[node, c][w] = sum_m cos(m phi_node) sum_l Y_lm(mu_ray) plane[c][k(l, m)][w] = sum_k B[node][k] plane[c][k][w]
+// with the node's basis row B[node][k] = Y_k(ray) cos(m(k) phi_node) (the per-m contraction of a ray-cell pair
+// followed by the node's azimuth series, folded into one K-long dot product). The (node, corner) entries of a bundle
+// are bucketed by corner cell once per geometry; for every cell, tiles of 128 entries form the GEMM
+// [128 x K] x [K x W] against the cell's plane on tcgen05 (BF16 operands split into high and low parts, three
+// products, FP32 accumulation in tensor memory: the bf16x3 form), once per plane and bundle; the node pass then reads
+// the four corner values of each node (transport_corner_wave_kernel).
+struct CornerEntries {
+    const int* ray;    // [entries] ray of the entry's node
+    const float* cp;   // [entries] the node's azimuth cosine
+    const int* slot;   // [entries] node * 4 + corner: the row of the output
+    const int4* tile;  // [tiles] (cell, first entry, entries, 0)
+};
+
+// One thread per ray: the four corner cells of each of its nodes. Pass 0 counts the entries of each cell (cnt),
+// pass 1 writes them at the cell's cursor (the order within a cell does not matter: each output row is its own dot
+// product).
+__global__ void corner_entries_kernel(Optics o, Rays b, NodeTable tab, int nq, int pass, int* cnt, int* cursor,
+                                      int* e_ray, float* e_cp, int* e_slot) {
+    for (int ray = blockIdx.x * blockDim.x + threadIdx.x; ray < b.nray; ray += gridDim.x * blockDim.x) {
+        const int s0 = b.seg_off[ray];
+        const long long node0 = (long long)s0 * nq;
+        const int nn = (b.seg_off[ray + 1] - s0) * nq;
+        for (int i = 0; i < nn; ++i) {
+            const float4 ms = tab.misc[node0 + i];
+            const int pk = __float_as_int(ms.w);
+            const int cell0 = (pk >> 16) * o.nc + (pk & 0xffff);
+            for (int c = 0; c < 4; ++c) {
+                const int cell = cell0 + (c & 1) + (c >> 1) * o.nc;
+                if (pass == 0) {
+                    atomicAdd(&cnt[cell], 1);
+                } else {
+                    const int at = atomicAdd(&cursor[cell], 1);
+                    e_ray[at] = ray;
+                    e_cp[at] = ms.z;
+                    e_slot[at] = (int)((node0 + i) * 4 + c);
+                }
+            }
+        }
+    }
+}
+
+constexpr int CORNER_THREADS = 128;
+
+static size_t corner_tc_smem(int np, int L) {
+    // A high/low tiles (2 x 16 KB), B high/low tiles (2 x np rows of 128 bytes), cos(m phi) rows, m of each k of a
+    // chunk, the barrier and the tensor-memory slot; 1 KB of alignment slack
+    return 1024 + 2 * 16384 + 2 * (size_t)np * 128 + (size_t)CORNER_THREADS * (L + 1) * 4 + 64 * 4 + 64;
+}
+
+// One CTA per tile of 128 entries of one corner cell: per chunk of 64 SH coefficients, thread r builds row r of the
+// A tile (B[entry][k] split into BF16 high and low parts) and the block builds the B tile (the cell's plane, np
+// wavelength rows, split likewise) in the 128-byte swizzle; one thread issues the 12 MMAs (four K steps of 16, three
+// products each) and waits for them (bounded) before the tiles are rebuilt. The epilogue stores each row's np FP32
+// values at its slot.
+__global__ void __launch_bounds__(CORNER_THREADS)
+    corner_tc_kernel(Optics o, CornerEntries ce, const float* __restrict__ y_tab, int kp,
+                     const float* __restrict__ plane, int np, uint32_t idesc, uint32_t tmem_cols,
+                     float* __restrict__ out) {
+    extern __shared__ uint8_t corner_raw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(corner_raw) + 1023) & ~(uintptr_t)1023);
+    uint8_t* a_hi = sm;
+    uint8_t* a_lo = sm + 16384;
+    uint8_t* b_hi = sm + 32768;
+    uint8_t* b_lo = b_hi + np * 128;
+    float* cm = reinterpret_cast<float*>(b_lo + np * 128);  // [CORNER_THREADS][L + 1]
+    const int L1 = o.L + 1;
+    int* mk = reinterpret_cast<int*>(cm + CORNER_THREADS * L1);  // m of the chunk's 64 coefficients
+    uint64_t* bar = reinterpret_cast<uint64_t*>(mk + 64);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int4 tile = ce.tile[blockIdx.x];
+    const int cell = tile.x, e0 = tile.y, ne = tile.z;
+    const int t = threadIdx.x, warp = t >> 5;
+    const int W = o.W, K = o.K;
+    if (t == 0) {
+        tcx::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tcx::tmem_alloc(tslot, tmem_cols);
+    // the entry's ray and its cos(m phi) series (the Chebyshev recurrence of azimuth_sum)
+    const bool valid = t < ne;
+    const int ray = valid ? ce.ray[e0 + t] : 0;
+    {
+        const float cpv = valid ? clampf(ce.cp[e0 + t], -1.0f, 1.0f) : 0.0f;
+        float* row = cm + t * L1;
+        float c0 = 1.0f, c1 = cpv;
+        row[0] = valid ? 1.0f : 0.0f;
+        if (L1 > 1) row[1] = valid ? c1 : 0.0f;
+        for (int m = 2; m < L1; ++m) {
+            const float c2 = (2.0f * cpv) * c1 - c0;
+            c0 = c1;
+            c1 = c2;
+            row[m] = valid ? c2 : 0.0f;
+        }
+    }
+    tcx::fence_before();
+    __syncthreads();
+    tcx::fence_after();
+    const uint32_t tmem = *tslot;
+    const float* yr = y_tab + (size_t)ray * kp;
+    const float* pc = plane + (size_t)cell * K * W;
+    const int nchunk = (K + 63) / 64;
+    bool ok = true;
+    for (int ch = 0; ch < nchunk && ok; ++ch) {
+        const int k0 = ch * 64;
+        if (t < 64) {
+            // m of coefficient k0 + t: k = l (l + 1) / 2 + m
+            const int k = k0 + t;
+            int l = (int)((sqrtf(8.0f * k + 1.0f) - 1.0f) * 0.5f);
+            while ((l + 1) * (l + 2) / 2 <= k) ++l;
+            while (l * (l + 1) / 2 > k) --l;
+            mk[t] = k - l * (l + 1) / 2;
+        }
+        __syncthreads();
+        // A row t: B[entry][k] for k in the chunk, 8 pieces of 8 coefficients
+        const float* crow = cm + t * L1;
+#pragma unroll 2
+        for (int p = 0; p < 8; ++p) {
+            float v[8];
+            const int kb = k0 + p * 8;
+            if (valid && kb + 8 <= K) {
+                const float4 y0 = *reinterpret_cast<const float4*>(yr + kb);
+                const float4 y1 = *reinterpret_cast<const float4*>(yr + kb + 4);
+                v[0] = y0.x; v[1] = y0.y; v[2] = y0.z; v[3] = y0.w;
+                v[4] = y1.x; v[5] = y1.y; v[6] = y1.z; v[7] = y1.w;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) v[e] = (valid && kb + e < K) ? yr[kb + e] : 0.0f;
+            }
+            __align__(16) __nv_bfloat16 h[8], lo[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const float x = v[e] * crow[mk[p * 8 + e]];
+                h[e] = __float2bfloat16_rn(x);
+                lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
+            }
+            *reinterpret_cast<uint4*>(a_hi + tcx::sw128_offset(t, p)) = *reinterpret_cast<const uint4*>(h);
+            *reinterpret_cast<uint4*>(a_lo + tcx::sw128_offset(t, p)) = *reinterpret_cast<const uint4*>(lo);
+        }
+        // B tile: np rows (wavelengths) x 8 pieces; consecutive threads take consecutive wavelengths (coalesced)
+        for (int q = t; q < np * 8; q += CORNER_THREADS) {
+            const int p = q / np, w = q - p * np;
+            __align__(16) __nv_bfloat16 h[8], lo[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int k = k0 + p * 8 + e;
+                const float x = (w < W && k < K) ? pc[(size_t)k * W + w] : 0.0f;
+                h[e] = __float2bfloat16_rn(x);
+                lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
+            }
+            *reinterpret_cast<uint4*>(b_hi + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(h);
+            *reinterpret_cast<uint4*>(b_lo + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(lo);
+        }
+        tcx::fence_proxy_async();
+        __syncthreads();
+        if (t == 0) {
+            tcx::fence_after();
+            const uint32_t ah = tcx::smem_u32(a_hi), al = tcx::smem_u32(a_lo);
+            const uint32_t bh = tcx::smem_u32(b_hi), bl = tcx::smem_u32(b_lo);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
+                tcx::mma_f16(tmem, tcx::sw128_desc(ah + kk * 32), tcx::sw128_desc(bh + kk * 32), idesc, acc);
+                tcx::mma_f16(tmem, tcx::sw128_desc(ah + kk * 32), tcx::sw128_desc(bl + kk * 32), idesc, 1u);
+                tcx::mma_f16(tmem, tcx::sw128_desc(al + kk * 32), tcx::sw128_desc(bh + kk * 32), idesc, 1u);
+            }
+            tcx::mma_commit(bar);
+        }
+        ok = tcx::mbar_wait(bar, ch & 1, 2u, &g_proj_error);  // the tiles may be rebuilt once the MMAs are done
+        ok = __all_sync(FULL_MASK, ok);
+        ok = __syncthreads_and(ok);
+        tcx::fence_after();
+    }
+    if (ok) {
+        float* dst = valid ? out + (size_t)ce.slot[e0 + t] * W : nullptr;
+        for (int c0 = 0; c0 < np; c0 += 16) {
+            float v[16];
+            tcx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);  // warp-wide
+            if (valid)
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (c0 + i < W) dst[c0 + i] = v[i];
+        }
+    }
+    tcx::fence_before();
+    __syncthreads();
+    if (warp == 0) tcx::tmem_dealloc(tmem, tmem_cols);
+}
+
+// Warm pass from the node table and the corner values (many wavelengths): transport_pair_wave_kernel with each
+// corner's SH value read from V[node * 4 + corner][w] instead of summed from the pair contractions.
+__global__ void __launch_bounds__(PAIR_WAVE_WARPS * 32)
+    transport_corner_wave_kernel(Optics o, Rays b, LaneInputs in, NodeTable tab, const float* __restrict__ cv,
+                                 int ray0, int nray, int wchunks, float4* rad) {
+    __shared__ float recs_all[PAIR_WAVE_WARPS][32 * TREC_WORDS];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const long long warp = (long long)blockIdx.x * PAIR_WAVE_WARPS + wid;
+    if (warp >= (long long)nray * wchunks) return;  // the whole warp leaves together
+    const int ray = ray0 + (int)(warp / wchunks);
+    const int w = (int)(warp % wchunks) * 32 + lane;
+    const bool wok = w < o.W;
+    const int wl = wok ? w : o.W - 1;  // idle lanes compute a valid wavelength and store nothing
+    const int W = o.W;
+    float* recs = recs_all[wid];
+    RayConst rc;
+    ray_constants(b, ray, rc);
+    const int nq = in.nq;
+    const int s0 = b.seg_off[ray];
+    const long long node0 = (long long)s0 * nq;
+    const int nn = (b.seg_off[ray + 1] - s0) * nq;
+    float total[4] = {0, 0, 0, 0}, comp[4] = {0, 0, 0, 0};
+    for (int base = 0; base < nn; base += 32) {
+        const int i = base + lane;
+        const int cnt = min(32, nn - base);
+        __syncwarp();
+        if (i < nn) {
+            TableRec* R = reinterpret_cast<TableRec*>(recs + lane * TREC_WORDS);
+            Node n;
+            table_node(o, rc, tab, node0 + i, n);
+            for (int k = 0; k < 4; ++k)
+                for (int u = 0; u < 4; ++u) R->T[4 * k + u] = n.T[k][u];
+            for (int c = 0; c < 4; ++c) {
+                R->sw[c] = n.sw[c];
+                R->cell[c] = n.cell[c];
+            }
+            R->ir = n.ir;
+            R->cp = n.cp;
+        }
+        __syncwarp();
+        for (int j = 0; j < cnt; ++j) {
+            const TableRec* R = reinterpret_cast<const TableRec*>(recs + j * TREC_WORDS);
+            const long long node = node0 + base + j;
+            const float att = tab.att[node * W + wl];
+            Node n;
+            for (int k = 0; k < 4; ++k)
+                for (int u = 0; u < 4; ++u) n.T[k][u] = R->T[4 * k + u];
+            for (int c = 0; c < 4; ++c) {
+                n.sw[c] = R->sw[c];
+                n.cell[c] = R->cell[c];
+            }
+            n.ir = R->ir;
+            n.cp = R->cp;
+            float aero[4];
+            for (int c = 0; c < 4; ++c) aero[c] = cv[(size_t)(node * 4 + c) * W + wl];
+            float val[4];
+            warm_value(o, rc, n, in.field, wl, aero, val);
+            for (int k = 0; k < 4; ++k) kahan(total[k], comp[k], val[k] * att);
+        }
+    }
+    if (wok) {
+        boundary_term(o, b, rc, in.boundary, ray, w, total);
+        rad[(size_t)ray * W + w] = make_float4(total[0], total[1], total[2], total[3]);
+    }
+}
+
+
 __global__ void add_kernel(const float* a, const float* b, float* out, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = a[i] + b[i];
@@ -2217,7 +2484,65 @@ static int plane_kp(const sosb_state* s) { return s->d.W <= 4 ? (s->K + 3) & ~3 
 static void invalidate_tables(BundleDev& b, bool geometry = true) {
     b.t_valid = false;
     b.t_too_big = false;
-    if (geometry) b.p_valid = false;
+    if (geometry) {
+        b.p_valid = false;
+        b.c_valid = false;
+    }
+}
+
+// (node, corner) entries of bundle b bucketed by corner cell (geometry only), the tiles of 128 entries within a cell,
+// the rays' basis table and the corner-value buffer; over half the free memory: the bundle stays on the pair form.
+static int build_corners(sosb_state* s, BundleDev& b, int nq) {
+    b.c_valid = false;
+    if (!s->corner_mma || b.nray == 0 || s->d.W <= 4) return 0;
+    const sosb_dims& d = s->d;
+    const int64_t nray = b.nray;
+    const int64_t entries = (int64_t)b.nseg * nq * 4;
+    const int kp = (s->K + 3) & ~3;
+    if (entries >= (int64_t)1 << 31) return 0;
+    const size_t need = (size_t)entries * (12 + (size_t)d.W * 4) + (size_t)nray * kp * sizeof(float);
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if (need > free_b / 2) return 0;
+    const int ns = s->ns;
+    LocalBuf cnt, off, cursor;
+    TRY(dalloc(s, cnt, (size_t)(ns + 1) * sizeof(int)));
+    TRY(dalloc(s, off, (size_t)(ns + 1) * sizeof(int)));
+    TRY(dalloc(s, cursor, (size_t)(ns + 1) * sizeof(int)));
+    CK(cudaMemsetAsync(cnt.p, 0, (size_t)(ns + 1) * sizeof(int), s->stream));
+    const NodeTable tab{P<float4>(b.t_frame), P<float4>(b.t_misc), P<float>(b.t_att)};
+    const int blocks = grid_for(nray, 128);
+    corner_entries_kernel<<<blocks, 128, 0, s->stream>>>(optics_of(s), rays_of(b), tab, nq, 0, P<int>(cnt), nullptr,
+                                                        nullptr, nullptr, nullptr);
+    TRY(launch_check(s));
+    bucket_scan_kernel<<<1, 1024, 0, s->stream>>>(P<int>(cnt), ns, P<int>(off), P<int>(cursor));
+    TRY(launch_check(s));
+    TRY(dalloc(s, b.c_ray, (size_t)entries * sizeof(int)));
+    TRY(dalloc(s, b.c_cp, (size_t)entries * sizeof(float)));
+    TRY(dalloc(s, b.c_slot, (size_t)entries * sizeof(int)));
+    corner_entries_kernel<<<blocks, 128, 0, s->stream>>>(optics_of(s), rays_of(b), tab, nq, 1, nullptr,
+                                                        P<int>(cursor), P<int>(b.c_ray), P<float>(b.c_cp),
+                                                        P<int>(b.c_slot));
+    TRY(launch_check(s));
+    std::vector<int> hoff(ns + 1);
+    CK(cudaMemcpyAsync(hoff.data(), off.p, (size_t)(ns + 1) * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    std::vector<int4> tiles;
+    for (int c = 0; c < ns; ++c)
+        for (int e = hoff[c]; e < hoff[c + 1]; e += 128) tiles.push_back(make_int4(c, e, std::min(128, hoff[c + 1] - e), 0));
+    TRY(dalloc(s, b.c_tile, std::max<size_t>(tiles.size(), 1) * sizeof(int4)));
+    if (!tiles.empty()) CK(cudaMemcpyAsync(b.c_tile.p, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                                           s->stream));
+    TRY(dalloc(s, b.y_tab, (size_t)nray * kp * sizeof(float)));
+    pair_basis_kernel<<<(unsigned)((nray * 32 + 127) / 128), 128, 0, s->stream>>>(optics_of(s), rays_of(b), kp,
+                                                                                 P<float>(b.y_tab));
+    TRY(launch_check(s));
+    TRY(dalloc(s, b.cv, (size_t)entries * d.W * sizeof(float)));
+    CK(cudaStreamSynchronize(s->stream));  // the host tile list outlives no call
+    b.c_ntiles = (int)tiles.size();
+    b.c_version = -1;
+    b.c_valid = true;
+    return 0;
 }
 
 // Ray-cell pairs of bundle b from its node table (geometry only): per-ray counts, offsets, the pairs, each node's
@@ -2483,7 +2808,28 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
         const long long warps = (long long)nray * wchunks;
         const long long blocks = (warps + WAVE_WARPS - 1) / WAVE_WARPS;
         Timer timer(s, read ? K_TABLE : K_TRANSPORT);
-        if (read && b.p_valid) {
+        if (read && b.c_valid) {
+            if (b.c_version != s->plane_version) {
+                // corner values of every (node, corner) entry of the bundle against the current plane (reused by the
+                // launches that follow on the same plane: the ground and the warm pass of one apply)
+                const int np = (d.W + 15) / 16 * 16;
+                const uint32_t cols = np <= 32 ? 32u : 64u;
+                const size_t smem = corner_tc_smem(np, d.L);
+                const CornerEntries ce{P<int>(b.c_ray), P<float>(b.c_cp), P<int>(b.c_slot), P<int4>(b.c_tile)};
+                if (b.c_ntiles > 0) {
+                    Timer ct(s, K_CORNER);
+                    corner_tc_kernel<<<(unsigned)b.c_ntiles, CORNER_THREADS, smem, s->stream>>>(
+                        optics_of(s), ce, P<float>(b.y_tab), (s->K + 3) & ~3, in.plane, np, tcx::idesc_bf16(128, np),
+                        cols, P<float>(b.cv));
+                    TRY(launch_check(s));
+                    s->corner_used = true;
+                }
+                b.c_version = s->plane_version;
+            }
+            const unsigned pb = (unsigned)((warps + PAIR_WAVE_WARPS - 1) / PAIR_WAVE_WARPS);
+            transport_corner_wave_kernel<<<pb, PAIR_WAVE_WARPS * 32, 0, s->stream>>>(
+                optics_of(s), rays_of(b), in, table, P<float>(b.cv), (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
+        } else if (read && b.p_valid) {
             const PairTable pt{P<int>(b.p_off), P<int>(b.p_cell), P<int>(b.p_ray), P<int4>(b.p_node),
                                P<float>(b.y_tab), P<float>(b.pair_A)};
             if (b.a_version != s->plane_version) {
@@ -2515,7 +2861,8 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
     TRY(launch_check(s));
     if (write.frame) {
         b.t_valid = true;
-        if (!b.p_valid) TRY(build_pairs(s, b, in.nq));
+        if (!b.c_valid) TRY(build_corners(s, b, in.nq));
+        if (!b.c_valid && !b.p_valid) TRY(build_pairs(s, b, in.nq));
     }
     return 0;
 }
@@ -2599,14 +2946,15 @@ static int run_project(sosb_state* s, BundleDev& b, int ncell, bool ground_only,
 
 // Bounded waits of the tensor-core projection that ran out since the last check (synchronises the stream).
 static int proj_check(sosb_state* s) {
-    if (s->proj_mode == PROJ_FP32) return 0;
+    if (s->proj_mode == PROJ_FP32 && !s->corner_used) return 0;
+    s->corner_used = false;
     unsigned flags = 0;
     CK(cudaStreamSynchronize(s->stream));
     CK(cudaMemcpyFromSymbol(&flags, g_proj_error, sizeof flags));
     if (flags) {
         const unsigned zero = 0;
         CK(cudaMemcpyToSymbol(g_proj_error, &zero, sizeof zero));
-        return fail(s, "E_TC_TIMEOUT: a tensor-core projection wait ran out (flags %u)", flags);
+        return fail(s, "E_TC_TIMEOUT: a tensor-core wait ran out (flags %u: 1 projection, 2 corner values)", flags);
     }
     return 0;
 }
@@ -2770,29 +3118,32 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
     }
     s->stream = s->own;
     {
-        const size_t p_smem = project_smem((d.L + 1) * (d.L + 2) / 2, d.W);
-        auto wave_table = d.L == 16 ? transport_table_wave_kernel<16>
-                                    : (d.L == 32 ? transport_table_wave_kernel<32> : transport_table_wave_kernel<0>);
-        if (cudaFuncSetAttribute(wave_table, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)table_wave_smem(d.L)) != cudaSuccess ||
-            cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p_smem) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(transport_wave_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)wave_smem(d.L)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_wave_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)wave_smem(d.L)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_warp_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_warp_kernel<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_warp_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess ||
-            cudaFuncSetAttribute(transport_warp_kernel<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)warp_smem((d.L + 1) * (d.L + 2) / 2)) != cudaSuccess) {
+        // Dynamic shared memory of the kernels whose needs depend on L, K and W: every handle's sizes must fit the
+        // device's opt-in limit, and the limit itself is what the attributes are set to, so that handles of
+        // different sizes in one process never lower a bound another handle relies on.
+        int dev = 0, optin = 0;
+        const int K = (d.L + 1) * (d.L + 2) / 2;
+        const size_t need = std::max({table_wave_smem(d.L), project_smem(K, d.W), wave_smem(d.L), warp_smem(K)});
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+            need > (size_t)optin) {
             cudaStreamDestroy(s->own);
             delete s;
             return 5;
         }
+        const void* fns[] = {(const void*)transport_table_wave_kernel<16>, (const void*)transport_table_wave_kernel<32>,
+                             (const void*)transport_table_wave_kernel<0>, (const void*)project_kernel,
+                             (const void*)transport_wave_kernel<false>, (const void*)transport_wave_kernel<true>,
+                             (const void*)transport_warp_kernel<1, false>, (const void*)transport_warp_kernel<4, false>,
+                             (const void*)transport_warp_kernel<1, true>, (const void*)transport_warp_kernel<4, true>,
+                             (const void*)corner_tc_kernel, (const void*)project_tc_kernel<PROJ_BF16X3>,
+                             (const void*)project_tc_kernel<PROJ_TF32>, (const void*)project_tc_kernel<PROJ_BF16>};
+        for (const void* fn : fns)
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+                cudaStreamDestroy(s->own);
+                delete s;
+                return 5;
+            }
     }
     // FP32 SH recurrence constants
     std::vector<float> a, b, dd;
@@ -2825,7 +3176,8 @@ int sosb_destroy(sosb_handle s) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
                         &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits,
                         &bd->t_frame, &bd->t_misc, &bd->t_att, &bd->b_hi, &bd->b_lo, &bd->p_off, &bd->p_cell,
-                        &bd->p_ray, &bd->p_node, &bd->y_tab, &bd->pair_A};
+                        &bd->p_ray, &bd->p_node, &bd->y_tab, &bd->pair_A, &bd->c_ray, &bd->c_cp, &bd->c_slot,
+                        &bd->c_tile, &bd->cv};
         for (DevBuf* b : bb) dfree(s, *b);
     }
     collect_timing(s);
@@ -2862,20 +3214,6 @@ int sosb_get_timing(sosb_handle s, double* ms, int64_t* launches, int n) {
 int sosb_set_projection(sosb_handle s, int mode) {
     if (!s) return 1;
     if (mode < PROJ_FP32 || mode > PROJ_BF16) return fail(s, "E_PROJECTION: unknown form %d", mode);
-    if (mode != PROJ_FP32) {
-        const int np = (s->d.W + 15) / 16 * 16;
-        cudaError_t e = cudaSuccess;
-        if (mode == PROJ_BF16X3)
-            e = cudaFuncSetAttribute(project_tc_kernel<PROJ_BF16X3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)project_tc_smem(mode, np));
-        else if (mode == PROJ_TF32)
-            e = cudaFuncSetAttribute(project_tc_kernel<PROJ_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)project_tc_smem(mode, np));
-        else
-            e = cudaFuncSetAttribute(project_tc_kernel<PROJ_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)project_tc_smem(mode, np));
-        if (e != cudaSuccess) return fail(s, "E_CUDA: %s", cudaGetErrorString(e));
-    }
     s->proj_mode = mode;
     graph_reset(s);
     return 0;
@@ -4219,6 +4557,15 @@ int sosb_solve_warm_batch(sosb_handle* hs, int n, int max_eval, double tol, cons
 int sosb_set_pairs(sosb_handle s, int enable) {
     if (!s) return 1;
     s->pairs = enable != 0;
+    invalidate_tables(s->cells);
+    invalidate_tables(s->obs);
+    graph_reset(s);
+    return 0;
+}
+
+int sosb_set_corner_mma(sosb_handle s, int enable) {
+    if (!s) return 1;
+    s->corner_mma = enable != 0;
     invalidate_tables(s->cells);
     invalidate_tables(s->obs);
     graph_reset(s);

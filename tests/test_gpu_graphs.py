@@ -39,6 +39,7 @@ def _solve(arrays, graphs, max_eval=64):
 @pytest.mark.parametrize('case', sorted(CASES))
 def test_graph_solve_equals_direct(case):
     arrays = small_state(**CASES[case])
+    _solve(arrays, True)  # the process's first solve of these shapes also times the launch shapes (autotuner)
     xg, sg, eg, lg = _solve(arrays, True)
     xd, sd, ed, ld = _solve(arrays, False)
     assert eg is None and ed is None

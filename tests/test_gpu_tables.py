@@ -18,7 +18,7 @@ CASES = {
 }
 
 
-def _run(arrays, tables, pairs=True):
+def _run(arrays, tables, pairs=True, corner=False):
     from sosfuse2_gb300.solver import Solver
     from sosfuse2_gb300.state import PackedState
 
@@ -26,6 +26,7 @@ def _run(arrays, tables, pairs=True):
     k = solver.kernel
     k.set_node_tables(tables)
     k._check(k.lib.sosb_set_pairs(k.h, int(pairs)))
+    k._check(k.lib.sosb_set_corner_mma(k.h, int(corner)))
     x = k.field(np.zeros(solver.state.shape, np.float32))
     out = []
     for _ in range(2):                      # the first pass over each bundle builds the table, the second reads it
@@ -65,3 +66,18 @@ def test_pairs_match_node_synthesis(case):
     for i, (a, b) in enumerate(zip(on, off)):
         ok, rel = _close(a, b)
         assert ok, (case, i, rel)
+
+
+@pytest.mark.parametrize('case', ['w8_l24', 'w33_l16', 'w6_l48'])
+def test_corner_mma_matches_pairs(case):
+    """Corner SH values from the tensor-core products (bf16x3: BF16 high and low parts, three products, FP32
+    accumulation) against the FP32 pair contractions, over two applications and their observer passes (the corner
+    values are redone for every new plane): within 1e-4 of each output's largest value (the split keeps about 16 bits
+    of every operand)."""
+    c = dict(CASES, w6_l48=dict(W=6, L=48, top=120.0, nh=4))[case]
+    arrays = small_state(**c)
+    mma = _run(arrays, True, pairs=True, corner=True)
+    fp32 = _run(arrays, True, pairs=True, corner=False)
+    for i, (a, b) in enumerate(zip(mma, fp32)):
+        err = np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
+        assert err <= 1e-4, (case, i, err)
