@@ -128,16 +128,22 @@ def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
     return arrays
 
 
-def solve(s, geometry, scope, max_eval=64, tolerance=1e-3, device=None):
-    """Solver.solve of a reference-assembled state on the GPU: (field [cells, slots, W] f4, stats)."""
+def solve_packed(arrays, max_eval=64, tolerance=1e-3, device=None):
+    """Solver.solve of a packed state on the GPU: (field [cells, slots, W] f4 host array, stats with the reference's
+    keys: seconds, evaluations, tolerance, converged, history); raises the reference's E_* errors."""
     from .solver import Solver
     from .state import PackedState
 
-    solver = Solver(PackedState(pack_state(s, geometry, scope, tolerance, max_eval)), device=device)
+    solver = Solver(PackedState(arrays), device=device)
     try:
         return solver.solve(max_eval, tolerance)
     finally:
         solver.kernel.close()
+
+
+def solve(s, geometry, scope, max_eval=64, tolerance=1e-3, device=None):
+    """Solver.solve of a reference-assembled state on the GPU: (field [cells, slots, W] f4, stats)."""
+    return solve_packed(pack_state(s, geometry, scope, tolerance, max_eval), max_eval, tolerance, device)
 
 
 def view_rays(s, hs, el, az):
