@@ -55,7 +55,8 @@ struct BundleDev {
     int ncell = 0;
     int64_t nray = 0, nseg = 0;
     DevBuf cell_off, ray_cell, p, frame, dir, dir_lo, dloc, pcp, seg_off, seg, lower, end_j, end_col, hits;
-    std::vector<int64_t> host_cell_off;
+    std::vector<int64_t> host_cell_off, host_seg_off;
+    int64_t host_seg_off_at(int64_t ray) const { return host_seg_off.empty() ? 0 : host_seg_off[(size_t)ray]; }
     // node table (NodeTable): valid once a launch over the whole bundle wrote it; too_big: over the memory budget
     DevBuf t_frame, t_misc, t_att;
     bool t_valid = false, t_too_big = false;
@@ -71,7 +72,7 @@ struct BundleDev {
     int64_t a_version = -1;  // plane version pair_A was contracted from
     // (node, corner) entries bucketed by corner cell for the tensor-core corner values (CornerEntries), valid with
     // the node table unless over the memory budget; cv the corner values of plane version c_version
-    DevBuf c_ray, c_cp, c_slot, c_tile, cv;
+    DevBuf c_ray, c_cp, c_slot, c_tile, cv, node_ray, vbuf;
     bool c_valid = false;
     int c_ntiles = 0;
     int64_t c_version = -1;
@@ -2009,6 +2010,81 @@ __global__ void __launch_bounds__(PAIR_WAVE_WARPS * 32)
 }
 
 
+// The warm pass from the corner values split in two launches for many wavelengths, so that the per-node work has the
+// whole grid's memory parallelism: corner_node_kernel (one thread per node and wavelength, consecutive threads the
+// wavelengths of one node) forms each node's value with its four corner values (warm_value) times its attenuation
+// into vbuf[node][w]; ray_sum_kernel (one thread per ray and wavelength) adds the nodes of the ray in node order
+// (Kahan), then the ground boundary term, as transport_corner_wave_kernel does in one launch.
+__global__ void __launch_bounds__(256)
+    corner_node_kernel(Optics o, Rays b, NodeTable tab, const int* __restrict__ node_ray, const float* __restrict__ cv,
+                       const float* __restrict__ field, long long node0, long long nodes, float4* __restrict__ vbuf) {
+    const int W = o.W;
+    const long long n = nodes * W;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long node = node0 + i / W;
+        const int w = (int)(i - (i / W) * W);
+        RayConst rc;
+        ray_constants(b, node_ray[node], rc);
+        Node nd;
+        table_node(o, rc, tab, node, nd);
+        float aero[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) aero[c] = cv[(size_t)(node * 4 + c) * W + w];
+        float val[4];
+        warm_value(o, rc, nd, field, w, aero, val);
+        const float att = tab.att[node * W + w];
+        vbuf[node * W + w] = make_float4(val[0] * att, val[1] * att, val[2] * att, val[3] * att);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    ray_sum_kernel(Optics o, Rays b, LaneInputs in, const float4* __restrict__ vbuf, int ray0, int nray,
+                   float4* __restrict__ rad) {
+    const int W = o.W;
+    const long long n = (long long)nray * W;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int ray = ray0 + (int)(i / W);
+        const int w = (int)(i - (i / W) * W);
+        const int s0 = b.seg_off[ray];
+        const long long nd0 = (long long)s0 * in.nq;
+        const int nn = (b.seg_off[ray + 1] - s0) * in.nq;
+        float total[4] = {0, 0, 0, 0}, comp[4] = {0, 0, 0, 0};
+        const float4* v = vbuf + nd0 * W + w;
+        int j = 0;
+        for (; j + 4 <= nn; j += 4) {  // four nodes' loads in flight, added in node order
+            float4 q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) q[u] = v[(size_t)(j + u) * W];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                kahan(total[0], comp[0], q[u].x);
+                kahan(total[1], comp[1], q[u].y);
+                kahan(total[2], comp[2], q[u].z);
+                kahan(total[3], comp[3], q[u].w);
+            }
+        }
+        for (; j < nn; ++j) {
+            const float4 q = v[(size_t)j * W];
+            kahan(total[0], comp[0], q.x);
+            kahan(total[1], comp[1], q.y);
+            kahan(total[2], comp[2], q.z);
+            kahan(total[3], comp[3], q.w);
+        }
+        RayConst rc;
+        ray_constants(b, ray, rc);
+        boundary_term(o, b, rc, in.boundary, ray, w, total);
+        rad[(size_t)ray * W + w] = make_float4(total[0], total[1], total[2], total[3]);
+    }
+}
+
+// Node -> ray index of a bundle (one thread per ray).
+__global__ void node_ray_kernel(Rays b, int nq, int* __restrict__ node_ray) {
+    for (int ray = blockIdx.x * blockDim.x + threadIdx.x; ray < b.nray; ray += gridDim.x * blockDim.x) {
+        const long long a = (long long)b.seg_off[ray] * nq, e = (long long)b.seg_off[ray + 1] * nq;
+        for (long long node = a; node < e; ++node) node_ray[node] = ray;
+    }
+}
+
 __global__ void add_kernel(const float* a, const float* b, float* out, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = a[i] + b[i];
@@ -2500,7 +2576,9 @@ static int build_corners(sosb_state* s, BundleDev& b, int nq) {
     const int64_t entries = (int64_t)b.nseg * nq * 4;
     const int kp = (s->K + 3) & ~3;
     if (entries >= (int64_t)1 << 31) return 0;
-    const size_t need = (size_t)entries * (12 + (size_t)d.W * 4) + (size_t)nray * kp * sizeof(float);
+    const size_t nodes = (size_t)b.nseg * nq;
+    const size_t need = (size_t)entries * (12 + (size_t)d.W * 4) + (size_t)nray * kp * sizeof(float) +
+                        nodes * (4 + (size_t)d.W * 16);
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     if (need > free_b / 2) return 0;
@@ -2538,6 +2616,10 @@ static int build_corners(sosb_state* s, BundleDev& b, int nq) {
                                                                                  P<float>(b.y_tab));
     TRY(launch_check(s));
     TRY(dalloc(s, b.cv, (size_t)entries * d.W * sizeof(float)));
+    TRY(dalloc(s, b.node_ray, std::max<size_t>(nodes, 1) * sizeof(int)));
+    TRY(dalloc(s, b.vbuf, std::max<size_t>(nodes, 1) * d.W * sizeof(float4)));
+    node_ray_kernel<<<blocks, 128, 0, s->stream>>>(rays_of(b), nq, P<int>(b.node_ray));
+    TRY(launch_check(s));
     CK(cudaStreamSynchronize(s->stream));  // the host tile list outlives no call
     b.c_ntiles = (int)tiles.size();
     b.c_version = -1;
@@ -2826,9 +2908,15 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
                 }
                 b.c_version = s->plane_version;
             }
-            const unsigned pb = (unsigned)((warps + PAIR_WAVE_WARPS - 1) / PAIR_WAVE_WARPS);
-            transport_corner_wave_kernel<<<pb, PAIR_WAVE_WARPS * 32, 0, s->stream>>>(
-                optics_of(s), rays_of(b), in, table, P<float>(b.cv), (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
+            const long long nd0 = (long long)b.host_seg_off_at(ray0) * in.nq;
+            const long long nd1 = (long long)b.host_seg_off_at(ray0 + nray) * in.nq;
+            corner_node_kernel<<<grid_for((nd1 - nd0) * d.W, 256), 256, 0, s->stream>>>(
+                optics_of(s), rays_of(b), table, P<int>(b.node_ray), P<float>(b.cv), field, nd0, nd1 - nd0,
+                P<float4>(b.vbuf));
+            TRY(launch_check(s));
+            ray_sum_kernel<<<grid_for(nray * d.W, 256), 256, 0, s->stream>>>(optics_of(s), rays_of(b), in,
+                                                                          P<float4>(b.vbuf), (int)ray0, (int)nray,
+                                                                          P<float4>(s->rad));
         } else if (read && b.p_valid) {
             const PairTable pt{P<int>(b.p_off), P<int>(b.p_cell), P<int>(b.p_ray), P<int4>(b.p_node),
                                P<float>(b.y_tab), P<float>(b.pair_A)};
@@ -3177,7 +3265,7 @@ int sosb_destroy(sosb_handle s) {
                         &bd->seg_off, &bd->seg, &bd->lower, &bd->end_j, &bd->end_col, &bd->hits,
                         &bd->t_frame, &bd->t_misc, &bd->t_att, &bd->b_hi, &bd->b_lo, &bd->p_off, &bd->p_cell,
                         &bd->p_ray, &bd->p_node, &bd->y_tab, &bd->pair_A, &bd->c_ray, &bd->c_cp, &bd->c_slot,
-                        &bd->c_tile, &bd->cv};
+                        &bd->c_tile, &bd->cv, &bd->node_ray, &bd->vbuf};
         for (DevBuf* b : bb) dfree(s, *b);
     }
     collect_timing(s);
@@ -3783,6 +3871,7 @@ int sosb_set_bundle(sosb_handle s, int which, const sosb_bundle* b) {
     bd.nray = pk.nray;
     bd.nseg = pk.nseg;
     bd.host_cell_off.assign(b->cell_off, b->cell_off + b->ncell + 1);
+    bd.host_seg_off.assign(pk.seg_off.begin(), pk.seg_off.end());
     TRY(dput_vec(s, bd.cell_off, pk.cell_off));
     TRY(dput_vec(s, bd.ray_cell, pk.ray_cell));
     TRY(dput_vec(s, bd.p, pk.p));
