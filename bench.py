@@ -9,7 +9,8 @@ deg at 1 or 2 deg, AOD U(0.02, 0.5), g U(0.5, 0.8), ozone U(250, 400) DU, albedo
 .config3), built before the timed region. A step solves one slice of S states (steps cycle through the 64 states)
 from their uploaded handles: the learned start (one network per SH order, trained before the timed region on solves
 the method generates) and the batched driver (every state's first evaluation, then its solve graph, on its own
-stream). `value` counts the converged solves whose observer radiance lies within 1e-3 of the plain solve's.
+stream). `value` counts the converged solves whose observer radiance lies within 1e-3 of the state's fixed point (its plain
+solve to tolerance 1e-5).
 `forms` times the same slices with the plain start batched and solved one at a time (`sequential`, the plain
 GB300 SOS), and adds the plain config-0 solve (its dominant kernel's roofline), the projection precision forms,
 make_table and the ground preparation. `e2e` is the headline form through the public API with host buffers: handles
@@ -504,6 +505,34 @@ def make_kernels(items, device):
     return ks, sts
 
 
+def truth_boxes(slices, items, device, tol=1e-5, max_eval=160):
+    """Observer radiance of each state's fixed point to a 100x tighter tolerance (plain start, batched), the
+    reference the timed solves' observer radiance is held to (<= 1e-3): {state: boxes or None when it does not
+    converge}."""
+    import torch
+
+    from sosfuse2_gb300 import _abi
+    from sosfuse2_gb300.solver import Solver
+
+    out = {}
+    for idx in slices:
+        ks, sts = make_kernels([items[i] for i in idx], device)
+        n = len(ks)
+        lib = ks[0].lib
+        outs = [k.field() for k in ks]
+        stats = (_abi.Stats * n)()
+        status = (ctypes.c_int32 * n)()
+        lib.sosb_solve_batch((ctypes.c_void_p * n)(*[k.h.value for k in ks]), n, max_eval, tol, None,
+                             (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs]), 1, stats, status, 0)
+        for j, (i, k, st) in enumerate(zip(idx, ks, sts)):
+            out[i] = None if status[j] else Solver(st, kernel=k).boxes(outs[j])
+        for k in ks:
+            k.close()
+        del ks, sts, outs
+        torch.cuda.empty_cache()
+    return out
+
+
 def solve_slice(form, ks, sts, nets):
     """One step of `form` on handles `ks`: 'learned' (learned start, batched), 'batched' (plain start, batched) or
     'sequential' (plain start, one solve in flight). Returns [(field, stats) or RuntimeError], kernel launches."""
@@ -682,8 +711,10 @@ def run_gb300(a, rank, world):
     if not a.no_forms:
         t_seq, r_seq, l_seq = time_form('sequential', one_pass, items, nets, device, dist)
         t_bat, r_bat, l_bat = time_form('batched', one_pass, items, nets, device, dist)
-    # accepted solves: converged, and (when the plain solve of the state is known) observer radiance within 1e-3
-    # of the plain solve's
+    # accepted solves: converged, with observer radiance within 1e-3 of the state's fixed point (a plain solve to a
+    # 100x tighter tolerance; a state whose tight solve does not converge keeps its converged solves unchecked)
+    truth = truth_boxes(one_pass, items, device)
+
     def accepted(per_state, slices):
         ok, errs = [], []
         for sl in slices:
@@ -693,8 +724,8 @@ def run_gb300(a, rank, world):
                 if ev is None:
                     continue
                 err = None
-                if not a.no_forms and r_seq.get(i, (None, None))[1] is not None:
-                    err = rel_boxes(bx, r_seq[i][1])
+                if truth.get(i) is not None:
+                    err = rel_boxes(bx, truth[i])
                     errs.append(err)
                 n += err is None or err <= 1e-3
             ok.append(n)
@@ -705,7 +736,7 @@ def run_gb300(a, rank, world):
     value = whole_job(value, world, dist)
     launches = plain0['launches'] + l_learn
     if not a.no_forms:
-        ok_seq, _ = accepted(r_seq, one_pass)
+        ok_seq, err_seq = accepted(r_seq, one_pass)
         ok_bat, err_bat = accepted(r_bat, one_pass)
         launches += l_seq + l_bat
         evals = lambda r, sl: [r[i][0] for s in sl for i in s if r[i][0] is not None]  # noqa: E731
@@ -713,12 +744,13 @@ def run_gb300(a, rank, world):
             learned=dict(value=value / world, seconds_per_step=statistics.mean(t_learn), states_per_step=S,
                          steps=len(timed), converged_accepted=sum(ok_learn),
                          evaluations_mean=statistics.mean(evals(r_learn, timed) or [0]),
-                         max_rel_observer_vs_plain=max(err_learn) if err_learn else None),
+                         max_rel_observer_vs_fixed_point=max(err_learn) if err_learn else None),
             batched=dict(value=sum(ok_bat) / sum(t_bat), seconds_per_step=statistics.mean(t_bat), steps=len(one_pass),
                          converged_accepted=sum(ok_bat), evaluations_mean=statistics.mean(evals(r_bat, one_pass) or [0]),
-                         max_rel_observer_vs_plain=max(err_bat) if err_bat else None),
+                         max_rel_observer_vs_fixed_point=max(err_bat) if err_bat else None),
             sequential=dict(value=sum(ok_seq) / sum(t_seq), seconds_per_step=statistics.mean(t_seq),
-                            steps=len(one_pass), converged=sum(ok_seq),
+                            steps=len(one_pass), converged_accepted=sum(ok_seq),
+                            max_rel_observer_vs_fixed_point=max(err_seq) if err_seq else None,
                             evaluations_mean=statistics.mean(evals(r_seq, one_pass) or [0]),
                             per_state={i: r_seq[i][0] for s in one_pass for i in s}),
             training=dict(seconds=train_s, per_order={L: r for L, r in train.items()}),
@@ -768,7 +800,8 @@ def run_gb300(a, rank, world):
         ms_per_step=statistics.mean(t_learn) * 1e3, higher_is_better=True, scaling='weak', vs_baseline=None,
         dtype='f32', data='synthetic (seeded states on the reference geometry rules, sosfuse2_gb300.synth.config3)',
         config=dict(workload=WORKLOAD, states_per_step=S, form='learned start + batched solves (solve graphs)',
-                    value_counts='converged solves whose observer radiance is within 1e-3 of the plain solve',
+                    value_counts='converged solves whose observer radiance is within 1e-3 of the fixed point (a plain '
+                                 'solve of the state to tolerance 1e-5)',
                     l2='each step reads more than the 129 MB L2 (states of 0.1-2 GB of source fields)',
                     parallelism=f'replicas x{world}'),
         forms=forms or None, roofline=plain0['roofline'], kernel_times=plain0['kernel_times'], cpu_baseline=cb,
