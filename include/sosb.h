@@ -271,6 +271,12 @@ int sosb_prepare_ground(sosb_handle h, double albedo, const double *ext, const d
  * (e.g. the single-scattering source apply(0)); stats->start_fallback records it. */
 int sosb_solve_warm(sosb_handle h, int max_eval, double tolerance, const float *x0_dev, double fallback_ss,
                     const float *fallback_dev, float *x_out, int x_out_is_device, sosb_stats *stats);
+/* No reference counterpart. Warm history (default off): sosb_solve_warm (and its batch form) first enters the pair
+ * (x = 0, g = fallback_dev) into the Anderson history - the single-scattering source apply(0) is the plain
+ * iteration's first evaluation - with its observer boxes, residual feature and Gram entries (no evaluation counted),
+ * so that the supplied start is the second iterate and the first warm evaluation already mixes with that direction
+ * instead of restarting the history. */
+int sosb_set_warm_history(sosb_handle h, int enable);
 /* Batched form of Solver.solve (no single counterpart in the reference, whose pipeline runs one state per process,
  * src/sosfuse2/jobs/pipeline_execution.py): n independent states, each its own handle and stream, driven by one host
  * thread with up to `threads` solves in flight (0: all); each state's first evaluation and then its solve graph

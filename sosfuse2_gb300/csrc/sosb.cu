@@ -132,6 +132,7 @@ struct sosb_state {
     bool pairs = true;     // corner SH by ray-cell pair contractions (sosb_set_pairs)
     bool corner_mma = true;  // corner SH values on the tensor cores, more than four wavelengths (sosb_set_corner_mma)
     bool corner_used = false;  // a corner GEMM ran since the last check of its bounded waits
+    bool warm_history = false;  // sosb_solve_warm seeds the Anderson history with (0, fallback) (sosb_set_warm_history)
     int proj_mode = 0;   // projection form (sosb_set_projection): PROJ_FP32, PROJ_BF16X3, PROJ_TF32, PROJ_BF16
     int64_t launches = 0;
     // per-evaluation history of the last solve on this handle: [evaluation][W] observer and source relative changes
@@ -4055,7 +4056,7 @@ __global__ void __launch_bounds__(CONTROL_THREADS)
 control_kernel(LoopDev* __restrict__ L, EvalCtrl* __restrict__ ctrl, const unsigned* __restrict__ met,
                const double* __restrict__ old_b, const double* __restrict__ new_b, const double* __restrict__ dots,
                float* __restrict__ obs, double* __restrict__ gram, double* __restrict__ hist,
-               unsigned* __restrict__ normmax, cudaGraphConditionalHandle cond, int set_cond) {
+               unsigned* __restrict__ normmax, cudaGraphConditionalHandle cond, int set_cond, int seed) {
     __shared__ unsigned long long s_rr[64];  // bits of non-negative doubles order as unsigned integers
     __shared__ double s_ss[64];
     __shared__ int s_done[64];
@@ -4072,13 +4073,26 @@ control_kernel(LoopDev* __restrict__ L, EvalCtrl* __restrict__ ctrl, const unsig
     }
     if (t == 0) s_bad = 0ull;
     __syncthreads();
-    for (int q = t; q < nobs * W; q += CONTROL_THREADS) {
+    if (seed) {
+        // history seed (no evaluation counted): the pair in ring slot ctrl->slot enters the Anderson history with
+        // its observer features and Gram entries; the next evaluation takes the next slot without a mix
+        if (t == 0) {
+            s_anderson = 1;
+            s_restart = 0;
+            s_stop = 0;
+            s_m = ctrl->m;
+            s_slot = ctrl->slot;
+            for (int j = 0; j < 4; ++j) s_order[j] = ctrl->order[j];
+        }
+        __syncthreads();
+    }
+    for (int q = t; q < nobs * W && !seed; q += CONTROL_THREADS) {
         const double nv = new_b[q], ov = old_b[q];  // [feature][W], q = i * W + w
         const double r = fabs(nv - ov) / fmax(fabs(nv), 1e-30);
         atomicMax(&s_rr[q % W], (unsigned long long)__double_as_longlong(r));
     }
     __syncthreads();
-    if (t < W) {
+    if (t < W && !seed) {
         const double r = __longlong_as_double((long long)s_rr[t]);
         const float mg = __uint_as_float(met[W + t]), df = __uint_as_float(met[2 * W + t]);
         const double ss = (double)(df / fmaxf(mg, 1e-30f));
@@ -4096,7 +4110,7 @@ control_kernel(LoopDev* __restrict__ L, EvalCtrl* __restrict__ ctrl, const unsig
         if (met[t]) atomicAdd(&s_bad, (unsigned long long)met[t]);
     }
     __syncthreads();
-    if (t == 0) {
+    if (t == 0 && !seed) {
         L->it = it;
         L->bad = s_bad;
         int stop = 0, anderson = 0, restart = 0;
@@ -4184,10 +4198,10 @@ control_kernel(LoopDev* __restrict__ L, EvalCtrl* __restrict__ ctrl, const unsig
             const int m = s_m;
             L->norder = m;
             for (int j = 0; j < 4; ++j) L->order[j] = s_order[j];
-            ctrl->mix = 1;
+            ctrl->mix = seed ? 0 : 1;  // after a seed the next evaluation starts from the supplied x
             ctrl->mix_m = m;
             for (int j = 0; j < 4; ++j) ctrl->mix_order[j] = j < m ? s_order[j] : s_order[m - 1];
-            if (it >= L->max_eval) {
+            if (!seed && it >= L->max_eval) {
                 stop = 1;
                 L->status = LOOP_BUDGET;
             }
@@ -4217,7 +4231,7 @@ control_kernel(LoopDev* __restrict__ L, EvalCtrl* __restrict__ ctrl, const unsig
             ctrl->done = mask;
         }
         L->go = stop ? 0 : 1;
-        if (set_cond) cudaGraphSetConditional(cond, stop ? 0u : 1u);
+        if (set_cond && !seed) cudaGraphSetConditional(cond, stop ? 0u : 1u);
     }
     if (t < 64) normmax[t] = 0u;  // the next evaluation's norm pass collects its maxima from zero
 }
@@ -4279,23 +4293,16 @@ static int loop_alloc(sosb_state* s, int max_eval) {
 // with the composition metrics; boxes(g); g into the ring; residual feature and FP64 Gram column; the control kernel
 // (source_iteration.py:309-635, one evaluation of the loop). set_cond: the control kernel sets the enclosing WHILE
 // node's condition.
-static int eval_body(sosb_state* s, bool set_cond) {
-    const sosb_dims& d = s->d;
-    const int W = d.W;
+// The end of an evaluation after g: g into ring slot ctrl->slot, the residual feature (g - x) / norm and its FP64
+// Gram column against the ring's slots, then the control kernel (seed: a history seed, see control_kernel).
+static int residual_tail(sosb_state* s, bool set_cond, bool seed) {
+    const int W = s->d.W;
     const long long n = (long long)s->ns * s->src * W;
     float* x = P<float>(s->fx);
     float* g = P<float>(s->fg);
     EvalCtrl* ctrl = P<EvalCtrl>(s->ctrl_dev);
     const Ring4 rg{{P<float>(s->ring_g[0]), P<float>(s->ring_g[1]), P<float>(s->ring_g[2]), P<float>(s->ring_g[3])}};
     const Ring4 rf{{P<float>(s->ring_f[0]), P<float>(s->ring_f[1]), P<float>(s->ring_f[2]), P<float>(s->ring_f[3])}};
-    {
-        Timer t(s, K_ANDERSON);
-        mix_kernel<<<grid_for(n, wave_threads(W)), wave_threads(W), 0, s->stream>>>(g, rg, ctrl, W, n, x);
-    }
-    TRY(launch_check(s));
-    TRY(boxes_dev(s, x, P<double>(s->box_old)));
-    TRY(apply_impl(s, x, g, 0ull, &ctrl->done));
-    TRY(boxes_dev(s, g, P<double>(s->box_new)));
     {
         Timer t(s, K_ANDERSON);
         ring_copy_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(g, rg, ctrl, n);
@@ -4324,11 +4331,35 @@ static int eval_body(sosb_state* s, bool set_cond) {
     {
         Timer t(s, K_ANDERSON);
         control_kernel<<<1, CONTROL_THREADS, 0, s->stream>>>(P<LoopDev>(s->loop_dev), ctrl, P<unsigned>(s->metrics),
-                                                P<double>(s->box_old), P<double>(s->box_new), P<double>(s->dots),
-                                                P<float>(s->obs_feat), P<double>(s->gram), P<double>(s->hist_dev),
-                                                P<unsigned>(s->normmax), s->cond, set_cond ? 1 : 0);
+                                                             P<double>(s->box_old), P<double>(s->box_new),
+                                                             P<double>(s->dots), P<float>(s->obs_feat),
+                                                             P<double>(s->gram), P<double>(s->hist_dev),
+                                                             P<unsigned>(s->normmax), s->cond, set_cond ? 1 : 0,
+                                                             seed ? 1 : 0);
     }
     return launch_check(s);
+}
+
+// One evaluation on the device, the same launches every time (the control block and the loop state carry what
+// changes): x = Anderson mix of the previous ring (or the fallback start after a restart); boxes(x); g = apply(x)
+// with the composition metrics; boxes(g); then residual_tail (source_iteration.py:309-635, one evaluation of the
+// loop). set_cond: the control kernel sets the enclosing WHILE node's condition.
+static int eval_body(sosb_state* s, bool set_cond) {
+    const int W = s->d.W;
+    const long long n = (long long)s->ns * s->src * W;
+    float* x = P<float>(s->fx);
+    float* g = P<float>(s->fg);
+    EvalCtrl* ctrl = P<EvalCtrl>(s->ctrl_dev);
+    const Ring4 rg{{P<float>(s->ring_g[0]), P<float>(s->ring_g[1]), P<float>(s->ring_g[2]), P<float>(s->ring_g[3])}};
+    {
+        Timer t(s, K_ANDERSON);
+        mix_kernel<<<grid_for(n, wave_threads(W)), wave_threads(W), 0, s->stream>>>(g, rg, ctrl, W, n, x);
+    }
+    TRY(launch_check(s));
+    TRY(boxes_dev(s, x, P<double>(s->box_old)));
+    TRY(apply_impl(s, x, g, 0ull, &ctrl->done));
+    TRY(boxes_dev(s, g, P<double>(s->box_new)));
+    return residual_tail(s, set_cond, false);
 }
 
 // The solve graph of the handle: a gate kernel (the condition from the loop state) and a WHILE node whose body is
@@ -4417,11 +4448,6 @@ struct SolveRun {
         TRY(loop_alloc(s, max_eval));
         const int W = s->d.W;
         const size_t bytes = (size_t)s->ns * s->src * W * sizeof(float);
-        if (x0)
-            CK(cudaMemcpyAsync(s->fx.p, x0, bytes, x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                               s->stream));
-        else
-            CK(cudaMemsetAsync(s->fx.p, 0, bytes, s->stream));
         // evaluation 1: ring slot 0, no mix (x is the start)
         EvalCtrl& c = *s->ctrl_host;
         std::memset(&c, 0, sizeof c);
@@ -4442,6 +4468,20 @@ struct SolveRun {
         CK(cudaMemcpyAsync(s->loop_dev.p, &L, sizeof L, cudaMemcpyHostToDevice, s->stream));
         CK(cudaMemsetAsync(s->gram.p, 0, (size_t)W * 16 * sizeof(double), s->stream));
         CK(cudaMemsetAsync(s->normmax.p, 0, 64 * sizeof(unsigned), s->stream));
+        if (fallback_dev && s->warm_history) {
+            // the pair (x = 0, g = the fallback start, the single-scattering source) enters the Anderson history
+            // first, so that the supplied start is the second iterate of the plain iteration, not a restart
+            CK(cudaMemsetAsync(s->fx.p, 0, bytes, s->stream));
+            CK(cudaMemcpyAsync(s->fg.p, fallback_dev, bytes, cudaMemcpyDeviceToDevice, s->stream));
+            TRY(boxes_dev(s, P<float>(s->fx), P<double>(s->box_old)));
+            TRY(boxes_dev(s, P<float>(s->fg), P<double>(s->box_new)));
+            TRY(residual_tail(s, false, true));
+        }
+        if (x0)
+            CK(cudaMemcpyAsync(s->fx.p, x0, bytes, x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               s->stream));
+        else
+            CK(cudaMemsetAsync(s->fx.p, 0, bytes, s->stream));
         return 0;
     }
 
@@ -4649,6 +4689,12 @@ int sosb_set_pairs(sosb_handle s, int enable) {
     invalidate_tables(s->cells);
     invalidate_tables(s->obs);
     graph_reset(s);
+    return 0;
+}
+
+int sosb_set_warm_history(sosb_handle s, int enable) {
+    if (!s) return 1;
+    s->warm_history = enable != 0;
     return 0;
 }
 

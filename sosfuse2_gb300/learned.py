@@ -450,9 +450,10 @@ def train_config3(orders=(16, 24, 32, 48), n_train=64, epochs=30, seed=10000, de
     return nets, reports
 
 
-def solve_batch(ws, kernels, states, max_eval=64, tolerance=1e-3, threads=0):
+def solve_batch(ws, kernels, states, max_eval=64, tolerance=1e-3, threads=0, history=True):
     """Learned-start batched solves: apply(0) on every handle concurrently, one network pass over the rows of the
-    states of each SH order, then the warm-started solves concurrently. `ws`: one WarmStart, or {L: WarmStart}.
+    states of each SH order, then the warm-started solves concurrently (history: the pair (0, g1) of the apply(0)
+    first enters each solve's Anderson history, sosb_set_warm_history). `ws`: one WarmStart, or {L: WarmStart}.
     Returns [(field, stats) or RuntimeError] per state."""
     import torch
 
@@ -492,6 +493,8 @@ def solve_batch(ws, kernels, states, max_eval=64, tolerance=1e-3, threads=0):
     stats = (_abi.Stats * n)()
     torch.cuda.synchronize()
     fallback_ss = min(w.fallback_ss for w in nets.values()) if nets is not None else ws.fallback_ss
+    for k in kernels:  # (0, g1) enters the Anderson history: the network's start is the second iterate
+        k._check(lib.sosb_set_warm_history(k.h, int(history)))
     lib.sosb_solve_warm_batch(handles, n, int(max_eval), float(tolerance),
                               (ctypes.c_void_p * n)(*[x.data_ptr() for x in starts]), float(fallback_ss),
                               (ctypes.c_void_p * n)(*[g.data_ptr() for g in g1]),
