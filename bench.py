@@ -9,8 +9,8 @@ deg at 1 or 2 deg, AOD U(0.02, 0.5), g U(0.5, 0.8), ozone U(250, 400) DU, albedo
 .config3), built before the timed region. A step solves one slice of S states (steps cycle through the 64 states)
 from their uploaded handles: the learned start (one network per SH order, trained before the timed region on solves
 the method generates) and the batched driver (every state's first evaluation, then its solve graph, on its own
-stream). `value` counts the converged solves whose observer radiance lies within 1e-3 of the state's fixed point (its plain
-solve to tolerance 1e-5).
+stream). Every form stops at tolerance 1e-4 (TOL); `value` counts the converged solves whose observer radiance lies within
+1e-3 of the state's fixed point (its plain solve to tolerance 1e-6).
 `forms` times the same slices with the plain start batched and solved one at a time (`sequential`, the plain
 GB300 SOS), and adds the plain config-0 solve (its dominant kernel's roofline), the projection precision forms,
 make_table and the ground preparation. `e2e` is the headline form through the public API with host buffers: handles
@@ -41,12 +41,19 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = 'converged solves/s on 1 GB300 at ≤1e-3 rel err: learned-start+batched vs plain'
+# Every form stops at TOL (the reference's stopping rule, max(observer change, source change) <= TOL from the second
+# evaluation); its error is then checked against the state's fixed point (a solve to TRUTH_TOL). At the reference's
+# default 1e-3 the rule bounds the last change, not the error: plain solves stopped there land up to 4.3e-3 from the
+# fixed point on these states, so the timed forms stop at 1e-4.
+TOL = 1e-4
+TRUTH_TOL = 1e-6
+MAX_EVAL = 96
 L2_BYTES = 129 << 20
 N_STATES = 64
 WORKLOAD = ('batched configuration: 64 seeded states (seeds 1000-1063) of uneven sizes: heights U{121..481} on 0-120 '
             'km x 10 solar-zenith nodes, 8-64 wavelengths 400-700 nm, L in {16,24,32,48}, observer elevations +6..-18 '
             'deg at 1 or 2 deg, AOD 0.02-0.5, g 0.5-0.8, ozone 250-400 DU, albedo 0.05-0.8, NO2 and O4 on, '
-            'stratospheric layer, nmu 1, nphi 2, path_n 4, tolerance 1e-3, at most 64 evaluations')
+            'stratospheric layer, nmu 1, nphi 2, path_n 4; stop tolerance 1e-4, at most 96 evaluations')
 
 
 # ------------------------------------------------------------------------------------------------ helpers
@@ -505,10 +512,9 @@ def make_kernels(items, device):
     return ks, sts
 
 
-def truth_boxes(slices, items, device, tol=1e-5, max_eval=160):
-    """Observer radiance of each state's fixed point to a 100x tighter tolerance (plain start, batched), the
-    reference the timed solves' observer radiance is held to (<= 1e-3): {state: boxes or None when it does not
-    converge}."""
+def truth_boxes(slices, items, device, tol=TRUTH_TOL, max_eval=256):
+    """Observer radiance of each state's fixed point (plain start, batched, stopped at TRUTH_TOL), the reference the
+    timed solves' observer radiance is held to (<= 1e-3): {state: boxes or None when it does not converge}."""
     import torch
 
     from sosfuse2_gb300 import _abi
@@ -541,7 +547,7 @@ def solve_slice(form, ks, sts, nets):
     n = len(ks)
     if form == 'learned':
         g0 = sum(w.mlp.gemm_launches for w in nets.values())
-        r = learned.solve_batch(nets, ks, sts)
+        r = learned.solve_batch(nets, ks, sts, max_eval=MAX_EVAL, tolerance=TOL)
         nl = sum(x[1]['kernel_launches'] for x in r if not isinstance(x, Exception))
         return r, nl + sum(w.mlp.gemm_launches for w in nets.values()) - g0
     lib = ks[0].lib
@@ -549,7 +555,7 @@ def solve_slice(form, ks, sts, nets):
     outs = [k.field() for k in ks]
     stats = (_abi.Stats * n)()
     status = (ctypes.c_int32 * n)()
-    lib.sosb_solve_batch(handles, n, 64, 1e-3, None, (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs]), 1,
+    lib.sosb_solve_batch(handles, n, MAX_EVAL, TOL, None, (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs]), 1,
                          stats, status, 1 if form == 'sequential' else 0)
     res = []
     for i, k in enumerate(ks):
@@ -692,7 +698,7 @@ def run_gb300(a, rank, world):
     build_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     orders = sorted({synth.config3_spec(i)['L'] for i in range(n_states)})
-    nets, train = learned.train_config3(orders, n_train=a.train_solves, epochs=a.epochs, device=device)
+    nets, train = learned.train_config3(orders, n_train=a.train_solves, epochs=a.epochs, device=device, tolerance=TOL)
     train_s = time.perf_counter() - t0
     S = max(1, min(a.batch, n_states))
     nslices = (n_states + S - 1) // S
@@ -711,8 +717,8 @@ def run_gb300(a, rank, world):
     if not a.no_forms:
         t_seq, r_seq, l_seq = time_form('sequential', one_pass, items, nets, device, dist)
         t_bat, r_bat, l_bat = time_form('batched', one_pass, items, nets, device, dist)
-    # accepted solves: converged, with observer radiance within 1e-3 of the state's fixed point (a plain solve to a
-    # 100x tighter tolerance; a state whose tight solve does not converge keeps its converged solves unchecked)
+    # accepted solves: converged, with observer radiance within 1e-3 of the state's fixed point (a plain solve to
+    # TRUTH_TOL; a state whose tight solve does not converge keeps its converged solves unchecked)
     truth = truth_boxes(one_pass, items, device)
 
     def accepted(per_state, slices):
@@ -800,8 +806,9 @@ def run_gb300(a, rank, world):
         ms_per_step=statistics.mean(t_learn) * 1e3, higher_is_better=True, scaling='weak', vs_baseline=None,
         dtype='f32', data='synthetic (seeded states on the reference geometry rules, sosfuse2_gb300.synth.config3)',
         config=dict(workload=WORKLOAD, states_per_step=S, form='learned start + batched solves (solve graphs)',
+                    tolerance=TOL, max_eval=MAX_EVAL,
                     value_counts='converged solves whose observer radiance is within 1e-3 of the fixed point (a plain '
-                                 'solve of the state to tolerance 1e-5)',
+                                 'solve of the state to tolerance 1e-6)',
                     l2='each step reads more than the 129 MB L2 (states of 0.1-2 GB of source fields)',
                     parallelism=f'replicas x{world}'),
         forms=forms or None, roofline=plain0['roofline'], kernel_times=plain0['kernel_times'], cpu_baseline=cb,

@@ -2823,7 +2823,8 @@ static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs&
             o, r, in, table, fl, 0, (int)b.nray, wchunks, P<float4>(s->rad));
     TRY(launch_check(s));
     b.t_valid = true;
-    if (!b.p_valid) TRY(build_pairs(s, b, in.nq));
+    if (!b.c_valid) TRY(build_corners(s, b, in.nq));
+    if (!b.c_valid && !b.p_valid) TRY(build_pairs(s, b, in.nq));
     done = true;
     return 0;
 }

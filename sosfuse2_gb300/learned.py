@@ -365,13 +365,13 @@ def generate(family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3, log=No
     return torch.cat(ws_rows), torch.cat(ws_targets), np.asarray(evals), np.asarray(ss_single)
 
 
-def train_warm_start(family, n_train=512, epochs=30, seed=10000, device='cuda:0', log=None):
+def train_warm_start(family, n_train=512, epochs=30, seed=10000, device='cuda:0', log=None, tolerance=1e-3, slow=24):
     """Generate n_train solves (seeds seed, seed+1, ...) and train the network; returns (WarmStart, report)."""
     from .state import PackedState
     from .synth import family_state
 
     t0 = time.perf_counter()
-    X, Y, evals, ss1 = generate(family, range(seed, seed + n_train), device)
+    X, Y, evals, ss1 = generate(family, range(seed, seed + n_train), device, tolerance=tolerance, slow=slow)
     t1 = time.perf_counter()
     st = PackedState(family_state(family, seed))
     ws = WarmStart(st.source_size, st.W, device=device)
@@ -436,17 +436,19 @@ def evaluate(ws, family, seeds, device='cuda:0', max_eval=64, tolerance=1e-3):
     return out
 
 
-def train_config3(orders=(16, 24, 32, 48), n_train=64, epochs=30, seed=10000, device='cuda:0', log=None):
+def train_config3(orders=(16, 24, 32, 48), n_train=64, epochs=30, seed=10000, device='cuda:0', log=None,
+                  tolerance=1e-4):
     """One network per SH order of the batched configuration (the network's input and output are the source slots,
-    10 + 2K of them), each trained on n_train solves of synth.config3_training_family(L) (seeds seed, seed + 1, ...);
-    returns ({L: WarmStart}, {L: report})."""
+    10 + 2K of them), each trained on n_train solves of synth.config3_training_family(L) (seeds seed, seed + 1, ...)
+    to `tolerance` (solves over 40 evaluations are skipped); returns ({L: WarmStart}, {L: report})."""
     from .synth import config3_table, config3_training_family
 
     table = config3_table()
     nets, reports = {}, {}
     for L in orders:
         fam = config3_training_family(L, table)
-        nets[L], reports[L] = train_warm_start(fam, n_train=n_train, epochs=epochs, seed=seed, device=device, log=log)
+        nets[L], reports[L] = train_warm_start(fam, n_train=n_train, epochs=epochs, seed=seed, device=device, log=log,
+                                               tolerance=tolerance, slow=40)
     return nets, reports
 
 
