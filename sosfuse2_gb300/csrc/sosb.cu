@@ -1088,6 +1088,93 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Ground sums of the bucketed pairs, many wavelengths, with the wavelength-independent work done once: one warp per
+// pair; per batch of 32 ground directions, lane j computes direction j's cosine pair, its Henyey-Greenstein pair
+// phase and its stratospheric table positions into shared memory, then lane = wavelength (two chunks above 32) adds
+// the batch's directions in order with its own ground values and table phase. The sums are those of
+// ground_pairs_wave_kernel, term for term and in the same order.
+constexpr int GPW_WARPS = 8;
+
+__global__ void __launch_bounds__(GPW_WARPS * 32)
+    ground_pairs_warp_kernel(Optics o, const float4* __restrict__ misc, const float4* __restrict__ dir,
+                             const int* __restrict__ entries, const int* __restrict__ total, float2* g) {
+    __shared__ float s_hg[GPW_WARPS][32], s_fu[GPW_WARPS][32], s_fd[GPW_WARPS][32];
+    __shared__ int s_iu[GPW_WARPS][32], s_id[GPW_WARPS][32];
+    const int W = o.W;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int items = *total;
+    const HgPair hk = hg_pair_constants(o.g);
+    const int w0 = lane, w1 = lane + 32;
+    for (int item = blockIdx.x * GPW_WARPS + wid; item < items; item += gridDim.x * GPW_WARPS) {
+        const int code = entries[item];
+        const long long node = code >> 1;
+        const int pr = code & 1;
+        const float4 ms = misc[node];
+        const float4 dv = dir[node];
+        const float ah = ms.x, ac = ms.y;
+        const float wa = pr ? ah * (1.0f - ac) : (1.0f - ah) * (1.0f - ac);
+        const float wb = pr ? ah * ac : (1.0f - ah) * ac;
+        const int ca = pair_cell(o, ms, pr), cb = ca + 1;
+        const bool merged = o.gsame != nullptr && o.gsame[ca] != 0;
+        float ground0 = 0.0f, sground0 = 0.0f, ground1 = 0.0f, sground1 = 0.0f;
+        for (int side = 0; side < (merged ? 1 : 2); ++side) {
+            const int cell = side ? cb : ca;
+            const float wc = side ? wb : wa;
+            const int g0 = o.goff[cell], g1 = o.goff[cell + 1];
+            const int shift = merged ? o.goff[cb] - g0 : 0;
+            for (int base = g0; base < g1; base += 32) {
+                const int gi = base + lane;
+                __syncwarp();
+                if (gi < g1) {
+                    const float4 gd = o.gdir4[gi];
+                    const float m0 = dv.x * gd.z + dv.y * gd.x;
+                    const float m1 = dv.z * gd.y;
+                    const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
+                    s_hg[wid][lane] = hg_pair(hk, up, dn);
+                    if (o.strato) {
+                        int iu, id;
+                        float fu, fd;
+                        strato_lut_pos_clamped(up, iu, fu);
+                        strato_lut_pos_clamped(dn, id, fd);
+                        s_iu[wid][lane] = iu;
+                        s_id[wid][lane] = id;
+                        s_fu[wid][lane] = fu;
+                        s_fd[wid][lane] = fd;
+                    }
+                }
+                __syncwarp();
+                const int cnt = min(32, g1 - base);
+                for (int j = 0; j < cnt; ++j) {
+                    const int gj = base + j;
+                    const float hg = s_hg[wid][j];
+                    if (w0 < W) {
+                        float gv = wc * o.gval[(size_t)gj * W + w0];
+                        if (merged) gv += wb * o.gval[(size_t)(gj + shift) * W + w0];
+                        ground0 += hg * gv;
+                        if (o.strato) {
+                            const float sph = (strato_lut_at(o, s_iu[wid][j], s_fu[wid][j], w0) +
+                                               strato_lut_at(o, s_id[wid][j], s_fd[wid][j], w0)) * 0.5f;
+                            sground0 += sph * gv;
+                        }
+                    }
+                    if (w1 < W) {
+                        float gv = wc * o.gval[(size_t)gj * W + w1];
+                        if (merged) gv += wb * o.gval[(size_t)(gj + shift) * W + w1];
+                        ground1 += hg * gv;
+                        if (o.strato) {
+                            const float sph = (strato_lut_at(o, s_iu[wid][j], s_fu[wid][j], w1) +
+                                               strato_lut_at(o, s_id[wid][j], s_fd[wid][j], w1)) * 0.5f;
+                            sground1 += sph * gv;
+                        }
+                    }
+                }
+            }
+        }
+        if (w0 < W) g[((size_t)node * 2 + pr) * W + w0] = make_float2(ground0, sground0);
+        if (w1 < W) g[((size_t)node * 2 + pr) * W + w1] = make_float2(ground1, sground1);
+    }
+}
+
 // Per-ray sum of the staged first light, many wavelengths: one warp per (ray, chunk of 32 wavelengths), lane =
 // wavelength walking the ray's nodes in order (the Kahan order of transport_wave_kernel).
 __global__ void __launch_bounds__(128)
@@ -2805,9 +2892,9 @@ static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs&
                                                                            P<int>(s->fl_entries),
                                                                            P<int>(s->fl_off) + s->ns, fl.g);
     } else {
-        const int gb = (int)std::min<long long>((2 * nodes * W + 255) / 256, 152LL * 64);
-        ground_pairs_wave_kernel<<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir, P<int>(s->fl_entries),
-                                                                         P<int>(s->fl_off) + s->ns, fl.g);
+        const int gb = (int)std::min<long long>((2 * nodes + GPW_WARPS - 1) / GPW_WARPS, 152LL * 32);
+        ground_pairs_warp_kernel<<<std::max(gb, 1), GPW_WARPS * 32, 0, s->stream>>>(
+            o, table.misc, fl.dir, P<int>(s->fl_entries), P<int>(s->fl_off) + s->ns, fl.g);
     }
     TRY(launch_check(s));
     if (W == 1)
