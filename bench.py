@@ -44,16 +44,16 @@ METRIC = 'converged solves/s on 1 GB300 at ≤1e-3 rel err: learned-start+batche
 # Every form stops at TOL (the reference's stopping rule, max(observer change, source change) <= TOL from the second
 # evaluation); its error is then checked against the state's fixed point (a solve to TRUTH_TOL). At the reference's
 # default 1e-3 the rule bounds the last change, not the error: plain solves stopped there land up to 4.3e-3 from the
-# fixed point on these states, so the timed forms stop at 1e-4.
+# fixed point on these states, so the timed forms stop at 1e-4, within the reference's budget of 64 evaluations.
 TOL = 1e-4
 TRUTH_TOL = 1e-6
-MAX_EVAL = 96
+MAX_EVAL = 64
 L2_BYTES = 129 << 20
 N_STATES = 64
 WORKLOAD = ('batched configuration: 64 seeded states (seeds 1000-1063) of uneven sizes: heights U{121..481} on 0-120 '
             'km x 10 solar-zenith nodes, 8-64 wavelengths 400-700 nm, L in {16,24,32,48}, observer elevations +6..-18 '
             'deg at 1 or 2 deg, AOD 0.02-0.5, g 0.5-0.8, ozone 250-400 DU, albedo 0.05-0.8, NO2 and O4 on, '
-            'stratospheric layer, nmu 1, nphi 2, path_n 4; stop tolerance 1e-4, at most 96 evaluations')
+            'stratospheric layer, nmu 1, nphi 2, path_n 4; stop tolerance 1e-4, at most 64 evaluations')
 
 
 # ------------------------------------------------------------------------------------------------ helpers
@@ -224,11 +224,21 @@ def bracket(dist):
 
 
 # ------------------------------------------------------------------------------------------------ CPU baseline
-# Evaluations of each batched state's plain GB300 solve and whether it converged (measured by this benchmark's GPU arm,
-# forms.sequential.per_state): the CPU port's per-evaluation cost is scaled to whole solves with them, because the
-# CPU port's own solve of one of these states takes hours; on the config-0-grid states the parity tests show the CUDA
-# solve and the oracle reach the same evaluation count.
-CONFIG3_EVALUATIONS = {}
+# Evaluations of each batched state's plain GB300 solve (tolerance 1e-4, at most 64 evaluations) and whether it
+# converged, measured by this benchmark's GPU arm (forms.sequential.per_state): the CPU port's per-evaluation cost is
+# scaled to whole solves with them, because the CPU port's own solve of one of these states takes hours; on the
+# config-0-grid states the parity tests show the CUDA solve and the oracle reach the same evaluation count.
+CONFIG3_EVALUATIONS = {0: (64, False), 1: (13, True), 2: (15, True), 3: (11, True), 4: (10, True), 5: (16, True),
+    6: (20, True), 7: (12, True), 8: (64, False), 9: (10, True), 10: (12, True), 11: (14, True), 12: (64, False),
+    13: (64, False), 14: (64, False), 15: (22, True), 16: (13, True), 17: (64, False), 18: (64, False),
+    19: (13, True), 20: (19, True), 21: (11, True), 22: (10, True), 23: (64, False), 24: (13, True), 25: (64, False),
+    26: (12, True), 27: (9, True), 28: (64, False), 29: (64, False), 30: (10, True), 31: (64, False),
+    32: (64, False), 33: (64, False), 34: (64, False), 35: (15, True), 36: (64, False), 37: (13, True),
+    38: (11, True), 39: (64, False), 40: (64, False), 41: (64, False), 42: (15, True), 43: (11, True),
+    44: (11, True), 45: (55, True), 46: (14, True), 47: (23, True), 48: (14, True), 49: (18, True), 50: (14, True),
+    51: (64, False), 52: (17, True), 53: (64, False), 54: (11, True), 55: (64, False), 56: (64, False),
+    57: (17, True), 58: (10, True), 59: (15, True), 60: (64, False), 61: (64, False), 62: (14, True),
+    63: (64, False)}
 
 _TABLE = None
 
@@ -298,7 +308,7 @@ def cpu_state(pool, procs, i):
     wall = time.perf_counter() - t
     surf = [r for r in res if r['surface']]
     rows = len(np.arange(6.0, -18.0 - 1e-9, -float(sp['solar_step'])))
-    E, conv = CONFIG3_EVALUATIONS.get(i, (10, True))
+    E, conv = CONFIG3_EVALUATIONS[i]
     first = sum(r['first'] for r in res) / len(res) * ns
     warm = sum(r['warm'] for r in res) / len(res) * ns
     ground = (sum(r['ground'] for r in surf) / max(len(surf), 1)) * nc
@@ -664,6 +674,67 @@ def plain_config0(a, device, dist):
                 l2='flushed between timed solves (512 MiB write outside the events)')
 
 
+def tensor_peak():
+    try:
+        m = json.loads((ROOT / 'MEASURED_PEAKS.json').read_text())
+        return float(m['bf16_tflops']), 'measured'
+    except (OSError, ValueError, KeyError):
+        return 1900.0, 'fallback'
+
+
+def corner_roofline(item, device):
+    """Roofline of the dominant kernel of the batched workload, the tensor-core corner values (corner_tc_kernel), on
+    one of its states: CUDA events around every launch of one solve (timing mode). Algorithmic work per evaluation:
+    2 K W flops per (node, corner) entry, the cell bundle once (its ground and warm pass share the plane) and the
+    observer bundle twice (boxes of x and of g); executed tensor work adds the bf16x3 split (x3) and the padding of K
+    to 64 and W to 16."""
+    from sosfuse2_gb300 import _abi
+
+    ks, sts = make_kernels([item], device)
+    k, st = ks[0], sts[0]
+    from sosfuse2_gb300.solver import Solver
+
+    solver = Solver(st, kernel=k)
+    k._check(k.lib.sosb_set_stream(k.h, None))
+    try:
+        solver.solve(MAX_EVAL, TOL, device_out=True)  # tables, entries, tuning
+    except RuntimeError:
+        pass
+    ncls = len(_abi.KERNEL_CLASSES)
+    ms = (_abi.c_dbl * ncls)()
+    cnt = (_abi.c_i64 * ncls)()
+    k.lib.sosb_set_timing(k.h, 1)
+    try:
+        _, stt = solver.solve(MAX_EVAL, TOL, device_out=True)
+        E = stt['evaluations']
+    except RuntimeError:
+        E = len(solver.history())
+    k.lib.sosb_get_timing(k.h, ms, cnt, ncls)
+    k.lib.sosb_set_timing(k.h, 0)
+    k.close()
+    m = st.meta
+    K, W = st.K, st.W
+    cell_entries = 4 * len(st['cell_seg_a']) * int(m['nq'])
+    obs_entries = 4 * len(st['query_seg_a']) * int(m['nq_query'])
+    i = _abi.KERNEL_CLASSES.index('corner')
+    flops = 2.0 * K * W * (cell_entries + 2 * obs_entries) * E
+    executed = flops * 3 * (math.ceil(K / 64) * 64 / K) * (math.ceil(W / 16) * 16 / W)
+    sec = ms[i] / 1e3
+    peak, kind = tensor_peak()
+    achieved = flops / sec / 1e12
+    classes = _abi.KERNEL_CLASSES
+    share = {classes[j]: ms[j] / max(sum(ms[c] for c in range(ncls) if classes[c] != 'corner'), 1e-30)
+             for j in range(ncls)}
+    return dict(kernel='corner_tc_kernel', bound='tensor', achieved=achieved, peak=peak, unit='TFLOP/s',
+                frac=achieved / peak, peak_source=kind, traffic=profiled_traffic('corner_tc_kernel'),
+                flops_per_evaluation=flops / max(E, 1), executed_tflops=executed / sec / 1e12,
+                mean_launch_ms=ms[i] / max(cnt[i], 1), launches=int(cnt[i]), evaluations=E,
+                state=m['config3'], class_ms={classes[j]: ms[j] for j in range(ncls)},
+                note='the corner class is also inside transport_table (nested timer); shares exclude it',
+                shares=share,
+                measured_on='CUDA events around each launch of one more solve of the state (timing mode)')
+
+
 def run_gb300(a, rank, world):
     import torch
 
@@ -765,7 +836,7 @@ def run_gb300(a, rank, world):
         forms['learned_batched_vs_plain_sequential'] = (forms['learned']['value']
                                                          / max(forms['sequential']['value'], 1e-30))
         forms['batched_vs_sequential'] = forms['batched']['value'] / max(forms['sequential']['value'], 1e-30)
-        forms['plain_config0'] = {k: v for k, v in plain0.items() if k not in ('roofline', 'kernel_times')}
+        forms['plain_config0'] = plain0
         forms['precision'] = _precision_form(device)
         fam = synth.config0_family()
         forms['table'] = _table_form(fam, device)
@@ -801,6 +872,7 @@ def run_gb300(a, rank, world):
             port.close()
         cb = dict(value=v, unit='solves/s', cores=port.procs, kind='port', nproc=os.cpu_count(),
                   sample=cpu_description(port.procs, recs))
+    roof = corner_roofline(items[3 if n_states > 3 else 0], device)
     out = dict(
         metric=METRIC, value=value, unit='solves/s', n_gpus=world, steps=a.steps, warmup=a.warmup,
         ms_per_step=statistics.mean(t_learn) * 1e3, higher_is_better=True, scaling='weak', vs_baseline=None,
@@ -811,7 +883,7 @@ def run_gb300(a, rank, world):
                                  'solve of the state to tolerance 1e-6)',
                     l2='each step reads more than the 129 MB L2 (states of 0.1-2 GB of source fields)',
                     parallelism=f'replicas x{world}'),
-        forms=forms or None, roofline=plain0['roofline'], kernel_times=plain0['kernel_times'], cpu_baseline=cb,
+        forms=forms or None, roofline=roof, kernel_times=roof.pop('class_ms'), cpu_baseline=cb,
         e2e=e2e, gpu_launches=int(launches), clocks=clk)
     print(json.dumps(out, default=float), flush=True)
 
