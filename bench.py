@@ -74,6 +74,10 @@ def args_():
     p.add_argument('--ground-only', action='store_true',
                    help='only the ground-preparation form (host against device, a config-0 family state)')
     p.add_argument('--plain-only', action='store_true', help='only the plain config-0 single-state solve')
+    p.add_argument('--profile-state', default=None, metavar='NH,W,L',
+                   help='the capture target of the committed ncu summaries: a state of the batched construction with '
+                        'NH heights, W wavelengths and order L (amounts of state 3), solved twice with every kernel '
+                        'launched directly (no solve graph)')
     return p.parse_args()
 
 
@@ -674,6 +678,37 @@ def plain_config0(a, device, dist):
                 l2='flushed between timed solves (512 MiB write outside the events)')
 
 
+def profile_state(nh, W, L, device):
+    """Two plain solves (tolerance 1e-3) of one state of the batched construction (heights nh on 0-120 km, W
+    wavelengths on 400-700 nm, order L, observer rows every 2 deg, the amounts of batched state 3), every kernel
+    launched directly: the capture target of the ncu summaries."""
+    import torch
+
+    from sosfuse2_gb300 import synth
+    from sosfuse2_gb300.solver import Solver
+    from sosfuse2_gb300.state import PackedState
+
+    sp = synth.config3_spec(3)
+    wl = np.linspace(400.0, 700.0, W)
+    shape = synth.Atmosphere(wl, seed=sp['seed'], top=synth.CONFIG3_TOP, no2_column=5e15, o4=True)
+    fam = synth.Family(np.linspace(0.0, synth.CONFIG3_TOP, nh), synth.REDUCED_CHI_DEG, L, 1, 2, 4, shape,
+                       name='profile', monitor_elevations=np.arange(6.0, -18.0 - 1e-9, -2.0))
+    a = {k: sp[k] for k in ('aod', 'g', 'ozone_du', 'albedo')}
+    atm = synth.Atmosphere(wl, seed=sp['seed'], top=synth.CONFIG3_TOP, no2_column=5e15, o4=True, **a)
+    solver = Solver(PackedState(fam.state(atm, sp['seed'])), device=device)
+    solver.kernel.set_graphs(False)
+    out = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        _, st = solver.solve(64, 1e-3, device_out=True)
+        torch.cuda.synchronize()
+        out.append(dict(seconds=time.perf_counter() - t, evaluations=st['evaluations']))
+    meta = solver.state.meta
+    solver.kernel.close()
+    return dict(nh=nh, W=W, L=L, rays=meta['rays'], segments=meta['segments'], solves=out)
+
+
 def tensor_peak():
     try:
         m = json.loads((ROOT / 'MEASURED_PEAKS.json').read_text())
@@ -751,6 +786,10 @@ def run_gb300(a, rank, world):
     if a.ground_only:
         if rank == 0:
             print(json.dumps(dict(ground=_ground_form(synth.config0_family(), device))), flush=True)
+        return
+    if a.profile_state:
+        nh, W, L = (int(v) for v in a.profile_state.split(','))
+        print(json.dumps(dict(profile_state=profile_state(nh, W, L, device))), flush=True)
         return
     dist = None
     if world > 1:
