@@ -349,18 +349,20 @@ class CpuPort:
         self.pool.join()
 
     def run(self, states):
-        """Samples of `states` (one step each): (whole-machine converged solves/s, per-step records)."""
+        """Samples of `states` (one step each): (whole-machine converged solves/s of the workload, per-step records):
+        the processes over the mean core-seconds of a solve of the sampled states, times the workload's fraction of
+        converged solves (CONFIG3_EVALUATIONS)."""
         recs = [cpu_state(self.pool, self.procs, i) for i in states]
-        core = sum(r['core_seconds'] for r in recs)
-        conv = sum(r['converged'] for r in recs)
-        return self.procs * conv / core, recs
+        mean_core = sum(r['core_seconds'] for r in recs) / len(recs)
+        frac = sum(c for _, c in CONFIG3_EVALUATIONS.values()) / len(CONFIG3_EVALUATIONS)
+        return self.procs * frac / mean_core, recs
 
 
 def cpu_description(procs, recs):
     return (f'{len(recs)} batched states (indices {[r["state"] for r in recs]}), each {recs[0]["cells"]} sample '
             f'cells (one per process on {procs} processes) and one observer row timed in core-seconds (first light '
             f'and one evaluation), scaled by cells and rows to one solve with the state\'s plain GB300 evaluation '
-            f'count; solves/s = processes x converged solves / core-seconds')
+            f'count; solves/s = processes / mean core-seconds per solve x the workload\'s converged fraction')
 
 
 def run_reference(a, rank):
