@@ -1883,57 +1883,58 @@ __global__ void corner_entries_kernel(Optics o, Rays b, NodeTable tab, int nq, i
     }
 }
 
-constexpr int CORNER_THREADS = 128;
+constexpr int CORNER_ROWS = 128;     // entries per tile (the MMA's M)
+constexpr int CORNER_THREADS = 256;  // two threads per row build the A tile (four 16-byte pieces each)
 
 static size_t corner_tc_smem(int np, int L) {
-    // A high/low tiles (2 x 16 KB), B high/low tiles (2 x np rows of 128 bytes), cos(m phi) rows, m of each k of a
-    // chunk, the barrier and the tensor-memory slot; 1 KB of alignment slack
-    return 1024 + 2 * 16384 + 2 * (size_t)np * 128 + (size_t)CORNER_THREADS * (L + 1) * 4 + 64 * 4 + 64;
+    // two stages of A high/low tiles (2 x 16 KB) and B high/low tiles (2 x np rows of 128 bytes), cos(m phi) rows,
+    // two barriers and the tensor-memory slot; 1 KB of alignment slack
+    return 1024 + 2 * (2 * 16384 + 2 * (size_t)np * 128) + (size_t)CORNER_ROWS * (L + 1) * 4 + 64;
 }
 
-// One CTA per tile of 128 entries of one corner cell: per chunk of 64 SH coefficients, thread r builds row r of the
-// A tile (B[entry][k] split into BF16 high and low parts) and the block builds the B tile (the cell's plane, np
-// wavelength rows, split likewise) in the 128-byte swizzle; one thread issues the 12 MMAs (four K steps of 16, three
-// products each) and waits for them (bounded) before the tiles are rebuilt. The epilogue stores each row's np FP32
-// values at its slot.
+// One CTA per tile of 128 entries of one corner cell, chunks of 64 SH coefficients in two shared-memory stages: the
+// block builds chunk ch (row r of the A tile, B[entry][k] split into BF16 high and low parts, by threads r and
+// r + 128, four pieces of 8 coefficients each; the B tile, the cell's plane for np wavelength rows, split likewise;
+// both in the 128-byte swizzle) while the MMAs of chunk ch - 1 run; one thread issues the 12 MMAs of a chunk (four K
+// steps of 16, three products each) and commits them to the stage's barrier, which the block waits on (bounded)
+// before it rebuilds that stage two chunks later. The epilogue (warps 0-3, one TMEM lane quarter each) stores each
+// row's np FP32 values at its slot.
 __global__ void __launch_bounds__(CORNER_THREADS)
     corner_tc_kernel(Optics o, CornerEntries ce, const float* __restrict__ y_tab, int kp,
                      const float* __restrict__ plane, int np, uint32_t idesc, uint32_t tmem_cols,
                      float* __restrict__ out) {
     extern __shared__ uint8_t corner_raw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(corner_raw) + 1023) & ~(uintptr_t)1023);
-    uint8_t* a_hi = sm;
-    uint8_t* a_lo = sm + 16384;
-    uint8_t* b_hi = sm + 32768;
-    uint8_t* b_lo = b_hi + np * 128;
-    float* cm = reinterpret_cast<float*>(b_lo + np * 128);  // [CORNER_THREADS][L + 1]
+    const size_t stage_bytes = 2 * 16384 + 2 * (size_t)np * 128;  // stage st: A high, A low, B high, B low
+    float* cm = reinterpret_cast<float*>(sm + 2 * stage_bytes);  // [CORNER_ROWS][L + 1]
     const int L1 = o.L + 1;
-    int* mk = reinterpret_cast<int*>(cm + CORNER_THREADS * L1);  // m of the chunk's 64 coefficients
-    uint64_t* bar = reinterpret_cast<uint64_t*>(mk + 64);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(cm + CORNER_ROWS * L1);  // [2], 8-byte aligned: L1 * 512 bytes
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
     const int4 tile = ce.tile[blockIdx.x];
     const int cell = tile.x, e0 = tile.y, ne = tile.z;
     const int t = threadIdx.x, warp = t >> 5;
+    const int row = t & (CORNER_ROWS - 1), half = t >> 7;
     const int W = o.W, K = o.K;
     if (t == 0) {
-        tcx::mbar_init(bar, 1);
+        tcx::mbar_init(&bar[0], 1);
+        tcx::mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tcx::tmem_alloc(tslot, tmem_cols);
-    // the entry's ray and its cos(m phi) series (the Chebyshev recurrence of azimuth_sum)
-    const bool valid = t < ne;
-    const int ray = valid ? ce.ray[e0 + t] : 0;
-    {
-        const float cpv = valid ? clampf(ce.cp[e0 + t], -1.0f, 1.0f) : 0.0f;
-        float* row = cm + t * L1;
+    // the row's entry: its ray and its cos(m phi) series (the Chebyshev recurrence of azimuth_sum)
+    const bool valid = row < ne;
+    const int ray = valid ? ce.ray[e0 + row] : 0;
+    if (half == 0) {
+        const float cpv = valid ? clampf(ce.cp[e0 + row], -1.0f, 1.0f) : 0.0f;
+        float* crow = cm + row * L1;
         float c0 = 1.0f, c1 = cpv;
-        row[0] = valid ? 1.0f : 0.0f;
-        if (L1 > 1) row[1] = valid ? c1 : 0.0f;
+        crow[0] = valid ? 1.0f : 0.0f;
+        if (L1 > 1) crow[1] = valid ? c1 : 0.0f;
         for (int m = 2; m < L1; ++m) {
             const float c2 = (2.0f * cpv) * c1 - c0;
             c0 = c1;
             c1 = c2;
-            row[m] = valid ? c2 : 0.0f;
+            crow[m] = valid ? c2 : 0.0f;
         }
     }
     tcx::fence_before();
@@ -1941,44 +1942,59 @@ __global__ void __launch_bounds__(CORNER_THREADS)
     tcx::fence_after();
     const uint32_t tmem = *tslot;
     const float* yr = y_tab + (size_t)ray * kp;
+    const float* crow = cm + row * L1;
     const float* pc = plane + (size_t)cell * K * W;
     const int nchunk = (K + 63) / 64;
     bool ok = true;
     for (int ch = 0; ch < nchunk && ok; ++ch) {
-        const int k0 = ch * 64;
-        if (t < 64) {
-            // m of coefficient k0 + t: k = l (l + 1) / 2 + m
-            const int k = k0 + t;
-            int l = (int)((sqrtf(8.0f * k + 1.0f) - 1.0f) * 0.5f);
-            while ((l + 1) * (l + 2) / 2 <= k) ++l;
-            while (l * (l + 1) / 2 > k) --l;
-            mk[t] = k - l * (l + 1) / 2;
+        const int st = ch & 1;
+        uint8_t* const ahi = sm + st * stage_bytes;
+        uint8_t* const alo = ahi + 16384;
+        uint8_t* const bhi = ahi + 32768;
+        uint8_t* const blo = bhi + np * 128;
+        if (ch >= 2) {
+            // the MMAs of chunk ch - 2 read this stage: wait for them before it is rebuilt
+            ok = tcx::mbar_wait(&bar[st], ((ch - 2) >> 1) & 1, 2u, &g_proj_error);
+            ok = __syncthreads_and(ok);
+            if (!ok) break;
+            tcx::fence_after();
         }
-        __syncthreads();
-        // A row t: B[entry][k] for k in the chunk, 8 pieces of 8 coefficients
-        const float* crow = cm + t * L1;
-#pragma unroll 2
-        for (int p = 0; p < 8; ++p) {
-            float v[8];
-            const int kb = k0 + p * 8;
-            if (valid && kb + 8 <= K) {
-                const float4 y0 = *reinterpret_cast<const float4*>(yr + kb);
-                const float4 y1 = *reinterpret_cast<const float4*>(yr + kb + 4);
-                v[0] = y0.x; v[1] = y0.y; v[2] = y0.z; v[3] = y0.w;
-                v[4] = y1.x; v[5] = y1.y; v[6] = y1.z; v[7] = y1.w;
-            } else {
+        const int k0 = ch * 64;
+        // A row `row`, pieces 4 half .. 4 half + 3; m of each coefficient by stepping (l, m) from the first one
+        {
+            const int kb0 = k0 + half * 32;
+            int l = (int)((sqrtf(8.0f * kb0 + 1.0f) - 1.0f) * 0.5f);
+            while ((l + 1) * (l + 2) / 2 <= kb0) ++l;
+            while (l * (l + 1) / 2 > kb0) --l;
+            int m = kb0 - l * (l + 1) / 2;
 #pragma unroll
-                for (int e = 0; e < 8; ++e) v[e] = (valid && kb + e < K) ? yr[kb + e] : 0.0f;
-            }
-            __align__(16) __nv_bfloat16 h[8], lo[8];
+            for (int pp = 0; pp < 4; ++pp) {
+                const int p = half * 4 + pp;
+                const int kb = k0 + p * 8;
+                float v[8];
+                if (valid && kb + 8 <= K) {
+                    const float4 y0 = *reinterpret_cast<const float4*>(yr + kb);
+                    const float4 y1 = *reinterpret_cast<const float4*>(yr + kb + 4);
+                    v[0] = y0.x; v[1] = y0.y; v[2] = y0.z; v[3] = y0.w;
+                    v[4] = y1.x; v[5] = y1.y; v[6] = y1.z; v[7] = y1.w;
+                } else {
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const float x = v[e] * crow[mk[p * 8 + e]];
-                h[e] = __float2bfloat16_rn(x);
-                lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
+                    for (int e = 0; e < 8; ++e) v[e] = (valid && kb + e < K) ? yr[kb + e] : 0.0f;
+                }
+                __align__(16) __nv_bfloat16 h[8], lo[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const float x = v[e] * crow[m < L1 ? m : 0];
+                    h[e] = __float2bfloat16_rn(x);
+                    lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
+                    if (++m > l) {
+                        ++l;
+                        m = 0;
+                    }
+                }
+                *reinterpret_cast<uint4*>(ahi + tcx::sw128_offset(row, p)) = *reinterpret_cast<const uint4*>(h);
+                *reinterpret_cast<uint4*>(alo + tcx::sw128_offset(row, p)) = *reinterpret_cast<const uint4*>(lo);
             }
-            *reinterpret_cast<uint4*>(a_hi + tcx::sw128_offset(t, p)) = *reinterpret_cast<const uint4*>(h);
-            *reinterpret_cast<uint4*>(a_lo + tcx::sw128_offset(t, p)) = *reinterpret_cast<const uint4*>(lo);
         }
         // B tile: np rows (wavelengths) x 8 pieces; consecutive threads take consecutive wavelengths (coalesced)
         for (int q = t; q < np * 8; q += CORNER_THREADS) {
@@ -1991,15 +2007,15 @@ __global__ void __launch_bounds__(CORNER_THREADS)
                 h[e] = __float2bfloat16_rn(x);
                 lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
             }
-            *reinterpret_cast<uint4*>(b_hi + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(h);
-            *reinterpret_cast<uint4*>(b_lo + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(lo);
+            *reinterpret_cast<uint4*>(bhi + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(h);
+            *reinterpret_cast<uint4*>(blo + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(lo);
         }
         tcx::fence_proxy_async();
         __syncthreads();
         if (t == 0) {
             tcx::fence_after();
-            const uint32_t ah = tcx::smem_u32(a_hi), al = tcx::smem_u32(a_lo);
-            const uint32_t bh = tcx::smem_u32(b_hi), bl = tcx::smem_u32(b_lo);
+            const uint32_t ah = tcx::smem_u32(ahi), al = tcx::smem_u32(alo);
+            const uint32_t bh = tcx::smem_u32(bhi), bl = tcx::smem_u32(blo);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
                 const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
@@ -2007,15 +2023,18 @@ __global__ void __launch_bounds__(CORNER_THREADS)
                 tcx::mma_f16(tmem, tcx::sw128_desc(ah + kk * 32), tcx::sw128_desc(bl + kk * 32), idesc, 1u);
                 tcx::mma_f16(tmem, tcx::sw128_desc(al + kk * 32), tcx::sw128_desc(bh + kk * 32), idesc, 1u);
             }
-            tcx::mma_commit(bar);
+            tcx::mma_commit(&bar[st]);
         }
-        ok = tcx::mbar_wait(bar, ch & 1, 2u, &g_proj_error);  // the tiles may be rebuilt once the MMAs are done
-        ok = __all_sync(FULL_MASK, ok);
+    }
+    if (ok) {
+        // the last commit covers every MMA issued before it
+        const int last = nchunk - 1;
+        ok = tcx::mbar_wait(&bar[last & 1], (last >> 1) & 1, 2u, &g_proj_error);
         ok = __syncthreads_and(ok);
         tcx::fence_after();
     }
-    if (ok) {
-        float* dst = valid ? out + (size_t)ce.slot[e0 + t] * W : nullptr;
+    if (ok && warp < 4) {
+        float* dst = valid ? out + (size_t)ce.slot[e0 + row] * W : nullptr;
         for (int c0 = 0; c0 < np; c0 += 16) {
             float v[16];
             tcx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);  // warp-wide
