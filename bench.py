@@ -873,6 +873,12 @@ def run_gb300(a, rank, world):
                             per_state={i: r_seq[i][0] for s in one_pass for i in s}),
             training=dict(seconds=train_s, per_order={L: r for L, r in train.items()}),
             build_seconds=build_s)
+        both = sorted(i for s_ in one_pass for i in s_
+                      if r_learn.get(i, (None, None))[0] is not None and r_seq.get(i, (None, None))[0] is not None)
+        forms['paired_evaluations'] = dict(
+            states=len(both), plain=statistics.mean([r_seq[i][0] for i in both]) if both else None,
+            learned=statistics.mean([r_learn[i][0] for i in both]) if both else None,
+            note='states both starts converge on; learned counts the apply(0) that feeds the network')
         forms['learned_vs_plain_batched'] = forms['learned']['value'] / max(forms['batched']['value'], 1e-30)
         forms['learned_batched_vs_plain_sequential'] = (forms['learned']['value']
                                                          / max(forms['sequential']['value'], 1e-30))
