@@ -1098,8 +1098,8 @@ constexpr int GPW_WARPS = 8;
 __global__ void __launch_bounds__(GPW_WARPS * 32)
     ground_pairs_warp_kernel(Optics o, const float4* __restrict__ misc, const float4* __restrict__ dir,
                              const int* __restrict__ entries, const int* __restrict__ total, float2* g) {
-    __shared__ float s_hg[GPW_WARPS][32], s_fu[GPW_WARPS][32], s_fd[GPW_WARPS][32];
-    __shared__ int s_iu[GPW_WARPS][32], s_id[GPW_WARPS][32];
+    // per staged direction: Henyey-Greenstein pair phase, the two table fractions and the two bins (16 bits each)
+    __shared__ float4 s_dir[GPW_WARPS][32];
     const int W = o.W;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int items = *total;
@@ -1130,30 +1130,27 @@ __global__ void __launch_bounds__(GPW_WARPS * 32)
                     const float m0 = dv.x * gd.z + dv.y * gd.x;
                     const float m1 = dv.z * gd.y;
                     const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
-                    s_hg[wid][lane] = hg_pair(hk, up, dn);
+                    int iu = 0, id = 0;
+                    float fu = 0.0f, fd = 0.0f;
                     if (o.strato) {
-                        int iu, id;
-                        float fu, fd;
                         strato_lut_pos_clamped(up, iu, fu);
                         strato_lut_pos_clamped(dn, id, fd);
-                        s_iu[wid][lane] = iu;
-                        s_id[wid][lane] = id;
-                        s_fu[wid][lane] = fu;
-                        s_fd[wid][lane] = fd;
                     }
+                    s_dir[wid][lane] = make_float4(hg_pair(hk, up, dn), fu, fd, __int_as_float(iu | (id << 16)));
                 }
                 __syncwarp();
                 const int cnt = min(32, g1 - base);
                 for (int j = 0; j < cnt; ++j) {
                     const int gj = base + j;
-                    const float hg = s_hg[wid][j];
+                    const float4 sd = s_dir[wid][j];
+                    const float hg = sd.x;
+                    const int bins = __float_as_int(sd.w), iu = bins & 0xffff, id = bins >> 16;
                     if (w0 < W) {
                         float gv = wc * o.gval[(size_t)gj * W + w0];
                         if (merged) gv += wb * o.gval[(size_t)(gj + shift) * W + w0];
                         ground0 += hg * gv;
                         if (o.strato) {
-                            const float sph = (strato_lut_at(o, s_iu[wid][j], s_fu[wid][j], w0) +
-                                               strato_lut_at(o, s_id[wid][j], s_fd[wid][j], w0)) * 0.5f;
+                            const float sph = (strato_lut_at(o, iu, sd.y, w0) + strato_lut_at(o, id, sd.z, w0)) * 0.5f;
                             sground0 += sph * gv;
                         }
                     }
@@ -1162,8 +1159,7 @@ __global__ void __launch_bounds__(GPW_WARPS * 32)
                         if (merged) gv += wb * o.gval[(size_t)(gj + shift) * W + w1];
                         ground1 += hg * gv;
                         if (o.strato) {
-                            const float sph = (strato_lut_at(o, s_iu[wid][j], s_fu[wid][j], w1) +
-                                               strato_lut_at(o, s_id[wid][j], s_fd[wid][j], w1)) * 0.5f;
+                            const float sph = (strato_lut_at(o, iu, sd.y, w1) + strato_lut_at(o, id, sd.z, w1)) * 0.5f;
                             sground1 += sph * gv;
                         }
                     }
@@ -1885,11 +1881,12 @@ __global__ void corner_entries_kernel(Optics o, Rays b, NodeTable tab, int nq, i
 
 constexpr int CORNER_ROWS = 128;     // entries per tile (the MMA's M)
 constexpr int CORNER_THREADS = 256;  // two threads per row build the A tile (four 16-byte pieces each)
+constexpr int CORNER_STAGES = 1;     // shared-memory stages of the A and B tiles
 
 static size_t corner_tc_smem(int np, int L) {
-    // two stages of A high/low tiles (2 x 16 KB) and B high/low tiles (2 x np rows of 128 bytes), cos(m phi) rows,
-    // two barriers and the tensor-memory slot; 1 KB of alignment slack
-    return 1024 + 2 * (2 * 16384 + 2 * (size_t)np * 128) + (size_t)CORNER_ROWS * (L + 1) * 4 + 64;
+    // CORNER_STAGES stages of A high/low tiles (2 x 16 KB) and B high/low tiles (2 x np rows of 128 bytes), cos(m phi)
+    // rows, the stages' barriers and the tensor-memory slot; 1 KB of alignment slack
+    return 1024 + CORNER_STAGES * (2 * 16384 + 2 * (size_t)np * 128) + (size_t)CORNER_ROWS * (L + 1) * 4 + 64;
 }
 
 // One CTA per tile of 128 entries of one corner cell, chunks of 64 SH coefficients in two shared-memory stages: the
@@ -1906,18 +1903,17 @@ __global__ void __launch_bounds__(CORNER_THREADS)
     extern __shared__ uint8_t corner_raw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(corner_raw) + 1023) & ~(uintptr_t)1023);
     const size_t stage_bytes = 2 * 16384 + 2 * (size_t)np * 128;  // stage st: A high, A low, B high, B low
-    float* cm = reinterpret_cast<float*>(sm + 2 * stage_bytes);  // [CORNER_ROWS][L + 1]
+    float* cm = reinterpret_cast<float*>(sm + CORNER_STAGES * stage_bytes);  // [CORNER_ROWS][L + 1]
     const int L1 = o.L + 1;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(cm + CORNER_ROWS * L1);  // [2], 8-byte aligned: L1 * 512 bytes
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(cm + CORNER_ROWS * L1);  // [stages], 8-byte aligned: L1 * 512 bytes
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + CORNER_STAGES);
     const int4 tile = ce.tile[blockIdx.x];
     const int cell = tile.x, e0 = tile.y, ne = tile.z;
     const int t = threadIdx.x, warp = t >> 5;
     const int row = t & (CORNER_ROWS - 1), half = t >> 7;
     const int W = o.W, K = o.K;
     if (t == 0) {
-        tcx::mbar_init(&bar[0], 1);
-        tcx::mbar_init(&bar[1], 1);
+        for (int q = 0; q < CORNER_STAGES; ++q) tcx::mbar_init(&bar[q], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tcx::tmem_alloc(tslot, tmem_cols);
@@ -1947,14 +1943,14 @@ __global__ void __launch_bounds__(CORNER_THREADS)
     const int nchunk = (K + 63) / 64;
     bool ok = true;
     for (int ch = 0; ch < nchunk && ok; ++ch) {
-        const int st = ch & 1;
+        const int st = ch % CORNER_STAGES;
         uint8_t* const ahi = sm + st * stage_bytes;
         uint8_t* const alo = ahi + 16384;
         uint8_t* const bhi = ahi + 32768;
         uint8_t* const blo = bhi + np * 128;
-        if (ch >= 2) {
-            // the MMAs of chunk ch - 2 read this stage: wait for them before it is rebuilt
-            ok = tcx::mbar_wait(&bar[st], ((ch - 2) >> 1) & 1, 2u, &g_proj_error);
+        if (ch >= CORNER_STAGES) {
+            // the MMAs of chunk ch - CORNER_STAGES read this stage: wait for them before it is rebuilt
+            ok = tcx::mbar_wait(&bar[st], ((ch - CORNER_STAGES) / CORNER_STAGES) & 1, 2u, &g_proj_error);
             ok = __syncthreads_and(ok);
             if (!ok) break;
             tcx::fence_after();
@@ -1981,16 +1977,21 @@ __global__ void __launch_bounds__(CORNER_THREADS)
 #pragma unroll
                     for (int e = 0; e < 8; ++e) v[e] = (valid && kb + e < K) ? yr[kb + e] : 0.0f;
                 }
-                __align__(16) __nv_bfloat16 h[8], lo[8];
+                float x[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    const float x = v[e] * crow[m < L1 ? m : 0];
-                    h[e] = __float2bfloat16_rn(x);
-                    lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
+                    x[e] = v[e] * crow[m < L1 ? m : 0];
                     if (++m > l) {
                         ++l;
                         m = 0;
                     }
+                }
+                __align__(16) __nv_bfloat162 h[4], lo[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {  // high parts two at a time, then the low parts of the remainders
+                    h[e] = __floats2bfloat162_rn(x[2 * e], x[2 * e + 1]);
+                    const float2 hf = __bfloat1622float2(h[e]);
+                    lo[e] = __floats2bfloat162_rn(x[2 * e] - hf.x, x[2 * e + 1] - hf.y);
                 }
                 *reinterpret_cast<uint4*>(ahi + tcx::sw128_offset(row, p)) = *reinterpret_cast<const uint4*>(h);
                 *reinterpret_cast<uint4*>(alo + tcx::sw128_offset(row, p)) = *reinterpret_cast<const uint4*>(lo);
@@ -2029,7 +2030,7 @@ __global__ void __launch_bounds__(CORNER_THREADS)
     if (ok) {
         // the last commit covers every MMA issued before it
         const int last = nchunk - 1;
-        ok = tcx::mbar_wait(&bar[last & 1], (last >> 1) & 1, 2u, &g_proj_error);
+        ok = tcx::mbar_wait(&bar[last % CORNER_STAGES], (last / CORNER_STAGES) & 1, 2u, &g_proj_error);
         ok = __syncthreads_and(ok);
         tcx::fence_after();
     }
