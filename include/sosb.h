@@ -237,6 +237,15 @@ int sosb_ray_segments(int64_t n, const double *p, const double *d, double top, c
                       int n_chi, const double *chi, const sosb_column_grid *table, double *edges, uint8_t *valid,
                       uint8_t *lower, int32_t *end_j, double *end_f, float *end_col, float *end_st, uint8_t *hits,
                       int threads);
+/* sosb_ray_segments on the device (the geometry CSR of ray_geometry.pack built by the GPU, one thread per ray): the
+ * same arguments and outputs, every array a device pointer (`table`, when not NULL, is a host struct whose h, up and
+ * down point to device arrays); asynchronous work on `stream` (a cudaStream_t, 0 the default stream), complete when
+ * the call returns. FP64 arithmetic: the cuts equal the host function's to rounding (the device may contract
+ * multiply-adds), so a segment whose length is within rounding of the 1e-8 threshold can differ. */
+int sosb_ray_segments_device(int64_t n, const double *p, const double *d, double top, const double *shells,
+                             int n_shells, int n_chi, const double *chi, const sosb_column_grid *table, double *edges,
+                             uint8_t *valid, uint8_t *lower, int32_t *end_j, double *end_f, float *end_col,
+                             float *end_st, uint8_t *hits, void *stream);
 /* Incoming-direction quadratures of n_cells cells (host threads; the project's restatement of the reference's ring
  * rule, src/sosfuse2/rays/incoming_rings.py): cell c at radius r[c] and solar zenith chi[c], nphi + 1 azimuth
  * planes, in each a sinh-mapped (a) Gauss-Legendre rule (u, wu on [0, 1], nmu nodes) between the cuts at the

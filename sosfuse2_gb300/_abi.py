@@ -97,6 +97,10 @@ SIGNATURES = {
     'sosb_prepare_ground': ([ctypes.c_void_p, c_dbl, P_f64, P_f64], c_int),
     'sosb_ray_segments': ([c_i64, P_f64, P_f64, c_dbl, P_f64, c_int, c_int, P_f64, ctypes.POINTER(ColumnGrid), P_f64,
                            P_u8, P_u8, P_i32, P_f64, P_f32, P_f32, P_u8, c_int], c_int),
+    'sosb_ray_segments_device': ([c_i64, ctypes.c_void_p, ctypes.c_void_p, c_dbl, ctypes.c_void_p, c_int, c_int,
+                                  ctypes.c_void_p, ctypes.POINTER(ColumnGrid), ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_void_p], c_int),
     'sosb_ring_quadrature': ([c_int, P_f64, P_f64, c_int, c_int, P_f64, c_int, c_int, c_dbl, P_f64, P_f64, P_i64,
                               P_f64, P_f64, c_i64, c_int], c_int),
     'sosb_column_table': ([c_int, P_f64, c_int, P_f64, P_f64, c_int, P_f64, P_f64, c_int, ctypes.POINTER(ProfileShape),

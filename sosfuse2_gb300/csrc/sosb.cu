@@ -3552,17 +3552,17 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
 // cylinder's two roots, the shells' crossings, and the end at the top or the ground (each absent cut repeats the end).
 // Returns the count (5 + 2 nshell) and whether the ray ends on the ground.
 constexpr int MAX_CUTS = 5 + 2 * 8;
-static int ray_cuts(const double p[3], const double d[3], double top, const double* shells, int nshell,
+SOS_HD int ray_cuts(const double p[3], const double d[3], double top, const double* shells, int nshell,
                     double cols[MAX_CUTS], bool* ground_out) {
     const double R = 6371.0;
     const double px = p[0], py = p[1], pz = p[2], dx = d[0], dy = d[1], dz = d[2];
     const double b = (px * dx + py * dy) + pz * dz;
     const double pp = (px * px + py * py) + pz * pz;
-    double end = -b + std::sqrt(std::max(b * b - pp + (R + top) * (R + top), 0.0));
+    double end = -b + sqrt(fmax(b * b - pp + (R + top) * (R + top), 0.0));
     const double disc = b * b - pp + R * R;
-    const double hit = -b - std::sqrt(std::max(disc, 0.0));
+    const double hit = -b - sqrt(fmax(disc, 0.0));
     const bool ground = disc >= 0.0 && b < 0.0 && hit >= -1e-7;
-    end = std::max(ground ? std::max(hit, 0.0) : end, 0.0);
+    end = fmax(ground ? fmax(hit, 0.0) : end, 0.0);
     const double tangent = (-b > 0.0 && -b < end) ? -b : end;
     const double aa = dx * dx + dy * dy, bb = px * dx + py * dy, cc = px * px + py * py - R * R;
     const double ds = bb * bb - aa * cc;
@@ -3571,18 +3571,26 @@ static int ray_cuts(const double p[3], const double d[3], double top, const doub
     cols[nc++] = tangent;
     cols[nc++] = end;
     for (int sign = -1; sign <= 1; sign += 2) {
-        const double root = (-bb + sign * std::sqrt(std::max(ds, 0.0))) / std::max(aa, 1e-30);
+        const double root = (-bb + sign * sqrt(fmax(ds, 0.0))) / fmax(aa, 1e-30);
         const bool ok = aa > 1e-20 && ds >= 0.0 && root > 0.0 && root < end && pz + root * dz < 0.0;
         cols[nc++] = ok ? root : end;
     }
     for (int k = 0; k < nshell && k < 8; ++k) {
         const double disc2 = b * b - pp + (R + shells[k]) * (R + shells[k]);
         for (int sign = -1; sign <= 1; sign += 2) {
-            const double root = -b + sign * std::sqrt(std::max(disc2, 0.0));
+            const double root = -b + sign * sqrt(fmax(disc2, 0.0));
             cols[nc++] = (disc2 > 0.0 && root > 0.0 && root < end) ? root : end;
         }
     }
-    std::sort(cols, cols + nc);
+    for (int i = 1; i < nc; ++i) {  // insertion sort (at most 21 cuts)
+        const double v = cols[i];
+        int j = i - 1;
+        while (j >= 0 && cols[j] > v) {
+            cols[j + 1] = cols[j];
+            --j;
+        }
+        cols[j + 1] = v;
+    }
     if (ground_out) *ground_out = ground;
     return nc;
 }
@@ -3653,21 +3661,35 @@ int sosb_column_table(int n_h, const double* h, int n_x, const double* x, const 
 
 // Bilinear lookup of a solar column table (synth.ColumnTable.lookup): columns [6] at height h (clipped to [0, top])
 // along zenith cosine mu from the up table when the ray escapes (mu >= the horizon cosine), else the down table.
-static void column_lookup(const sosb_column_grid& t, double h, double mu, double out[6]) {
+// index of the last grid value <= x (std::upper_bound - 1)
+SOS_HD int upper_index(const double* g, int n, double x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (g[mid] <= x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo - 1;
+}
+
+SOS_HD void column_lookup(const sosb_column_grid& t, double h, double mu, double out[6]) {
     const double R = 6371.0;
-    h = std::min(std::max(h, 0.0), t.top);
+    h = fmin(fmax(h, 0.0), t.top);
     const double r = R + h;
-    const double rr = std::max(r, R);
-    const double mg = -std::sqrt(std::max(0.0, 1.0 - (R / rr) * (R / rr)));
+    const double rr = fmax(r, R);
+    const double mg = -sqrt(fmax(0.0, 1.0 - (R / rr) * (R / rr)));
     const bool escape = mu >= mg;
-    const double x = escape ? std::sqrt(std::min(std::max((mu - mg) / (1.0 - mg), 0.0), 1.0))
-                            : std::sqrt(std::min(std::max((mg - mu) / (1.0 + mg), 0.0), 1.0));
+    const double x = escape ? sqrt(fmin(fmax((mu - mg) / (1.0 - mg), 0.0), 1.0))
+                            : sqrt(fmin(fmax((mg - mu) / (1.0 + mg), 0.0), 1.0));
     // i = clip(searchsorted(h_grid, h, 'right') - 1, 0, n_h - 2)
-    int i = (int)(std::upper_bound(t.h, t.h + t.n_h, h) - t.h) - 1;
-    i = std::min(std::max(i, 0), t.n_h - 2);
+    int i = upper_index(t.h, t.n_h, h);
+    i = i < 0 ? 0 : (i > t.n_h - 2 ? t.n_h - 2 : i);
     const double a = (h - t.h[i]) / (t.h[i + 1] - t.h[i]);
     const double f = x * (double)(t.n_x - 1);
-    const int j = std::min(std::max((int)f, 0), t.n_x - 2);
+    int j = (int)f;
+    j = j < 0 ? 0 : (j > t.n_x - 2 ? t.n_x - 2 : j);
     const double bb = f - (double)j;
     const double* tab = escape ? t.up : t.down;
     const double* t00 = tab + ((size_t)i * t.n_x + j) * 6;
@@ -3679,6 +3701,70 @@ static void column_lookup(const sosb_column_grid& t, double h, double mu, double
                  a * bb * t11[k];
 }
 
+// The segments and ray-end quantities of ray r (sosb_ray_segments; host threads or one device thread per ray).
+struct SegArgs {
+    const double *p, *d;
+    double top;
+    const double* shells;
+    int n_shells, n_chi;
+    const double* chi;
+    sosb_column_grid grid;  // the column table (its arrays on the side that runs the segments)
+    int has_grid;           // 0: no ground columns
+    double* edges;
+    uint8_t *valid, *lower, *hits;
+    int32_t* end_j;
+    double* end_f;
+    float *end_col, *end_st;
+};
+
+SOS_HD void ray_segments_one(const SegArgs& g, int64_t r) {
+    const double R = 6371.0;
+    const int ncut = 5 + 2 * g.n_shells;
+    const double* pr = g.p + r * 3;
+    const double* dr = g.d + r * 3;
+    double* e = g.edges + r * ncut;
+    double cuts[MAX_CUTS];
+    ray_cuts(pr, dr, g.top, g.shells, g.n_shells, cuts, nullptr);
+    for (int k = 0; k < ncut; ++k) e[k] = cuts[k];
+    for (int k = 0; k + 1 < ncut; ++k) {
+        const double a = cuts[k], b = cuts[k + 1];
+        g.valid[r * (ncut - 1) + k] = (b - a) > 1e-8;
+        double qa[3], qb[3];
+        for (int c = 0; c < 3; ++c) {
+            qa[c] = pr[c] + a * dr[c];
+            qb[c] = pr[c] + b * dr[c];
+        }
+        g.lower[r * (ncut - 1) + k] =
+            ((qa[0] * qa[0] + qa[1] * qa[1]) + qa[2] * qa[2]) <= ((qb[0] * qb[0] + qb[1] * qb[1]) + qb[2] * qb[2]);
+    }
+    const double end = cuts[ncut - 1];
+    double qe[3];
+    for (int c = 0; c < 3; ++c) qe[c] = pr[c] + end * dr[c];
+    const double re = sqrt((qe[0] * qe[0] + qe[1] * qe[1]) + qe[2] * qe[2]);
+    const double ch = acos(fmin(fmax(qe[2] / re, -1.0), 1.0));
+    int j = upper_index(g.chi, g.n_chi, ch);
+    j = j < 0 ? 0 : (j > g.n_chi - 2 ? g.n_chi - 2 : j);
+    g.end_j[r] = j;
+    g.end_f[r] = fmin(fmax((ch - g.chi[j]) / (g.chi[j + 1] - g.chi[j]), 0.0), 1.0);
+    const bool hit = re < R + 1e-5;
+    g.hits[r] = hit;
+    if (g.has_grid) {
+        double cols[6] = {0, 0, 0, 0, 0, 0};
+        if (hit) {
+            const double r0 = sqrt((pr[0] * pr[0] + pr[1] * pr[1]) + pr[2] * pr[2]);
+            const double mu = ((pr[0] * dr[0] + pr[1] * dr[1]) + pr[2] * dr[2]) / r0;
+            column_lookup(g.grid, r0 - R, mu, cols);
+        }
+        for (int k = 0; k < 5; ++k) g.end_col[r * 5 + k] = (float)cols[k];
+        g.end_st[r] = (float)cols[5];
+    }
+}
+
+__global__ void ray_segments_kernel(SegArgs g, int64_t n) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        ray_segments_one(g, r);
+}
+
 int sosb_ray_segments(int64_t n, const double* p, const double* d, double top, const double* shells, int n_shells,
                       int n_chi, const double* chi, const sosb_column_grid* table, double* edges, uint8_t* valid,
                       uint8_t* lower, int32_t* end_j, double* end_f, float* end_col, float* end_st, uint8_t* hits,
@@ -3687,46 +3773,9 @@ int sosb_ray_segments(int64_t n, const double* p, const double* d, double top, c
         !chi || n_shells < 0 || n_shells > 8 || (n_shells > 0 && !shells))
         return 1;
     if (table && (!end_col || !end_st || table->n_h < 2 || table->n_x < 2)) return 1;
-    const double R = 6371.0;
-    const int ncut = 5 + 2 * n_shells;
-    auto ray = [&](int64_t r) {
-        const double* pr = p + r * 3;
-        const double* dr = d + r * 3;
-        double* e = edges + r * ncut;
-        ray_cuts(pr, dr, top, shells, n_shells, e, nullptr);
-        for (int k = 0; k + 1 < ncut; ++k) {
-            const double a = e[k], b = e[k + 1];
-            valid[r * (ncut - 1) + k] = (b - a) > 1e-8;
-            double qa[3], qb[3];
-            for (int c = 0; c < 3; ++c) {
-                qa[c] = pr[c] + a * dr[c];
-                qb[c] = pr[c] + b * dr[c];
-            }
-            lower[r * (ncut - 1) + k] =
-                ((qa[0] * qa[0] + qa[1] * qa[1]) + qa[2] * qa[2]) <= ((qb[0] * qb[0] + qb[1] * qb[1]) + qb[2] * qb[2]);
-        }
-        const double end = e[ncut - 1];
-        double qe[3];
-        for (int c = 0; c < 3; ++c) qe[c] = pr[c] + end * dr[c];
-        const double re = std::sqrt((qe[0] * qe[0] + qe[1] * qe[1]) + qe[2] * qe[2]);
-        const double ch = std::acos(std::min(std::max(qe[2] / re, -1.0), 1.0));
-        int j = (int)(std::upper_bound(chi, chi + n_chi, ch) - chi) - 1;
-        j = std::min(std::max(j, 0), n_chi - 2);
-        end_j[r] = j;
-        end_f[r] = std::min(std::max((ch - chi[j]) / (chi[j + 1] - chi[j]), 0.0), 1.0);
-        const bool hit = re < R + 1e-5;
-        hits[r] = hit;
-        if (table) {
-            double cols[6] = {0, 0, 0, 0, 0, 0};
-            if (hit) {
-                const double r0 = std::sqrt((pr[0] * pr[0] + pr[1] * pr[1]) + pr[2] * pr[2]);
-                const double mu = ((pr[0] * dr[0] + pr[1] * dr[1]) + pr[2] * dr[2]) / r0;
-                column_lookup(*table, r0 - R, mu, cols);
-            }
-            for (int k = 0; k < 5; ++k) end_col[r * 5 + k] = (float)cols[k];
-            end_st[r] = (float)cols[5];
-        }
-    };
+    const SegArgs g{p, d, top, shells, n_shells, n_chi, chi, table ? *table : sosb_column_grid{}, table ? 1 : 0,
+                    edges, valid, lower, hits, end_j, end_f, end_col, end_st};
+    auto ray = [&](int64_t r) { ray_segments_one(g, r); };
     const int64_t chunk = 4096;
     const int64_t nchunk = (n + chunk - 1) / chunk;
     const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(threads > 0 ? threads : (int)std::thread::hardware_concurrency(), nchunk));
@@ -3739,6 +3788,26 @@ int sosb_ray_segments(int64_t n, const double* p, const double* d, double top, c
         });
     for (auto& t : pool) t.join();
     return 0;
+}
+
+int sosb_ray_segments_device(int64_t n, const double* p, const double* d, double top, const double* shells,
+                             int n_shells, int n_chi, const double* chi, const sosb_column_grid* table, double* edges,
+                             uint8_t* valid, uint8_t* lower, int32_t* end_j, double* end_f, float* end_col,
+                             float* end_st, uint8_t* hits, void* stream) {
+    if (n < 0 || (n > 0 && (!p || !d || !edges || !valid || !lower || !end_j || !end_f || !hits)) || n_chi < 2 ||
+        !chi || n_shells < 0 || n_shells > 8 || (n_shells > 0 && !shells))
+        return 1;
+    if (table && (!end_col || !end_st || table->n_h < 2 || table->n_x < 2 || !table->h || !table->up ||
+                  !table->down))
+        return 1;
+    if (n == 0) return 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const SegArgs g{p, d, top, shells, n_shells, n_chi, chi, table ? *table : sosb_column_grid{}, table ? 1 : 0,
+                    edges, valid, lower, hits, end_j, end_f, end_col, end_st};
+    ray_segments_kernel<<<grid_for(n, 128), 128, 0, st>>>(g, n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? 0 : 3;
 }
 
 // Incoming-direction quadrature of one cell (synth.ring_quadrature, the reference's ring rule restated: per azimuth

@@ -147,6 +147,25 @@ def ring_quadrature(r, chi, nmu, nphi, heights, rings=True, a=4.0):
 
 
 _NATIVE = True
+_DEVICE = None
+
+
+class device_geometry:
+    """Context in which the ray segments and ray-end quantities of the bundles (sosb_ray_segments) are built on the
+    GPU `device` (sosb_ray_segments_device, one thread per ray) instead of on host threads; the quadratures, the column
+    tables and the CSR compaction stay on the host."""
+
+    def __init__(self, device='cuda:0'):
+        self.device = device
+
+    def __enter__(self):
+        global _DEVICE
+        self.previous, _DEVICE = _DEVICE, self.device
+        return self
+
+    def __exit__(self, *exc):
+        global _DEVICE
+        _DEVICE = self.previous
 
 
 class numpy_geometry:
@@ -447,6 +466,48 @@ def _ray_block(p, d, chi_grid, top, table, with_ground_columns):
                 seg_lower=lower[v], end_j=end_j, end_f=end_f, end_col=end_col, end_st=end_st, hits=hits)
 
 
+def ray_block_device(p, d, chi_grid, top, table, with_ground_columns, device='cuda:0'):
+    """_ray_block with the segments built on the GPU (sosb_ray_segments_device); the results come back as the same
+    host arrays."""
+    import torch
+
+    from . import _abi, build
+
+    lib = _abi.library(build.build())
+    dev = torch.device(device)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float64), device=dev)  # noqa: E731
+    shells = t(_shells(top))
+    pd, dd, chi = t(p), t(d), t(chi_grid)
+    n, ncut = len(d), 5 + 2 * len(_shells(top))
+    edges = torch.empty((n, ncut), dtype=torch.float64, device=dev)
+    valid = torch.empty((n, ncut - 1), dtype=torch.uint8, device=dev)
+    lower = torch.empty((n, ncut - 1), dtype=torch.uint8, device=dev)
+    end_j = torch.empty(n, dtype=torch.int32, device=dev)
+    end_f = torch.empty(n, dtype=torch.float64, device=dev)
+    end_col = torch.zeros((n, 5), dtype=torch.float32, device=dev)
+    end_st = torch.zeros(n, dtype=torch.float32, device=dev)
+    hits = torch.empty(n, dtype=torch.uint8, device=dev)
+    grid, keep = None, None
+    if with_ground_columns:
+        keep = [t(table.h), t(table.up), t(table.down)]
+        grid = _abi.ColumnGrid(n_h=len(table.h), n_x=len(table.x), top=table.top,
+                               h=ctypes.cast(keep[0].data_ptr(), _abi.P_f64),
+                               up=ctypes.cast(keep[1].data_ptr(), _abi.P_f64),
+                               down=ctypes.cast(keep[2].data_ptr(), _abi.P_f64))
+    vp = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    rc = lib.sosb_ray_segments_device(n, vp(pd), vp(dd), float(top), vp(shells), len(shells), len(chi), vp(chi),
+                                      None if grid is None else ctypes.byref(grid), vp(edges), vp(valid), vp(lower),
+                                      vp(end_j), vp(end_f), vp(end_col), vp(end_st), vp(hits), stream)
+    if rc:
+        raise RuntimeError(f'E_SEGMENTS: sosb_ray_segments_device returned {rc}')
+    v = valid.cpu().numpy().astype(bool)
+    e = edges.cpu().numpy()
+    return dict(seg_off=np.r_[0, np.cumsum(v.sum(1))].astype(np.int64), seg_a=e[:, :-1][v], seg_b=e[:, 1:][v],
+                seg_lower=lower.cpu().numpy()[v], end_j=end_j.cpu().numpy(), end_f=end_f.cpu().numpy(),
+                end_col=end_col.cpu().numpy(), end_st=end_st.cpu().numpy(), hits=hits.cpu().numpy())
+
+
 def ray_block_numpy(p, d, chi_grid, top, table, with_ground_columns):
     """The NumPy restatement of _ray_block (ray_edges, compact_segments and the end quantities), the reference the
     native sosb_ray_segments is checked against."""
@@ -494,8 +555,12 @@ def build_bundle(points, dirs_local, weights, chi_grid, top, table, atm, with_gr
     parts = []
     for r0 in range(0, len(d), block):
         r1 = min(r0 + block, len(d))
-        block_fn = _ray_block if _NATIVE else ray_block_numpy
-        parts.append(block_fn(P[ray_cell[r0:r1]], d[r0:r1], chi_grid, top, table, with_ground_columns))
+        if _DEVICE is not None and _NATIVE:
+            parts.append(ray_block_device(P[ray_cell[r0:r1]], d[r0:r1], chi_grid, top, table, with_ground_columns,
+                                          _DEVICE))
+        else:
+            block_fn = _ray_block if _NATIVE else ray_block_numpy
+            parts.append(block_fn(P[ray_cell[r0:r1]], d[r0:r1], chi_grid, top, table, with_ground_columns))
     seg_off = [np.zeros(1, np.int64)]
     base = 0
     for part in parts:

@@ -1,0 +1,54 @@
+"""The geometry CSR on the device (sosb_ray_segments_device, one thread per ray) against the host builder
+(sosb_ray_segments, the reference's ray_geometry.pack restated and checked against its NumPy restatement in
+tests/test_ray_segments.py), on every cell ray and observer ray of the config-0 family (27,224 + 560 rays, ground
+columns from its solar column table): the same segments (validity and lower-end flags), the cuts to FP64 rounding
+(1e-12 relative), the same end intervals and fractions, the same ground hits and columns. Then a whole bundle built
+under synth.device_geometry() equals the host-built one."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rays(fam, prefix):
+    b = fam.cells if prefix == 'cell' else fam.query
+    cell = np.repeat(np.arange(len(b['cell_off']) - 1), np.diff(b['cell_off']))
+    return np.ascontiguousarray(b['p'][cell]), np.ascontiguousarray(b['d'])
+
+
+def test_device_segments_equal_host():
+    from sosfuse2_gb300 import synth
+
+    fam = synth.config0_family()
+    for prefix, ground in (('cell', True), ('query', False)):
+        p, d = _rays(fam, prefix)
+        host = synth._ray_block(p, d, fam.chi, fam.top, fam.table, ground)
+        dev = synth.ray_block_device(p, d, fam.chi, fam.top, fam.table, ground)
+        np.testing.assert_array_equal(dev['seg_off'], host['seg_off'])
+        np.testing.assert_array_equal(dev['seg_lower'], host['seg_lower'])
+        for k in ('seg_a', 'seg_b'):
+            scale = np.maximum(np.abs(host[k]), 1.0)
+            assert np.max(np.abs(dev[k] - host[k]) / scale) <= 1e-12, k
+        np.testing.assert_array_equal(dev['end_j'], host['end_j'])
+        np.testing.assert_array_equal(dev['hits'], host['hits'])
+        assert np.max(np.abs(dev['end_f'] - host['end_f'])) <= 1e-9
+        for k in ('end_col', 'end_st'):
+            assert np.max(np.abs(dev[k] - host[k]) / np.maximum(np.abs(host[k]), 1e-30)) <= 1e-6, k
+
+
+def test_device_geometry_bundle_equals_host():
+    from sosfuse2_gb300 import synth
+
+    atm = synth.Atmosphere([550.0], seed=3, top=80.0)
+    h = np.r_[0.0, np.geomspace(0.5, 80.0, 5)]
+    host = synth.make_state(h, [0.0, 60.0, 90.0, 96.0, 110.0, 180.0], atm.wl, 16, 1, 2, 4, atm, seed=3, sun_scale=1)
+    with synth.device_geometry():
+        dev = synth.make_state(h, [0.0, 60.0, 90.0, 96.0, 110.0, 180.0], atm.wl, 16, 1, 2, 4, atm, seed=3,
+                               sun_scale=1)
+    for k in [k for k in host if k.startswith(('cell_', 'query_'))]:
+        a, b = np.asarray(dev[k]), np.asarray(host[k])
+        if a.dtype.kind == 'f':
+            assert np.allclose(a, b, rtol=1e-12, atol=1e-12), k
+        else:
+            np.testing.assert_array_equal(a, b, err_msg=k)
