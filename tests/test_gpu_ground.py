@@ -2,12 +2,15 @@
 src/sosfuse2/solve/engine_core.py:103-147) against the host preparation of the same state (synth.Family.ground): a
 handle whose ground arrays were prepared on the device gives the same first light, applications and observer boxes
 as one given the host arrays. Both evaluate the ray values in FP64 and round once to FP32, so the bound is relative
-1e-6 (the two exponentials may differ in the last bit of a double)."""
+1e-6 (the two exponentials may differ in the last bit of a double). Pinned to the reference: over the reference's own
+ground rays of two golden states (tests/golden/ground_walk1.npz, ground_strato15.npz) the device preparation gives
+the applications of the reference's prepared arrays, and the first light the reference's own first-light moments."""
 
 import numpy as np
 import pytest
 
-from conftest import rel_l2_per_wave
+from conftest import GOLDEN, rel_l2_per_wave
+from test_ground_host import reference_ground
 
 pytestmark = pytest.mark.gpu
 
@@ -91,5 +94,24 @@ def test_table_of_device_ground_state_matches_host():
     a, _ = make_table(host, field, hs, el, az, log=lambda m: None, family=fam)
     b, _ = make_table(dev, field, hs, el, az, log=lambda m: None, family=fam)
     assert np.max(np.abs(a - b)) <= 1e-6 * np.abs(a).max()
+    host.kernel.close()
+    dev.kernel.close()
+
+
+@pytest.mark.parametrize('name', ['walk1', 'strato15'])
+def test_device_ground_matches_reference(name):
+    from sosfuse2_gb300.solver import Solver
+    from sosfuse2_gb300.state import PackedState
+    from test_gpu_parity import close_field
+
+    rays, albedo, ext, strato_ext, _ = reference_ground(name)
+    host = Solver(PackedState(GOLDEN / f'{name}.npz'), device='cuda:0')
+    dev = Solver(PackedState(GOLDEN / f'{name}.npz'), device='cuda:0')
+    dev.kernel.set_ground_rays(rays)
+    dev.kernel.prepare_ground(albedo, ext, strato_ext)
+    m, f, _ = dev.kernel.launch(0, True)
+    close_field(m.cpu().numpy(), dev.state['first_moments'])
+    g_host, g_dev = host.apply(host.kernel.field()), dev.apply(dev.kernel.field())
+    assert np.all(rel_l2_per_wave(g_dev.cpu().numpy(), g_host.cpu().numpy()) <= 1e-6)
     host.kernel.close()
     dev.kernel.close()

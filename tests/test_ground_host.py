@@ -1,11 +1,17 @@
 """The ground-ray arrays handed to sosb_prepare_ground carry everything the preparation needs: a NumPy restatement
 of the device algorithm (per-ray FP64 values, kept rays per cell in ray order, per-cell factor sums times
 2 C ext[0]) over `synth.Family.ground_rays()` reproduces the host preparation `synth.Family.ground` of the same
-state (engine_core.Solver.prepare_ground, src/sosfuse2/solve/engine_core.py:103-147)."""
+state (engine_core.Solver.prepare_ground, src/sosfuse2/solve/engine_core.py:103-147); and, pinned to the reference,
+the same restatement over the reference's own ground rays of two golden states (tests/golden/ground_*.npz, written by
+tests/golden/make_ground_fixture.py from precompute/host_cache._ground_values and atmosphere/stratosphere.attach)
+reproduces the gm, goff, gdir and gval those reference functions produced."""
 
 import math
 
 import numpy as np
+import pytest
+
+from conftest import GOLDEN
 
 
 def _prepare(rays, ns, albedo, ext, strato_ext):
@@ -42,3 +48,21 @@ def test_ground_rays_reproduce_host_preparation():
     assert np.array_equal(got[1], want[1]) and np.array_equal(got[2], want[2])
     for a, b in ((got[0], want[0]), (got[3], want[3])):
         assert np.max(np.abs(a - b)) <= 1e-6 * np.abs(b).max()
+
+
+def reference_ground(name):
+    """The reference's ground rays of a golden state in the sosb_set_ground_rays layout, and its prepared arrays."""
+    z = np.load(GOLDEN / f'ground_{name}.npz')
+    rays = dict(cell=z['ray_cell'], loc=z['ray_loc'], weight=z['ray_weight'], cols=z['ray_cols'],
+                cos_sun=z['ray_cos_sun'], ok=z['ray_ok'])
+    strato_ext = z['strato_ext'] if len(z['strato_ext']) else None
+    return rays, float(z['albedo']), z['ext'], strato_ext, (z['gm'], z['goff'], z['gdir'], z['gval'])
+
+
+@pytest.mark.parametrize('name', ['walk1', 'strato15'])
+def test_restatement_reproduces_reference_prepare_ground(name):
+    rays, albedo, ext, strato_ext, want = reference_ground(name)
+    got = _prepare(rays, len(want[1]) - 1, albedo, ext, strato_ext)
+    assert np.array_equal(got[1], want[1]) and np.array_equal(got[2], want[2])
+    assert np.array_equal(got[3], want[3])
+    assert np.max(np.abs(got[0] - want[0])) <= 1e-6 * np.abs(want[0]).max()
