@@ -75,6 +75,9 @@ typedef struct {
     const float *strato_sun_col;/* [n_sun_h][n_sun_x] */
     const float *strato_eigen;  /* [K][W] */
     const float *strato_sca_source; /* [W] */
+    const float *aer2;          /* [7] two-layer tropospheric aerosol profile (the AEROSOL_2L kernel vector of
+                                 * atmosphere/tropo_profile.py:203-225: [bl_top - w/2, 1/w, a_bl, k_bl, a_ft, k_ft,
+                                 * bl_top]), or NULL for the exponential profile exp(-h / height) */
 } sosb_constants;
 
 /* Host arrays of one ray bundle (ray_geometry.Bundle, src/sosfuse2/solve/ray_geometry.py:290-392): destination

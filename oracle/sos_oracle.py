@@ -241,7 +241,9 @@ class StatePack:
 
 def profile_at(h, pk):
     """Air, tropospheric aerosol, O3, NO2, O4 number-density shapes at FP32 heights (numpy_reference.py:187-223).
-    Density table columns: air, ozone, NO2 on the uniform profile grid; mask bit 0/1 selects tabulated air/ozone."""
+    Density table columns: air, ozone, NO2 on the uniform profile grid; mask bit 0/1 selects tabulated air/ozone; a
+    state with the two-layer tropospheric aerosol (array 'aer2') takes that shape for the aerosol
+    (atmosphere/tropo_profile.py:295-304)."""
     h = np.asarray(h, F)
     tab = pk['density_table']
     inv = 1.0 / pk.meta['profile_step_km']
@@ -258,9 +260,21 @@ def profile_at(h, pk):
         prof[:, 0] = t[:, 0]
     if mask & 2:
         prof[:, 2] = t[:, 1]
+    if 'aer2' in pk:
+        prof[:, 1] = aerosol_two_layer(h, pk['aer2'])
     q = prof[:, 0] / F(pk.meta['air_surface'])
     prof[:, 4] = q * q
     return prof
+
+
+def aerosol_two_layer(h, k):
+    """FP32 two-layer aerosol shape: smoothstep blend of the boundary-layer and free-troposphere exponentials
+    (atmosphere/tropo_profile.py:295-304, kernel.cu aerosol_two_layer)."""
+    h = np.asarray(h, F)
+    k = np.asarray(k, F)
+    x = np.clip((h - k[0]) * k[1], F(0), F(1))
+    s = x * x * (F(3) - F(2) * x)
+    return ((k[2] * np.exp(-h * k[3])) * (F(1) - s) + (k[4] * np.exp(-(np.maximum(h, k[0]) - k[6]) * k[5])) * s).astype(F)
 
 
 def strato_profile(h, pk):

@@ -139,6 +139,8 @@ struct Optics {
     const uint8_t* gsame;  // [ns] 1 when cell c + 1 (same height, next solar zenith) has c's ground directions, or null
     const float2* strato_lut2;  // [STRATO_LUT_BINS][W] (value, next value - value) of strato_lut, or null
     const float4* gdir4;        // [*] gdir padded to 16 bytes, or null
+    int aer2_on;                // two-layer tropospheric aerosol profile instead of exp(-h / height)
+    float aer2[7];              // its vector [bl_top - w/2, 1/w, a_bl, k_bl, a_ft, k_ft, bl_top]
 };
 
 constexpr int STRATO_LUT_BINS = 4096;
@@ -167,6 +169,17 @@ struct Profile {
     float v[5];
 };
 
+// Two-layer tropospheric aerosol shape (kernel.cu aerosol_two_layer, FP32 mirror atmosphere/tropo_profile.py:295-304):
+// a smoothstep over [P0, P0 + 1/P1] from the boundary layer P2 exp(-h P3) to the free troposphere
+// P4 exp(-(max(h, P0) - P6) P5), each product and sum rounded on its own.
+SOS_HD float aerosol_two_layer(float h, const float* P) {
+    const float x = clampf(SOS_MUL(SOS_ADD(h, -P[0]), P[1]), 0.0f, 1.0f);
+    const float s = SOS_MUL(SOS_MUL(x, x), SOS_ADD(3.0f, -SOS_MUL(2.0f, x)));
+    const float bl = SOS_MUL(SOS_MUL(P[2], expf(-SOS_MUL(h, P[3]))), SOS_ADD(1.0f, -s));
+    const float ft = SOS_MUL(SOS_MUL(P[4], expf(-SOS_MUL(SOS_ADD(fmaxf(h, P[0]), -P[6]), P[5]))), s);
+    return SOS_ADD(bl, ft);
+}
+
 SOS_HD Profile profile_at(const Optics& o, float h) {
     float hc = clampf(h, 0.0f, o.top_km);
     float x = hc * o.inv_step;
@@ -180,7 +193,7 @@ SOS_HD Profile profile_at(const Optics& o, float h) {
     float tab2 = t0[2] + f * (t1[2] - t0[2]);
     Profile p;
     p.v[0] = (o.density_mask & 1) ? tab0 : expf(-h / 8.0f);
-    p.v[1] = expf(-h / o.height);
+    p.v[1] = o.aer2_on ? aerosol_two_layer(h, o.aer2) : expf(-h / o.height);
     p.v[2] = (o.density_mask & 2) ? tab1 : fmaxf(0.0f, 1.0f - fabsf(h - 25.0f) / 15.0f);
     p.v[3] = tab2;
     float q = p.v[0] / o.air_surface;

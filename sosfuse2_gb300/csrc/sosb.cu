@@ -133,6 +133,8 @@ struct sosb_state {
     bool corner_mma = true;  // corner SH values on the tensor cores, more than four wavelengths (sosb_set_corner_mma)
     bool corner_used = false;  // a corner GEMM ran since the last check of its bounded waits
     bool warm_history = false;  // sosb_solve_warm seeds the Anderson history with (0, fallback) (sosb_set_warm_history)
+    int aer2_on = 0;     // two-layer tropospheric aerosol profile (sosb_constants.aer2)
+    float aer2[7] = {};
     int proj_mode = 0;   // projection form (sosb_set_projection): PROJ_FP32, PROJ_BF16X3, PROJ_TF32, PROJ_BF16
     int64_t launches = 0;
     // per-evaluation history of the last solve on this handle: [evaluation][W] observer and source relative changes
@@ -1529,8 +1531,9 @@ __global__ void plane_kernel(const float* __restrict__ field, const float* __res
         }
         const int hi = cell / nc;
         const float* f = field + (size_t)cell * src * W + w;
-        float v = f[(size_t)(10 + k) * W] * ha[hi];
-        if (strato) v += f[(size_t)(10 + K + k) * W] * sd[hi];
+        // each product and the sum rounded on its own (sh_layout.combined_coefficients)
+        float v = __fmul_rn(f[(size_t)(10 + k) * W], ha[hi]);
+        if (strato) v = __fadd_rn(v, __fmul_rn(f[(size_t)(10 + K + k) * W], sd[hi]));
         plane[i] = v;
     }
 }
@@ -2541,6 +2544,8 @@ static Optics optics_of(const sosb_state* s) {
     o.gsame = P<uint8_t>(s->gsame);
     o.strato_lut2 = P<float2>(s->s_lut2);
     o.gdir4 = P<float4>(s->gdir4);
+    o.aer2_on = s->aer2_on;
+    for (int i = 0; i < 7; ++i) o.aer2[i] = s->aer2[i];
     return o;
 }
 
@@ -3499,6 +3504,8 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
         }
         TRY(dput_vec(s, s->gsame, same));
     }
+    s->aer2_on = c->aer2 != nullptr;
+    for (int i = 0; i < 7; ++i) s->aer2[i] = c->aer2 ? c->aer2[i] : 0.0f;
     TRY(dput(s, s->rf, c->rf, 6 * 4));
     TRY(dput(s, s->af, c->af, K * 4));
     TRY(dput(s, s->ext0, c->ext0, W * 4));

@@ -77,6 +77,21 @@ def observer_rays(s):
     return raws
 
 
+def thin_layer_cut(arrays, strat):
+    """The thin-layer skip of the combined SH plane (sh_layout.combined_coefficients with skip_thin,
+    src/sosfuse2/backends/sh_layout.py:135-152) applied to the packed densities: on grids of at most 128 heights the
+    aerosol density ha and the stratospheric source density at or below 1e-7 of the air density hr become 0. Those
+    densities enter only the plane, which the device forms as aerosol slots x ha + stratospheric slots x density."""
+    hr = np.asarray(arrays['hr'], 'f4')
+    if len(hr) > 128:
+        return arrays
+    cut = np.float32(1e-7) * hr
+    for k in ('ha', 'strato_density') if strat else ('ha',):
+        v = np.asarray(arrays[k], 'f4')
+        arrays[k] = np.where(v > cut, v, np.float32(0)).astype('f4')
+    return arrays
+
+
 def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
     """Packed-state arrays of a reference-assembled state `s` (create_configured) with its TransientGeometry."""
     from sosfuse2.backends.sh_layout import source_size
@@ -90,8 +105,8 @@ def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
     L, K, W = s.kernel.L, s.kernel.K, s.W
     if c['domain'].top_km > 80.0:
         raise ValueError('E_DOMAIN: the extended top above 80 km is not packed')
-    if 'tropo_lut' in c or 'aer2' in c or c.get('sh_combine'):
-        raise ValueError('E_FLAGS: tabulated tropospheric phase, two-layer aerosol and the combined plane are not packed')
+    if 'tropo_lut' in c:
+        raise ValueError('E_FLAGS: the tabulated tropospheric phase is not packed')
     u4, w4 = np.polynomial.legendre.leggauss(4)
     opt = c['density_optics']
     meta = dict(
@@ -108,6 +123,15 @@ def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
         sun_h=c['sun_h'], sun_col=c['sun_col'], gm=c['gm'], gd=c['gd'], gv=c['gv'],
         density_table=np.asarray(opt['table'], 'f4'), rf=np.asarray(s.rf, 'f4'), af=np.asarray(s.af[:K], 'f4'),
         ext0=np.asarray(s.ext[0], 'f4'), solar=np.asarray(s.solar, 'f8'), box_ww=(w4[:, None] * w4[None, :] / 4).ravel())
+    if 'aer2' in c:  # AEROSOL_2L: the two-layer profile's kernel vector
+        arrays['aer2'] = np.asarray(c['aer2'], 'f4')
+        meta['aerosol_profile'] = 'two_layer'
+    if c.get('sh_combine') and c.get('sh_combine_skip'):
+        # The device always forms the combined plane (aerosol slots x ha + stratospheric slots x their density); the
+        # thin-layer skip of sh_layout.combined_coefficients (src/sosfuse2/backends/sh_layout.py:135-152) zeroes a
+        # density at or below 1e-7 of the air density on grids of at most 128 heights, and those densities enter
+        # only that plane.
+        meta['sh_combine_skip'] = True
     if strat:
         from sosfuse2.atmosphere.stratosphere import eigen_by_sh
 
@@ -118,6 +142,8 @@ def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
             strato_eigen=np.asarray(eigen_by_sh(s.strato, L), 'f4'), strato_sca_source=np.asarray(s.strato['sca'], 'f4'))
         meta.update(strato_center=float(prof['center']), strato_sigma=float(prof['sigma']),
                     strato_norm=float(prof['norm']))
+    if meta.get('sh_combine_skip'):
+        thin_layer_cut(arrays, strat)
     for k, v in _bundle(groups, c, strat).items():
         arrays['cell_' + k] = v
     for k, v in _bundle(raws, cq, strat).items():

@@ -117,6 +117,8 @@ class PackedState:
                         strato_chi=(a['strato_chi'], f4), strato_density=(a['strato_density'], f4),
                         strato_sun_col=(a['strato_sun_col'], f4), strato_eigen=(a['strato_eigen'], f4),
                         strato_sca_source=(a['strato_sca_source'], f4))
+        if 'aer2' in a:
+            spec.update(aer2=(a['aer2'], f4))
         for name, (v, dt) in spec.items():
             arr = self._arr(v, dt)
             ct = dict((f[0], f[1]) for f in _abi.Constants._fields_)[name]

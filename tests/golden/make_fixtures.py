@@ -47,6 +47,11 @@ FIXTURES = dict(
     # family members whose iteration keeps a large source change; records whether the reference converges and its
     # per-evaluation history either way
     slow1=dict(strato=False, wavelengths=[550.0], parameters=dict(aod550=0.3, g=0.78)),
+    # the walkthrough state with the two-layer tropospheric aerosol profile (troposphere_profile block, the
+    # reference's defaults: boundary layer to 2 km, free troposphere AOD 0.0797 with a 1.85 km scale height), the
+    # AEROSOL_2L profile in the transport
+    aer2=dict(strato=False, wavelengths=[550.0],
+              blocks=dict(troposphere_profile=dict(status='enabled', model='two_layer'))),
 )
 
 
@@ -114,6 +119,7 @@ def make(name, spec, out_dir=HERE):
     a = SimpleNamespace(reduced=True, settings_json=None, stratosphere=None)
     st = wt.example_state()
     st['parameters'].update(spec.get('parameters', {}))
+    st.update(copy.deepcopy(spec.get('blocks', {})))
     if spec['strato']:
         st['stratosphere'] = dict(status='enabled', profile='gaussian', center_km=21.0, sigma_km=3.0, g=0.63, ssa=1.0)
     state = rs.effective_state(st, a)
