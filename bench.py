@@ -155,11 +155,12 @@ def peaks():
         return 6800.0, 'fallback'
 
 
-def profiled_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary (profiles/*.txt, 'traffic_bytes_per_launch')."""
+def profiled_traffic(kernel, key='traffic_bytes_per_launch'):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (profiles/*.txt, 'traffic_bytes_per_launch'),
+    or per unit of work with key 'traffic_bytes_per_unit'."""
     for f in sorted((ROOT / 'profiles').glob('*.txt')):
         for line in f.read_text().splitlines():
-            if line.startswith(f'traffic_bytes_per_launch {kernel} '):
+            if line.startswith(f'{key} {kernel} '):
                 try:
                     return float(line.split()[2])
                 except ValueError:
@@ -762,8 +763,15 @@ def corner_roofline(item, device):
     classes = _abi.KERNEL_CLASSES
     share = {classes[j]: ms[j] / max(sum(ms[c] for c in range(ncls) if classes[c] != 'corner'), 1e-30)
              for j in range(ncls)}
+    per_unit = profiled_traffic('corner_tc_kernel', 'traffic_bytes_per_unit')
+    # DRAM bytes of the average launch (cell bundle once, observer bundle twice per evaluation): the bytes per
+    # (entry, wavelength) of the committed capture (profiles/corner_tc_kernel_profile_state.txt, a smaller state)
+    # times this state's units per launch
+    traffic = per_unit * (cell_entries + 2 * obs_entries) / 3.0 * W if per_unit is not None else None
     return dict(kernel='corner_tc_kernel', bound='tensor', achieved=achieved, peak=peak, unit='TFLOP/s',
-                frac=achieved / peak, peak_source=kind, traffic=profiled_traffic('corner_tc_kernel'),
+                frac=achieved / peak, peak_source=kind, traffic=traffic,
+                traffic_source='profiles/corner_tc_kernel_profile_state.txt: DRAM bytes per (entry, wavelength) of '
+                               'the profile state, scaled by this state\'s entries x W per launch',
                 flops_per_evaluation=flops / max(E, 1), executed_tflops=executed / sec / 1e12,
                 mean_launch_ms=ms[i] / max(cnt[i], 1), launches=int(cnt[i]), evaluations=E,
                 state=m['config3'], class_ms={classes[j]: ms[j] for j in range(ncls)},

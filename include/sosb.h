@@ -78,6 +78,11 @@ typedef struct {
     const float *aer2;          /* [7] two-layer tropospheric aerosol profile (the AEROSOL_2L kernel vector of
                                  * atmosphere/tropo_profile.py:203-225: [bl_top - w/2, 1/w, a_bl, k_bl, a_ft, k_ft,
                                  * bl_top]), or NULL for the exponential profile exp(-h / height) */
+    int32_t tropo_bins;         /* tabulated tropospheric phase (TROPO_MIE, atmosphere/tropo_mie.py:141-177): bins */
+    const float *tropo_lut;     /* [tropo_bins + 1][W] phase per sr at u = -1 + 2 i / tropo_bins, linear in u; or NULL
+                                 * for the Henyey-Greenstein phase of g */
+    const float *tropo_eigen;   /* [K][W] its SH eigenvalues chi_l / (2l + 1), replacing af in the composition; or
+                                 * NULL */
 } sosb_constants;
 
 /* Host arrays of one ray bundle (ray_geometry.Bundle, src/sosfuse2/solve/ray_geometry.py:290-392): destination

@@ -26,8 +26,9 @@ Pins: tests/test_oracle_golden.py against the reference's outputs of tests/golde
 radiance table of the walkthrough state (tests/golden/table_walk1.npz). oracle/fp64.py evaluates the same operations
 in float64 for the per-pixel error report.
 
-Out of scope here (not on the fixtures' path): the extended top above 80 km, the tabulated tropospheric Mie phase,
-the two-layer aerosol profile and the combined SH plane.
+Optional state features follow the reference where a golden state carries them: the two-layer tropospheric aerosol
+profile (tests/golden/aer2.npz) and the tabulated tropospheric Mie phase with its per-wavelength eigenvalues
+(tests/golden/mie1.npz, mie15.npz). Out of scope here: the extended top above 80 km.
 """
 
 import json
@@ -277,6 +278,18 @@ def aerosol_two_layer(h, k):
     return ((k[2] * np.exp(-h * k[3])) * (F(1) - s) + (k[4] * np.exp(-(np.maximum(h, k[0]) - k[6]) * k[5])) * s).astype(F)
 
 
+def tropo_phase(u, pk):
+    """Tabulated tropospheric phase per sr, linear in u on tropo_bins + 1 nodes, FP32: u[...] -> [..., W]
+    (numpy_reference.py:409-420)."""
+    lut = pk['tropo_lut']
+    bins = len(lut) - 1
+    x = (np.clip(np.asarray(u, F), F(-1), F(1)) + F(1)) * F(bins / 2)
+    i = np.minimum(x.astype(np.int32), bins - 1)
+    f = (x - i.astype(F))[..., None]
+    a = lut[i]
+    return a + f * (lut[i + 1] - a)
+
+
 def strato_profile(h, pk):
     t = (h - F(pk.meta['strato_center'])) / F(pk.meta['strato_sigma'])
     return np.exp(F(-0.5) * (t * t)) / F(pk.meta['strato_norm'])
@@ -461,7 +474,7 @@ def _transport(pk, b, field, first, boundary, query):
     rt = _ray_table(pk, b, rows)
     g = F(pk.meta['g'])
     mix = F(pk.meta['mix'])
-    phase = hg_phase(rt['d32'][:, 2], g)
+    phase = tropo_phase(rt['d32'][:, 2], pk) if 'tropo_lut' in pk else hg_phase(rt['d32'][:, 2], g)
     if pk.strato:
         sphase = legendre_phase(rt['d32'][:, 2], pk['strato_chi'])
     total = np.zeros((n, W, 4), F)
@@ -551,18 +564,23 @@ def _sample_value(pk, r, q, field, first, phase, sphase, g, mix, hr, ha):
             gdc = gd[cells]
             m0 = mu[:, None] * gdc[:, :, 2] + exd[:, None] * gdc[:, :, 0]
             m1 = abs(eyd)[:, None] * gdc[:, :, 1]
-            ph = (hg_phase(np.clip(m0 + m1, F(-1), F(1)), g) + hg_phase(np.clip(m0 - m1, F(-1), F(1)), g)) / F(2)
-            wph = q['sw'][:, corner, None] * ph
+            if 'tropo_lut' in pk:  # per wavelength from the table
+                ph = (tropo_phase(np.clip(m0 + m1, F(-1), F(1)), pk)
+                      + tropo_phase(np.clip(m0 - m1, F(-1), F(1)), pk)) / F(2)
+                wph = q['sw'][:, corner, None, None] * ph
+            else:
+                ph = (hg_phase(np.clip(m0 + m1, F(-1), F(1)), g) + hg_phase(np.clip(m0 - m1, F(-1), F(1)), g)) / F(2)
+                wph = q['sw'][:, corner, None] * ph
             if strat:
                 sph = (legendre_phase(np.clip(m0 + m1, F(-1), F(1)), pk['strato_chi'])
                        + legendre_phase(np.clip(m0 - m1, F(-1), F(1)), pk['strato_chi'])) / F(2)
                 swph = q['sw'][:, corner, None, None] * sph
             # sum over the cell's ground directions (the reference adds them one by one, in the same order)
             gvc = gv[cells]
-            ground += np.einsum('ng,ngw->nw', wph, gvc, dtype=F)
+            ground += np.einsum('ngw,ngw->nw' if wph.ndim == 3 else 'ng,ngw->nw', wph, gvc, dtype=F)
             if strat:
                 sground += np.einsum('ngw,ngw->nw', swph, gvc, dtype=F)
-        beam = (q['prof'][:, 1, None] * pk['asca']) * (sun * phase[:, None] + ground)
+        beam = (q['prof'][:, 1, None] * pk['asca']) * (sun * (phase if phase.ndim == 2 else phase[:, None]) + ground)
         if strat:
             sbeam = (q['st_prof'][:, None] * pk['strato_sca']) * (sun * sphase + sground)
         ray = (sun * q['prof'][:, 0, None]) * pk['ext'][0]
@@ -707,7 +725,8 @@ def compose(pk, moment):
     out = np.empty((pk.ns, pk.source_size, pk.W), F)
     out[:, :4] = (moment[:, :4] * (F(3 / (8 * math.pi)) * ext0)[None, None, :]).astype(F)
     out[:, 4:10] = (moment[:, 4:10] * pk['rf'][None, :, None] * ext0[None, None, :]).astype(F)
-    out[:, 10:10 + K] = (moment[:, 4:] * pk['af'][None, :, None] * pk['asca'][None, None, :]).astype(F)
+    eigen = pk['tropo_eigen'][None, :, :] if 'tropo_lut' in pk else pk['af'][None, :, None]
+    out[:, 10:10 + K] = (moment[:, 4:] * eigen * pk['asca'][None, None, :]).astype(F)
     if pk.strato:
         out[:, 10 + K:] = (moment[:, 4:] * pk['strato_eigen'][None, :, :]
                            * pk['strato_sca_source'][None, None, :]).astype(F)

@@ -44,6 +44,7 @@ class Constants(ctypes.Structure):
         ('rf', P_f32), ('af', P_f32), ('ext0', P_f32), ('solar', P_f64), ('box_ww', P_f64),
         ('strato_ext', P_f32), ('strato_sca', P_f32), ('strato_chi', P_f32), ('strato_density', P_f32),
         ('strato_sun_col', P_f32), ('strato_eigen', P_f32), ('strato_sca_source', P_f32), ('aer2', P_f32),
+        ('tropo_bins', c_int), ('tropo_lut', P_f32), ('tropo_eigen', P_f32),
     ]
 
 

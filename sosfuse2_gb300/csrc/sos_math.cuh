@@ -141,6 +141,9 @@ struct Optics {
     const float4* gdir4;        // [*] gdir padded to 16 bytes, or null
     int aer2_on;                // two-layer tropospheric aerosol profile instead of exp(-h / height)
     float aer2[7];              // its vector [bl_top - w/2, 1/w, a_bl, k_bl, a_ft, k_ft, bl_top]
+    int tropo_bins;             // tabulated tropospheric phase (TROPO_MIE) on tropo_bins + 1 nodes, or 0 for HG
+    const float* tropo_lut;     // [tropo_bins + 1][W] tropospheric phase per sr on a uniform grid of u in [-1, 1]
+    const float2* tropo_lut2;   // [tropo_bins][W] (value, next value - value) of tropo_lut, or null
 };
 
 constexpr int STRATO_LUT_BINS = 4096;
@@ -548,6 +551,31 @@ SOS_HD float strato_lut_at(const Optics& o, int i, float f, int w) {
     return a + f * (b - a);
 }
 
+// Tabulated tropospheric phase (TROPO_MIE), linear in u between the table's nodes (numpy_reference.tropo_phase,
+// numpy_reference.py:409-420; kernel.cu tropo_phase): position of u, value at a position, value at u.
+SOS_HD void tropo_lut_pos(const Optics& o, float u, int& i, float& f) {
+    const float x = (clampf(u, -1.0f, 1.0f) + 1.0f) * (0.5f * (float)o.tropo_bins);
+    i = (int)x;
+    i = i > o.tropo_bins - 1 ? o.tropo_bins - 1 : i;
+    f = x - (float)i;
+}
+
+SOS_HD float tropo_lut_at(const Optics& o, int i, float f, int w) {
+    if (o.tropo_lut2) {
+        const float2 p = o.tropo_lut2[(size_t)i * o.W + w];
+        return p.x + f * p.y;
+    }
+    const float a = o.tropo_lut[(size_t)i * o.W + w], b = o.tropo_lut[(size_t)(i + 1) * o.W + w];
+    return a + f * (b - a);
+}
+
+SOS_HD float tropo_phase_at(const Optics& o, float u, int w) {
+    int i;
+    float f;
+    tropo_lut_pos(o, u, i, f);
+    return tropo_lut_at(o, i, f, w);
+}
+
 // strato_lut_pos for u already in [-1, 1].
 SOS_HD void strato_lut_pos_clamped(float u, int& i, float& f) {
     const float x = (u + 1.0f) * (0.5f * STRATO_LUT_BINS);
@@ -581,19 +609,25 @@ SOS_HD void ground_sums(const Optics& o, const Node& n, int w0, int nw, float gr
                 const float m0 = n.mu * gd[2] + n.exd * gd[0];
                 const float m1 = aeyd * gd[1];
                 const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
-                const float ph = hg_pair(hk, up, dn);
-                int iu = 0, id = 0;
-                float fu = 0.0f, fd = 0.0f;
+                const float ph = o.tropo_bins ? 0.0f : hg_pair(hk, up, dn);
+                int iu = 0, id = 0, tu = 0, td = 0;
+                float fu = 0.0f, fd = 0.0f, gu = 0.0f, gd_ = 0.0f;
                 if (o.strato) {
                     strato_lut_pos(up, iu, fu);
                     strato_lut_pos(dn, id, fd);
+                }
+                if (o.tropo_bins) {
+                    tropo_lut_pos(o, up, tu, gu);
+                    tropo_lut_pos(o, dn, td, gd_);
                 }
                 for (int k = 0; k < NW; ++k) {
                     if (k >= nw) break;
                     const int w = w0 + k;
                     float gv = wc * o.gval[(size_t)gi * W + w];
                     if (merged) gv += wb * o.gval[(size_t)(gi + shift) * W + w];
-                    ground[k] += ph * gv;
+                    const float phw =
+                        o.tropo_bins ? (tropo_lut_at(o, tu, gu, w) + tropo_lut_at(o, td, gd_, w)) * 0.5f : ph;
+                    ground[k] += phw * gv;
                     if (o.strato) {
                         const float sph = (strato_lut_at(o, iu, fu, w) + strato_lut_at(o, id, fd, w)) * 0.5f;
                         sground[k] += sph * gv;
@@ -618,7 +652,8 @@ SOS_HD void first_light_value(const Optics& o, const RayConst& rc, const Node& n
     for (int k = 0; k < 5; ++k) optical += col[k] * o.ext[k * W + w];
     if (o.strato) optical += stc * o.strato_ext[w];
     const float sun = expf(-optical) * lit;
-    const float beam = (n.prof.v[1] * o.asca[w]) * (sun * phase + ground);
+    const float ph = o.tropo_bins ? tropo_phase_at(o, rc.d32[2], w) : phase;  // TROPO_MIE: the table, per wavelength
+    const float beam = (n.prof.v[1] * o.asca[w]) * (sun * ph + ground);
     const float ray_ = (sun * n.prof.v[0]) * o.ext[w];
     const float sbeam = o.strato ? (n.st_prof * o.strato_sca[w]) * (sun * sphase + sground) : 0.0f;
     for (int k = 0; k < 4; ++k) {

@@ -102,6 +102,7 @@ struct sosb_state {
     bool have_constants = false;
     // constants
     DevBuf h, chi, hr, ha, ext, asca, table, sun_h, sun_col, gm, goff, gdir, gval, rf, af, ext0;
+    DevBuf t_lut, t_lut2;  // tabulated tropospheric phase and its (value, step) pairs
     DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src, s_lut, s_lut2, gsame, gdir4;
     DevBuf sh_a, sh_b, sh_d;
     DevBuf u_hi, u_lo, wu_hi, wu_lo, uq_hi, uq_lo, wuq_hi, wuq_lo, box_ww, solar;
@@ -135,6 +136,8 @@ struct sosb_state {
     bool warm_history = false;  // sosb_solve_warm seeds the Anderson history with (0, fallback) (sosb_set_warm_history)
     int aer2_on = 0;     // two-layer tropospheric aerosol profile (sosb_constants.aer2)
     float aer2[7] = {};
+    int tropo_bins = 0;  // tabulated tropospheric phase (sosb_constants.tropo_lut), 0 for Henyey-Greenstein
+    int af_w = 0;        // af holds per-wavelength eigenvalues [K][W] (sosb_constants.tropo_eigen)
     int proj_mode = 0;   // projection form (sosb_set_projection): PROJ_FP32, PROJ_BF16X3, PROJ_TF32, PROJ_BF16
     int64_t launches = 0;
     // per-evaluation history of the last solve on this handle: [evaluation][W] observer and source relative changes
@@ -960,19 +963,25 @@ __global__ void __launch_bounds__(256)
                 const float m0 = dv.x * gd.z + dv.y * gd.x;
                 const float m1 = dv.z * gd.y;
                 const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
-                const float ph = hg_pair(hk, up, dn);
-                int iu = 0, id = 0;
-                float fu = 0.0f, fd = 0.0f;
+                const float ph = o.tropo_bins ? 0.0f : hg_pair(hk, up, dn);
+                int iu = 0, id = 0, tu = 0, td = 0;
+                float fu = 0.0f, fd = 0.0f, gu = 0.0f, gd_ = 0.0f;
                 if (o.strato) {
                     strato_lut_pos_clamped(up, iu, fu);
                     strato_lut_pos_clamped(dn, id, fd);
+                }
+                if (o.tropo_bins) {
+                    tropo_lut_pos(o, up, tu, gu);
+                    tropo_lut_pos(o, dn, td, gd_);
                 }
 #pragma unroll
                 for (int w = 0; w < WM; ++w) {
                     if (w >= W) break;
                     float gv = wc * o.gval[(size_t)gi * W + w];
                     if (merged) gv += wb * o.gval[(size_t)(gi + shift) * W + w];
-                    ground[w] += ph * gv;
+                    const float phw =
+                        o.tropo_bins ? (tropo_lut_at(o, tu, gu, w) + tropo_lut_at(o, td, gd_, w)) * 0.5f : ph;
+                    ground[w] += phw * gv;
                     if (o.strato) {
                         const float sph = (strato_lut_at(o, iu, fu, w) + strato_lut_at(o, id, fd, w)) * 0.5f;
                         sground[w] += sph * gv;
@@ -1075,7 +1084,10 @@ __global__ void __launch_bounds__(256)
                 const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
                 float gv = wc * o.gval[(size_t)gi * W + w];
                 if (merged) gv += wb * o.gval[(size_t)(gi + shift) * W + w];
-                ground += hg_pair(hk, up, dn) * gv;
+                const float ph = o.tropo_bins
+                                     ? (tropo_phase_at(o, up, w) + tropo_phase_at(o, dn, w)) * 0.5f
+                                     : hg_pair(hk, up, dn);
+                ground += ph * gv;
                 if (o.strato) {
                     int iu, id;
                     float fu, fd;
@@ -1100,8 +1112,10 @@ constexpr int GPW_WARPS = 8;
 __global__ void __launch_bounds__(GPW_WARPS * 32)
     ground_pairs_warp_kernel(Optics o, const float4* __restrict__ misc, const float4* __restrict__ dir,
                              const int* __restrict__ entries, const int* __restrict__ total, float2* g) {
-    // per staged direction: Henyey-Greenstein pair phase, the two table fractions and the two bins (16 bits each)
+    // per staged direction: Henyey-Greenstein pair phase, the two stratospheric table fractions and bins (16 bits
+    // each); with the tabulated tropospheric phase, its two fractions and bins in s_tro
     __shared__ float4 s_dir[GPW_WARPS][32];
+    __shared__ float4 s_tro[GPW_WARPS][32];
     const int W = o.W;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int items = *total;
@@ -1138,7 +1152,15 @@ __global__ void __launch_bounds__(GPW_WARPS * 32)
                         strato_lut_pos_clamped(up, iu, fu);
                         strato_lut_pos_clamped(dn, id, fd);
                     }
-                    s_dir[wid][lane] = make_float4(hg_pair(hk, up, dn), fu, fd, __int_as_float(iu | (id << 16)));
+                    if (o.tropo_bins) {
+                        int tu, td;
+                        float gu, gd_;
+                        tropo_lut_pos(o, up, tu, gu);
+                        tropo_lut_pos(o, dn, td, gd_);
+                        s_tro[wid][lane] = make_float4(gu, gd_, __int_as_float(tu), __int_as_float(td));
+                    }
+                    s_dir[wid][lane] =
+                        make_float4(o.tropo_bins ? 0.0f : hg_pair(hk, up, dn), fu, fd, __int_as_float(iu | (id << 16)));
                 }
                 __syncwarp();
                 const int cnt = min(32, g1 - base);
@@ -1147,10 +1169,15 @@ __global__ void __launch_bounds__(GPW_WARPS * 32)
                     const float4 sd = s_dir[wid][j];
                     const float hg = sd.x;
                     const int bins = __float_as_int(sd.w), iu = bins & 0xffff, id = bins >> 16;
+                    float4 st = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (o.tropo_bins) st = s_tro[wid][j];
                     if (w0 < W) {
                         float gv = wc * o.gval[(size_t)gj * W + w0];
                         if (merged) gv += wb * o.gval[(size_t)(gj + shift) * W + w0];
-                        ground0 += hg * gv;
+                        const float ph = o.tropo_bins ? (tropo_lut_at(o, __float_as_int(st.z), st.x, w0) +
+                                                         tropo_lut_at(o, __float_as_int(st.w), st.y, w0)) * 0.5f
+                                                      : hg;
+                        ground0 += ph * gv;
                         if (o.strato) {
                             const float sph = (strato_lut_at(o, iu, sd.y, w0) + strato_lut_at(o, id, sd.z, w0)) * 0.5f;
                             sground0 += sph * gv;
@@ -1159,7 +1186,10 @@ __global__ void __launch_bounds__(GPW_WARPS * 32)
                     if (w1 < W) {
                         float gv = wc * o.gval[(size_t)gj * W + w1];
                         if (merged) gv += wb * o.gval[(size_t)(gj + shift) * W + w1];
-                        ground1 += hg * gv;
+                        const float ph = o.tropo_bins ? (tropo_lut_at(o, __float_as_int(st.z), st.x, w1) +
+                                                         tropo_lut_at(o, __float_as_int(st.w), st.y, w1)) * 0.5f
+                                                      : hg;
+                        ground1 += ph * gv;
                         if (o.strato) {
                             const float sph = (strato_lut_at(o, iu, sd.y, w1) + strato_lut_at(o, id, sd.z, w1)) * 0.5f;
                             sground1 += sph * gv;
@@ -2205,7 +2235,7 @@ __global__ void add_kernel(const float* a, const float* b, float* out, int n) {
 __global__ void compose_kernel(const float* __restrict__ warm, const float* __restrict__ first, const float* __restrict__ x,
                                const float* __restrict__ rf, const float* __restrict__ af, const float* __restrict__ asca,
                                const float* __restrict__ ext0, const float* __restrict__ s_eigen,
-                               const float* __restrict__ s_sca, int K, int src, int W, long long n,
+                               const float* __restrict__ s_sca, int K, int src, int W, int af_w, long long n,
                                unsigned long long done_mask, const unsigned long long* __restrict__ done_dev,
                                float* __restrict__ out, unsigned* __restrict__ metrics) {
     __shared__ unsigned sm_bad[64], sm_mag[64], sm_dif[64];
@@ -2244,7 +2274,7 @@ __global__ void compose_kernel(const float* __restrict__ warm, const float* __re
         } else if (slot < 10 + K) {
             const int k = slot - 10;
             const float m = warm[mb + (size_t)(4 + k) * W] + first[mb + (size_t)(4 + k) * W];
-            v = (m * af[k]) * asca[w];
+            v = (m * af[af_w ? k * W + w : k]) * asca[w];  // af_w: per-wavelength eigenvalues [K][W] (TROPO_MIE)
         } else {
             const int k = slot - 10 - K;
             const float m = warm[mb + (size_t)(4 + k) * W] + first[mb + (size_t)(4 + k) * W];
@@ -2546,6 +2576,9 @@ static Optics optics_of(const sosb_state* s) {
     o.gdir4 = P<float4>(s->gdir4);
     o.aer2_on = s->aer2_on;
     for (int i = 0; i < 7; ++i) o.aer2[i] = s->aer2[i];
+    o.tropo_bins = s->tropo_bins;
+    o.tropo_lut = s->tropo_bins ? P<float>(s->t_lut) : nullptr;
+    o.tropo_lut2 = s->tropo_bins ? P<float2>(s->t_lut2) : nullptr;
     return o;
 }
 
@@ -3245,7 +3278,7 @@ static int apply_impl(sosb_state* s, const float* field, float* out, unsigned lo
     Timer timer(s, K_COMPOSE);
     compose_kernel<<<grid_for(n, wave_threads(d.W)), wave_threads(d.W), 0, s->stream>>>(
         P<float>(s->moments), P<float>(s->first_moments), field, P<float>(s->rf), P<float>(s->af), P<float>(s->asca),
-        P<float>(s->ext0), P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, done_mask, done_dev,
+        P<float>(s->ext0), P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, s->af_w, n, done_mask, done_dev,
         out,
         P<unsigned>(s->metrics));
     return launch_check(s);
@@ -3372,7 +3405,7 @@ int sosb_destroy(sosb_handle s) {
                       &s->ring_g[1], &s->ring_g[2], &s->ring_g[3], &s->ring_f[0], &s->ring_f[1], &s->ring_f[2],
                       &s->ring_f[3], &s->fl_val0, &s->fl_coef, &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off,
                       &s->fl_cursor, &s->fl_entries, &s->gr_off, &s->gr_loc, &s->gr_w, &s->gr_cols, &s->gr_cos,
-                      &s->gr_ok, &s->gr_value, &s->gr_cnt, &s->gr_cursor};
+                      &s->gr_ok, &s->gr_value, &s->gr_cnt, &s->gr_cursor, &s->t_lut, &s->t_lut2};
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
@@ -3507,7 +3540,19 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
     s->aer2_on = c->aer2 != nullptr;
     for (int i = 0; i < 7; ++i) s->aer2[i] = c->aer2 ? c->aer2[i] : 0.0f;
     TRY(dput(s, s->rf, c->rf, 6 * 4));
-    TRY(dput(s, s->af, c->af, K * 4));
+    s->af_w = c->tropo_eigen != nullptr;
+    TRY(dput(s, s->af, c->tropo_eigen ? c->tropo_eigen : c->af, (size_t)K * (s->af_w ? W : 1) * 4));
+    s->tropo_bins = 0;
+    if (c->tropo_lut) {
+        if (c->tropo_bins < 2 || c->tropo_bins > (1 << 24)) return fail(s, "E_CONSTANTS: tropo_bins %d", c->tropo_bins);
+        const size_t nb = (size_t)c->tropo_bins;
+        TRY(dput(s, s->t_lut, c->tropo_lut, (nb + 1) * W * 4));
+        std::vector<float2> lut2(nb * W);
+        for (size_t i = 0; i < nb * W; ++i)
+            lut2[i] = make_float2(c->tropo_lut[i], c->tropo_lut[i + W] - c->tropo_lut[i]);
+        TRY(dput_vec(s, s->t_lut2, lut2));
+        s->tropo_bins = c->tropo_bins;
+    }
     TRY(dput(s, s->ext0, c->ext0, W * 4));
     TRY(dput(s, s->solar, c->solar, W * 8));
     TRY(dput(s, s->box_ww, c->box_ww, d.box_points * 8));
@@ -4131,7 +4176,7 @@ int sosb_compose_static(sosb_handle s, const float* moments_dev, const float* fi
     const long long n = (long long)s->ns * s->src * d.W;
     compose_kernel<<<grid_for(n, wave_threads(d.W)), wave_threads(d.W), 0, s->stream>>>(
         moments_dev, first_moments_dev, x_dev, P<float>(s->rf), P<float>(s->af), P<float>(s->asca), P<float>(s->ext0),
-        P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, n, (unsigned long long)done_mask, nullptr,
+        P<float>(s->s_eigen), P<float>(s->s_sca_src), s->K, s->src, d.W, s->af_w, n, (unsigned long long)done_mask, nullptr,
         out_dev, scratch);
     TRY(launch_check(s));
     unsigned words[3 * SOSB_STATIC_WAVES];

@@ -105,8 +105,6 @@ def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
     L, K, W = s.kernel.L, s.kernel.K, s.W
     if c['domain'].top_km > 80.0:
         raise ValueError('E_DOMAIN: the extended top above 80 km is not packed')
-    if 'tropo_lut' in c:
-        raise ValueError('E_FLAGS: the tabulated tropospheric phase is not packed')
     u4, w4 = np.polynomial.legendre.leggauss(4)
     opt = c['density_optics']
     meta = dict(
@@ -121,8 +119,15 @@ def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
         u=np.asarray(c['u'], 'f8'), wu=np.asarray(c['wu'], 'f8'), uq=np.asarray(cq['u'], 'f8'),
         wuq=np.asarray(cq['wu'], 'f8'), h=c['h'], chi=c['chi'], hr=c['hr'], ha=c['ha'], ext=c['ext'], asca=c['asca'],
         sun_h=c['sun_h'], sun_col=c['sun_col'], gm=c['gm'], gd=c['gd'], gv=c['gv'],
-        density_table=np.asarray(opt['table'], 'f4'), rf=np.asarray(s.rf, 'f4'), af=np.asarray(s.af[:K], 'f4'),
+        density_table=np.asarray(opt['table'], 'f4'), rf=np.asarray(s.rf, 'f4'), af=np.asarray(s.af[:K] if s.af is not None else np.zeros(K), 'f4'),
         ext0=np.asarray(s.ext[0], 'f4'), solar=np.asarray(s.solar, 'f8'), box_ww=(w4[:, None] * w4[None, :] / 4).ravel())
+    if 'tropo_lut' in c:  # TROPO_MIE: the per-wavelength phase table and the SH eigenvalues chi_l / (2l + 1)
+        from sosfuse2.atmosphere.tropo_mie import eigen_by_sh as tropo_eigen
+
+        bins = int(c['tropo_bins'])
+        arrays['tropo_lut'] = np.asarray(c['tropo_lut'], 'f4').reshape(bins + 1, W)
+        arrays['tropo_eigen'] = np.asarray(tropo_eigen(s.tropo, L), 'f4')
+        meta['tropo_bins'] = bins
     if 'aer2' in c:  # AEROSOL_2L: the two-layer profile's kernel vector
         arrays['aer2'] = np.asarray(c['aer2'], 'f4')
         meta['aerosol_profile'] = 'two_layer'

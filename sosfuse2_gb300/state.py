@@ -119,6 +119,9 @@ class PackedState:
                         strato_sca_source=(a['strato_sca_source'], f4))
         if 'aer2' in a:
             spec.update(aer2=(a['aer2'], f4))
+        if 'tropo_lut' in a:
+            spec.update(tropo_lut=(a['tropo_lut'], f4), tropo_eigen=(a['tropo_eigen'], f4))
+            c.tropo_bins = len(a['tropo_lut']) - 1
         for name, (v, dt) in spec.items():
             arr = self._arr(v, dt)
             ct = dict((f[0], f[1]) for f in _abi.Constants._fields_)[name]

@@ -15,7 +15,7 @@ def pytest_configure(config):
 
 
 def fixture_names():
-    return [n for n in ('walk1', 'strato1', 'strato15', 'slow1', 'aer2') if (GOLDEN / f'{n}.npz').exists()]
+    return [n for n in ('walk1', 'strato1', 'strato15', 'slow1', 'aer2', 'mie1', 'mie15') if (GOLDEN / f'{n}.npz').exists()]
 
 
 @pytest.fixture(scope='session')

@@ -52,6 +52,13 @@ FIXTURES = dict(
     # AEROSOL_2L profile in the transport
     aer2=dict(strato=False, wavelengths=[550.0],
               blocks=dict(troposphere_profile=dict(status='enabled', model='two_layer'))),
+    # the walkthrough state with the tabulated tropospheric Mie phase (troposphere_phase block, the shipped rural
+    # table): the TROPO_MIE phase table in the first light and the per-wavelength eigenvalues in the composition; at
+    # 550 nm and over a 15-wavelength chunk (the many-wavelength kernels)
+    mie1=dict(strato=False, wavelengths=[550.0],
+              blocks=dict(troposphere_phase=dict(status='enabled', model='mie', optics_table='default'))),
+    mie15=dict(strato=False, wavelengths=(450.0 + 20.0 * np.arange(15)).tolist(),
+               blocks=dict(troposphere_phase=dict(status='enabled', model='mie', optics_table='default'))),
 )
 
 

@@ -40,6 +40,8 @@ extern "C" int host_transport(const sosb_dims* d, const sosb_constants* c, const
     o.sh_a = sa.data(); o.sh_b = sb.data(); o.sh_d = sdg.data();
     o.aer2_on = c->aer2 != nullptr;
     for (int i = 0; i < 7; ++i) o.aer2[i] = c->aer2 ? c->aer2[i] : 0.0f;
+    o.tropo_bins = c->tropo_lut ? c->tropo_bins : 0;
+    o.tropo_lut = c->tropo_lut;
     std::vector<float> lut;
     if (d->strato) {
         lut.resize((size_t)(STRATO_LUT_BINS + 1) * W);

