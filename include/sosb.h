@@ -160,6 +160,15 @@ int sosb_set_pairs(sosb_handle h, int enable);
  * accumulation in tensor memory), and the node pass reads each node's four corner values. 0: off (pair form).
  * E_TC_TIMEOUT when a tensor-core wait ran out. */
 int sosb_set_corner_mma(sosb_handle h, int enable);
+/* No reference counterpart (the first light's ground sums, numpy_reference.py:526-558, on CUDA cores there). Ground
+ * sums on the tensor cores (default on, more than four wavelengths, Henyey-Greenstein tropospheric phase): the items
+ * (node, corner pair) bucketed by the pair's first cell form, per tile of 128 items, [128 x directions] x [directions
+ * x W] products of the pair phases times the corner weights with the ground values (BF16 high and low parts, three
+ * products, FP32 accumulation in tensor memory); the stratospheric phase enters through the leading factors of its
+ * table over the wavelengths (rank chosen at sosb_set_constants so that every table row is within 2e-6 of its
+ * largest value; a table that needs more than 8 factors, or a tabulated tropospheric phase, keeps the CUDA-core
+ * kernel). 0: off (CUDA cores). E_TC_TIMEOUT when a tensor-core wait ran out. */
+int sosb_set_ground_mma(sosb_handle h, int enable);
 /* Replaces: Kernel.setup (source_solver.py:1243-1339) and constants_device (source_solver.py:2248). */
 int sosb_set_constants(sosb_handle h, const sosb_constants *c);
 /* Replaces: ray_geometry.upload_geometry / device_geometry (ray_geometry.py:205-287) of the cell bundle

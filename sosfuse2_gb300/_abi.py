@@ -113,6 +113,7 @@ SIGNATURES = {
     'sosb_solve': ([ctypes.c_void_p, c_int, c_dbl, ctypes.c_void_p, ctypes.c_void_p, c_int, ctypes.POINTER(Stats)],
                    c_int),
     'sosb_set_corner_mma': ([ctypes.c_void_p, c_int], c_int),
+    'sosb_set_ground_mma': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_warm_history': ([ctypes.c_void_p, c_int], c_int),
     'sosb_history': ([ctypes.c_void_p, c_int, P_i32, P_f64, P_f64], c_int),
     'sosb_compose_static': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,

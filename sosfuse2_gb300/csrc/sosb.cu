@@ -132,6 +132,10 @@ struct sosb_state {
     bool autotune = true;  // time the table launch shapes once per shape (sosb_set_autotune)
     bool pairs = true;     // corner SH by ray-cell pair contractions (sosb_set_pairs)
     bool corner_mma = true;  // corner SH values on the tensor cores, more than four wavelengths (sosb_set_corner_mma)
+    bool ground_mma = true;  // first-light ground sums on the tensor cores, more than four wavelengths
+    int g_rank = 0;          // factors of the stratospheric phase table (strato_factors); 0: none within tolerance
+    DevBuf g_su2, g_sv;      // their (value, step) table [STRATO_LUT_BINS][rank] and wavelength factors [rank][W]
+    DevBuf gt_cnt, gt_off, gt_cursor, gt_tile;  // tiles of the ground-sum buckets
     bool corner_used = false;  // a corner GEMM ran since the last check of its bounded waits
     bool warm_history = false;  // sosb_solve_warm seeds the Anderson history with (0, fallback) (sosb_set_warm_history)
     int aer2_on = 0;     // two-layer tropospheric aerosol profile (sosb_constants.aer2)
@@ -2083,6 +2087,213 @@ __global__ void __launch_bounds__(CORNER_THREADS)
     if (warp == 0) tcx::tmem_dealloc(tmem, tmem_cols);
 }
 
+// ------------------------------------------------------------------ first-light ground sums on the tensor cores
+// The ground sums of the items (node, corner pair) of one bucket (the pair's first cell ca; its second is ca + 1)
+// are products over the pair's ground directions k in [goff[ca], goff[ca + 2]), contiguous in the CSR:
+//   ground[item][w]  = sum_k hg_pair(item, k) wgt(item, k) gval[k][w]
+//   sground[item][w] = sum_k sum_r U_r(item, k) wgt(item, k) V_r[w] gval[k][w]
+// with wgt the corner weight of the side k belongs to and the stratospheric pair phase written as
+// (sph(up, w) + sph(dn, w)) / 2 = sum_r (U_r(up) + U_r(dn)) / 2 V_r[w], the leading factors of its table
+// (strato_factors). Each is a [items x directions] x [directions x W] product: A rows are built from the item's
+// direction and the ground directions, B from the ground values (times V_r), both split into BF16 high and low parts
+// (three MMAs, FP32 accumulation in tensor memory).
+constexpr int GTC_ROWS = 128;     // items per tile (the MMA's M)
+constexpr int GTC_THREADS = 256;  // two threads per row build the A tile
+constexpr int GTC_MAX_RANK = 8;   // most stratospheric phase factors the product takes
+
+struct GroundTc {
+    const int* entries;  // item codes node * 2 + pr, bucketed by the pair's first cell
+    const int4* tile;    // [tiles] (first cell ca, first item, items, 0)
+    const int* ntiles;   // number of tiles (device)
+    const float2* su2;   // [STRATO_LUT_BINS][rank] (value, next value - value) of the factors U_r on the table's grid
+    const float* sv;     // [rank][W] the factors V_r
+    int rank;
+};
+
+static size_t ground_tc_smem(int np) { return 1024 + 2 * 16384 + 2 * (size_t)np * 128 + 64; }
+
+// Tiles of at most GTC_ROWS items of one bucket: pass 0 counts each bucket's tiles, pass 1 writes them at the offsets
+// bucket_scan_kernel made of the counts.
+__global__ void ground_tiles_kernel(const int* __restrict__ off, int ns, int pass, int* cnt, const int* toff,
+                                    int4* tile) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ns; c += gridDim.x * blockDim.x) {
+        const int e0 = off[c], n = off[c + 1] - e0;
+        const int nt = (n + GTC_ROWS - 1) / GTC_ROWS;
+        if (pass == 0) {
+            cnt[c] = nt;
+            continue;
+        }
+        const int at = toff[c];
+        for (int i = 0; i < nt; ++i)
+            tile[at + i] = make_int4(c, e0 + i * GTC_ROWS, min(GTC_ROWS, n - i * GTC_ROWS), 0);
+    }
+}
+
+// One CTA per tile of 128 items of one bucket, one shared-memory stage; steps = (chunk of 64 directions) x (part:
+// 0 the Henyey-Greenstein product into accumulator 0, r + 1 the stratospheric factor r into accumulator 1). Per step
+// threads r and r + 128 build row r of the A tile (four 16-byte pieces each), all threads the B tile (np wavelength
+// rows), thread 0 issues the 12 MMAs (four K steps of 16, three products each) and commits them to the stage's
+// barrier, which the block waits on (bounded) before the next step rebuilds the stage. The epilogue (warps 0-3, one
+// tensor-memory lane quarter each) stores (ground, sground) of each valid row's np wavelengths.
+__global__ void __launch_bounds__(GTC_THREADS)
+    ground_tc_kernel(Optics o, const float4* __restrict__ misc, const float4* __restrict__ dir, GroundTc gt, int np,
+                     uint32_t idesc, uint32_t tmem_cols, float2* __restrict__ g) {
+    if ((int)blockIdx.x >= *gt.ntiles) return;  // the whole CTA leaves before any barrier or tensor-memory use
+    extern __shared__ uint8_t gtc_raw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(gtc_raw) + 1023) & ~(uintptr_t)1023);
+    uint8_t* const ahi = sm;
+    uint8_t* const alo = sm + 16384;
+    uint8_t* const bhi = sm + 32768;
+    uint8_t* const blo = bhi + np * 128;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(blo + np * 128);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int4 tile = gt.tile[blockIdx.x];
+    const int ca = tile.x, e0 = tile.y, ne = tile.z;
+    const int t = threadIdx.x, warp = t >> 5;
+    const int row = t & (GTC_ROWS - 1), half = t >> 7;
+    const int W = o.W;
+    if (t == 0) {
+        tcx::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tcx::tmem_alloc(tslot, tmem_cols);
+    // the row's item: its direction terms and corner weights (the arithmetic of ground_pairs_warp_kernel)
+    const bool valid = row < ne;
+    const int code = valid ? gt.entries[e0 + row] : 0;
+    float4 dv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float wa = 0.0f, wb = 0.0f;
+    if (valid) {
+        const long long node = code >> 1;
+        const int pr = code & 1;
+        const float4 ms = misc[node];
+        dv = dir[node];
+        const float ah = ms.x, ac = ms.y;
+        wa = pr ? ah * (1.0f - ac) : (1.0f - ah) * (1.0f - ac);
+        wb = pr ? ah * ac : (1.0f - ah) * ac;
+    }
+    const int k0 = o.goff[ca], k1 = o.goff[ca + 1], k2 = o.goff[ca + 2];
+    const int parts = 1 + (o.strato ? gt.rank : 0);
+    const int steps = (k2 - k0 + 63) / 64 * parts;
+    const HgPair hk = hg_pair_constants(o.g);
+    tcx::fence_before();
+    __syncthreads();
+    tcx::fence_after();
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+    for (int s = 0; s < steps && ok; ++s) {
+        const int ch = s / parts, part = s - ch * parts;
+        if (s > 0) {
+            // the MMAs of step s - 1 read the stage: wait for them before it is rebuilt
+            ok = tcx::mbar_wait(bar, (s - 1) & 1, 4u, &g_proj_error);
+            ok = __syncthreads_and(ok);
+            if (!ok) break;
+            tcx::fence_after();
+        }
+        const int kc = k0 + ch * 64;
+        const int r = part - 1;
+#pragma unroll
+        for (int pp = 0; pp < 4; ++pp) {
+            const int p = half * 4 + pp;
+            float x[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int k = kc + p * 8 + e;
+                float v = 0.0f;
+                if (valid && k < k2) {
+                    const float4 gd = o.gdir4[k];
+                    const float m0 = dv.x * gd.z + dv.y * gd.x;
+                    const float m1 = dv.z * gd.y;
+                    const float up = clampf(m0 + m1, -1.0f, 1.0f), dn = clampf(m0 - m1, -1.0f, 1.0f);
+                    float ph;
+                    if (part == 0) {
+                        ph = hg_pair(hk, up, dn);
+                    } else {
+                        int iu, id;
+                        float fu, fd;
+                        strato_lut_pos_clamped(up, iu, fu);
+                        strato_lut_pos_clamped(dn, id, fd);
+                        const float2 a = gt.su2[(size_t)iu * gt.rank + r], b = gt.su2[(size_t)id * gt.rank + r];
+                        ph = ((a.x + fu * a.y) + (b.x + fd * b.y)) * 0.5f;
+                    }
+                    v = ph * (k < k1 ? wa : wb);
+                }
+                x[e] = v;
+            }
+            __align__(16) __nv_bfloat162 h[4], lo[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                h[e] = __floats2bfloat162_rn(x[2 * e], x[2 * e + 1]);
+                const float2 hf = __bfloat1622float2(h[e]);
+                lo[e] = __floats2bfloat162_rn(x[2 * e] - hf.x, x[2 * e + 1] - hf.y);
+            }
+            *reinterpret_cast<uint4*>(ahi + tcx::sw128_offset(row, p)) = *reinterpret_cast<const uint4*>(h);
+            *reinterpret_cast<uint4*>(alo + tcx::sw128_offset(row, p)) = *reinterpret_cast<const uint4*>(lo);
+        }
+        // B tile: np rows (wavelengths) x 8 pieces; consecutive threads take consecutive wavelengths (coalesced)
+        for (int q = t; q < np * 8; q += GTC_THREADS) {
+            const int p = q / np, w = q - p * np;
+            const float vs = (part == 0 || w >= W) ? 1.0f : gt.sv[r * W + w];
+            __align__(16) __nv_bfloat16 h[8], lo[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int k = kc + p * 8 + e;
+                const float x = (w < W && k < k2) ? o.gval[(size_t)k * W + w] * vs : 0.0f;
+                h[e] = __float2bfloat16_rn(x);
+                lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
+            }
+            *reinterpret_cast<uint4*>(bhi + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(h);
+            *reinterpret_cast<uint4*>(blo + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(lo);
+        }
+        tcx::fence_proxy_async();
+        __syncthreads();
+        if (t == 0) {
+            tcx::fence_after();
+            const uint32_t ah = tcx::smem_u32(ahi), al = tcx::smem_u32(alo);
+            const uint32_t bh = tcx::smem_u32(bhi), bl = tcx::smem_u32(blo);
+            const uint32_t acc_col = part == 0 ? 0u : (uint32_t)np;
+            const bool fresh = ch == 0 && part <= 1;  // the first product into this accumulator
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                const uint32_t acc = (fresh && kk == 0) ? 0u : 1u;
+                tcx::mma_f16(tmem + acc_col, tcx::sw128_desc(ah + kk * 32), tcx::sw128_desc(bh + kk * 32), idesc, acc);
+                tcx::mma_f16(tmem + acc_col, tcx::sw128_desc(ah + kk * 32), tcx::sw128_desc(bl + kk * 32), idesc, 1u);
+                tcx::mma_f16(tmem + acc_col, tcx::sw128_desc(al + kk * 32), tcx::sw128_desc(bh + kk * 32), idesc, 1u);
+            }
+            tcx::mma_commit(bar);
+        }
+    }
+    if (ok && steps > 0) {
+        // the last commit covers every MMA issued before it
+        ok = tcx::mbar_wait(bar, (steps - 1) & 1, 4u, &g_proj_error);
+        ok = __syncthreads_and(ok);
+        tcx::fence_after();
+    }
+    if (ok && warp < 4) {
+        float2* dst = valid ? g + (size_t)code * W : nullptr;
+        if (steps == 0) {  // no ground directions: the accumulators were never written
+            if (valid)
+                for (int w = 0; w < W; ++w) dst[w] = make_float2(0.0f, 0.0f);
+        } else {
+            for (int c0 = 0; c0 < np; c0 += 16) {
+                float vg[16], vs[16];
+                tcx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, vg);  // warp-wide
+                if (parts > 1)
+                    tcx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(np + c0), vs);
+                else
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) vs[i] = 0.0f;
+                if (valid)
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
+                        if (c0 + i < W) dst[c0 + i] = make_float2(vg[i], vs[i]);
+            }
+        }
+    }
+    tcx::fence_before();
+    __syncthreads();
+    if (warp == 0) tcx::tmem_dealloc(tmem, tmem_cols);
+}
+
 // Warm pass from the node table and the corner values (many wavelengths): transport_pair_wave_kernel with each
 // corner's SH value read from V[node * 4 + corner][w] instead of summed from the pair contractions.
 __global__ void __launch_bounds__(PAIR_WAVE_WARPS * 32)
@@ -2949,6 +3160,32 @@ static int run_first_light_staged(sosb_state* s, BundleDev& b, const LaneInputs&
             ground_pairs_kernel<4><<<std::max(gb, 1), 256, 0, s->stream>>>(o, table.misc, fl.dir,
                                                                            P<int>(s->fl_entries),
                                                                            P<int>(s->fl_off) + s->ns, fl.g);
+    } else if (s->ground_mma && !s->tropo_bins && (!d.strato || s->g_rank > 0)) {
+        // tiles of the buckets on the device (no host round trip), then one CTA per tile; CTAs beyond the count
+        // leave at once (at most one partial tile per bucket above items / 128)
+        TRY(dalloc(s, s->gt_cnt, (size_t)(s->ns + 1) * sizeof(int)));
+        TRY(dalloc(s, s->gt_off, (size_t)(s->ns + 1) * sizeof(int)));
+        TRY(dalloc(s, s->gt_cursor, (size_t)(s->ns + 1) * sizeof(int)));
+        const long long max_tiles = (2 * nodes + GTC_ROWS - 1) / GTC_ROWS + s->ns;
+        TRY(dalloc(s, s->gt_tile, (size_t)max_tiles * sizeof(int4)));
+        const int tb = (s->ns + 255) / 256;
+        ground_tiles_kernel<<<tb, 256, 0, s->stream>>>(P<int>(s->fl_off), s->ns, 0, P<int>(s->gt_cnt), nullptr,
+                                                      nullptr);
+        TRY(launch_check(s));
+        bucket_scan_kernel<<<1, 1024, 0, s->stream>>>(P<int>(s->gt_cnt), s->ns, P<int>(s->gt_off),
+                                                       P<int>(s->gt_cursor));
+        TRY(launch_check(s));
+        ground_tiles_kernel<<<tb, 256, 0, s->stream>>>(P<int>(s->fl_off), s->ns, 1, nullptr, P<int>(s->gt_off),
+                                                      P<int4>(s->gt_tile));
+        TRY(launch_check(s));
+        const int np = (W + 15) / 16 * 16;
+        const int acc_cols = d.strato ? 2 * np : np;
+        const uint32_t cols = acc_cols <= 32 ? 32u : (acc_cols <= 64 ? 64u : 128u);
+        const GroundTc gt{P<int>(s->fl_entries), P<int4>(s->gt_tile), P<int>(s->gt_off) + s->ns,
+                          P<float2>(s->g_su2), P<float>(s->g_sv), s->g_rank};
+        ground_tc_kernel<<<(unsigned)max_tiles, GTC_THREADS, ground_tc_smem(np), s->stream>>>(
+            o, table.misc, fl.dir, gt, np, tcx::idesc_bf16(128, np), cols, fl.g);
+        s->corner_used = true;  // the bounded waits' flags are read by proj_check
     } else {
         const int gb = (int)std::min<long long>((2 * nodes + GPW_WARPS - 1) / GPW_WARPS, 152LL * 32);
         ground_pairs_warp_kernel<<<std::max(gb, 1), GPW_WARPS * 32, 0, s->stream>>>(
@@ -3189,7 +3426,8 @@ static int proj_check(sosb_state* s) {
     if (flags) {
         const unsigned zero = 0;
         CK(cudaMemcpyToSymbol(g_proj_error, &zero, sizeof zero));
-        return fail(s, "E_TC_TIMEOUT: a tensor-core wait ran out (flags %u: 1 projection, 2 corner values)", flags);
+        return fail(s, "E_TC_TIMEOUT: a tensor-core wait ran out (flags %u: 1 projection, 2 corner values, 4 ground sums)",
+                    flags);
     }
     return 0;
 }
@@ -3371,7 +3609,8 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
                              (const void*)transport_wave_kernel<false>, (const void*)transport_wave_kernel<true>,
                              (const void*)transport_warp_kernel<1, false>, (const void*)transport_warp_kernel<4, false>,
                              (const void*)transport_warp_kernel<1, true>, (const void*)transport_warp_kernel<4, true>,
-                             (const void*)corner_tc_kernel, (const void*)project_tc_kernel<PROJ_BF16X3>,
+                             (const void*)corner_tc_kernel, (const void*)ground_tc_kernel,
+                             (const void*)project_tc_kernel<PROJ_BF16X3>,
                              (const void*)project_tc_kernel<PROJ_TF32>, (const void*)project_tc_kernel<PROJ_BF16>};
         for (const void* fn : fns)
             if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
@@ -3405,7 +3644,8 @@ int sosb_destroy(sosb_handle s) {
                       &s->ring_g[1], &s->ring_g[2], &s->ring_g[3], &s->ring_f[0], &s->ring_f[1], &s->ring_f[2],
                       &s->ring_f[3], &s->fl_val0, &s->fl_coef, &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off,
                       &s->fl_cursor, &s->fl_entries, &s->gr_off, &s->gr_loc, &s->gr_w, &s->gr_cols, &s->gr_cos,
-                      &s->gr_ok, &s->gr_value, &s->gr_cnt, &s->gr_cursor, &s->t_lut, &s->t_lut2};
+                      &s->gr_ok, &s->gr_value, &s->gr_cnt, &s->gr_cursor, &s->t_lut, &s->t_lut2, &s->g_su2,
+                      &s->g_sv, &s->gt_cnt, &s->gt_off, &s->gt_cursor, &s->gt_tile};
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
@@ -3482,6 +3722,81 @@ static int put_ds(sosb_state* s, DevBuf& hi, DevBuf& lo, const double* v, int n)
     split_nodes(v, n, h, l);
     TRY(dput_vec(s, hi, h));
     return dput_vec(s, lo, l);
+}
+
+// Leading factors of a phase table lut[i][w] (rows i < n, W wavelengths): lut ~= U V with V's rows the eigenvectors
+// of lut^T lut of the largest eigenvalues (cyclic Jacobi in FP64) and U = lut V^T; the smallest rank r <= rmax whose
+// error in every row is at most tol times that row's largest magnitude (the phase varies over orders of magnitude in
+// u, little across wavelengths at one u). Returns r, 0 when no rank up to rmax is within tol.
+static int strato_factors(const std::vector<double>& lut, int n, int W, int rmax, double tol, std::vector<double>& U,
+                          std::vector<double>& V) {
+    std::vector<double> G((size_t)W * W, 0.0), E((size_t)W * W, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int a = 0; a < W; ++a)
+            for (int b = a; b < W; ++b) G[(size_t)a * W + b] += lut[(size_t)i * W + a] * lut[(size_t)i * W + b];
+    for (int a = 0; a < W; ++a) {
+        for (int b = 0; b < a; ++b) G[(size_t)a * W + b] = G[(size_t)b * W + a];
+        E[(size_t)a * W + a] = 1.0;
+    }
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0.0, diag = 0.0;
+        for (int a = 0; a < W; ++a) {
+            diag += G[(size_t)a * W + a] * G[(size_t)a * W + a];
+            for (int b = a + 1; b < W; ++b) off += G[(size_t)a * W + b] * G[(size_t)a * W + b];
+        }
+        if (off <= 1e-30 * diag) break;
+        for (int p = 0; p < W; ++p)
+            for (int q = p + 1; q < W; ++q) {
+                const double gpq = G[(size_t)p * W + q];
+                if (std::fabs(gpq) < 1e-300) continue;
+                const double theta = (G[(size_t)q * W + q] - G[(size_t)p * W + p]) / (2.0 * gpq);
+                const double tt = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(tt * tt + 1.0), sn = tt * c;
+                for (int k = 0; k < W; ++k) {  // G <- J^T G J, E <- E J
+                    const double gkp = G[(size_t)k * W + p], gkq = G[(size_t)k * W + q];
+                    G[(size_t)k * W + p] = c * gkp - sn * gkq;
+                    G[(size_t)k * W + q] = sn * gkp + c * gkq;
+                }
+                for (int k = 0; k < W; ++k) {
+                    const double gpk = G[(size_t)p * W + k], gqk = G[(size_t)q * W + k];
+                    G[(size_t)p * W + k] = c * gpk - sn * gqk;
+                    G[(size_t)q * W + k] = sn * gpk + c * gqk;
+                }
+                for (int k = 0; k < W; ++k) {
+                    const double ekp = E[(size_t)k * W + p], ekq = E[(size_t)k * W + q];
+                    E[(size_t)k * W + p] = c * ekp - sn * ekq;
+                    E[(size_t)k * W + q] = sn * ekp + c * ekq;
+                }
+            }
+    }
+    std::vector<int> order(W);
+    for (int a = 0; a < W; ++a) order[a] = a;
+    std::sort(order.begin(), order.end(),
+              [&](int x, int y) { return G[(size_t)x * W + x] > G[(size_t)y * W + y]; });
+    for (int r = 1; r <= std::min(rmax, W); ++r) {
+        V.assign((size_t)r * W, 0.0);
+        for (int j = 0; j < r; ++j)
+            for (int w = 0; w < W; ++w) V[(size_t)j * W + w] = E[(size_t)w * W + order[j]];
+        U.assign((size_t)n * r, 0.0);
+        bool within = true;
+        for (int i = 0; i < n && within; ++i) {
+            const double* row = &lut[(size_t)i * W];
+            double big = 0.0;
+            for (int w = 0; w < W; ++w) big = std::max(big, std::fabs(row[w]));
+            for (int j = 0; j < r; ++j) {
+                double u = 0.0;
+                for (int w = 0; w < W; ++w) u += row[w] * V[(size_t)j * W + w];
+                U[(size_t)i * r + j] = u;
+            }
+            for (int w = 0; w < W && within; ++w) {
+                double v = 0.0;
+                for (int j = 0; j < r; ++j) v += U[(size_t)i * r + j] * V[(size_t)j * W + w];
+                within = std::fabs(v - row[w]) <= tol * big;
+            }
+        }
+        if (within) return r;
+    }
+    return 0;
 }
 
 int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
@@ -3585,6 +3900,24 @@ int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
         for (size_t i = 0; i < (size_t)STRATO_LUT_BINS * W; ++i)
             lut2[i] = make_float2(lut[i], lut[i + W] - lut[i]);
         TRY(dput_vec(s, s->s_lut2, lut2));
+        // factors of the table for the tensor-core ground sums
+        std::vector<double> lut64((size_t)(STRATO_LUT_BINS + 1) * W);
+        for (size_t i = 0; i < lut64.size(); ++i) lut64[i] = lut[i];
+        std::vector<double> U, V;
+        s->g_rank = strato_factors(lut64, STRATO_LUT_BINS + 1, W, GTC_MAX_RANK, 2e-6, U, V);
+        if (s->g_rank > 0) {
+            const int R = s->g_rank;
+            std::vector<float2> su2((size_t)STRATO_LUT_BINS * R);
+            for (int i = 0; i < STRATO_LUT_BINS; ++i)
+                for (int r = 0; r < R; ++r) {
+                    const float a = (float)U[(size_t)i * R + r], b = (float)U[(size_t)(i + 1) * R + r];
+                    su2[(size_t)i * R + r] = make_float2(a, b - a);
+                }
+            std::vector<float> sv((size_t)R * W);
+            for (size_t i = 0; i < sv.size(); ++i) sv[i] = (float)V[i];
+            TRY(dput_vec(s, s->g_su2, su2));
+            TRY(dput_vec(s, s->g_sv, sv));
+        }
     }
     CK(cudaStreamSynchronize(s->stream));
     s->have_constants = true;
@@ -4924,6 +5257,14 @@ int sosb_set_pairs(sosb_handle s, int enable) {
 int sosb_set_warm_history(sosb_handle s, int enable) {
     if (!s) return 1;
     s->warm_history = enable != 0;
+    return 0;
+}
+
+int sosb_set_ground_mma(sosb_handle s, int enable) {
+    if (!s) return 1;
+    s->ground_mma = enable != 0;
+    s->have_first = false;  // the next apply recomputes its first light with the chosen kernel
+    graph_reset(s);
     return 0;
 }
 
