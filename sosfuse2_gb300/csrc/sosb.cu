@@ -1916,6 +1916,41 @@ __global__ void corner_entries_kernel(Optics o, Rays b, NodeTable tab, int nq, i
     }
 }
 
+// Pass 1 of the entries, one warp per ray, lanes over its nodes 32 at a time: the entries of one cell from one batch
+// take consecutive positions (one atomic per distinct cell and corner), so the rows of a tile that share a ray are
+// neighbours and a warp's loads of their basis rows hit few distinct addresses.
+__global__ void corner_entries_fill_kernel(Optics o, Rays b, NodeTable tab, int nq, int* cursor, int* e_ray,
+                                           float* e_cp, int* e_slot) {
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long ray = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < b.nray; ray += nwarps) {
+        const int s0 = b.seg_off[ray];
+        const long long node0 = (long long)s0 * nq;
+        const int nn = (b.seg_off[ray + 1] - s0) * nq;
+        for (int base = 0; base < nn; base += 32) {
+            const int i = base + lane;
+            const bool act = i < nn;
+            const float4 ms = act ? tab.misc[node0 + i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const int pk = __float_as_int(ms.w);
+            const int cell0 = (pk >> 16) * o.nc + (pk & 0xffff);
+            for (int c = 0; c < 4; ++c) {
+                const int cell = act ? cell0 + (c & 1) + (c >> 1) * o.nc : -1;
+                const unsigned peers = __match_any_sync(FULL_MASK, cell);
+                const int leader = __ffs(peers) - 1;
+                int at = 0;
+                if (act && lane == leader) at = atomicAdd(&cursor[cell], __popc(peers));
+                at = __shfl_sync(FULL_MASK, at, leader);
+                if (act) {
+                    const int k = at + __popc(peers & ((1u << lane) - 1u));
+                    e_ray[k] = (int)ray;
+                    e_cp[k] = ms.z;
+                    e_slot[k] = (int)((node0 + i) * 4 + c);
+                }
+            }
+        }
+    }
+}
+
 constexpr int CORNER_ROWS = 128;     // entries per tile (the MMA's M)
 constexpr int CORNER_THREADS = 256;  // two threads per row build the A tile (four 16-byte pieces each)
 constexpr int CORNER_STAGES = 1;     // shared-memory stages of the A and B tiles
@@ -2955,9 +2990,8 @@ static int build_corners(sosb_state* s, BundleDev& b, int nq) {
     TRY(dalloc(s, b.c_ray, (size_t)entries * sizeof(int)));
     TRY(dalloc(s, b.c_cp, (size_t)entries * sizeof(float)));
     TRY(dalloc(s, b.c_slot, (size_t)entries * sizeof(int)));
-    corner_entries_kernel<<<blocks, 128, 0, s->stream>>>(optics_of(s), rays_of(b), tab, nq, 1, nullptr,
-                                                        P<int>(cursor), P<int>(b.c_ray), P<float>(b.c_cp),
-                                                        P<int>(b.c_slot));
+    corner_entries_fill_kernel<<<(unsigned)std::min<int64_t>((nray + 3) / 4, 152LL * 64), 128, 0, s->stream>>>(
+        optics_of(s), rays_of(b), tab, nq, P<int>(cursor), P<int>(b.c_ray), P<float>(b.c_cp), P<int>(b.c_slot));
     TRY(launch_check(s));
     std::vector<int> hoff(ns + 1);
     CK(cudaMemcpyAsync(hoff.data(), off.p, (size_t)(ns + 1) * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
