@@ -508,6 +508,7 @@ struct LaneInputs {
     int nq;
     int first;
     int kp;
+    int table_only;         // write the node table only (no radiance): the corner path computes the values after it
 };
 
 // Henyey-Greenstein phase (per sr) of the pair of scattering cosines (up, dn), averaged:

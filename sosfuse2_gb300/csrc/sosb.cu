@@ -501,7 +501,8 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
     float* Y = recs + 32 * REC_WORDS + 4 * L1 * 32;  // this ray's SH basis, shared by the warp
     RayConst rc;
     ray_constants(b, ray, rc);
-    if (in.first == 0) {
+    const bool values = !in.table_only;
+    if (in.first == 0 && values) {
         for (int m = lane; m <= o.L; m += 32) sh_basis_column(o, rc.d32[2], rc.st, m, Y);
         __syncwarp();
     }
@@ -584,6 +585,13 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
             beta0 = beta1;
             const float att = R->ds * expf(-((tau - tauc) + acc));
             if (tab.att && wok) tab.att[((long long)s0 * nq + base + j) * o.W + w] = att;
+            if (!values) {  // table only: the optical-depth prefix and nothing else
+                if (flags & 2) {
+                    acc = acc + R->wpc * ((beta0 + ext6(o, R->pb, wl)) + 4.0f * ext6(o, R->pmc, wl));
+                    kahan(tau, tauc, acc);
+                }
+                continue;
+            }
             Node n;
             n.r = DS{R->r_h, R->r_l};
             n.qz = DS{R->qz_h, R->qz_l};
@@ -643,7 +651,7 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
             }
         }
     }
-    if (wok && !PREP) {
+    if (wok && !PREP && values) {
         boundary_term(o, b, rc, in.boundary, ray, w, total);
         rad[(size_t)ray * o.W + w] = make_float4(total[0], total[1], total[2], total[3]);
     }
@@ -3280,6 +3288,7 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
         if (done) return 0;
     }
     const FirstLightBufs no_fl{nullptr, nullptr, nullptr, nullptr};
+    bool table_only = false;
     if (d.W <= 4) {
         // sample-parallel: one warp per ray
         const long long blocks = (nray * 32 + TRANSPORT_THREADS - 1) / TRANSPORT_THREADS;
@@ -3360,15 +3369,27 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
                                     : (d.L == 32 ? transport_table_wave_kernel<32> : transport_table_wave_kernel<0>);
             kernel<<<(unsigned)blocks, WAVE_WARPS * 32, table_wave_smem(d.L), s->stream>>>(
                 optics_of(s), rays_of(b), in, table, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
-        } else
+        } else {
+            // a warm launch that writes the table: with the corner values on the tensor cores it writes the table
+            // only, then the bundle's corner entries are built and the launch is served by the corner path below
+            LaneInputs win = in;
+            win.table_only = write.frame && !first && s->corner_mma ? 1 : 0;
+            table_only = win.table_only != 0;
             transport_wave_kernel<false><<<(unsigned)blocks, WAVE_WARPS * 32, wave_smem(d.L), s->stream>>>(
-                optics_of(s), rays_of(b), in, write, no_fl, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
+                optics_of(s), rays_of(b), win, write, no_fl, (int)ray0, (int)nray, wchunks, P<float4>(s->rad));
+        }
     }
     TRY(launch_check(s));
     if (write.frame) {
         b.t_valid = true;
         if (!b.c_valid) TRY(build_corners(s, b, in.nq));
+        if (table_only && !b.c_valid) {
+            // no room for the corner entries: the pairs or the per-lane synthesis from the table serve the launch
+            if (!b.p_valid) TRY(build_pairs(s, b, in.nq));
+            return run_transport(s, b, ray0, nray, field, boundary, first, query);
+        }
         if (!b.c_valid && !b.p_valid) TRY(build_pairs(s, b, in.nq));
+        if (table_only) return run_transport(s, b, ray0, nray, field, boundary, first, query);
     }
     return 0;
 }
