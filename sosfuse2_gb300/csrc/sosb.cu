@@ -1965,17 +1965,20 @@ constexpr int CORNER_STAGES = 1;     // shared-memory stages of the A and B tile
 
 static size_t corner_tc_smem(int np, int L) {
     // CORNER_STAGES stages of A high/low tiles (2 x 16 KB) and B high/low tiles (2 x np rows of 128 bytes), cos(m phi)
-    // rows, the stages' barriers and the tensor-memory slot; 1 KB of alignment slack
-    return 1024 + CORNER_STAGES * (2 * 16384 + 2 * (size_t)np * 128) + (size_t)CORNER_ROWS * (L + 1) * 4 + 64;
+    // rows, the rows' rays, the order m of every coefficient (bytes, rounded up to 16), the stages' barriers and the
+    // tensor-memory slot; 1 KB of alignment slack
+    const size_t K = (size_t)(L + 1) * (L + 2) / 2;
+    return 1024 + CORNER_STAGES * (2 * 16384 + 2 * (size_t)np * 128) + (size_t)CORNER_ROWS * (L + 1) * 4 +
+           CORNER_ROWS * 4 + ((K + 15) & ~(size_t)15) + 64;
 }
 
-// One CTA per tile of 128 entries of one corner cell, chunks of 64 SH coefficients in two shared-memory stages: the
-// block builds chunk ch (row r of the A tile, B[entry][k] split into BF16 high and low parts, by threads r and
-// r + 128, four pieces of 8 coefficients each; the B tile, the cell's plane for np wavelength rows, split likewise;
-// both in the 128-byte swizzle) while the MMAs of chunk ch - 1 run; one thread issues the 12 MMAs of a chunk (four K
+// One CTA per tile of 128 entries of one corner cell, chunks of 64 SH coefficients in CORNER_STAGES shared-memory
+// stages: the block builds chunk ch (the A tile a row per warp at a time, lanes over the row's coefficients: the
+// entry's basis row times its cos(m phi), split into BF16 high and low parts; the B tile, the cell's plane for np
+// wavelength rows, split likewise; both in the 128-byte swizzle); one thread issues the 12 MMAs of a chunk (four K
 // steps of 16, three products each) and commits them to the stage's barrier, which the block waits on (bounded)
-// before it rebuilds that stage two chunks later. The epilogue (warps 0-3, one TMEM lane quarter each) stores each
-// row's np FP32 values at its slot.
+// before it rebuilds that stage. The epilogue (warps 0-3, one TMEM lane quarter each) stores each row's np FP32
+// values at its slot.
 __global__ void __launch_bounds__(CORNER_THREADS)
     corner_tc_kernel(Optics o, CornerEntries ce, const float* __restrict__ y_tab, int kp,
                      const float* __restrict__ plane, int np, uint32_t idesc, uint32_t tmem_cols,
@@ -1985,7 +1988,9 @@ __global__ void __launch_bounds__(CORNER_THREADS)
     const size_t stage_bytes = 2 * 16384 + 2 * (size_t)np * 128;  // stage st: A high, A low, B high, B low
     float* cm = reinterpret_cast<float*>(sm + CORNER_STAGES * stage_bytes);  // [CORNER_ROWS][L + 1]
     const int L1 = o.L + 1;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(cm + CORNER_ROWS * L1);  // [stages], 8-byte aligned: L1 * 512 bytes
+    int* rays_s = reinterpret_cast<int*>(cm + CORNER_ROWS * L1);  // [CORNER_ROWS] the rows' rays
+    uint8_t* mk = reinterpret_cast<uint8_t*>(rays_s + CORNER_ROWS);  // [K] the order m of each coefficient
+    uint64_t* bar = reinterpret_cast<uint64_t*>(mk + ((o.K + 15) & ~15));  // [stages], 8-byte aligned
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + CORNER_STAGES);
     const int4 tile = ce.tile[blockIdx.x];
     const int cell = tile.x, e0 = tile.y, ne = tile.z;
@@ -1999,8 +2004,8 @@ __global__ void __launch_bounds__(CORNER_THREADS)
     if (warp == 0) tcx::tmem_alloc(tslot, tmem_cols);
     // the row's entry: its ray and its cos(m phi) series (the Chebyshev recurrence of azimuth_sum)
     const bool valid = row < ne;
-    const int ray = valid ? ce.ray[e0 + row] : 0;
     if (half == 0) {
+        rays_s[row] = valid ? ce.ray[e0 + row] : 0;
         const float cpv = valid ? clampf(ce.cp[e0 + row], -1.0f, 1.0f) : 0.0f;
         float* crow = cm + row * L1;
         float c0 = 1.0f, c1 = cpv;
@@ -2013,13 +2018,18 @@ __global__ void __launch_bounds__(CORNER_THREADS)
             crow[m] = valid ? c2 : 0.0f;
         }
     }
+    for (int k = t; k < K; k += CORNER_THREADS) {  // k = l (l + 1) / 2 + m
+        int l = (int)((sqrtf(8.0f * k + 1.0f) - 1.0f) * 0.5f);
+        while ((l + 1) * (l + 2) / 2 <= k) ++l;
+        while (l * (l + 1) / 2 > k) --l;
+        mk[k] = (uint8_t)(k - l * (l + 1) / 2);
+    }
     tcx::fence_before();
     __syncthreads();
     tcx::fence_after();
     const uint32_t tmem = *tslot;
-    const float* yr = y_tab + (size_t)ray * kp;
-    const float* crow = cm + row * L1;
     const float* pc = plane + (size_t)cell * K * W;
+    const int lane = t & 31;
     const int nchunk = (K + 63) / 64;
     bool ok = true;
     for (int ch = 0; ch < nchunk && ok; ++ch) {
@@ -2036,45 +2046,29 @@ __global__ void __launch_bounds__(CORNER_THREADS)
             tcx::fence_after();
         }
         const int k0 = ch * 64;
-        // A row `row`, pieces 4 half .. 4 half + 3; m of each coefficient by stepping (l, m) from the first one
+        // A tile: warp `warp` builds rows warp, warp + 8, ...; lane l takes coefficients k0 + 2l and k0 + 2l + 1 of
+        // the row (one coalesced 8-byte load per lane from the row's basis row), times cos(m phi) of the row, split
+        // into BF16 high and low parts, one 4-byte store per lane and part: a warp writes one 128-byte tile row
         {
-            const int kb0 = k0 + half * 32;
-            int l = (int)((sqrtf(8.0f * kb0 + 1.0f) - 1.0f) * 0.5f);
-            while ((l + 1) * (l + 2) / 2 <= kb0) ++l;
-            while (l * (l + 1) / 2 > kb0) --l;
-            int m = kb0 - l * (l + 1) / 2;
-#pragma unroll
-            for (int pp = 0; pp < 4; ++pp) {
-                const int p = half * 4 + pp;
-                const int kb = k0 + p * 8;
-                float v[8];
-                if (valid && kb + 8 <= K) {
-                    const float4 y0 = *reinterpret_cast<const float4*>(yr + kb);
-                    const float4 y1 = *reinterpret_cast<const float4*>(yr + kb + 4);
-                    v[0] = y0.x; v[1] = y0.y; v[2] = y0.z; v[3] = y0.w;
-                    v[4] = y1.x; v[5] = y1.y; v[6] = y1.z; v[7] = y1.w;
-                } else {
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) v[e] = (valid && kb + e < K) ? yr[kb + e] : 0.0f;
+            const int ka = k0 + 2 * lane;
+            const int ma = ka < K ? mk[ka] : 0, mb = ka + 1 < K ? mk[ka + 1] : 0;
+            const int piece = lane >> 2, sub = (lane & 3) * 4;
+            for (int r = warp; r < CORNER_ROWS; r += CORNER_THREADS / 32) {
+                float2 y = make_float2(0.0f, 0.0f);
+                if (r < ne) {
+                    const float* yr = y_tab + (size_t)rays_s[r] * kp;
+                    if (ka + 1 < K)
+                        y = *reinterpret_cast<const float2*>(yr + ka);
+                    else if (ka < K)
+                        y.x = yr[ka];
                 }
-                float x[8];
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    x[e] = v[e] * crow[m < L1 ? m : 0];
-                    if (++m > l) {
-                        ++l;
-                        m = 0;
-                    }
-                }
-                __align__(16) __nv_bfloat162 h[4], lo[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {  // high parts two at a time, then the low parts of the remainders
-                    h[e] = __floats2bfloat162_rn(x[2 * e], x[2 * e + 1]);
-                    const float2 hf = __bfloat1622float2(h[e]);
-                    lo[e] = __floats2bfloat162_rn(x[2 * e] - hf.x, x[2 * e + 1] - hf.y);
-                }
-                *reinterpret_cast<uint4*>(ahi + tcx::sw128_offset(row, p)) = *reinterpret_cast<const uint4*>(h);
-                *reinterpret_cast<uint4*>(alo + tcx::sw128_offset(row, p)) = *reinterpret_cast<const uint4*>(lo);
+                const float* cr = cm + r * L1;
+                const float x0 = y.x * cr[ma], x1 = y.y * cr[mb];
+                const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+                const float2 hf = __bfloat1622float2(h);
+                const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+                *reinterpret_cast<__nv_bfloat162*>(ahi + tcx::sw128_offset(r, piece) + sub) = h;
+                *reinterpret_cast<__nv_bfloat162*>(alo + tcx::sw128_offset(r, piece) + sub) = lo;
             }
         }
         // B tile: np rows (wavelengths) x 8 pieces; consecutive threads take consecutive wavelengths (coalesced)
