@@ -1962,6 +1962,7 @@ __global__ void corner_entries_fill_kernel(Optics o, Rays b, NodeTable tab, int 
 constexpr int CORNER_ROWS = 128;     // entries per tile (the MMA's M)
 constexpr int CORNER_THREADS = 256;  // two threads per row build the A tile (four 16-byte pieces each)
 constexpr int CORNER_STAGES = 1;     // shared-memory stages of the A and B tiles
+constexpr int CORNER_ROW_BATCH = 8;  // A-tile rows whose basis loads a warp issues together (16 rows a warp)
 
 static size_t corner_tc_smem(int np, int L) {
     // CORNER_STAGES stages of A high/low tiles (2 x 16 KB) and B high/low tiles (2 x np rows of 128 bytes), cos(m phi)
@@ -1979,7 +1980,7 @@ static size_t corner_tc_smem(int np, int L) {
 // steps of 16, three products each) and commits them to the stage's barrier, which the block waits on (bounded)
 // before it rebuilds that stage. The epilogue (warps 0-3, one TMEM lane quarter each) stores each row's np FP32
 // values at its slot.
-__global__ void __launch_bounds__(CORNER_THREADS)
+__global__ void __launch_bounds__(CORNER_THREADS, 4)
     corner_tc_kernel(Optics o, CornerEntries ce, const float* __restrict__ y_tab, int kp,
                      const float* __restrict__ plane, int np, uint32_t idesc, uint32_t tmem_cols,
                      float* __restrict__ out) {
@@ -2048,27 +2049,39 @@ __global__ void __launch_bounds__(CORNER_THREADS)
         const int k0 = ch * 64;
         // A tile: warp `warp` builds rows warp, warp + 8, ...; lane l takes coefficients k0 + 2l and k0 + 2l + 1 of
         // the row (one coalesced 8-byte load per lane from the row's basis row), times cos(m phi) of the row, split
-        // into BF16 high and low parts, one 4-byte store per lane and part: a warp writes one 128-byte tile row
+        // into BF16 high and low parts, one 4-byte store per lane and part: a warp writes one 128-byte tile row. The
+        // loads of CORNER_ROW_BATCH rows are issued before any is used.
         {
+            constexpr int WARPS = CORNER_THREADS / 32;
             const int ka = k0 + 2 * lane;
             const int ma = ka < K ? mk[ka] : 0, mb = ka + 1 < K ? mk[ka + 1] : 0;
             const int piece = lane >> 2, sub = (lane & 3) * 4;
-            for (int r = warp; r < CORNER_ROWS; r += CORNER_THREADS / 32) {
-                float2 y = make_float2(0.0f, 0.0f);
-                if (r < ne) {
-                    const float* yr = y_tab + (size_t)rays_s[r] * kp;
-                    if (ka + 1 < K)
-                        y = *reinterpret_cast<const float2*>(yr + ka);
-                    else if (ka < K)
-                        y.x = yr[ka];
+#pragma unroll 1
+            for (int r0 = warp; r0 < CORNER_ROWS; r0 += WARPS * CORNER_ROW_BATCH) {
+                float2 y[CORNER_ROW_BATCH];
+#pragma unroll
+                for (int u = 0; u < CORNER_ROW_BATCH; ++u) {
+                    const int r = r0 + u * WARPS;
+                    y[u] = make_float2(0.0f, 0.0f);
+                    if (r < ne) {
+                        const float* yr = y_tab + (size_t)rays_s[r] * kp;
+                        if (ka + 1 < K)
+                            y[u] = *reinterpret_cast<const float2*>(yr + ka);
+                        else if (ka < K)
+                            y[u].x = yr[ka];
+                    }
                 }
-                const float* cr = cm + r * L1;
-                const float x0 = y.x * cr[ma], x1 = y.y * cr[mb];
-                const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-                const float2 hf = __bfloat1622float2(h);
-                const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
-                *reinterpret_cast<__nv_bfloat162*>(ahi + tcx::sw128_offset(r, piece) + sub) = h;
-                *reinterpret_cast<__nv_bfloat162*>(alo + tcx::sw128_offset(r, piece) + sub) = lo;
+#pragma unroll
+                for (int u = 0; u < CORNER_ROW_BATCH; ++u) {
+                    const int r = r0 + u * WARPS;
+                    const float* cr = cm + r * L1;
+                    const float x0 = y[u].x * cr[ma], x1 = y[u].y * cr[mb];
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+                    const float2 hf = __bfloat1622float2(h);
+                    const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+                    *reinterpret_cast<__nv_bfloat162*>(ahi + tcx::sw128_offset(r, piece) + sub) = h;
+                    *reinterpret_cast<__nv_bfloat162*>(alo + tcx::sw128_offset(r, piece) + sub) = lo;
+                }
             }
         }
         // B tile: np rows (wavelengths) x 8 pieces; consecutive threads take consecutive wavelengths (coalesced)
