@@ -1966,11 +1966,11 @@ constexpr int CORNER_ROW_BATCH = 8;  // A-tile rows whose basis loads a warp iss
 
 static size_t corner_tc_smem(int np, int L) {
     // CORNER_STAGES stages of A high/low tiles (2 x 16 KB) and B high/low tiles (2 x np rows of 128 bytes), cos(m phi)
-    // rows, the rows' rays, the order m of every coefficient (bytes, rounded up to 16), the stages' barriers and the
-    // tensor-memory slot; 1 KB of alignment slack
+    // rows, the rows' rays and output slots, the order m of every coefficient (bytes, rounded up to 16), the stages'
+    // barriers and the tensor-memory slot; 1 KB of alignment slack
     const size_t K = (size_t)(L + 1) * (L + 2) / 2;
     return 1024 + CORNER_STAGES * (2 * 16384 + 2 * (size_t)np * 128) + (size_t)CORNER_ROWS * (L + 1) * 4 +
-           CORNER_ROWS * 4 + ((K + 15) & ~(size_t)15) + 64;
+           2 * CORNER_ROWS * 4 + ((K + 15) & ~(size_t)15) + 64;
 }
 
 // One CTA per tile of 128 entries of one corner cell, chunks of 64 SH coefficients in CORNER_STAGES shared-memory
@@ -1978,8 +1978,8 @@ static size_t corner_tc_smem(int np, int L) {
 // entry's basis row times its cos(m phi), split into BF16 high and low parts; the B tile, the cell's plane for np
 // wavelength rows, split likewise; both in the 128-byte swizzle); one thread issues the 12 MMAs of a chunk (four K
 // steps of 16, three products each) and commits them to the stage's barrier, which the block waits on (bounded)
-// before it rebuilds that stage. The epilogue (warps 0-3, one TMEM lane quarter each) stores each row's np FP32
-// values at its slot.
+// before it rebuilds that stage. The epilogue moves the rows through shared memory and writes each row's W FP32
+// values at its slot, lanes over the wavelengths.
 __global__ void __launch_bounds__(CORNER_THREADS, 4)
     corner_tc_kernel(Optics o, CornerEntries ce, const float* __restrict__ y_tab, int kp,
                      const float* __restrict__ plane, int np, uint32_t idesc, uint32_t tmem_cols,
@@ -1990,7 +1990,8 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
     float* cm = reinterpret_cast<float*>(sm + CORNER_STAGES * stage_bytes);  // [CORNER_ROWS][L + 1]
     const int L1 = o.L + 1;
     int* rays_s = reinterpret_cast<int*>(cm + CORNER_ROWS * L1);  // [CORNER_ROWS] the rows' rays
-    uint8_t* mk = reinterpret_cast<uint8_t*>(rays_s + CORNER_ROWS);  // [K] the order m of each coefficient
+    int* slots_s = rays_s + CORNER_ROWS;                              // [CORNER_ROWS] the rows' output slots
+    uint8_t* mk = reinterpret_cast<uint8_t*>(slots_s + CORNER_ROWS);  // [K] the order m of each coefficient
     uint64_t* bar = reinterpret_cast<uint64_t*>(mk + ((o.K + 15) & ~15));  // [stages], 8-byte aligned
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + CORNER_STAGES);
     const int4 tile = ce.tile[blockIdx.x];
@@ -2007,6 +2008,7 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
     const bool valid = row < ne;
     if (half == 0) {
         rays_s[row] = valid ? ce.ray[e0 + row] : 0;
+        slots_s[row] = valid ? ce.slot[e0 + row] : 0;
         const float cpv = valid ? clampf(ce.cp[e0 + row], -1.0f, 1.0f) : 0.0f;
         float* crow = cm + row * L1;
         float c0 = 1.0f, c1 = cpv;
@@ -2121,19 +2123,26 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
         ok = __syncthreads_and(ok);
         tcx::fence_after();
     }
+    // epilogue: warps 0-3 (one tensor-memory lane quarter each) move the rows into shared memory (stage 0, free once
+    // the last MMAs are done; row stride np + 1 keeps the lanes' stores on distinct banks), then every warp writes
+    // whole rows at their slots, lanes over the wavelengths (coalesced)
+    float* stage = reinterpret_cast<float*>(sm);
+    const int sp = np + 1;
     if (ok && warp < 4) {
-        float* dst = valid ? out + (size_t)ce.slot[e0 + row] * W : nullptr;
         for (int c0 = 0; c0 < np; c0 += 16) {
             float v[16];
             tcx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);  // warp-wide
-            if (valid)
 #pragma unroll
-                for (int i = 0; i < 16; ++i)
-                    if (c0 + i < W) dst[c0 + i] = v[i];
+            for (int i = 0; i < 16; ++i) stage[row * sp + c0 + i] = v[i];
         }
     }
     tcx::fence_before();
     __syncthreads();
+    if (ok)
+        for (int r = warp; r < ne; r += CORNER_THREADS / 32) {
+            float* dst = out + (size_t)slots_s[r] * W;
+            for (int w = lane; w < W; w += 32) dst[w] = stage[r * sp + w];
+        }
     if (warp == 0) tcx::tmem_dealloc(tmem, tmem_cols);
 }
 
