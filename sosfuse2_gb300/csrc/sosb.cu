@@ -2033,6 +2033,12 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
     const uint32_t tmem = *tslot;
     const float* pc = plane + (size_t)cell * K * W;
     const int lane = t & 31;
+    int bt_p[2], bt_w[2];  // this thread's B-tile tasks q = t, t + CORNER_THREADS of np * 8 (piece -1: none)
+    for (int i = 0; i < 2; ++i) {
+        const int q = t + i * CORNER_THREADS;
+        bt_p[i] = q < np * 8 ? q / np : -1;
+        bt_w[i] = q < np * 8 ? q - bt_p[i] * np : 0;
+    }
     const int nchunk = (K + 63) / 64;
     bool ok = true;
     for (int ch = 0; ch < nchunk && ok; ++ch) {
@@ -2043,7 +2049,9 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
         uint8_t* const blo = bhi + np * 128;
         if (ch >= CORNER_STAGES) {
             // the MMAs of chunk ch - CORNER_STAGES read this stage: wait for them before it is rebuilt
-            ok = tcx::mbar_wait(&bar[st], ((ch - CORNER_STAGES) / CORNER_STAGES) & 1, 2u, &g_proj_error);
+            // one thread waits (bounded) on the barrier, the block on it
+            const unsigned parity = ((ch - CORNER_STAGES) / CORNER_STAGES) & 1;
+            ok = t == 0 ? tcx::mbar_wait(&bar[st], parity, 2u, &g_proj_error) : true;
             ok = __syncthreads_and(ok);
             if (!ok) break;
             tcx::fence_after();
@@ -2086,9 +2094,11 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
                 }
             }
         }
-        // B tile: np rows (wavelengths) x 8 pieces; consecutive threads take consecutive wavelengths (coalesced)
-        for (int q = t; q < np * 8; q += CORNER_THREADS) {
-            const int p = q / np, w = q - p * np;
+        // B tile: np rows (wavelengths) x 8 pieces; consecutive threads take consecutive wavelengths (coalesced);
+        // a thread's (piece, wavelength) tasks were worked out once, before the chunks
+        for (int i = 0; i < 2; ++i) {
+            const int p = bt_p[i], w = bt_w[i];
+            if (p < 0) continue;
             __align__(16) __nv_bfloat16 h[8], lo[8];
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
@@ -2119,7 +2129,8 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
     if (ok) {
         // the last commit covers every MMA issued before it
         const int last = nchunk - 1;
-        ok = tcx::mbar_wait(&bar[last % CORNER_STAGES], (last / CORNER_STAGES) & 1, 2u, &g_proj_error);
+        const unsigned parity = (last / CORNER_STAGES) & 1;
+        ok = t == 0 ? tcx::mbar_wait(&bar[last % CORNER_STAGES], parity, 2u, &g_proj_error) : true;
         ok = __syncthreads_and(ok);
         tcx::fence_after();
     }
@@ -2243,7 +2254,7 @@ __global__ void __launch_bounds__(GTC_THREADS)
         const int ch = s / parts, part = s - ch * parts;
         if (s > 0) {
             // the MMAs of step s - 1 read the stage: wait for them before it is rebuilt
-            ok = tcx::mbar_wait(bar, (s - 1) & 1, 4u, &g_proj_error);
+            ok = t == 0 ? tcx::mbar_wait(bar, (s - 1) & 1, 4u, &g_proj_error) : true;
             ok = __syncthreads_and(ok);
             if (!ok) break;
             tcx::fence_after();
@@ -2323,7 +2334,7 @@ __global__ void __launch_bounds__(GTC_THREADS)
     }
     if (ok && steps > 0) {
         // the last commit covers every MMA issued before it
-        ok = tcx::mbar_wait(bar, (steps - 1) & 1, 4u, &g_proj_error);
+        ok = t == 0 ? tcx::mbar_wait(bar, (steps - 1) & 1, 4u, &g_proj_error) : true;
         ok = __syncthreads_and(ok);
         tcx::fence_after();
     }
