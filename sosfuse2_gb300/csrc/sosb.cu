@@ -1962,7 +1962,7 @@ __global__ void corner_entries_fill_kernel(Optics o, Rays b, NodeTable tab, int 
 constexpr int CORNER_ROWS = 128;     // entries per tile (the MMA's M)
 constexpr int CORNER_THREADS = 256;  // two threads per row build the A tile (four 16-byte pieces each)
 constexpr int CORNER_STAGES = 1;     // shared-memory stages of the A and B tiles
-constexpr int CORNER_ROW_BATCH = 8;  // A-tile rows whose basis loads a warp issues together (16 rows a warp)
+constexpr int CORNER_ROW_BATCH = 4;  // A-tile steps (two rows each) whose basis loads a warp issues together
 
 static size_t corner_tc_smem(int np, int L) {
     // CORNER_STAGES stages of A high/low tiles (2 x 16 KB) and B high/low tiles (2 x np rows of 128 bytes), cos(m phi)
@@ -2057,40 +2057,51 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
             tcx::fence_after();
         }
         const int k0 = ch * 64;
-        // A tile: warp `warp` builds rows warp, warp + 8, ...; lane l takes coefficients k0 + 2l and k0 + 2l + 1 of
-        // the row (one coalesced 8-byte load per lane from the row's basis row), times cos(m phi) of the row, split
-        // into BF16 high and low parts, one 4-byte store per lane and part: a warp writes one 128-byte tile row. The
-        // loads of CORNER_ROW_BATCH rows are issued before any is used.
+        // A tile: warp `warp` builds rows warp, warp + 8, ..., two rows per step: lanes 0-15 one row, lanes 16-31
+        // the next, lane l taking coefficients k0 + 4 (l mod 16) .. + 3 of its row (one coalesced 16-byte load from the
+        // row's basis row), times cos(m phi) of the row, split into BF16 high and low parts, one 8-byte store per
+        // part: a warp writes two 128-byte tile rows a step. The loads of CORNER_ROW_BATCH steps are issued first.
         {
             constexpr int WARPS = CORNER_THREADS / 32;
-            const int ka = k0 + 2 * lane;
-            const int ma = ka < K ? mk[ka] : 0, mb = ka + 1 < K ? mk[ka + 1] : 0;
-            const int piece = lane >> 2, sub = (lane & 3) * 4;
+            const int hl = lane >> 4, q = lane & 15;
+            const int ka = k0 + 4 * q;
+            int mq[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) mq[e] = ka + e < K ? mk[ka + e] : 0;
+            const int piece = q >> 1, sub = (q & 1) * 8;
 #pragma unroll 1
-            for (int r0 = warp; r0 < CORNER_ROWS; r0 += WARPS * CORNER_ROW_BATCH) {
-                float2 y[CORNER_ROW_BATCH];
+            for (int s0 = 0; s0 < CORNER_ROWS / (2 * WARPS); s0 += CORNER_ROW_BATCH) {
+                float4 y[CORNER_ROW_BATCH];
 #pragma unroll
                 for (int u = 0; u < CORNER_ROW_BATCH; ++u) {
-                    const int r = r0 + u * WARPS;
-                    y[u] = make_float2(0.0f, 0.0f);
+                    const int r = warp + WARPS * (2 * (s0 + u) + hl);
+                    y[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     if (r < ne) {
-                        const float* yr = y_tab + (size_t)rays_s[r] * kp;
-                        if (ka + 1 < K)
-                            y[u] = *reinterpret_cast<const float2*>(yr + ka);
-                        else if (ka < K)
-                            y[u].x = yr[ka];
+                        const float* yr = y_tab + (size_t)rays_s[r] * kp + ka;
+                        if (ka + 3 < K) {
+                            y[u] = *reinterpret_cast<const float4*>(yr);
+                        } else {
+                            if (ka < K) y[u].x = yr[0];
+                            if (ka + 1 < K) y[u].y = yr[1];
+                            if (ka + 2 < K) y[u].z = yr[2];
+                        }
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < CORNER_ROW_BATCH; ++u) {
-                    const int r = r0 + u * WARPS;
+                    const int r = warp + WARPS * (2 * (s0 + u) + hl);
                     const float* cr = cm + r * L1;
-                    const float x0 = y[u].x * cr[ma], x1 = y[u].y * cr[mb];
-                    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-                    const float2 hf = __bfloat1622float2(h);
-                    const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
-                    *reinterpret_cast<__nv_bfloat162*>(ahi + tcx::sw128_offset(r, piece) + sub) = h;
-                    *reinterpret_cast<__nv_bfloat162*>(alo + tcx::sw128_offset(r, piece) + sub) = lo;
+                    const float x0 = y[u].x * cr[mq[0]], x1 = y[u].y * cr[mq[1]];
+                    const float x2 = y[u].z * cr[mq[2]], x3 = y[u].w * cr[mq[3]];
+                    __align__(8) __nv_bfloat162 h[2], lo[2];
+                    h[0] = __floats2bfloat162_rn(x0, x1);
+                    h[1] = __floats2bfloat162_rn(x2, x3);
+                    const float2 f0 = __bfloat1622float2(h[0]), f1 = __bfloat1622float2(h[1]);
+                    lo[0] = __floats2bfloat162_rn(x0 - f0.x, x1 - f0.y);
+                    lo[1] = __floats2bfloat162_rn(x2 - f1.x, x3 - f1.y);
+                    const uint32_t off = tcx::sw128_offset(r, piece) + sub;
+                    *reinterpret_cast<uint2*>(ahi + off) = *reinterpret_cast<const uint2*>(h);
+                    *reinterpret_cast<uint2*>(alo + off) = *reinterpret_cast<const uint2*>(lo);
                 }
             }
         }
