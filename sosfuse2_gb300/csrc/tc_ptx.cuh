@@ -9,6 +9,7 @@
 namespace tcx {
 
 constexpr long long WAIT_CYCLES = 4000000000LL;  // about two seconds at the maximum SM clock
+constexpr unsigned MBAR_SUSPEND_NS = 100000;     // longest suspension of one try of a barrier phase (0.1 ms)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -20,14 +21,16 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
+// One try of a barrier phase; the thread may be suspended up to the hint (ns) while the phase is incomplete, so a
+// waiting thread issues few instructions.
 __device__ __forceinline__ bool mbar_try(uint64_t* bar, unsigned parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(MBAR_SUSPEND_NS)
         : "memory");
     return ok != 0;
 }
