@@ -47,6 +47,8 @@ typedef struct {
     int32_t box_points;   /* Gauss-Legendre points per observer box (16) */
     double top_km, profile_step_km, mix, g, height, albedo, air_surface;
     double strato_center, strato_sigma, strato_norm;
+    double lower_end_km;  /* extended top (above 80 km): support end of the components other than air, 0 for none */
+    double air_end_km;    /* extended top: support end of the air (numpy_reference.py:158-183) */
 } sosb_dims;
 
 /* Host arrays of the per-state constants. Arrays of an absent layer may be NULL. */

@@ -28,7 +28,9 @@ in float64 for the per-pixel error report.
 
 Optional state features follow the reference where a golden state carries them: the two-layer tropospheric aerosol
 profile (tests/golden/aer2.npz) and the tabulated tropospheric Mie phase with its per-wavelength eigenvalues
-(tests/golden/mie1.npz, mie15.npz). Out of scope here: the extended top above 80 km.
+(tests/golden/mie1.npz, mie15.npz); the component support of an extended top above 80 km (meta 'support': the ends
+of the lower components and of the air, numpy_reference.py:158-183,221-222,254-256,606-609), restated from the
+reference's code, which builds such a top only on its full grid, so no golden state pins it.
 """
 
 import json
@@ -265,7 +267,28 @@ def profile_at(h, pk):
         prof[:, 1] = aerosol_two_layer(h, pk['aer2'])
     q = prof[:, 0] / F(pk.meta['air_surface'])
     prof[:, 4] = q * q
+    sup = support(pk)
+    if sup is not None:  # zero strictly above each component's support end (numpy_reference.py:168-172,221-222)
+        prof[:, 0] = np.where(h > sup[1], F(0), prof[:, 0])
+        prof[:, 1:] = np.where(h[:, None] > sup[0], F(0), prof[:, 1:])
     return prof
+
+
+def support(pk):
+    """(lower end, air end) of an extended top (FP32 km), or None: the components other than air end at the lower
+    end, the air at the air end (numpy_reference.py:158-166, foundation/top.py:26-32)."""
+    s = pk.meta.get('support')
+    return None if not s else (F(s['lower_end']), F(s['air_end']))
+
+
+def support_height(h, inside_h, sup):
+    """A segment end's height within one FP32 ulp of a support end moves to the side the segment lies on
+    (numpy_reference.py:175-183)."""
+    for edge in sup:
+        above = np.nextafter(edge, F(np.inf))
+        near = (h >= np.nextafter(edge, F(-np.inf))) & (h <= above)
+        h = np.where(near, np.where(inside_h > edge, above, edge), h)
+    return h
 
 
 def aerosol_two_layer(h, k):
@@ -292,7 +315,9 @@ def tropo_phase(u, pk):
 
 def strato_profile(h, pk):
     t = (h - F(pk.meta['strato_center'])) / F(pk.meta['strato_sigma'])
-    return np.exp(F(-0.5) * (t * t)) / F(pk.meta['strato_norm'])
+    out = np.exp(F(-0.5) * (t * t)) / F(pk.meta['strato_norm'])
+    sup = support(pk)
+    return out if sup is None else np.where(h > sup[0], F(0), out)
 
 
 def extinction(prof, pk, st_prof=None):
@@ -425,10 +450,16 @@ def path_point(pp, dd, t):
     return q, q2, r
 
 
-def beta_at(rays, t, pk):
-    """Extinction [n, W] at DS path coordinate t."""
+def beta_at(rays, t, pk, inside=None):
+    """Extinction [n, W] at DS path coordinate t; at a segment end (inside = the segment's midpoint) its height
+    snaps to the segment's side of a support end (numpy_reference.py:250-257)."""
     r = path_point(rays['pp'], rays['dd'], t)[2]
     h = np.clip(ds_value(ds_sub(r, (EARTH_R, F(0)))), F(0), F(pk.meta['top_km']))
+    sup = support(pk)
+    if inside is not None and sup is not None:
+        ri = path_point(rays['pp'], rays['dd'], inside)[2]
+        ih = np.clip(ds_value(ds_sub(ri, (EARTH_R, F(0)))), F(0), F(pk.meta['top_km']))
+        h = support_height(h, ih, sup)
     return extinction(profile_at(h, pk), pk, strato_profile(h, pk) if pk.strato else None)
 
 
@@ -491,7 +522,8 @@ def _transport(pk, b, field, first, boundary, query):
         r = _sub(rt, act)
         # Simpson prefix over the panels [a, t_0], [t_0, t_1], ..., [t_{nq-1}, b] (numpy_reference.py:236-291)
         t0 = ds(seg['a'])
-        beta0 = beta_at(r, t0, pk)
+        inside = ds((seg['a'] + seg['b']) / 2)
+        beta0 = beta_at(r, t0, pk, inside)
         acc = np.zeros((len(act), W), F)
         for step in range(len(u)):
             q = sample(r, seg, u[step], wu[step], pk)
@@ -511,7 +543,7 @@ def _transport(pk, b, field, first, boundary, query):
         tm = ds_add(t0, tend)
         tm = (tm[0] * F(0.5), tm[1] * F(0.5))
         wpan = ds_value(ds_sub(tend, t0)) / F(6)
-        beta_end = beta_at(r, tend, pk)
+        beta_end = beta_at(r, tend, pk, inside)
         acc = acc + wpan[:, None] * ((beta0 + beta_end) + F(4) * beta_at(r, tm, pk))
         t, c = kahan_add(tau[act], tauc[act], acc)
         tau[act], tauc[act] = t, c
@@ -611,6 +643,12 @@ def _sample_value(pk, r, q, field, first, phase, sphase, g, mix, hr, ha):
                 saero = lane_tree_sum(q['cm'][:, :, None] * scache) * pk['strato_density'][irc, None]
             rm = field[cell, :4].transpose(0, 2, 1)
             density = hr[irc]
+            sup = support(pk)
+            if sup is not None:  # numpy_reference.py:606-609
+                density = np.where(q['h'] > sup[1], F(0), density)
+                aero = np.where(q['h'][:, None] > sup[0], F(0), aero)
+                if strat:
+                    saero = np.where(q['h'][:, None] > sup[0], F(0), saero)
         trace = (rm[:, :, 0] + rm[:, :, 1]) + rm[:, :, 2]
         tensor = np.zeros((n, W, 4), F)
         for k in range(4):

@@ -32,7 +32,7 @@ class Dims(ctypes.Structure):
         'L', 'W', 'nh', 'nc', 'nq', 'nq_query', 'strato', 'density_rows', 'density_mask', 'n_sun_h', 'n_sun_x',
         'monitors', 'n_monitor_rows', 'n_dirs', 'box_points')] + [(n, c_dbl) for n in (
         'top_km', 'profile_step_km', 'mix', 'g', 'height', 'albedo', 'air_surface', 'strato_center', 'strato_sigma',
-        'strato_norm')]
+        'strato_norm', 'lower_end_km', 'air_end_km')]
 
 
 class Constants(ctypes.Structure):

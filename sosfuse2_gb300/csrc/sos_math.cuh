@@ -141,6 +141,8 @@ struct Optics {
     const float4* gdir4;        // [*] gdir padded to 16 bytes, or null
     int aer2_on;                // two-layer tropospheric aerosol profile instead of exp(-h / height)
     float aer2[7];              // its vector [bl_top - w/2, 1/w, a_bl, k_bl, a_ft, k_ft, bl_top]
+    int support;                // extended top: components vanish above their support ends
+    float lower_end, air_end;   // support ends of the components other than air and of the air (km)
     int tropo_bins;             // tabulated tropospheric phase (TROPO_MIE) on tropo_bins + 1 nodes, or 0 for HG
     const float* tropo_lut;     // [tropo_bins + 1][W] tropospheric phase per sr on a uniform grid of u in [-1, 1]
     const float2* tropo_lut2;   // [tropo_bins][W] (value, next value - value) of tropo_lut, or null
@@ -201,10 +203,29 @@ SOS_HD Profile profile_at(const Optics& o, float h) {
     p.v[3] = tab2;
     float q = p.v[0] / o.air_surface;
     p.v[4] = q * q;
+    if (o.support) {  // zero strictly above each component's support end (numpy_reference.py:168-172,221-222)
+        if (h > o.air_end) p.v[0] = 0.0f;
+        if (h > o.lower_end)
+            for (int k = 1; k < 5; ++k) p.v[k] = 0.0f;
+    }
     return p;
 }
 
+// A segment end's height within one FP32 ulp of a support end moves to the side the segment lies on (inside_h: the
+// height of the segment's midpoint; numpy_reference.py:175-183).
+SOS_HD float support_height(const Optics& o, float h, float inside_h) {
+    if (!o.support) return h;
+    const float edges[2] = {o.lower_end, o.air_end};
+    for (int i = 0; i < 2; ++i) {
+        const float edge = edges[i];
+        const float above = nextafterf(edge, INFINITY);
+        if (h >= nextafterf(edge, -INFINITY) && h <= above) h = inside_h > edge ? above : edge;
+    }
+    return h;
+}
+
 SOS_HD float strato_profile(const Optics& o, float h) {
+    if (o.support && h > o.lower_end) return 0.0f;
     float t = (h - o.strato_center) / o.strato_sigma;
     return expf(-0.5f * (t * t)) / o.strato_norm;
 }
@@ -257,6 +278,7 @@ struct Node {
     float fr[4];      // cos, sin of the interpolated cell angle; cos, sin of the node's longitude (frame inputs)
     float ah, ac;     // bilinear fractions in height and solar zenith
     int j;            // solar-zenith interval
+    int above;        // extended top: bit 0 above the lower components' support end, bit 1 above the air's
 };
 
 struct RayConst {
@@ -264,6 +286,8 @@ struct RayConst {
     float B[3][3];    // frame rows B[k][i]
     float d32[3], dloc[3], pu[4], direct[4], st, weight, end_f;
 };
+
+SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }  // exact
 
 SOS_HD void path_point(const RayConst& rc, DS t, DS q[3], DS q2[3], DS& r) {
     for (int k = 0; k < 3; ++k) {
@@ -279,6 +303,24 @@ SOS_HD float beta_at(const Optics& o, const RayConst& rc, DS t, int w) {
     DS q[3], q2[3], r;
     path_point(rc, t, q, q2, r);
     float h = path_height(o, r);
+    Profile p = profile_at(o, h);
+    return extinction(o, p, o.strato ? strato_profile(o, h) : 0.0f, w);
+}
+
+// Height h of an end of segment [a, b] with the support snap of an extended top (the segment's midpoint decides the
+// side; numpy_reference.py:250-257).
+SOS_HD float segment_end_height(const Optics& o, const RayConst& rc, float h, DS a, DS b) {
+    if (!o.support) return h;
+    DS q[3], q2[3], r;
+    path_point(rc, ds_half(ds_add(a, b)), q, q2, r);
+    return support_height(o, h, path_height(o, r));
+}
+
+// beta_at at an end t of segment [a, b].
+SOS_HD float beta_end(const Optics& o, const RayConst& rc, DS t, DS a, DS b, int w) {
+    DS q[3], q2[3], r;
+    path_point(rc, t, q, q2, r);
+    const float h = segment_end_height(o, rc, path_height(o, r), a, b);
     Profile p = profile_at(o, h);
     return extinction(o, p, o.strato ? strato_profile(o, h) : 0.0f, w);
 }
@@ -350,6 +392,7 @@ SOS_HD void sample_node(const Optics& o, const RayConst& rc, DS a, DS b, bool lo
     n.qz = q[2];
     float h = path_height(o, r);
     n.h = h;
+    n.above = o.support ? (h > o.lower_end ? 1 : 0) | (h > o.air_end ? 2 : 0) : 0;
     DS xy = ds_sqrt(ds_add(q2[0], q2[1]));
     float rho = ds_val(xy);
     float cx = 1.0f, sx = 0.0f;
@@ -695,13 +738,15 @@ SOS_HD void warm_value(const Optics& o, const RayConst& rc, const Node& n, const
         const float* f = field + (size_t)cell * o.src * W + w;
         const float rm[4] = {f[0], f[W], f[2 * W], f[3 * W]};
         const float trace = (rm[0] + rm[1]) + rm[2];
-        const float dens = o.hr[n.ir + (c >> 1)];
+        // an extended top's supports by the node's height (numpy_reference.py:604-609)
+        const float dens = (n.above & 2) ? 0.0f : o.hr[n.ir + (c >> 1)];
+        const float ae = (n.above & 1) ? 0.0f : aero[c];
         float tens[4];
         for (int k = 0; k < 4; ++k) {
             float rot = 0.0f;
             for (int u = 0; u < 4; ++u) rot += n.T[k][u] * rm[u];
             tens[k] = dens * (mix * rot + ((1.0f - mix) / 3.0f * trace) * rc.pu[k]);
-            tens[k] += (aero[c] * rc.pu[k]) / 2.0f;
+            tens[k] += (ae * rc.pu[k]) / 2.0f;
             val[k] += n.sw[c] * tens[k];
         }
         const float tr = (tens[0] + tens[1]) + tens[2];
@@ -942,7 +987,7 @@ SOS_HD void transport_lane(const Optics& o, const Rays& b, const LaneInputs& in,
         const DS a = DS{sg.x, sg.y}, bb = DS{sg.z, sg.w};
         const bool lower = b.lower[s] != 0;
         DS t0 = a;
-        float beta0 = beta_at(o, rc, t0, w);
+        float beta0 = beta_end(o, rc, t0, a, bb, w);
         float acc = 0.0f;
         for (int step = 0; step < in.nq; ++step) {
             Node n;
@@ -993,7 +1038,7 @@ SOS_HD void transport_lane(const Optics& o, const Rays& b, const LaneInputs& in,
         DS tm = ds_add(t0, bb);
         tm = DS{tm.h * 0.5f, tm.l * 0.5f};
         const float wpan = ds_val(ds_sub(bb, t0)) / 6.0f;
-        acc = acc + wpan * ((beta0 + beta_at(o, rc, bb, w)) + 4.0f * beta_at(o, rc, tm, w));
+        acc = acc + wpan * ((beta0 + beta_end(o, rc, bb, a, bb, w)) + 4.0f * beta_at(o, rc, tm, w));
         kahan(tau, tauc, acc);
     }
     boundary_term(o, b, rc, in.boundary, ray, w, total);

@@ -226,9 +226,13 @@ struct NodeTable {
     float* att;     // [nodes][W] quadrature weight x attenuation from the ray's origin
 };
 
+// misc.w packs ir (bits 16-29), j (bits 0-15) and the node's support bits (30: above the lower components' end, 31:
+// above the air's)
 __device__ __forceinline__ float4 table_misc(const Node& n) {
-    return make_float4(n.ah, n.ac, n.cp, __int_as_float((n.ir << 16) | n.j));
+    return make_float4(n.ah, n.ac, n.cp, __int_as_float((n.ir << 16) | n.j | (n.above << 30)));
 }
+
+__device__ __forceinline__ int misc_ir(int pk) { return (pk >> 16) & 0x3fff; }
 
 // Node of a table entry: frame rotation, corners and azimuth cosine (what warm_value and the SH synthesis read).
 __device__ __forceinline__ void table_node(const Optics& o, const RayConst& rc, const NodeTable& tab, long long id,
@@ -237,8 +241,9 @@ __device__ __forceinline__ void table_node(const Optics& o, const RayConst& rc, 
     const float4 ms = tab.misc[id];
     node_frame(rc, fr.x, fr.y, fr.z, fr.w, n);
     const int pk = __float_as_int(ms.w);
-    node_corners(o, pk >> 16, pk & 0xffff, ms.x, ms.y, n);
+    node_corners(o, misc_ir(pk), pk & 0xffff, ms.x, ms.y, n);
     n.cp = ms.z;
+    n.above = (int)((unsigned)pk >> 30);
 }
 
 // First light of a cell bundle in stages (few wavelengths): a preparation launch stores per node the first-light
@@ -258,7 +263,6 @@ constexpr unsigned FULL_MASK = 0xffffffffu;
 // basis rows of the warps of a block, each padded to kp = K rounded up to 4
 static size_t warp_smem(int K) { return sizeof(float) * (size_t)((K + 3) & ~3) * (TRANSPORT_THREADS / 32); }
 
-SOS_HD DS ds_half(DS a) { return DS{a.h * 0.5f, a.l * 0.5f}; }
 
 // Sample-parallel transport for few wavelengths (W <= WM): one warp per ray, lane i takes the ray's node i (batches
 // of 32 nodes, segment-major). Each lane evaluates its node's geometry and its Simpson panel [previous node, node]
@@ -328,7 +332,7 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
                 t0 = a;
                 DS q[3], q2[3], r;
                 path_point(rc, a, q, q2, r);
-                const float h = path_height(o, r);
+                const float h = segment_end_height(o, rc, path_height(o, r), a, bb);
                 const Profile pa = profile_at(o, h);
                 const float sa = o.strato ? strato_profile(o, h) : 0.0f;
 #pragma unroll
@@ -357,7 +361,7 @@ __global__ void __launch_bounds__(TRANSPORT_THREADS)
             if (step == nq - 1) {
                 DS q[3], q2[3], r;
                 path_point(rc, bb, q, q2, r);
-                float h = path_height(o, r);
+                float h = segment_end_height(o, rc, path_height(o, r), a, bb);
                 const Profile pb = profile_at(o, h);
                 const float sb = o.strato ? strato_profile(o, h) : 0.0f;
                 const DS tm = ds_half(ds_add(n.t, bb));
@@ -467,10 +471,12 @@ SOS_HD float ext6(const Optics& o, const float* p6, int w) {
     return b;
 }
 
-SOS_HD void profile6(const Optics& o, const RayConst& rc, DS t, float* p6) {
+// Profiles at path coordinate t; at an end of segment [a, b] (end = true) with the support snap of an extended top.
+SOS_HD void profile6(const Optics& o, const RayConst& rc, DS t, float* p6, bool end = false, DS a = DS{0.0f, 0.0f},
+                     DS b = DS{0.0f, 0.0f}) {
     DS q[3], q2[3], r;
     path_point(rc, t, q, q2, r);
-    const float h = path_height(o, r);
+    const float h = end ? segment_end_height(o, rc, path_height(o, r), a, b) : path_height(o, r);
     const Profile p = profile_at(o, h);
     for (int k = 0; k < 5; ++k) p6[k] = p.v[k];
     p6[5] = o.strato ? strato_profile(o, h) : 0.0f;
@@ -546,9 +552,9 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
                 for (int u = 0; u < 4; ++u) R->T[4 * k + u] = n.T[k][u];
             for (int k = 0; k < 5; ++k) R->prof[k] = n.prof.v[k];
             R->wpan = 0.0f;  // set below, once the previous node's coordinate is known
-            if (step == 0) profile6(o, rc, a, R->pa);
+            if (step == 0) profile6(o, rc, a, R->pa, true, a, bb);
             if (step == nq - 1) {
-                profile6(o, rc, bb, R->pb);
+                profile6(o, rc, bb, R->pb, true, a, bb);
                 profile6(o, rc, ds_half(ds_add(n.t, bb)), R->pmc);
                 R->wpc = ds_val(ds_sub(bb, n.t)) / 6.0f;
             }
@@ -698,7 +704,7 @@ __global__ void pair_build_kernel(Optics o, Rays b, NodeTable tab, int nq, int p
         for (int i = 0; i < nn; ++i) {
             const float4 ms = tab.misc[node0 + i];
             const int pk = __float_as_int(ms.w);
-            const int cell0 = (pk >> 16) * o.nc + (pk & 0xffff);
+            const int cell0 = misc_ir(pk) * o.nc + (pk & 0xffff);
             int idx[4];
             for (int c = 0; c < 4; ++c) {
                 const int cell = cell0 + (c & 1) + (c >> 1) * o.nc;
@@ -764,7 +770,7 @@ __global__ void pair_contract_wave_kernel(Optics o, PairTable pt, const float* _
 // Corner pair pr of a node (cells (ir + pr, j) and (ir + pr, j + 1)): its first cell, the key of its bucket.
 __device__ __forceinline__ int pair_cell(const Optics& o, float4 ms, int pr) {
     const int pk = __float_as_int(ms.w);
-    return ((pk >> 16) + pr) * o.nc + (pk & 0xffff);
+    return (misc_ir(pk) + pr) * o.nc + (pk & 0xffff);
 }
 
 // Ground directions a pair visits: the first cell's, plus the second cell's unless the two share them.
@@ -1908,7 +1914,7 @@ __global__ void corner_entries_kernel(Optics o, Rays b, NodeTable tab, int nq, i
         for (int i = 0; i < nn; ++i) {
             const float4 ms = tab.misc[node0 + i];
             const int pk = __float_as_int(ms.w);
-            const int cell0 = (pk >> 16) * o.nc + (pk & 0xffff);
+            const int cell0 = misc_ir(pk) * o.nc + (pk & 0xffff);
             for (int c = 0; c < 4; ++c) {
                 const int cell = cell0 + (c & 1) + (c >> 1) * o.nc;
                 if (pass == 0) {
@@ -1940,7 +1946,7 @@ __global__ void corner_entries_fill_kernel(Optics o, Rays b, NodeTable tab, int 
             const bool act = i < nn;
             const float4 ms = act ? tab.misc[node0 + i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             const int pk = __float_as_int(ms.w);
-            const int cell0 = (pk >> 16) * o.nc + (pk & 0xffff);
+            const int cell0 = misc_ir(pk) * o.nc + (pk & 0xffff);
             for (int c = 0; c < 4; ++c) {
                 const int cell = act ? cell0 + (c & 1) + (c >> 1) * o.nc : -1;
                 const unsigned peers = __match_any_sync(FULL_MASK, cell);
@@ -2868,6 +2874,9 @@ static Optics optics_of(const sosb_state* s) {
     o.gdir4 = P<float4>(s->gdir4);
     o.aer2_on = s->aer2_on;
     for (int i = 0; i < 7; ++i) o.aer2[i] = s->aer2[i];
+    o.support = d.lower_end_km > 0.0 ? 1 : 0;
+    o.lower_end = (float)d.lower_end_km;
+    o.air_end = (float)d.air_end_km;
     o.tropo_bins = s->tropo_bins;
     o.tropo_lut = s->tropo_bins ? P<float>(s->t_lut) : nullptr;
     o.tropo_lut2 = s->tropo_bins ? P<float2>(s->t_lut2) : nullptr;
@@ -2961,7 +2970,7 @@ static int table_for(sosb_state* s, BundleDev& b, int nq, bool whole, int first,
     }
     if (!whole) return 0;
     const sosb_dims& d = s->d;
-    if (d.nh > 32768 || d.nc > 65536) {  // (ir << 16 | j) packing
+    if (d.nh > 16384 || d.nc > 65536) {  // (ir << 16 | j) packing with two support bits above ir
         b.t_too_big = true;
         return 0;
     }

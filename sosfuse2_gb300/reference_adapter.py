@@ -103,8 +103,6 @@ def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
     raws = observer_rays(s)
     cq = s.kernel.setup(s, raws[0]['nq'])
     L, K, W = s.kernel.L, s.kernel.K, s.W
-    if c['domain'].top_km > 80.0:
-        raise ValueError('E_DOMAIN: the extended top above 80 km is not packed')
     u4, w4 = np.polynomial.legendre.leggauss(4)
     opt = c['density_optics']
     meta = dict(
@@ -128,6 +126,9 @@ def pack_state(s, geometry, scope, tolerance=1e-3, max_eval=64):
         arrays['tropo_lut'] = np.asarray(c['tropo_lut'], 'f4').reshape(bins + 1, W)
         arrays['tropo_eigen'] = np.asarray(tropo_eigen(s.tropo, L), 'f4')
         meta['tropo_bins'] = bins
+    dom = c['domain']
+    if dom.top_km > dom.lower_end:  # extended top: the components' support ends (numpy_reference.py:158-183)
+        meta['support'] = dict(lower_end=float(dom.lower_end), air_end=float(dom.air_end))
     if 'aer2' in c:  # AEROSOL_2L: the two-layer profile's kernel vector
         arrays['aer2'] = np.asarray(c['aer2'], 'f4')
         meta['aerosol_profile'] = 'two_layer'

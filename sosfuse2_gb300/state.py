@@ -90,6 +90,9 @@ class PackedState:
             air_surface=float(m['air_surface']),
             strato_center=float(m.get('strato_center', 0.0)), strato_sigma=float(m.get('strato_sigma', 1.0)),
             strato_norm=float(m.get('strato_norm', 1.0)))
+        sup = m.get('support')
+        if sup:  # extended top: the components' support ends
+            d.lower_end_km, d.air_end_km = float(sup['lower_end']), float(sup['air_end'])
         return d
 
     def ground_csr(self):

@@ -38,6 +38,9 @@ extern "C" int host_transport(const sosb_dims* d, const sosb_constants* c, const
     o.strato_sun_col = c->strato_sun_col; o.gm = c->gm; o.goff = goff.data(); o.gdir = c->gdir; o.gval = c->gval;
     o.strato_ext = c->strato_ext; o.strato_sca = c->strato_sca; o.strato_chi = c->strato_chi;
     o.sh_a = sa.data(); o.sh_b = sb.data(); o.sh_d = sdg.data();
+    o.support = d->lower_end_km > 0.0 ? 1 : 0;
+    o.lower_end = (float)d->lower_end_km;
+    o.air_end = (float)d->air_end_km;
     o.aer2_on = c->aer2 != nullptr;
     for (int i = 0; i < 7; ++i) o.aer2[i] = c->aer2 ? c->aer2[i] : 0.0f;
     o.tropo_bins = c->tropo_lut ? c->tropo_bins : 0;

@@ -50,3 +50,31 @@ def test_apply_and_boxes_match_oracle(case):
     big = np.abs(b_ref) > 1e-6 * np.abs(b_ref).max()
     assert np.all(np.abs(b[big] - b_ref[big]) <= 1e-3 * np.abs(b_ref[big]))
     k.close()
+
+
+@pytest.mark.parametrize('air_end', [80.0, 120.0])
+def test_extended_top_matches_oracle(air_end):
+    """An extended top (components supported to 80 km, the air to `air_end`) on the GPU against the oracle's
+    restatement of the reference's support rules: apply(0), apply(g1) and the observer boxes."""
+    from test_host_transport import _extended_state
+
+    from oracle import sos_oracle as so
+    from sosfuse2_gb300.solver import Solver
+    from sosfuse2_gb300.state import PackedState
+
+    arrays = _extended_state(air_end)
+    ref = so.Oracle(so.StatePack(dict(arrays)))
+    solver = Solver(PackedState(dict(arrays)), device='cuda:0')
+    k = solver.kernel
+    zero = np.zeros(solver.state.shape, np.float32)
+    g1_ref = ref.apply(zero)
+    g1 = solver.apply(k.field(zero)).cpu().numpy()
+    assert np.all(rel_l2_per_wave(g1, g1_ref) <= 1e-4)
+    g2_ref = ref.apply(g1_ref)
+    g2 = solver.apply(k.field(g1_ref)).cpu().numpy()
+    assert np.all(rel_l2_per_wave(g2, g2_ref) <= 1e-4)
+    b_ref = ref.boxes(g1_ref)
+    b = solver.boxes(k.field(g1_ref))
+    big = np.abs(b_ref) > 1e-6 * np.abs(b_ref).max()
+    assert np.all(np.abs(b[big] - b_ref[big]) <= 1e-3 * np.abs(b_ref[big]))
+    k.close()
