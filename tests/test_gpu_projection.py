@@ -18,6 +18,7 @@ CASES = {
     'w3_l32_top120': dict(W=3, L=32, top=120.0, nh=7),
     'w8_l24': dict(W=8, L=24, top=80.0, nh=6),
     'w33_l16': dict(W=33, L=16, top=80.0, nh=5),
+    'w6_l48': dict(W=6, L=48, top=120.0, nh=4),
 }
 BOUND = {1: 2e-5, 2: 2e-3, 3: 6e-3}  # bf16x3, TF32, BF16
 
