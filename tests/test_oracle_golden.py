@@ -114,7 +114,7 @@ def test_nonconvergence_matches_reference():
 @pytest.mark.skipif(not (GOLDEN / 'mie15.npz').exists(), reason='mie15 fixture not generated')
 def test_mie15_nonconvergence_matches_reference():
     """The Mie-phase state over 15 wavelengths does not converge in the reference's own solve (13 of 15 wavelengths
-    within 1e-3 after 64 evaluations); over its first 24 evaluations (the CPU suite's time; the GPU parity test runs
+    within 1e-3 after 64 evaluations); over its first 12 evaluations (the CPU suite's time; the GPU parity test runs
     all 64) the oracle follows the history the reference printed (its maximum over the wavelengths, six digits)
     within 0.2 %: the largest gaps, 0.14 %, follow the Anderson steps where a wavelength's change jumps (evaluation
     11), from the FP32 regrouping of the sums."""
@@ -123,10 +123,10 @@ def test_mie15_nonconvergence_matches_reference():
     ref_obs, ref_src = reference_history(pk.meta)
     hist = []
     with pytest.raises(RuntimeError, match='E_NOT_CONVERGED'):
-        so.Oracle(pk).solve(max_eval=24, log=lambda it, rr, ss, done: hist.append((max(rr), max(ss))))
+        so.Oracle(pk).solve(max_eval=12, log=lambda it, rr, ss, done: hist.append((max(rr), max(ss))))
     obs = np.array([[h[0]] for h in hist])
     src = np.array([[h[1]] for h in hist])
-    assert ref_obs.shape == (64, 1) and obs.shape == (24, 1)
-    ref_obs, ref_src = ref_obs[:24], ref_src[:24]
+    assert ref_obs.shape == (64, 1) and obs.shape == (12, 1)
+    ref_obs, ref_src = ref_obs[:12], ref_src[:12]
     assert np.all(np.abs(obs - ref_obs) <= 2e-3 * ref_obs), np.c_[obs, ref_obs]
     assert np.all(np.abs(src - ref_src) <= 2e-3 * ref_src), np.c_[src, ref_src]
