@@ -103,6 +103,7 @@ struct sosb_state {
     // constants
     DevBuf h, chi, hr, ha, ext, asca, table, sun_h, sun_col, gm, goff, gdir, gval, rf, af, ext0;
     DevBuf t_lut, t_lut2;  // tabulated tropospheric phase and its (value, step) pairs
+    DevBuf plane_tiles;    // the corner products' B tiles of the current plane (plane_tiles_kernel)
     DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src, s_lut, s_lut2, gsame, gdir4;
     DevBuf sh_a, sh_b, sh_d;
     DevBuf u_hi, u_lo, wu_hi, wu_lo, uq_hi, uq_lo, wuq_hi, wuq_lo, box_ww, solar;
@@ -1930,6 +1931,35 @@ __global__ void corner_entries_kernel(Optics o, Rays b, NodeTable tab, int nq, i
     }
 }
 
+// B tiles of the corner products for every cell and chunk of 64 SH coefficients, once per plane: the plane rows
+// [k][w] split into BF16 high and low parts in the 128-byte-swizzled K-major layout of the tile (np wavelength rows of
+// 8 pieces), high tile then low tile, so that a CTA copies a chunk's 2 np x 128 bytes as they are. One thread per
+// (cell, chunk, piece, wavelength row), wavelengths fastest (coalesced plane reads).
+__global__ void plane_tiles_kernel(const float* __restrict__ plane, int ns, int K, int W, int np, int nchunk,
+                                   uint8_t* __restrict__ tiles) {
+    const long long n = (long long)ns * nchunk * 8 * np;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % np);
+        const long long r = i / np;
+        const int p = (int)(r % 8);
+        const long long cc = r / 8;  // cell * nchunk + chunk
+        const int ch = (int)(cc % nchunk);
+        const long long cell = cc / nchunk;
+        const float* pc = plane + (size_t)cell * K * W;
+        __align__(16) __nv_bfloat16 h[8], lo[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int k = ch * 64 + p * 8 + e;
+            const float x = (w < W && k < K) ? pc[(size_t)k * W + w] : 0.0f;
+            h[e] = __float2bfloat16_rn(x);
+            lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
+        }
+        uint8_t* base = tiles + (size_t)cc * (2 * (size_t)np * 128);
+        *reinterpret_cast<uint4*>(base + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(h);
+        *reinterpret_cast<uint4*>(base + (size_t)np * 128 + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(lo);
+    }
+}
+
 // Pass 1 of the entries, one warp per ray, lanes over its nodes 32 at a time: the entries of one cell from one batch
 // take consecutive positions (one atomic per distinct cell and corner), so the rows of a tile that share a ray are
 // neighbours and a warp's loads of their basis rows hit few distinct addresses.
@@ -1988,7 +2018,7 @@ static size_t corner_tc_smem(int np, int L) {
 // values at its slot, lanes over the wavelengths.
 __global__ void __launch_bounds__(CORNER_THREADS, 4)
     corner_tc_kernel(Optics o, CornerEntries ce, const float* __restrict__ y_tab, int kp,
-                     const float* __restrict__ plane, int np, uint32_t idesc, uint32_t tmem_cols,
+                     const uint4* __restrict__ btiles, int np, uint32_t idesc, uint32_t tmem_cols,
                      float* __restrict__ out) {
     extern __shared__ uint8_t corner_raw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(corner_raw) + 1023) & ~(uintptr_t)1023);
@@ -2037,14 +2067,9 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
     __syncthreads();
     tcx::fence_after();
     const uint32_t tmem = *tslot;
-    const float* pc = plane + (size_t)cell * K * W;
     const int lane = t & 31;
-    int bt_p[2], bt_w[2];  // this thread's B-tile tasks q = t, t + CORNER_THREADS of np * 8 (piece -1: none)
-    for (int i = 0; i < 2; ++i) {
-        const int q = t + i * CORNER_THREADS;
-        bt_p[i] = q < np * 8 ? q / np : -1;
-        bt_w[i] = q < np * 8 ? q - bt_p[i] * np : 0;
-    }
+    const int nchunk_all = (K + 63) / 64;
+    const uint4* bcell = btiles + (size_t)cell * nchunk_all * (16 * np);  // the cell's B tiles, 16 np pieces a chunk
     const int nchunk = (K + 63) / 64;
     bool ok = true;
     for (int ch = 0; ch < nchunk && ok; ++ch) {
@@ -2111,21 +2136,12 @@ __global__ void __launch_bounds__(CORNER_THREADS, 4)
                 }
             }
         }
-        // B tile: np rows (wavelengths) x 8 pieces; consecutive threads take consecutive wavelengths (coalesced);
-        // a thread's (piece, wavelength) tasks were worked out once, before the chunks
-        for (int i = 0; i < 2; ++i) {
-            const int p = bt_p[i], w = bt_w[i];
-            if (p < 0) continue;
-            __align__(16) __nv_bfloat16 h[8], lo[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int k = k0 + p * 8 + e;
-                const float x = (w < W && k < K) ? pc[(size_t)k * W + w] : 0.0f;
-                h[e] = __float2bfloat16_rn(x);
-                lo[e] = __float2bfloat16_rn(x - __bfloat162float(h[e]));
-            }
-            *reinterpret_cast<uint4*>(bhi + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(h);
-            *reinterpret_cast<uint4*>(blo + tcx::sw128_offset(w, p)) = *reinterpret_cast<const uint4*>(lo);
+        // B tile: the chunk's high and low tiles of the cell's plane, already split and swizzled (plane_tiles_kernel),
+        // copied in 16-byte pieces
+        {
+            const uint4* src = bcell + (size_t)ch * (16 * np);
+            uint4* dst = reinterpret_cast<uint4*>(bhi);
+            for (int q = t; q < 16 * np; q += CORNER_THREADS) dst[q] = src[q];
         }
         tcx::fence_proxy_async();
         __syncthreads();
@@ -3375,8 +3391,8 @@ static int run_transport(sosb_state* s, BundleDev& b, int64_t ray0, int64_t nray
                 if (b.c_ntiles > 0) {
                     Timer ct(s, K_CORNER);
                     corner_tc_kernel<<<(unsigned)b.c_ntiles, CORNER_THREADS, smem, s->stream>>>(
-                        optics_of(s), ce, P<float>(b.y_tab), (s->K + 3) & ~3, in.plane, np, tcx::idesc_bf16(128, np),
-                        cols, P<float>(b.cv));
+                        optics_of(s), ce, P<float>(b.y_tab), (s->K + 3) & ~3, P<uint4>(s->plane_tiles), np,
+                        tcx::idesc_bf16(128, np), cols, P<float>(b.cv));
                     TRY(launch_check(s));
                     s->corner_used = true;
                 }
@@ -3543,7 +3559,17 @@ static int run_plane(sosb_state* s, const float* field) {
     Timer timer(s, K_PLANE);
     plane_kernel<<<grid_for(n, 256), 256, 0, s->stream>>>(field, P<float>(s->ha), P<float>(s->s_density), d.nc, s->K,
                                                           s->src, d.W, d.strato, kp, n, P<float>(s->plane));
-    return launch_check(s);
+    TRY(launch_check(s));
+    if (s->corner_mma && d.W > 4) {
+        // the corner products' B tiles of this plane
+        const int np = (d.W + 15) / 16 * 16, nchunk = (s->K + 63) / 64;
+        TRY(dalloc(s, s->plane_tiles, (size_t)s->ns * nchunk * 2 * np * 128));
+        const long long nt = (long long)s->ns * nchunk * 8 * np;
+        plane_tiles_kernel<<<grid_for(nt, 256), 256, 0, s->stream>>>(P<float>(s->plane), s->ns, s->K, d.W, np, nchunk,
+                                                                     P<uint8_t>(s->plane_tiles));
+        TRY(launch_check(s));
+    }
+    return 0;
 }
 
 static int check_ready(sosb_state* s, bool need_obs) {
@@ -3750,7 +3776,7 @@ int sosb_destroy(sosb_handle s) {
                       &s->ring_f[3], &s->fl_val0, &s->fl_coef, &s->fl_dir, &s->fl_g, &s->fl_cnt, &s->fl_off,
                       &s->fl_cursor, &s->fl_entries, &s->gr_off, &s->gr_loc, &s->gr_w, &s->gr_cols, &s->gr_cos,
                       &s->gr_ok, &s->gr_value, &s->gr_cnt, &s->gr_cursor, &s->t_lut, &s->t_lut2, &s->g_su2,
-                      &s->g_sv, &s->gt_cnt, &s->gt_off, &s->gt_cursor, &s->gt_tile};
+                      &s->g_sv, &s->gt_cnt, &s->gt_off, &s->gt_cursor, &s->gt_tile, &s->plane_tiles};
     for (DevBuf* b : bufs) dfree(s, *b);
     for (BundleDev* bd : {&s->cells, &s->obs}) {
         DevBuf* bb[] = {&bd->cell_off, &bd->ray_cell, &bd->p, &bd->frame, &bd->dir, &bd->dir_lo, &bd->dloc, &bd->pcp,
