@@ -132,9 +132,8 @@ int sosb_set_stream(sosb_handle h, void *stream);
  * double-single geometry and the optical-depth prefix. 0 turns them off (every launch recomputes). */
 int sosb_set_node_tables(sosb_handle h, int enable);
 /* Projection form (no reference counterpart; the reference projects in compensated FP32 on CUDA cores):
- * 0 FP32 CUDA cores (compensated sums; the default up to four wavelengths), 1 bf16x3 tensor cores (split BF16
- * operands, three products, FP32 accumulation; the default above four wavelengths), 2 TF32 tensor cores, 3 BF16
- * tensor cores. Forms 1-3 contract the SH rows per cell with
+ * 0 FP32 CUDA cores (compensated sums, the default), 1 bf16x3 tensor cores (split BF16 operands, three products,
+ * FP32 accumulation), 2 TF32 tensor cores, 3 BF16 tensor cores. Forms 1-3 contract the SH rows per cell with
  * tcgen05.mma against a basis table built once per cell bundle; the Rayleigh rows and the ground flux stay FP32.
  * E_PROJECTION for an unknown form; E_TC_TIMEOUT when a tensor-core wait ran out. */
 int sosb_set_projection(sosb_handle h, int mode);

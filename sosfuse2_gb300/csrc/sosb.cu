@@ -3712,9 +3712,6 @@ int sosb_create(const sosb_dims* dims, sosb_handle* out) {
     s->K = (d.L + 1) * (d.L + 2) / 2;
     s->src = 10 + s->K * (d.strato ? 2 : 1);
     s->ns = d.nh * d.nc;
-    // projection: bf16x3 on the tensor cores above four wavelengths (within 2e-5 of the compensated FP32 sums at
-    // half their time), the FP32 form below, where an N = 16 tile is mostly padding
-    s->proj_mode = d.W > 4 ? PROJ_BF16X3 : PROJ_FP32;
     cudaError_t e = cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete s;
