@@ -104,6 +104,8 @@ struct sosb_state {
     DevBuf h, chi, hr, ha, ext, asca, table, sun_h, sun_col, gm, goff, gdir, gval, rf, af, ext0;
     DevBuf t_lut, t_lut2;  // tabulated tropospheric phase and its (value, step) pairs
     DevBuf plane_tiles;    // the corner products' B tiles of the current plane (plane_tiles_kernel)
+    const float* plane_field = nullptr;  // the field the current plane was built from
+    bool plane_keep = false;  // one-shot: the next run_plane of plane_field keeps the current plane
     DevBuf s_ext, s_sca, s_chi, s_density, s_sun_col, s_eigen, s_sca_src, s_lut, s_lut2, gsame, gdir4;
     DevBuf sh_a, sh_b, sh_d;
     DevBuf u_hi, u_lo, wu_hi, wu_lo, uq_hi, uq_lo, wuq_hi, wuq_lo, box_ww, solar;
@@ -3551,6 +3553,12 @@ static int proj_check(sosb_state* s) {
 }
 
 static int run_plane(sosb_state* s, const float* field) {
+    if (s->plane_keep && s->plane_field == field) {  // the plane of this field is current (eval_body)
+        s->plane_keep = false;
+        return 0;
+    }
+    s->plane_keep = false;
+    s->plane_field = field;
     const sosb_dims& d = s->d;
     const int kp = plane_kp(s);
     const long long n = (long long)s->ns * (kp ? kp : s->K) * d.W;
@@ -5047,6 +5055,7 @@ static int eval_body(sosb_state* s, bool set_cond) {
     }
     TRY(launch_check(s));
     TRY(boxes_dev(s, x, P<double>(s->box_old)));
+    s->plane_keep = true;  // apply(x) reads the plane boxes(x) just built: nothing writes x in between
     TRY(apply_impl(s, x, g, 0ull, &ctrl->done));
     TRY(boxes_dev(s, g, P<double>(s->box_new)));
     return residual_tail(s, set_cond, false);
