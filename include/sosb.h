@@ -171,6 +171,11 @@ int sosb_set_corner_mma(sosb_handle h, int enable);
  * largest value; a table that needs more than 8 factors, or a tabulated tropospheric phase, keeps the CUDA-core
  * kernel). 0: off (CUDA cores). E_TC_TIMEOUT when a tensor-core wait ran out. */
 int sosb_set_ground_mma(sosb_handle h, int enable);
+/* No reference counterpart; host only (no GPU). The factorisation sosb_set_constants applies to the stratospheric
+ * phase table for the tensor-core ground sums: lut [n][W] ~= U [n][r] V [r][W], V's rows the leading eigenvectors of
+ * lut^T lut (cyclic Jacobi, FP64), U = lut V^T, r the smallest rank <= rmax with every row within tol of its largest
+ * magnitude. Writes U (n * rmax doubles at most) and V (rmax * W) and returns r in *rank (0: none within tol). */
+int sosb_phase_factors(const double *lut, int n, int W, int rmax, double tol, double *U, double *V, int *rank);
 /* Replaces: Kernel.setup (source_solver.py:1243-1339) and constants_device (source_solver.py:2248). */
 int sosb_set_constants(sosb_handle h, const sosb_constants *c);
 /* Replaces: ray_geometry.upload_geometry / device_geometry (ray_geometry.py:205-287) of the cell bundle

@@ -114,6 +114,7 @@ SIGNATURES = {
                    c_int),
     'sosb_set_corner_mma': ([ctypes.c_void_p, c_int], c_int),
     'sosb_set_ground_mma': ([ctypes.c_void_p, c_int], c_int),
+    'sosb_phase_factors': ([P_f64, c_int, c_int, c_int, c_dbl, P_f64, P_f64, ctypes.POINTER(c_int)], c_int),
     'sosb_set_warm_history': ([ctypes.c_void_p, c_int], c_int),
     'sosb_history': ([ctypes.c_void_p, c_int, P_i32, P_f64, P_f64], c_int),
     'sosb_compose_static': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,

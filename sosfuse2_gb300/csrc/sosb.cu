@@ -3935,6 +3935,15 @@ static int strato_factors(const std::vector<double>& lut, int n, int W, int rmax
     return 0;
 }
 
+int sosb_phase_factors(const double* lut, int n, int W, int rmax, double tol, double* U, double* V, int* rank) {
+    if (!lut || !U || !V || !rank || n < 1 || W < 1 || rmax < 1) return 1;
+    std::vector<double> l(lut, lut + (size_t)n * W), u, v;
+    *rank = strato_factors(l, n, W, rmax, tol, u, v);
+    std::copy(u.begin(), u.end(), U);
+    std::copy(v.begin(), v.end(), V);
+    return 0;
+}
+
 int sosb_set_constants(sosb_handle s, const sosb_constants* c) {
     if (!s || !c) return 1;
     const sosb_dims& d = s->d;
