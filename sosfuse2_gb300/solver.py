@@ -271,8 +271,8 @@ class Solver:
 
 class BatchSolver:
     """Many independent states solved together (sosb_solve_batch): each state has its own handle and stream; one
-    library thread replays an evaluation graph per active state each round, so the GPU overlaps their launches, and
-    reads their reports (`threads`: solves in flight, 0 all)."""
+    library thread enqueues every state's first evaluation and solve graph (the loop runs on the device), so the GPU
+    overlaps their launches, and waits only for the streams to finish (`threads`: solves in flight, 0 all)."""
 
     def __init__(self, states, device=None):
         self.kernels = [Kernel(st, device) for st in states]
