@@ -244,6 +244,12 @@ typedef struct {
 int sosb_column_table(int n_h, const double *h, int n_x, const double *x, const double *shells, int n_shells,
                       const double *gl_u, const double *gl_w, int n_gl, const sosb_profile_shape *shape, double *up,
                       double *down, int threads);
+/* sosb_column_table on the device: one thread per (table, height, x), the same column function. h[n_h], x[n_x],
+ * gl_u/gl_w[n_gl], up/down [n_h][n_x][6] are device pointers, shells[n_shells] host values; synchronises `stream`.
+ * Returns 3 on a CUDA error. */
+int sosb_column_table_device(int n_h, const double *h, int n_x, const double *x, const double *shells, int n_shells,
+                             const double *gl_u, const double *gl_w, int n_gl, const sosb_profile_shape *shape,
+                             double *up, double *down, void *stream);
 /* A solar column table (sosb_column_table's output with its grids) for lookups: heights h[n_h] (ascending, to
  * top), abscissae x uniform on [0, 1] (n_x values), up/down [n_h][n_x][6]. */
 typedef struct {

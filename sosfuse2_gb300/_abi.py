@@ -106,6 +106,9 @@ SIGNATURES = {
                               P_f64, P_f64, c_i64, c_int], c_int),
     'sosb_column_table': ([c_int, P_f64, c_int, P_f64, P_f64, c_int, P_f64, P_f64, c_int, ctypes.POINTER(ProfileShape),
                            P_f64, P_f64, c_int], c_int),
+    'sosb_column_table_device': ([c_int, ctypes.c_void_p, c_int, ctypes.c_void_p, P_f64, c_int, ctypes.c_void_p,
+                                  ctypes.c_void_p, c_int, ctypes.POINTER(ProfileShape), ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_void_p], c_int),
     'sosb_evaluate': ([ctypes.c_void_p, c_int, c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                        ctypes.c_void_p, ctypes.c_void_p], c_int),
     'sosb_apply': ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], c_int),

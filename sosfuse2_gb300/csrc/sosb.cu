@@ -4125,11 +4125,11 @@ SOS_HD int ray_cuts(const double p[3], const double d[3], double top, const doub
     return nc;
 }
 
-static void column_along(double r0, double mu, const sosb_profile_shape& a, const double* shells, int nshell,
+SOS_HD void column_along(double r0, double mu, const sosb_profile_shape& a, const double* shells, int nshell,
                          const double* u, const double* wu, int n, double out[6]) {
     const double R = 6371.0;
     const double px = 0.0, py = 0.0, pz = r0;
-    const double dx = std::sqrt(std::max(1.0 - mu * mu, 0.0)), dy = 0.0, dz = mu;
+    const double dx = sqrt(fmax(1.0 - mu * mu, 0.0)), dy = 0.0, dz = mu;
     const double pv[3] = {px, py, pz}, dv[3] = {dx, dy, dz};
     double cols[MAX_CUTS];
     const int nc = ray_cuts(pv, dv, a.top, shells, nshell, cols, nullptr);
@@ -4140,18 +4140,18 @@ static void column_along(double r0, double mu, const sosb_profile_shape& a, cons
         for (int q = 0; q < n; ++q) {
             const double t = s0 + (s1 - s0) * u[q];
             const double qx = px + t * dx, qy = py + t * dy, qz = pz + t * dz;
-            const double h = std::sqrt((qx * qx + qy * qy) + qz * qz) - R;
+            const double h = sqrt((qx * qx + qy * qy) + qz * qz) - R;
             const double w = (s1 - s0) * wu[q];
-            const double hc = std::min(std::max(h, 0.0), a.top);
-            const double air = std::exp(-hc / 8.0);
+            const double hc = fmin(fmax(h, 0.0), a.top);
+            const double air = exp(-hc / 8.0);
             const double z = (hc - a.ozone_peak) / 5.0;
             const double no2 = (hc - a.no2_center) / 4.0;
-            const double prof[5] = {air, std::exp(-hc / a.aerosol_height), std::exp(1.0 - z - std::exp(-z)) * a.ozone_norm,
-                                    std::exp(-0.5 * (no2 * no2)), air * air};
+            const double prof[5] = {air, exp(-hc / a.aerosol_height), exp(1.0 - z - exp(-z)) * a.ozone_norm,
+                                    exp(-0.5 * (no2 * no2)), air * air};
             for (int c = 0; c < 5; ++c) seg[c] += w * prof[c];
             if (a.strato) {
                 const double v = (h - a.strato_center) / a.strato_sigma;
-                sst += w * (std::exp(-0.5 * (v * v)) / a.strato_norm);
+                sst += w * (exp(-0.5 * (v * v)) / a.strato_norm);
             }
         }
         for (int c = 0; c < 5; ++c) out[c] += seg[c];
@@ -4187,6 +4187,62 @@ int sosb_column_table(int n_h, const double* h, int n_x, const double* x, const 
         });
     for (auto& t : pool) t.join();
     return 0;
+}
+
+// The solar column table on the device: one thread per (up or down table, height, x), the column function of
+// sosb_column_table (the same FP64 operations; a compiler may contract them differently on the two sides).
+struct ColArgs {
+    int n_h, n_x, n_gl, nshell;
+    const double *h, *x, *gl_u, *gl_w;
+    double shells[8];
+    sosb_profile_shape a;
+    double *up, *down;
+};
+
+__global__ void column_table_kernel(ColArgs g) {
+    const long long nhx = (long long)g.n_h * g.n_x, n = 2 * nhx;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int dn = t >= nhx ? 1 : 0;
+        const long long ij = t - dn * nhx;
+        const int i = (int)(ij / g.n_x), j = (int)(ij - (long long)i * g.n_x);
+        const double R = 6371.0, r = R + g.h[i];
+        const double mg = -sqrt(fmax(0.0, 1.0 - (R / r) * (R / r)));
+        double mu;
+        if (!dn) {
+            mu = mg + (1.0 - mg) * (g.x[j] * g.x[j]);
+            if (j == 0) mu = mg + 1e-9;
+        } else {
+            mu = mg - (1.0 + mg) * (g.x[j] * g.x[j]);
+            if (j == 0) mu = mg - 1e-9;
+            mu = fmax(mu, -1.0);
+        }
+        column_along(r, mu, g.a, g.shells, g.nshell, g.gl_u, g.gl_w, g.n_gl, (dn ? g.down : g.up) + ij * 6);
+    }
+}
+
+int sosb_column_table_device(int n_h, const double* h, int n_x, const double* x, const double* shells, int n_shells,
+                             const double* gl_u, const double* gl_w, int n_gl, const sosb_profile_shape* shape,
+                             double* up, double* down, void* stream) {
+    if (n_h < 1 || n_x < 1 || !h || !x || !gl_u || !gl_w || n_gl < 1 || !shape || !up || !down) return 1;
+    if (n_shells < 0 || n_shells > 8 || (n_shells > 0 && !shells)) return 1;
+    ColArgs g{};
+    g.n_h = n_h;
+    g.n_x = n_x;
+    g.n_gl = n_gl;
+    g.nshell = n_shells;
+    g.h = h;
+    g.x = x;
+    g.gl_u = gl_u;
+    g.gl_w = gl_w;
+    for (int k = 0; k < n_shells; ++k) g.shells[k] = shells[k];  // host values
+    g.a = *shape;
+    g.up = up;
+    g.down = down;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    column_table_kernel<<<grid_for(2LL * n_h * n_x, 128), 128, 0, st>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? 0 : 3;
 }
 
 // Bilinear lookup of a solar column table (synth.ColumnTable.lookup): columns [6] at height h (clipped to [0, top])

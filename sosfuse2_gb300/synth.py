@@ -151,9 +151,10 @@ _DEVICE = None
 
 
 class device_geometry:
-    """Context in which the ray segments and ray-end quantities of the bundles (sosb_ray_segments) are built on the
-    GPU `device` (sosb_ray_segments_device, one thread per ray) instead of on host threads; the quadratures, the column
-    tables and the CSR compaction stay on the host."""
+    """Context in which the ray segments and ray-end quantities of the bundles (sosb_ray_segments) and the solar column
+    tables (sosb_column_table) are built on the GPU `device` (sosb_ray_segments_device, one thread per ray;
+    sosb_column_table_device, one thread per table entry) instead of on host threads; the quadratures and the CSR
+    compaction stay on the host."""
 
     def __init__(self, device='cuda:0'):
         self.device = device
@@ -363,8 +364,9 @@ def column_rows(atm, shells, h, x, n=32):
     return up, down
 
 
-def native_column_table(atm, shells, h, x, n=32, threads=0):
-    """The same tables by libsosb's sosb_column_table (host threads; built in-tree on first use)."""
+def native_column_table(atm, shells, h, x, n=32, threads=0, device=None):
+    """The same tables by libsosb's sosb_column_table (host threads; built in-tree on first use), or by
+    sosb_column_table_device on `device` (the same column function on the GPU, results back in host arrays)."""
     from . import _abi, build
 
     lib = _abi.library(build.build())
@@ -377,6 +379,21 @@ def native_column_table(atm, shells, h, x, n=32, threads=0):
     x = np.ascontiguousarray(x, np.float64)
     sh = np.ascontiguousarray(shells, np.float64)
     u, wu = (np.ascontiguousarray(v, np.float64) for v in gauss01(n))
+    if device is not None:
+        import torch
+
+        dev = torch.device(device)
+        t = lambda a: torch.as_tensor(a, device=dev)  # noqa: E731
+        hd, xd, ud, wd = t(h), t(x), t(u), t(wu)
+        upd = torch.empty((len(h), len(x), 6), dtype=torch.float64, device=dev)
+        downd = torch.empty_like(upd)
+        vp = lambda a: ctypes.c_void_p(a.data_ptr())  # noqa: E731
+        stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        rc = lib.sosb_column_table_device(len(h), vp(hd), len(x), vp(xd), _abi.ptr(sh, _abi.P_f64), len(sh), vp(ud),
+                                          vp(wd), n, ctypes.byref(shape), vp(upd), vp(downd), stream)
+        if rc:
+            raise RuntimeError(f'E_COLUMN_TABLE: sosb_column_table_device returned {rc}')
+        return upd.cpu().numpy(), downd.cpu().numpy()
     up = np.empty((len(h), len(x), 6))
     down = np.empty_like(up)
     rc = lib.sosb_column_table(len(h), _abi.ptr(h, _abi.P_f64), len(x), _abi.ptr(x, _abi.P_f64),
@@ -394,8 +411,11 @@ class ColumnTable:
         self.top = atm.top
         self.h = np.linspace(0, math.sqrt(atm.top), SUN_HEIGHT_INTERVALS * scale + 1) ** 2
         self.x = np.linspace(0, 1, 400 * scale + 1)
-        build = native_column_table if _NATIVE else column_rows
-        self.up, self.down = build(atm, shells, self.h, self.x, n)
+        if _NATIVE and _DEVICE is not None:
+            self.up, self.down = native_column_table(atm, shells, self.h, self.x, n, device=_DEVICE)
+        else:
+            build = native_column_table if _NATIVE else column_rows
+            self.up, self.down = build(atm, shells, self.h, self.x, n)
 
     def lookup(self, h, mu):
         """Columns [n, 6] and whether the ray escapes (mu >= horizon cosine)."""

@@ -70,3 +70,21 @@ def test_device_geometry_bundle_equals_host():
             assert np.allclose(a, b, rtol=CUT_RTOL, atol=CUT_RTOL), k
         else:
             np.testing.assert_array_equal(a, b, err_msg=k)
+
+
+def test_device_column_table_equals_host():
+    """The solar column table on the device (sosb_column_table_device, one thread per (table, height, x)) against
+    the host threads' table (sosb_column_table, itself checked against its NumPy restatement in
+    tests/test_column_table.py) for the config-0 family's atmosphere and shells: every column within 1e-12 relative
+    (the two compilers may contract the FP64 operations differently)."""
+    from sosfuse2_gb300 import synth
+
+    atm = synth.Atmosphere([550.0], seed=3, top=100.0, strato_tau=0.01, no2_column=5e15)
+    shells = synth._shells(100.0)
+    h = np.linspace(0, np.sqrt(100.0), 41) ** 2
+    x = np.linspace(0, 1, 201)
+    up, down = synth.native_column_table(atm, shells, h, x)
+    up_d, down_d = synth.native_column_table(atm, shells, h, x, device='cuda:0')
+    for a, b in ((up_d, up), (down_d, down)):
+        scale = np.maximum(np.abs(b), 1e-300)
+        assert np.max(np.abs(a - b) / scale * (np.abs(b) > 1e-200)) <= 1e-12
