@@ -75,8 +75,10 @@ def test_device_geometry_bundle_equals_host():
 def test_device_column_table_equals_host():
     """The solar column table on the device (sosb_column_table_device, one thread per (table, height, x)) against
     the host threads' table (sosb_column_table, itself checked against its NumPy restatement in
-    tests/test_column_table.py) for the config-0 family's atmosphere and shells: every column within 1e-12 relative
-    (the two compilers may contract the FP64 operations differently)."""
+    tests/test_column_table.py) on 0-100 km with the shells and the stratospheric layer: every column within 1e-12 of
+    the component's largest column. The two compilers contract the FP64 operations differently, which moves columns
+    far below the largest by more than that relative to themselves: a ray from the top going up has a path of about
+    1e-17 km whose length is rounding, and columns of 1e-26 and less differ in their twelfth digit."""
     from sosfuse2_gb300 import synth
 
     atm = synth.Atmosphere([550.0], seed=3, top=100.0, strato_tau=0.01, no2_column=5e15)
@@ -86,5 +88,5 @@ def test_device_column_table_equals_host():
     up, down = synth.native_column_table(atm, shells, h, x)
     up_d, down_d = synth.native_column_table(atm, shells, h, x, device='cuda:0')
     for a, b in ((up_d, up), (down_d, down)):
-        scale = np.maximum(np.abs(b), 1e-300)
-        assert np.max(np.abs(a - b) / scale * (np.abs(b) > 1e-200)) <= 1e-12
+        top = np.abs(b).max(axis=(0, 1))  # per component
+        assert np.all(np.abs(a - b).max(axis=(0, 1)) <= 1e-12 * top)
