@@ -76,3 +76,33 @@ def test_ground_entry_points_reject_null_handles(lib):
     ext = (ctypes.c_double * 5)()
     assert lib.sosb_prepare_ground(None, 0.3, ext, None) == 1
 
+
+
+def test_handle_free_entry_points_reject_bad_arguments():
+    """The entry points without a handle check their arguments on the host before any CUDA call: an empty grid, more
+    than eight shells, a missing array or fewer than two solar-zenith nodes return 1 with nothing launched (so this
+    runs without a GPU); the per-handle switches reject a NULL handle."""
+    import numpy as np
+
+    lib = _abi.library()
+    a = np.zeros(64)
+    p = a.ctypes.data_as(ctypes.c_void_p)
+    pd = _abi.ptr(a, _abi.P_f64)
+    shape = _abi.ProfileShape()
+    col = lib.sosb_column_table_device
+    assert col(0, p, 2, p, None, 0, p, p, 4, ctypes.byref(shape), p, p, None) == 1  # no heights
+    assert col(2, p, 2, p, pd, 9, p, p, 4, ctypes.byref(shape), p, p, None) == 1  # nine shells
+    assert col(2, p, 2, p, None, 1, p, p, 4, ctypes.byref(shape), p, p, None) == 1  # shells missing
+    assert col(2, p, 2, p, None, 0, p, p, 4, None, p, p, None) == 1  # no profile shape
+    assert col(2, p, 2, p, None, 0, p, p, 4, ctypes.byref(shape), p, None, None) == 1  # no down table
+    seg = lib.sosb_ray_segments_device
+    outs = [p] * 9
+    assert seg(1, p, p, 80.0, None, 0, 1, p, None, *outs) == 1  # one solar-zenith node
+    assert seg(1, p, p, 80.0, pd, 9, 4, p, None, *outs) == 1  # nine shells
+    assert seg(-1, p, p, 80.0, None, 0, 4, p, None, *outs) == 1  # negative ray count
+    grid = _abi.ColumnGrid(n_h=1, n_x=2)
+    assert seg(1, p, p, 80.0, None, 0, 4, p, ctypes.byref(grid), *outs) == 1  # a one-height table
+    assert lib.sosb_set_ground_mma(None, 1) == 1
+    assert lib.sosb_set_corner_mma(None, 1) == 1
+    rank = ctypes.c_int(-1)
+    assert lib.sosb_phase_factors(pd, 0, 4, 8, 2e-6, pd, pd, ctypes.byref(rank)) == 1
